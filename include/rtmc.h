@@ -1,0 +1,220 @@
+/*
+ * rtmc.h -- C ABI of librtmc, the GB300 radiative-transfer Monte Carlo engine.
+ *
+ * Plain C: fixed-width integers, doubles and pointers only.  Every entry point returns
+ * an int status (RTMC_OK == 0); on failure rtmc_last_error() gives the message.  A
+ * context is used by one host thread at a time; independent contexts may run side by
+ * side (one per MATLAB parfor worker, say).
+ *
+ * Reference: cottereau/RadiativeTransferMonteCarlo (MATLAB).  Each entry point names
+ * the reference code it replaces.
+ */
+#ifndef RTMC_H
+#define RTMC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RTMC_ABI_VERSION 1
+#define RTMC_MAX_BND 4
+#define RTMC_ZOE_N 181 /* Zoeppritz table on 0:0.5:90 degrees (MaterialClass.m:1809) */
+
+enum rtmc_status {
+    RTMC_OK = 0,
+    RTMC_ERR_ARG = 1,      /* invalid argument (message says which) */
+    RTMC_ERR_CUDA = 2,     /* CUDA runtime error */
+    RTMC_ERR_ALLOC = 3,    /* host or device allocation failed */
+    RTMC_ERR_DEVICE = 4,   /* a kernel reported an error status (bounds, watchdog) */
+    RTMC_ERR_NOTABLES = 5  /* tables handle missing or incompatible with the problem */
+};
+
+enum rtmc_psdf {
+    RTMC_PSDF_EXP = 0,        /* MaterialClass.Exponential, MaterialClass.m:479-517 */
+    RTMC_PSDF_GAUSSIAN = 1,   /* MaterialClass.Gaussian, :560-599 */
+    RTMC_PSDF_POWER_LAW = 2,  /* MaterialClass.PowerLaw, :519-558 */
+    RTMC_PSDF_TRIANGULAR = 3, /* MaterialClass.Triangular, :601-630 (3D only) */
+    RTMC_PSDF_LOW_PASS = 4,   /* MaterialClass.LowPass, :632-662 (3D only) */
+    RTMC_PSDF_VON_KARMAN = 5, /* MaterialClass.VonKarman, :664-710 */
+    RTMC_PSDF_CONST = 6       /* isotropic constant sigma per table (MaterialClass.preset, :1765-1785) */
+};
+
+enum rtmc_frame { RTMC_FRAME_CARTESIAN = 0, RTMC_FRAME_CYLINDRICAL = 1, RTMC_FRAME_SPHERICAL = 2 };
+enum rtmc_axis_mode { RTMC_AXIS_IGNORED = 0, RTMC_AXIS_RANGE = 1, RTMC_AXIS_BINNED = 2 };
+enum rtmc_precision { RTMC_FP32 = 0, RTMC_FP64 = 1 };
+
+/* ---------------------------------------------------------------------------------- */
+/* Host FP64 table builders                                                            */
+/* ---------------------------------------------------------------------------------- */
+
+typedef struct rtmc_tables rtmc_tables; /* opaque, host-side FP64 inverse-CDF tables */
+
+typedef struct {
+    int32_t d;          /* 2 or 3 */
+    int32_t acoustics;  /* 1 acoustic, 0 elastic */
+    int32_t psdf;       /* enum rtmc_psdf */
+    int32_t reserved;
+    double freq;        /* Hz */
+    double v[2];        /* acoustic: v[0]; elastic: vp, vs */
+    double cv[3];       /* acoustic: CV kappa, CV rho; elastic: CV lambda, mu, rho */
+    double corr[3];     /* acoustic: corr(kappa,rho); elastic: corr(l,m), corr(l,r), corr(m,r) */
+    double lc;          /* correlation length */
+    double nu;          /* Hurst number (Von Karman only) */
+    double sigma_const[4]; /* RTMC_PSDF_CONST: sigma of table (i,j), row-major {PP,PS,SP,SS} */
+    int64_t n_theta;    /* pdf grid size; the reference uses 1e6 (0 selects 1e6) */
+} rtmc_material;
+
+typedef struct {
+    int32_t n_tables;   /* 1 acoustic, 4 elastic */
+    int32_t reserved;
+    int64_t n_knots[4];
+    double Sigma[4];    /* row-major 2x2 for elastic, Sigma[0] for acoustic */
+    double Sigmapr[4];
+    double mean_free_time[2];
+    double p2p, s2s;
+    double diffusivity;
+    double transport_mean_free_path[2];
+    double g;           /* acoustic anisotropy coefficient */
+} rtmc_tables_info;
+
+/* Replaces MaterialClass.prepareSigma / prepareSigmaOne / calcSigmaIsotropic / getPSDF
+ * (MaterialClass.m:2379-2463, :172-359, :381-455): cross-sections, Sigma and Sigma' by
+ * adaptive Gauss-Kronrod quadrature, the pdf on n_theta points, cumsum cdf scaled by
+ * pi/n_theta and the diff(cdf) > 1e-8 knot filter. */
+int rtmc_tables_build(const rtmc_material *material, rtmc_tables **out);
+
+/* Wraps caller-built knots, e.g. the GridVectors/Values of MATLAB griddedInterpolant
+ * objects in material.invcdf (MaterialClass.m:2462); mean free times etc. come from the
+ * caller, so the info block is filled with zeros apart from n_tables and n_knots. */
+int rtmc_tables_from_knots(int32_t n_tables, const int64_t *n_knots, const double *const *cdf,
+                           const double *const *theta, rtmc_tables **out);
+
+int rtmc_tables_get_info(const rtmc_tables *tables, rtmc_tables_info *info);
+
+/* copies knots of table t (0..n_tables-1) into caller buffers of n_knots[t] doubles */
+int rtmc_tables_get_knots(const rtmc_tables *tables, int32_t t, double *cdf, double *theta);
+
+/* host evaluation of invcdf{t}(u): griddedInterpolant linear, linear extrapolation */
+int rtmc_tables_eval(const rtmc_tables *tables, int32_t t, int64_t n, const double *u, double *theta);
+
+void rtmc_tables_free(rtmc_tables *tables);
+
+/* Replaces MaterialClass.Zoeppritz + ZoeppritzFluid (MaterialClass.m:1786-1885,
+ * ZoeppritzFluid.m:1-244): energy coefficients of a solid/fluid interface at n angles.
+ * out is row-major [7][n]: E_Rpp, E_Rpsv, E_Tpp, E_Rsvsv, E_Rsp, E_Tsp, E_Rsh. */
+int rtmc_zoeppritz_fluid(int32_t n, const double *angles_deg, double vp1, double vs1, double rho1,
+                         double vp2, double vs2, double rho2, double *out);
+
+/* ---------------------------------------------------------------------------------- */
+/* Transport: the packet x time loop of radiativeTransfer.m:40-158                     */
+/* ---------------------------------------------------------------------------------- */
+
+typedef struct rtmc_context rtmc_context;
+
+typedef struct {
+    int32_t d;            /* 2 or 3 */
+    int32_t frame;        /* enum rtmc_frame */
+    int32_t acoustics;
+    int32_t precision;    /* enum rtmc_precision */
+    int32_t src_dir;      /* 0 'uniform', 1 'outgoing', 2 'upper' (initializeParticle.m:40-47) */
+    int32_t polarization; /* 0 'P', 1 'S' */
+    int32_t n_sub;        /* sub-steps per observation interval (propagateParticleSmallDt.m:4-7) */
+    int32_t n_obs;        /* observation instants = Nt - 1 (t = 0 is never filled) */
+    int32_t n_bnd;        /* plane boundaries, <= RTMC_MAX_BND */
+    int32_t hist_shift;   /* a unit count adds 1 << hist_shift (int64 fixed point) */
+    int32_t reserved[2];
+    int64_t n_particles;
+    int64_t pid0;         /* global id of the first particle (replica sharding) */
+    uint64_t seed;
+    double src_pos[3];
+    double src_lambda;    /* Gaussian source radius (initializeParticle.m:23) */
+    double v[2];          /* propagation speed of P (or acoustic) and S particles */
+    double mft[2];        /* mean free time per mode; INFINITY disables scattering */
+    double p2p, s2s;      /* mode-conservation probabilities (MaterialClass.m:2439-2440) */
+    double qrate[2];      /* omega*h/Q per mode; 0 when Q = Inf (propagateParticleSmallDt.m:57-82) */
+    double h;             /* sub-step length */
+    /* observation axes 0..3 = X, Y, Z, PSI in the frame of observeTime.m:14-127 */
+    int32_t axis_mode[4];    /* enum rtmc_axis_mode */
+    int32_t axis_nedges[4];  /* edges of a binned axis; 2 for a range-checked axis */
+    const double *axis_edges[4];
+    int64_t axis_stride[4];  /* histogram stride of a binned axis */
+    int64_t time_stride;
+    int64_t mode_stride;
+    int64_t hist_len;        /* int64 elements of the histogram */
+    int32_t bnd_dir[RTMC_MAX_BND];    /* 1, 2, 3: plane normal to x, y, z */
+    int32_t bnd_absorb[RTMC_MAX_BND]; /* 1 'absorbing', 0 'reflective' */
+    double bnd_val[RTMC_MAX_BND];
+    double zoe_rpp[RTMC_ZOE_N];       /* E_Rpp on 0:0.5:90 deg (elastic reflective plane) */
+    double zoe_rsvsv[RTMC_ZOE_N];     /* E_Rsvsv on 0:0.5:90 deg */
+} rtmc_problem;
+
+typedef struct {
+    int64_t scatter_events;  /* accepted scatterings (the throughput unit) */
+    int64_t boundary_hits;
+    int64_t kills;           /* Q-kills */
+    int64_t absorbed;        /* absorbing-boundary deaths */
+    int64_t observations;    /* counts added to the histogram */
+    int64_t conversions;     /* P<->S changes at boundaries */
+    int64_t device_status;   /* non-zero: a kernel guard tripped */
+    int64_t reserved;
+    double kernel_ms;        /* transport kernel, CUDA events on the context stream */
+    double total_ms;         /* whole call, CUDA events (copies included) */
+    double h2d_bytes;
+    double d2h_bytes;
+} rtmc_stats;
+
+/* context on CUDA device `device` with its own stream */
+int rtmc_create(int32_t device, rtmc_context **out);
+void rtmc_destroy(rtmc_context *ctx);
+
+/* last error message of ctx (or of the calling thread when ctx is NULL) */
+const char *rtmc_last_error(const rtmc_context *ctx);
+int32_t rtmc_abi_version(void);
+
+/* sizeof of the ABI structs {rtmc_material, rtmc_tables_info, rtmc_problem, rtmc_stats},
+ * for bindings that mirror them (ctypes, MEX) to check their layout */
+int rtmc_abi_sizes(int64_t out[4]);
+
+/* Replaces the packet loop radiativeTransfer.m:40-158 (initializeParticle +
+ * propagateParticleSmallDt + observeTime for every packet and time instant).  hist_out
+ * is a HOST buffer of problem->hist_len int64 (column-major [N1,N2,(..),Nt,modes], as the
+ * uint32 array E of initializeObservation.m:133); the call uploads tables and edges,
+ * runs on the GPU and copies the histogram back.  stats may be NULL. */
+int rtmc_forward(rtmc_context *ctx, const rtmc_problem *problem, const rtmc_tables *tables,
+                 int64_t *hist_out, rtmc_stats *stats);
+
+/* Same, with the histogram left in device memory owned by ctx (no host copy);
+ * rtmc_copy_histogram reads it back later. */
+int rtmc_forward_device(rtmc_context *ctx, const rtmc_problem *problem, const rtmc_tables *tables,
+                        rtmc_stats *stats);
+int rtmc_copy_histogram(rtmc_context *ctx, int64_t *hist_out, int64_t n);
+
+/* rtmc_forward plus the final state of every particle, for particle-by-particle checks:
+ * state_out is a HOST buffer of n_particles x 16 doubles {x[3] at the last event, dir[3],
+ * perp[3], mode (0 P, 1 S), alive, scatterings, boundary crossings, sub-step of the last
+ * event, sub-step of death (-1 alive), event counter}.  No counterpart in the reference
+ * (whose particle struct P, initializeParticle.m:163-170, is internal to the loop). */
+int rtmc_forward_trace(rtmc_context *ctx, const rtmc_problem *problem, const rtmc_tables *tables,
+                       int64_t *hist_out, double *state_out, rtmc_stats *stats);
+
+/* pinned host memory for fast copies (cudaMallocHost); free with rtmc_host_free */
+int rtmc_host_alloc(int64_t bytes, void **out);
+int rtmc_host_free(void *p);
+
+/* enable (1, default) or disable (0) reuse of the device copy of a tables handle across
+ * calls; with 0 every call uploads its tables again (end-to-end timing) */
+int rtmc_set_table_cache(rtmc_context *ctx, int32_t enable);
+
+/* writes a device buffer larger than L2 (timing hygiene between measured runs) */
+int rtmc_flush_l2(rtmc_context *ctx);
+
+/* kernel time of the last forward call in ms (CUDA events) and its launch count */
+int rtmc_last_timing(const rtmc_context *ctx, double *kernel_ms, int32_t *launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* RTMC_H */

@@ -1,0 +1,148 @@
+"""ctypes wrapper of the C oracle (oracle/rtmc_oracle.c).
+
+TEST INFRASTRUCTURE ONLY: imported by tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline leg, as the checker.  The product library never calls it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+SRC = HERE / "rtmc_oracle.c"
+LIB = HERE / "_build" / "liboracle.so"
+
+ST_NAMES = ("scatter_events", "boundary_hits", "kills", "absorbed", "observations", "conversions")
+
+
+def build(force: bool = False) -> Path:
+    """gcc -O2 -fopenmp; FMA contraction off so x86 and Arm builds give the same bits."""
+    if not force and LIB.exists() and LIB.stat().st_mtime >= SRC.stat().st_mtime:
+        return LIB
+    LIB.parent.mkdir(exist_ok=True)
+    tmp = LIB.with_suffix(".tmp.so")
+    subprocess.run(["gcc", "-O2", "-std=c11", "-D_GNU_SOURCE", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared",
+                    str(SRC), "-o", str(tmp), "-lm"], check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+class OracleProblem(C.Structure):
+    _fields_ = [("d", C.c_int32), ("frame", C.c_int32), ("acoustics", C.c_int32), ("scheme", C.c_int32),
+                ("u24", C.c_int32), ("src_dir", C.c_int32), ("polarization", C.c_int32), ("n_sub", C.c_int32),
+                ("n_obs", C.c_int32), ("n_bnd", C.c_int32), ("hist_shift", C.c_int32), ("nthreads", C.c_int32),
+                ("n_particles", C.c_int64), ("pid0", C.c_int64), ("seed", C.c_uint64),
+                ("src_pos", C.c_double * 3), ("src_lambda", C.c_double), ("v", C.c_double * 2),
+                ("mft", C.c_double * 2), ("p2p", C.c_double), ("s2s", C.c_double), ("qrate", C.c_double * 2),
+                ("h", C.c_double), ("axis_mode", C.c_int32 * 4), ("axis_nedges", C.c_int32 * 4),
+                ("axis_edges", C.POINTER(C.c_double) * 4), ("axis_stride", C.c_int64 * 4),
+                ("time_stride", C.c_int64), ("mode_stride", C.c_int64), ("hist_len", C.c_int64),
+                ("bnd_dir", C.c_int32 * 4), ("bnd_absorb", C.c_int32 * 4), ("bnd_val", C.c_double * 4),
+                ("zoe_rpp", C.POINTER(C.c_double)), ("zoe_rsvsv", C.POINTER(C.c_double)),
+                ("tab_n", C.c_int64 * 4), ("tab_cdf", C.POINTER(C.c_double) * 4),
+                ("tab_theta", C.POINTER(C.c_double) * 4)]
+
+
+_lib = None
+
+
+def load():
+    global _lib
+    if _lib is None:
+        lib = C.CDLL(str(build()))
+        lib.oracle_run.restype = C.c_int
+        lib.oracle_run.argtypes = [C.POINTER(OracleProblem), C.POINTER(C.c_int64), C.POINTER(C.c_int64),
+                                   C.POINTER(C.c_double)]
+        lib.oracle_philox4x32_10.restype = None
+        lib.oracle_philox4x32_10.argtypes = [C.POINTER(C.c_uint32)] * 3
+        lib.oracle_invcdf.restype = C.c_double
+        lib.oracle_invcdf.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int64, C.c_double]
+        lib.oracle_max_threads.restype = C.c_int
+        _lib = lib
+    return _lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def philox(ctr, key):
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    load().oracle_philox4x32_10(c, k, o)
+    return list(o)
+
+
+def run(prob, knots, scheme: str = "event", u24: bool | None = None, nthreads: int | None = None,
+        n_particles: int | None = None, pid0: int | None = None, want_state: bool = False):
+    """Run the oracle on a TransportProblem-like object with the given table knots
+    [(cdf, theta), ...].  scheme 'substep' (reference order) or 'event' (snap, GPU stream).
+    Returns (int64 histogram, stats dict, final states [N,16] or None)."""
+    lib = load()
+    P = OracleProblem()
+    P.d, P.frame, P.acoustics = prob.d, prob.frame, int(prob.acoustics)
+    P.scheme = 0 if scheme == "substep" else 1
+    P.u24 = int(prob.precision == 0) if u24 is None else int(u24)
+    P.src_dir, P.polarization, P.n_sub, P.n_obs = prob.src_dir, prob.polarization, prob.n_sub, prob.n_obs
+    P.n_bnd, P.hist_shift = len(prob.bnd), prob.hist_shift
+    P.nthreads = nthreads or max(1, lib.oracle_max_threads())
+    P.n_particles = prob.n_particles if n_particles is None else n_particles
+    P.pid0 = prob.pid0 if pid0 is None else pid0
+    P.seed = prob.seed
+    for i in range(3):
+        P.src_pos[i] = prob.src_pos[i]
+    P.src_lambda = prob.src_lambda
+    for m in range(2):
+        P.v[m] = prob.v[m]
+        P.mft[m] = prob.mft[m]
+        P.qrate[m] = prob.qrate[m]
+    P.p2p, P.s2s, P.h = prob.p2p, prob.s2s, prob.h
+    keep = []
+    for a in range(4):
+        # the oracle range-checks every integrated axis as the reference does
+        mode = prob.axis_mode[a]
+        e = prob.axis_edges[a]
+        if mode == 0 and e is not None and not (prob.d == 2 and a == 2):
+            mode = 1
+        P.axis_mode[a] = mode
+        if mode:
+            ea = np.ascontiguousarray(e, dtype=np.float64)
+            keep.append(ea)
+            P.axis_nedges[a] = ea.size
+            P.axis_edges[a] = _dp(ea)
+        P.axis_stride[a] = prob.axis_stride[a]
+    P.time_stride, P.mode_stride, P.hist_len = prob.time_stride, prob.mode_stride, prob.hist_len
+    for b, (bd, bv, ab) in enumerate(prob.bnd):
+        P.bnd_dir[b], P.bnd_val[b], P.bnd_absorb[b] = bd, bv, int(ab)
+    if prob.zoe_rpp is not None:
+        zr = np.ascontiguousarray(prob.zoe_rpp, dtype=np.float64)
+        zs = np.ascontiguousarray(prob.zoe_rsvsv, dtype=np.float64)
+        keep += [zr, zs]
+        P.zoe_rpp, P.zoe_rsvsv = _dp(zr), _dp(zs)
+    for i, (c, t) in enumerate(knots):
+        c = np.ascontiguousarray(c, dtype=np.float64)
+        t = np.ascontiguousarray(t, dtype=np.float64)
+        keep += [c, t]
+        P.tab_n[i] = c.size
+        P.tab_cdf[i] = _dp(c)
+        P.tab_theta[i] = _dp(t)
+    hist = np.zeros(prob.hist_len, dtype=np.int64)
+    stats = np.zeros(8, dtype=np.int64)
+    fs = np.zeros((P.n_particles, 16)) if want_state else None
+    rc = lib.oracle_run(C.byref(P), hist.ctypes.data_as(C.POINTER(C.c_int64)),
+                        stats.ctypes.data_as(C.POINTER(C.c_int64)), _dp(fs) if want_state else None)
+    if rc:
+        raise RuntimeError(f"oracle_run failed ({rc})")
+    return hist, dict(zip(ST_NAMES, map(int, stats[:6]))), fs
+
+
+def table_knots(tables) -> list:
+    """[(cdf, theta)] of a product tables handle, to feed both sides the same tables."""
+    n = tables.info().n_tables
+    return [tables.knots(i) for i in range(n)]

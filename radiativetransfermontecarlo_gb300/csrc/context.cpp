@@ -1,0 +1,503 @@
+// Context, device memory and the rtmc_forward entry points of librtmc.
+//
+// rtmc_forward replaces the packet x time loop of radiativeTransfer.m:40-158: it stages
+// the inverse-CDF tables (host FP64 knots -> device knots + slopes + Chen-Asau guide
+// table), the observation edges and the Zoeppritz tables, zeroes the int64 histogram,
+// launches the fused transport kernel and copies the histogram back.
+#include "rtmc_internal.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+using namespace rtmc;
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t cap = 0;
+    int grow(size_t bytes)
+    {
+        if (bytes <= cap) return 0;
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e != cudaSuccess) return (int)e;
+        cap = bytes;
+        return 0;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        cap = 0;
+    }
+};
+
+struct rtmc_context {
+    int device = 0;
+    int num_sms = 0;
+    int max_smem_optin = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_k0 = nullptr, ev_k1 = nullptr, ev_end = nullptr;
+    std::string err;
+    DevBuf hist, tabs, aux, stats, flush, trace;
+    uint64_t tabs_gen = 0;
+    int tabs_prec = -1;
+    DevTables<float> tf{};
+    DevTables<double> td{};
+    int64_t hist_len = 0;
+    double last_kernel_ms = 0;
+    int last_launches = 0;
+    int cache_tables = 1;
+};
+
+namespace {
+
+int cuda_fail(rtmc_context *c, cudaError_t e, const char *what)
+{
+    return fail(c ? &c->err : nullptr, RTMC_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call, what)                                                                                               \
+    do {                                                                                                             \
+        cudaError_t _e = (call);                                                                                     \
+        if (_e != cudaSuccess) return cuda_fail(ctx, _e, what);                                                      \
+    } while (0)
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Stage the tables in precision R: FP64 knots of u, R angles, R slopes, int32 guide.
+template <typename R> int upload_tables(rtmc_context *ctx, const rtmc_tables *t, DevTables<R> *dt)
+{
+    const int G = kGuideN;
+    size_t off[4][4], total = 0;
+    for (int i = 0; i < t->n_tables; ++i) {
+        const size_t n = t->cdf[i].size();
+        off[i][0] = total; total = align_up(total + n * sizeof(double), 256);
+        off[i][1] = total; total = align_up(total + n * sizeof(R), 256);
+        off[i][2] = total; total = align_up(total + n * sizeof(R), 256);
+        off[i][3] = total; total = align_up(total + (size_t)(G + 1) * sizeof(int32_t), 256);
+    }
+    if (ctx->tabs.grow(total)) return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for tables failed");
+    std::vector<unsigned char> host(total, 0);
+    for (int i = 0; i < t->n_tables; ++i) {
+        const std::vector<double> &c = t->cdf[i], &th = t->theta[i];
+        const size_t n = c.size();
+        std::memcpy(host.data() + off[i][0], c.data(), n * sizeof(double));
+        R *rt = reinterpret_cast<R *>(host.data() + off[i][1]);
+        R *rs = reinterpret_cast<R *>(host.data() + off[i][2]);
+        for (size_t k = 0; k < n; ++k) {
+            rt[k] = (R)th[k];
+            rs[k] = (k + 1 < n) ? (R)((th[k + 1] - th[k]) / (c[k + 1] - c[k])) : (R)0;
+        }
+        int32_t *g = reinterpret_cast<int32_t *>(host.data() + off[i][3]);
+        size_t k = 0;
+        for (int j = 0; j <= G; ++j) {
+            const double target = (double)j / (double)G;
+            while (k + 1 <= n - 2 && c[k + 1] <= target) ++k;
+            g[j] = (int32_t)k;
+        }
+        unsigned char *base = static_cast<unsigned char *>(ctx->tabs.p);
+        dt->cdf[i] = reinterpret_cast<const double *>(base + off[i][0]);
+        dt->theta[i] = reinterpret_cast<const R *>(base + off[i][1]);
+        dt->slope[i] = reinterpret_cast<const R *>(base + off[i][2]);
+        dt->guide[i] = reinterpret_cast<const int32_t *>(base + off[i][3]);
+        dt->n[i] = (int32_t)n;
+    }
+    for (int i = t->n_tables; i < 4; ++i) *(&dt->cdf[0] + i) = nullptr;
+    CK(cudaMemcpyAsync(ctx->tabs.p, host.data(), total, cudaMemcpyHostToDevice, ctx->stream), "table upload");
+    CK(cudaStreamSynchronize(ctx->stream), "table upload");
+    return RTMC_OK;
+}
+
+int check_problem(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t)
+{
+    std::string *e = &ctx->err;
+    if (P->d != 2 && P->d != 3) return fail(e, RTMC_ERR_ARG, "dimension must be 2 or 3");
+    if (P->frame < 0 || P->frame > 2) return fail(e, RTMC_ERR_ARG, "frame must be cartesian, cylindrical or spherical");
+    if (P->precision != RTMC_FP32 && P->precision != RTMC_FP64) return fail(e, RTMC_ERR_ARG, "unknown precision");
+    if (P->src_dir < 0 || P->src_dir > 2) return fail(e, RTMC_ERR_ARG, "source direction must be uniform, outgoing or upper");
+    if (P->n_sub < 1 || P->n_obs < 1) return fail(e, RTMC_ERR_ARG, "n_sub and n_obs must be >= 1");
+    if ((int64_t)P->n_sub * P->n_obs >= (int64_t)1 << 30)
+        return fail(e, RTMC_ERR_ARG, "n_sub * n_obs must stay below 2^30 sub-steps");
+    if (P->n_particles < 0 || P->pid0 < 0) return fail(e, RTMC_ERR_ARG, "particle count and first id must be >= 0");
+    if (P->hist_shift < 0 || P->hist_shift > 62) return fail(e, RTMC_ERR_ARG, "hist_shift must be in [0, 62]");
+    if (P->n_bnd < 0 || P->n_bnd > RTMC_MAX_BND) return fail(e, RTMC_ERR_ARG, "at most 4 plane boundaries");
+    for (int b = 0; b < P->n_bnd; ++b) {
+        if (P->bnd_dir[b] < 1 || P->bnd_dir[b] > 3)
+            return fail(e, RTMC_ERR_ARG, "plane boundary dir must be 1, 2 or 3 (cylindrical dir 4 is not supported)");
+        if (!std::isfinite(P->bnd_val[b])) return fail(e, RTMC_ERR_ARG, "boundary position must be finite");
+    }
+    const int nm = P->acoustics ? 1 : 2;
+    for (int m = 0; m < nm; ++m) {
+        if (!(P->v[m] > 0) || !std::isfinite(P->v[m])) return fail(e, RTMC_ERR_ARG, "propagation speeds must be positive");
+        if (!(P->mft[m] > 0)) return fail(e, RTMC_ERR_ARG, "mean free times must be positive (Inf disables scattering)");
+        if (!(P->qrate[m] >= 0) || !std::isfinite(P->qrate[m])) return fail(e, RTMC_ERR_ARG, "qrate must be finite and >= 0");
+    }
+    if (!(P->h > 0) || !std::isfinite(P->h)) return fail(e, RTMC_ERR_ARG, "sub-step h must be positive");
+    if (!std::isfinite(P->src_lambda) || P->src_lambda < 0) return fail(e, RTMC_ERR_ARG, "source lambda must be >= 0");
+    int st = validate_tables(t, e);
+    if (st) return st;
+    if (t->n_tables != (P->acoustics ? 1 : 4))
+        return fail(e, RTMC_ERR_NOTABLES, "acoustic problems need 1 table, elastic problems 4");
+    if (P->hist_len <= 0) return fail(e, RTMC_ERR_ARG, "hist_len must be positive");
+    int64_t maxidx = (int64_t)P->n_obs * P->time_stride + (nm - 1) * P->mode_stride;
+    int tot_edges = 0;
+    for (int a = 0; a < 4; ++a) {
+        const int am = P->axis_mode[a];
+        if (am < 0 || am > 2) return fail(e, RTMC_ERR_ARG, "axis mode must be ignored, range or binned");
+        if (am == RTMC_AXIS_IGNORED) continue;
+        const int ne = P->axis_nedges[a];
+        if (ne < 2 || !P->axis_edges[a]) return fail(e, RTMC_ERR_ARG, "an observed axis needs at least 2 edges");
+        if (am == RTMC_AXIS_RANGE && ne != 2) return fail(e, RTMC_ERR_ARG, "a range-checked axis has exactly 2 edges");
+        for (int k = 0; k < ne; ++k)
+            if (std::isnan(P->axis_edges[a][k])) return fail(e, RTMC_ERR_ARG, "bin edges must not be NaN");
+        for (int k = 1; k < ne; ++k)
+            if (!(P->axis_edges[a][k] > P->axis_edges[a][k - 1]))
+                return fail(e, RTMC_ERR_ARG, "bin edges must be strictly increasing");
+        tot_edges += ne;
+        if (am == RTMC_AXIS_BINNED) {
+            if (P->axis_stride[a] < 0) return fail(e, RTMC_ERR_ARG, "negative stride");
+            maxidx += (int64_t)(ne - 2) * P->axis_stride[a];
+        }
+    }
+    if (tot_edges > kMaxEdges) return fail(e, RTMC_ERR_ARG, "too many bin edges (4096 at most over all axes)");
+    if (P->time_stride < 0 || P->mode_stride < 0 || maxidx >= P->hist_len)
+        return fail(e, RTMC_ERR_ARG, "histogram strides exceed hist_len");
+    return RTMC_OK;
+}
+
+template <typename R>
+void fill_params(rtmc_context *ctx, const rtmc_problem *P, const DevTables<R> &tab, DevParams<R> *p, int *n_edges_out,
+                 std::vector<R> *edges, std::vector<R> *zoe)
+{
+    std::memset(p, 0, sizeof *p);
+    p->d = P->d; p->frame = P->frame; p->acoustics = P->acoustics; p->src_dir = P->src_dir;
+    p->polarization = P->acoustics ? 0 : P->polarization;
+    p->n_sub = P->n_sub; p->n_obs = P->n_obs; p->n_bnd = P->n_bnd;
+    p->hist_shift = P->hist_shift;
+    p->s_end = P->n_sub * P->n_obs;
+    p->max_events = 4 * p->s_end + 64;
+    p->n_particles = P->n_particles; p->pid0 = P->pid0;
+    p->key0 = (uint32_t)P->seed; p->key1 = (uint32_t)(P->seed >> 32);
+    for (int i = 0; i < 3; ++i) p->src_pos[i] = (R)P->src_pos[i];
+    p->src_lambda = (R)P->src_lambda;
+    for (int m = 0; m < 2; ++m) {
+        const int mm = P->acoustics ? 0 : m;
+        p->step[m] = (R)(P->v[mm] * P->h);
+        const double mft = P->mft[mm];
+        p->scat_on[m] = std::isfinite(mft) ? 1 : 0;
+        p->inv_lam[m] = p->scat_on[m] ? (R)(1.0 / (P->h / mft)) : (R)0;
+        p->kill_on[m] = P->qrate[mm] > 0 ? 1 : 0;
+        p->inv_q[m] = p->kill_on[m] ? (R)(1.0 / P->qrate[mm]) : (R)0;
+    }
+    p->p2p = (R)P->p2p; p->s2s = (R)P->s2s;
+    if (!P->acoustics) {
+        p->vs_over_vp = (R)(P->v[1] / P->v[0]);
+        p->vp_over_vs = (R)(P->v[0] / P->v[1]);
+    }
+    p->cos_half_pi = (R)std::cos(M_PI / 2);
+    edges->clear();
+    for (int a = 0; a < 4; ++a) {
+        p->ax_mode[a] = P->axis_mode[a];
+        if (P->axis_mode[a] == RTMC_AXIS_IGNORED) continue;
+        const int ne = P->axis_nedges[a];
+        const double *E = P->axis_edges[a];
+        p->ax_n[a] = ne;
+        p->ax_off[a] = (int)edges->size();
+        for (int k = 0; k < ne; ++k) edges->push_back((R)E[k]);
+        p->ax_lo[a] = (R)E[0];
+        p->ax_hi[a] = (R)E[ne - 1];
+        p->ax_stride[a] = P->axis_stride[a];
+        const double w = (E[ne - 1] - E[0]) / (ne - 1);
+        bool uni = true;
+        for (int k = 1; k < ne; ++k)
+            if (std::fabs((E[k] - E[k - 1]) - w) > 1e-6 * std::fabs(w)) uni = false;
+        p->ax_uniform[a] = uni ? 1 : 0;
+        p->ax_inv_w[a] = (R)(1.0 / w);
+    }
+    p->time_stride = P->time_stride; p->mode_stride = P->mode_stride; p->hist_len = P->hist_len;
+    *n_edges_out = (int)edges->size();
+    p->n_edges = *n_edges_out;
+    for (int b = 0; b < P->n_bnd; ++b) {
+        p->bnd_dir[b] = P->bnd_dir[b];
+        p->bnd_absorb[b] = P->bnd_absorb[b];
+        p->bnd_val[b] = (R)P->bnd_val[b];
+    }
+    zoe->resize(2 * RTMC_ZOE_N);
+    for (int k = 0; k < RTMC_ZOE_N; ++k) {
+        (*zoe)[k] = (R)P->zoe_rpp[k];
+        (*zoe)[RTMC_ZOE_N + k] = (R)P->zoe_rsvsv[k];
+    }
+    p->tab = tab;
+    (void)ctx;
+}
+
+template <typename R>
+int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t *host_out, rtmc_stats *st,
+        double *trace_out)
+{
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    CK(cudaEventRecord(ctx->ev_start, ctx->stream), "event");
+    double h2d = 0, d2h = 0;
+    DevTables<R> *dt;
+    if constexpr (sizeof(R) == 4) dt = &ctx->tf; else dt = &ctx->td;
+    const int prec = sizeof(R) == 4 ? RTMC_FP32 : RTMC_FP64;
+    if (!ctx->cache_tables || ctx->tabs_gen != t->gen || ctx->tabs_prec != prec) {
+        int s = upload_tables<R>(ctx, t, dt);
+        if (s) { ctx->tabs_gen = 0; return s; }
+        ctx->tabs_gen = t->gen;
+        ctx->tabs_prec = prec;
+        for (int i = 0; i < t->n_tables; ++i) h2d += (double)t->cdf[i].size() * (8 + 2 * sizeof(R)) + (kGuideN + 1) * 4.0;
+    }
+    DevParams<R> p;
+    std::vector<R> edges, zoe;
+    int n_edges = 0;
+    fill_params<R>(ctx, P, *dt, &p, &n_edges, &edges, &zoe);
+    // aux buffer: edges | zoe | stats
+    const size_t eb = align_up(std::max<size_t>(1, edges.size()) * sizeof(R), 256);
+    const size_t zb = align_up(zoe.size() * sizeof(R), 256);
+    if (ctx->aux.grow(eb + zb)) return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for edges failed");
+    if (ctx->stats.grow(256)) return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for counters failed");
+    unsigned char *aux = static_cast<unsigned char *>(ctx->aux.p);
+    if (!edges.empty())
+        CK(cudaMemcpyAsync(aux, edges.data(), edges.size() * sizeof(R), cudaMemcpyHostToDevice, ctx->stream), "edges");
+    CK(cudaMemcpyAsync(aux + eb, zoe.data(), zoe.size() * sizeof(R), cudaMemcpyHostToDevice, ctx->stream), "zoeppritz");
+    h2d += (double)(edges.size() + zoe.size()) * sizeof(R);
+    p.edges = reinterpret_cast<const R *>(aux);
+    p.zoe = reinterpret_cast<const R *>(aux + eb);
+    const size_t hist_bytes = (size_t)P->hist_len * sizeof(int64_t);
+    if (ctx->hist.grow(hist_bytes)) return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for the histogram failed");
+    CK(cudaMemsetAsync(ctx->hist.p, 0, hist_bytes, ctx->stream), "histogram clear");
+    CK(cudaMemsetAsync(ctx->stats.p, 0, 256, ctx->stream), "counter clear");
+    ctx->hist_len = P->hist_len;
+    p.hist = static_cast<unsigned long long *>(ctx->hist.p);
+    p.stats = static_cast<unsigned long long *>(ctx->stats.p);
+    p.status = reinterpret_cast<int32_t *>(static_cast<unsigned char *>(ctx->stats.p) + 128);
+    const size_t trace_bytes = (size_t)P->n_particles * 16 * sizeof(double);
+    p.trace = nullptr;
+    if (trace_out && trace_bytes) {
+        if (ctx->trace.grow(trace_bytes)) return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for traces failed");
+        p.trace = static_cast<double *>(ctx->trace.p);
+    }
+
+    // launch shape: whole histogram in shared memory when it fits, else global atomics
+    const size_t edge_smem = align_up((size_t)n_edges * sizeof(R), 16);
+    const size_t hist_smem = (size_t)P->hist_len * sizeof(uint32_t);
+    int smem_mode = (edge_smem + hist_smem + 1024 <= (size_t)ctx->max_smem_optin) ? 1 : 0;
+    int block = smem_mode ? 1024 : 256;
+    size_t smem = edge_smem + (smem_mode ? hist_smem : 0);
+    int bps = 0;
+    if (transport_set_smem(prec, smem_mode, smem) != 0) return fail(&ctx->err, RTMC_ERR_CUDA, "cudaFuncSetAttribute failed");
+    if (smem_mode) {
+        // the largest block that fits the register file, one block per SM
+        for (; block >= 128; block /= 2) {
+            bps = 0;
+            if (transport_occupancy(prec, 1, block, smem, &bps) == 0 && bps >= 1) break;
+        }
+        if (bps < 1) { smem_mode = 0; block = 256; smem = edge_smem; transport_set_smem(prec, 0, smem); }
+    }
+    p.hist_smem = smem_mode;
+    if (!smem_mode) {
+        if (transport_occupancy(prec, 0, block, smem, &bps) != 0 || bps < 1)
+            return fail(&ctx->err, RTMC_ERR_CUDA, "transport kernel does not fit on the device");
+    }
+    int64_t grid = (int64_t)ctx->num_sms * bps;
+    const int64_t need = (P->n_particles + block - 1) / block;
+    grid = std::max<int64_t>(1, std::min<int64_t>(grid, need));
+    if (smem_mode && P->n_particles / grid >= ((int64_t)1 << 32) - 1)
+        return fail(&ctx->err, RTMC_ERR_ARG, "too many particles per block for 32-bit shared-memory counts");
+    CK(cudaEventRecord(ctx->ev_k0, ctx->stream), "event");
+    int le = 0;
+    if (P->n_particles > 0) {
+        if constexpr (sizeof(R) == 4) le = launch_transport_f32(p, (int)grid, block, smem, ctx->stream);
+        else le = launch_transport_f64(p, (int)grid, block, smem, ctx->stream);
+    }
+    if (le) return cuda_fail(ctx, (cudaError_t)le, "transport launch");
+    CK(cudaEventRecord(ctx->ev_k1, ctx->stream), "event");
+    int64_t dstats[32];
+    CK(cudaMemcpyAsync(dstats, ctx->stats.p, 256, cudaMemcpyDeviceToHost, ctx->stream), "counters");
+    if (host_out) {
+        CK(cudaMemcpyAsync(host_out, ctx->hist.p, hist_bytes, cudaMemcpyDeviceToHost, ctx->stream), "histogram copy");
+        d2h += (double)hist_bytes;
+    }
+    if (p.trace) {
+        CK(cudaMemcpyAsync(trace_out, p.trace, trace_bytes, cudaMemcpyDeviceToHost, ctx->stream), "trace copy");
+        d2h += (double)trace_bytes;
+    }
+    CK(cudaEventRecord(ctx->ev_end, ctx->stream), "event");
+    CK(cudaStreamSynchronize(ctx->stream), "transport");
+    float kms = 0, tms = 0;
+    cudaEventElapsedTime(&kms, ctx->ev_k0, ctx->ev_k1);
+    cudaEventElapsedTime(&tms, ctx->ev_start, ctx->ev_end);
+    ctx->last_kernel_ms = kms;
+    ctx->last_launches = P->n_particles > 0 ? 1 : 0;
+    const int32_t status = (int32_t)(dstats[16] & 0xffffffff);
+    if (st) {
+        std::memset(st, 0, sizeof *st);
+        st->scatter_events = dstats[0];
+        st->boundary_hits = dstats[1];
+        st->kills = dstats[2];
+        st->absorbed = dstats[3];
+        st->observations = dstats[4];
+        st->conversions = dstats[5];
+        st->device_status = status;
+        st->kernel_ms = kms;
+        st->total_ms = tms;
+        st->h2d_bytes = h2d;
+        st->d2h_bytes = d2h + 256;
+    }
+    if (status) return fail(&ctx->err, RTMC_ERR_DEVICE, "a transport guard tripped (event cap or histogram index)");
+    return RTMC_OK;
+}
+
+int forward(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t *host_out, rtmc_stats *st,
+            double *trace_out = nullptr)
+{
+    if (!ctx || !P) return fail(ctx ? &ctx->err : nullptr, RTMC_ERR_ARG, "rtmc_forward: NULL argument");
+    int s = check_problem(ctx, P, t);
+    if (s) return s;
+    return P->precision == RTMC_FP64 ? run<double>(ctx, P, t, host_out, st, trace_out)
+                                     : run<float>(ctx, P, t, host_out, st, trace_out);
+}
+
+} // namespace
+
+extern "C" int32_t rtmc_abi_version(void) { return RTMC_ABI_VERSION; }
+
+extern "C" int rtmc_abi_sizes(int64_t out[4])
+{
+    if (!out) return fail(nullptr, RTMC_ERR_ARG, "rtmc_abi_sizes: NULL argument");
+    out[0] = (int64_t)sizeof(rtmc_material);
+    out[1] = (int64_t)sizeof(rtmc_tables_info);
+    out[2] = (int64_t)sizeof(rtmc_problem);
+    out[3] = (int64_t)sizeof(rtmc_stats);
+    return RTMC_OK;
+}
+
+extern "C" int rtmc_create(int32_t device, rtmc_context **out)
+{
+    if (!out) return fail(nullptr, RTMC_ERR_ARG, "rtmc_create: NULL argument");
+    *out = nullptr;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0) return fail(nullptr, RTMC_ERR_CUDA, "no CUDA device available");
+    if (device < 0 || device >= n) return fail(nullptr, RTMC_ERR_ARG, "device index out of range");
+    auto *ctx = new (std::nothrow) rtmc_context();
+    if (!ctx) return fail(nullptr, RTMC_ERR_ALLOC, "out of host memory");
+    ctx->device = device;
+    e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->max_smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_start);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_k0);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_k1);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_end);
+    if (e != cudaSuccess) {
+        rtmc_destroy(ctx);
+        return fail(nullptr, RTMC_ERR_CUDA, std::string("rtmc_create: ") + cudaGetErrorString(e));
+    }
+    *out = ctx;
+    return RTMC_OK;
+}
+
+extern "C" void rtmc_destroy(rtmc_context *ctx)
+{
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    ctx->hist.release();
+    ctx->tabs.release();
+    ctx->aux.release();
+    ctx->stats.release();
+    ctx->flush.release();
+    ctx->trace.release();
+    if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
+    if (ctx->ev_k0) cudaEventDestroy(ctx->ev_k0);
+    if (ctx->ev_k1) cudaEventDestroy(ctx->ev_k1);
+    if (ctx->ev_end) cudaEventDestroy(ctx->ev_end);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+extern "C" const char *rtmc_last_error(const rtmc_context *ctx)
+{
+    if (ctx) return ctx->err.c_str();
+    return g_thread_error.c_str();
+}
+
+extern "C" int rtmc_forward(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t *hist_out,
+                            rtmc_stats *st)
+{
+    if (!hist_out) return fail(ctx ? &ctx->err : nullptr, RTMC_ERR_ARG, "rtmc_forward: hist_out is NULL");
+    return forward(ctx, P, t, hist_out, st);
+}
+
+extern "C" int rtmc_forward_device(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, rtmc_stats *st)
+{
+    return forward(ctx, P, t, nullptr, st);
+}
+
+extern "C" int rtmc_forward_trace(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t *hist_out,
+                                  double *state_out, rtmc_stats *st)
+{
+    if (!hist_out || !state_out)
+        return fail(ctx ? &ctx->err : nullptr, RTMC_ERR_ARG, "rtmc_forward_trace: NULL output buffer");
+    return forward(ctx, P, t, hist_out, st, state_out);
+}
+
+extern "C" int rtmc_copy_histogram(rtmc_context *ctx, int64_t *hist_out, int64_t n)
+{
+    if (!ctx || !hist_out) return fail(ctx ? &ctx->err : nullptr, RTMC_ERR_ARG, "rtmc_copy_histogram: NULL argument");
+    if (n < 0 || n > ctx->hist_len) return fail(&ctx->err, RTMC_ERR_ARG, "rtmc_copy_histogram: n exceeds the histogram");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    CK(cudaMemcpyAsync(hist_out, ctx->hist.p, (size_t)n * 8, cudaMemcpyDeviceToHost, ctx->stream), "histogram copy");
+    CK(cudaStreamSynchronize(ctx->stream), "histogram copy");
+    return RTMC_OK;
+}
+
+extern "C" int rtmc_host_alloc(int64_t bytes, void **out)
+{
+    if (!out || bytes <= 0) return fail(nullptr, RTMC_ERR_ARG, "rtmc_host_alloc: bad argument");
+    cudaError_t e = cudaMallocHost(out, (size_t)bytes);
+    if (e != cudaSuccess) { *out = nullptr; return fail(nullptr, RTMC_ERR_ALLOC, "cudaMallocHost failed"); }
+    return RTMC_OK;
+}
+
+extern "C" int rtmc_host_free(void *p)
+{
+    if (p && cudaFreeHost(p) != cudaSuccess) return fail(nullptr, RTMC_ERR_CUDA, "cudaFreeHost failed");
+    return RTMC_OK;
+}
+
+extern "C" int rtmc_set_table_cache(rtmc_context *ctx, int32_t enable)
+{
+    if (!ctx) return fail(nullptr, RTMC_ERR_ARG, "rtmc_set_table_cache: NULL context");
+    ctx->cache_tables = enable ? 1 : 0;
+    return RTMC_OK;
+}
+
+extern "C" int rtmc_flush_l2(rtmc_context *ctx)
+{
+    if (!ctx) return fail(nullptr, RTMC_ERR_ARG, "rtmc_flush_l2: NULL context");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const size_t bytes = (size_t)512 << 20;
+    if (ctx->flush.grow(bytes)) return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for the L2 flush failed");
+    CK(cudaMemsetAsync(ctx->flush.p, 0x5a, bytes, ctx->stream), "L2 flush");
+    CK(cudaStreamSynchronize(ctx->stream), "L2 flush");
+    return RTMC_OK;
+}
+
+extern "C" int rtmc_last_timing(const rtmc_context *ctx, double *kernel_ms, int32_t *launches)
+{
+    if (!ctx) return fail(nullptr, RTMC_ERR_ARG, "rtmc_last_timing: NULL context");
+    if (kernel_ms) *kernel_ms = ctx->last_kernel_ms;
+    if (launches) *launches = ctx->last_launches;
+    return RTMC_OK;
+}

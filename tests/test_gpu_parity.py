@@ -1,0 +1,145 @@
+"""GPU transport vs the CPU oracle, through the C ABI (rtmc_forward_trace / rtmc_forward).
+
+Same Philox stream on both sides ("event" oracle): FP64 trajectories must match to
+1e-9 relative (both sides run the same event sequence; libm vs CUDA math differ in the
+last bits) and bins exactly away from edge ties; FP32 trajectories match the oracle fed
+the same 24-bit uniforms to 1e-3 relative for >= 99% of particles (the rest leave the
+shared path when a float rounding flips an integer sub-step count).  Independent streams
+("substep" oracle, the reference's own sub-step order): histograms agree within 3 sigma
+of the Monte Carlo error.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from radiativetransfermontecarlo_gb300 import MaterialClass, build_problem, colon, get_context, normalise
+from radiativetransfermontecarlo_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def _run_both(geo, src, mat, obs, opts, n, precision):
+    src = dict(src, numberParticles=n)
+    opts = dict(opts, precision=precision, exact_count=True)
+    prob, grid, N = build_problem(geo, src, mat, obs, opts)
+    P, keep = prob.to_ctypes()
+    hist, states, stats = get_context(0).forward_trace(P, prob.tables)
+    ref_hist, ref_stats, ref_states = O.run(prob, O.table_knots(prob.tables), scheme="event", want_state=True)
+    return prob, grid, N, hist, states, stats, ref_hist, ref_states, ref_stats
+
+
+def _l1_diff(a, b, chunk=1 << 24):
+    tot = 0
+    for s in range(0, a.size, chunk):
+        tot += int(np.abs(a[s:s + chunk] - b[s:s + chunk]).sum())
+    return tot
+
+
+def _path_match(states, ref_states, tol):
+    same = np.all(states[:, 9:16] == ref_states[:, 9:16], axis=1)
+    close = np.all(np.abs(states[:, :9] - ref_states[:, :9]) <= tol * (1 + np.abs(ref_states[:, :9])), axis=1)
+    return same & close
+
+
+CASES = {
+    "c1_acoustic3d": lambda: W.c1_acoustic3d(),
+    "c2_elastic3d": lambda: W.c2_elastic3d(),
+    "c3_halfspace2d": lambda: W.c3_halfspace2d(t_end=2.0),
+}
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_fp64_trajectories_and_bins_match_oracle(name):
+    geo, src, mat, obs, opts = CASES[name]()
+    n = 20000 if name != "c3_halfspace2d" else 4000
+    prob, grid, N, hist, states, stats, ref_hist, ref_states, ref_stats = _run_both(geo, src, mat, obs, opts, n, "fp64")
+    assert stats["device_status"] == 0
+    ok = _path_match(states, ref_states, 1e-9)
+    assert ok.mean() == 1.0, f"{(~ok).sum()} particles left the oracle's trajectory"
+    assert stats["scatter_events"] == ref_stats["scatter_events"]
+    assert stats["boundary_hits"] == ref_stats["boundary_hits"]
+    assert stats["kills"] == ref_stats["kills"]
+    # bins: identical except for observations sitting on a bin edge to rounding
+    diff = _l1_diff(hist, ref_hist) >> prob.hist_shift
+    assert diff <= max(4, 1e-6 * stats["observations"]), diff
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_fp32_trajectories_match_oracle_with_same_uniforms(name):
+    geo, src, mat, obs, opts = CASES[name]()
+    n = 20000 if name != "c3_halfspace2d" else 4000
+    prob, grid, N, hist, states, stats, ref_hist, ref_states, ref_stats = _run_both(geo, src, mat, obs, opts, n, "fp32")
+    assert stats["device_status"] == 0
+    ok = _path_match(states, ref_states, 1e-3)
+    assert ok.mean() >= 0.99, ok.mean()
+    rel = abs(stats["scatter_events"] - ref_stats["scatter_events"]) / max(1, ref_stats["scatter_events"])
+    assert rel < 0.01
+
+
+def test_energy_conserved_unbounded_q_inf():
+    geo, src, mat, obs, opts = W.c1_acoustic3d()
+    for precision in ("fp32", "fp64"):
+        prob, grid, N = build_problem(geo, dict(src, numberParticles=300_000), mat, obs,
+                                      dict(opts, precision=precision, exact_count=True))
+        P, keep = prob.to_ctypes()
+        hist, stats = get_context(0).forward(P, prob.tables)
+        dens, energy = normalise(hist, grid, N)
+        assert np.all(energy[1:, 0] == 1.0) and energy[0, 0] == 0.0
+
+
+def test_fp32_vs_substep_oracle_within_3_sigma():
+    """Independent random streams: GPU FP32 (event scheme) vs the reference-order sub-step oracle."""
+    geo, src, mat, obs, opts = W.c1_acoustic3d()
+    n = 200_000
+    prob, grid, N = build_problem(geo, dict(src, numberParticles=n), mat, obs,
+                                  dict(opts, precision="fp32", exact_count=True, seed=11))
+    P, keep = prob.to_ctypes()
+    g, _ = get_context(0).forward(P, prob.tables)
+    r, _, _ = O.run(prob, O.table_knots(prob.tables), scheme="substep")
+    g = g.reshape(grid.shape, order="F")[:, 0, :, 0].astype(float)
+    r = r.reshape(grid.shape, order="F")[:, 0, :, 0].astype(float)
+    mask = (g + r) > 50
+    z = (g - r)[mask] / np.sqrt(g + r)[mask]
+    assert np.mean(np.abs(z) < 3) > 0.99
+    assert abs(np.mean(z)) < 0.05
+    assert np.mean(z ** 2) < 1.2
+
+
+def test_energy_density_fp32_vs_fp64_rel_l2():
+    geo, src, mat, obs, opts = W.c1_acoustic3d()
+    out = {}
+    for precision in ("fp32", "fp64"):
+        prob, grid, N = build_problem(geo, dict(src, numberParticles=2_000_000), mat, obs,
+                                      dict(opts, precision=precision, exact_count=True))
+        P, keep = prob.to_ctypes()
+        hist, _ = get_context(0).forward(P, prob.tables)
+        out[precision] = normalise(hist, grid, N)[0]
+    a, b = out["fp32"], out["fp64"]
+    rel = np.linalg.norm(a - b) / np.linalg.norm(b)
+    assert rel < 0.005, rel
+
+
+def test_absorbing_boundary_and_2d_acoustic():
+    geo = {"dimension": 2, "frame": "cartesian", "bnd": [{"dir": 1, "val": 1.0, "type": "absorbing"},
+                                                           {"dir": 2, "val": -0.5}]}
+    mat = MaterialClass(geo, 4, True, 1, [0.2, 0.2], 0.3, "exp", 0.3)
+    src = {"lambda": 0.05, "position": [0, 0]}
+    obs = {"x": colon(-3, 0.1, 3), "y": colon(-3, 0.1, 3), "time": colon(0, 0.05, 3)}
+    for precision, tol, need in (("fp64", 1e-9, 1.0), ("fp32", 1e-3, 0.99)):
+        prob, grid, N, hist, states, stats, ref_hist, ref_states, ref_stats = _run_both(
+            geo, src, mat, obs, {"seed": 5}, 10000, precision)
+        assert stats["device_status"] == 0
+        assert ref_stats["absorbed"] > 100 and ref_stats["boundary_hits"] > ref_stats["absorbed"]
+        assert _path_match(states, ref_states, tol).mean() >= need
+
+
+def test_determinism_bit_identical():
+    geo, src, mat, obs, opts = W.c2_elastic3d()
+    prob, grid, N = build_problem(geo, dict(src, numberParticles=200_000), mat, obs, dict(opts, exact_count=True))
+    P, keep = prob.to_ctypes()
+    a, sa = get_context(0).forward(P, prob.tables)
+    b, sb = get_context(0).forward(P, prob.tables)
+    assert np.array_equal(a, b)
+    assert sa["observations"] == (a >> prob.hist_shift).sum()
