@@ -184,9 +184,11 @@ def run_our_arm(args, rank, world, dist):
     from radiativetransfermontecarlo_gb300 import workloads as W
     device = int(os.environ.get("LOCAL_RANK", 0))
     n = args.particles
-    geo, src, mat, obs, opts = W.c2_elastic3d(n=n, precision="fp32")
+    geo, src, mat, obs, opts = W.c2_elastic3d(n=n, precision="fp32", t_end=args.t_end)
     prob, grid, N = build_problem(geo, src, mat, obs, dict(opts, exact_count=True, pid0=rank * n))
     ctx = get_context(device)
+    if args.block or args.ring or args.index_mb:
+        ctx.set_launch(args.block, args.ring, args.index_mb)
     P32, keep32 = prob.to_ctypes()
 
     def barrier():
@@ -200,7 +202,7 @@ def run_our_arm(args, rank, world, dist):
     for _ in range(args.warmup):
         step(P32)
     # timed region: device time of each step from CUDA events on the library stream
-    dev_ms, kern_ms, events, obs_n = [], [], 0, 0
+    dev_ms, kern_ms, fold_ms, events, obs_n = [], [], [], 0, 0
     barrier()
     with ClockSampler(device) as clk:
         t_wall = time.perf_counter()
@@ -209,6 +211,8 @@ def run_our_arm(args, rank, world, dist):
             st = step(P32)
             dev_ms.append(st["total_ms"])
             kern_ms.append(st["kernel_ms"])
+            fold_ms.append(st["fold_ms"])
+            launches_per_step = ctx.last_timing()[1]
             events += st["scatter_events"]
             obs_n += st["observations"]
         t_wall = time.perf_counter() - t_wall
@@ -244,11 +248,12 @@ def run_our_arm(args, rank, world, dist):
                                "algorithmic_bytes_per_launch": alg_bytes,
                                "basis": f"{ALG_BYTES_PER_OBS} B (int64 read+write) per observation binned; "
                                         f"peak {peak_kind}"},
-                  "gpu_launches": args.steps, "clocks": clocks,
-                  "events_per_step": events / args.steps, "observations_per_step": obs_n / args.steps}
+                  "gpu_launches": args.steps * launches_per_step, "clocks": clocks,
+                  "events_per_step": events / args.steps, "observations_per_step": obs_n / args.steps,
+                  "transport_ms": kmean, "fold_ms": float(np.mean(fold_ms)), "sink": int(st["sink"])}
     # FP64 leg (same seed: the same trajectories up to rounding), then the accuracy check
     if rank == 0 and not args.no_fp64:
-        geo, src, mat, obs, opts = W.c2_elastic3d(n=n, precision="fp64")
+        geo, src, mat, obs, opts = W.c2_elastic3d(n=n, precision="fp64", t_end=args.t_end)
         prob64, _, _ = build_problem(geo, src, mat, obs, dict(opts, exact_count=True, pid0=0))
         prob64.tables = prob.tables
         P64, keep64 = prob64.to_ctypes()
@@ -299,6 +304,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--particles", type=int, default=10_000_000)
+    ap.add_argument("--t-end", type=float, default=5.0, help="last observation time (profiling cases only)")
+    ap.add_argument("--block", type=int, default=0, help="threads per block (0: automatic)")
+    ap.add_argument("--ring", type=int, default=0, help="segments per lane (0: automatic)")
+    ap.add_argument("--index-mb", type=int, default=0, help="index-array budget in MB (0: automatic, -1: global atomics)")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

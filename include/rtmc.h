@@ -158,8 +158,10 @@ typedef struct {
     int64_t observations;    /* counts added to the histogram */
     int64_t conversions;     /* P<->S changes at boundaries */
     int64_t device_status;   /* non-zero: a kernel guard tripped */
-    int64_t reserved;
-    double kernel_ms;        /* transport kernel, CUDA events on the context stream */
+    int32_t launches;        /* kernel launches of the call */
+    int32_t sink;            /* 0 shared-memory histogram, 1 global atomics, 2 index array + slice fold */
+    double kernel_ms;        /* transport kernel(s), CUDA events on the context stream */
+    double fold_ms;          /* slice-fold kernel(s) of the index path */
     double total_ms;         /* whole call, CUDA events (copies included) */
     double h2d_bytes;
     double d2h_bytes;
@@ -202,6 +204,12 @@ int rtmc_forward_trace(rtmc_context *ctx, const rtmc_problem *problem, const rtm
 /* pinned host memory for fast copies (cudaMallocHost); free with rtmc_host_free */
 int rtmc_host_alloc(int64_t bytes, void **out);
 int rtmc_host_free(void *p);
+
+/* Launch shape of the transport (0 = automatic for each field): threads per block,
+ * trajectory segments per lane in the shared-memory ring, and the device scratch budget
+ * in MB for the time-major observation-index array of large histograms (-1: no index
+ * array, observations go straight to the histogram with 64-bit global atomics). */
+int rtmc_set_launch(rtmc_context *ctx, int32_t block, int32_t ring_cap, int32_t index_mb);
 
 /* enable (1, default) or disable (0) reuse of the device copy of a tables handle across
  * calls; with 0 every call uploads its tables again (end-to-end timing) */

@@ -53,7 +53,8 @@ class RtmcProblem(C.Structure):
 class RtmcStats(C.Structure):
     _fields_ = [("scatter_events", C.c_int64), ("boundary_hits", C.c_int64), ("kills", C.c_int64),
                 ("absorbed", C.c_int64), ("observations", C.c_int64), ("conversions", C.c_int64),
-                ("device_status", C.c_int64), ("reserved", C.c_int64), ("kernel_ms", C.c_double),
+                ("device_status", C.c_int64), ("launches", C.c_int32), ("sink", C.c_int32),
+                ("kernel_ms", C.c_double), ("fold_ms", C.c_double),
                 ("total_ms", C.c_double), ("h2d_bytes", C.c_double), ("d2h_bytes", C.c_double)]
 
     def as_dict(self):
@@ -86,6 +87,7 @@ SIGNATURES = {
     "rtmc_host_free": (C.c_int, [_P]),
     "rtmc_flush_l2": (C.c_int, [_P]),
     "rtmc_set_table_cache": (C.c_int, [_P, C.c_int32]),
+    "rtmc_set_launch": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32]),
     "rtmc_last_timing": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
 }
 
@@ -239,6 +241,15 @@ class Context:
         check(self.lib.rtmc_copy_histogram(self.handle, out.ctypes.data_as(C.POINTER(C.c_int64)), out.size),
               self.handle)
         return out
+
+    def set_launch(self, block: int = 0, ring_cap: int = 0, index_mb: int = 0):
+        check(self.lib.rtmc_set_launch(self.handle, block, ring_cap, index_mb), self.handle)
+
+    def last_timing(self):
+        ms = C.c_double()
+        n = C.c_int32()
+        check(self.lib.rtmc_last_timing(self.handle, C.byref(ms), C.byref(n)), self.handle)
+        return ms.value, n.value
 
     def set_table_cache(self, enable: bool):
         check(self.lib.rtmc_set_table_cache(self.handle, 1 if enable else 0), self.handle)

@@ -43,9 +43,9 @@ struct rtmc_context {
     int num_sms = 0;
     int max_smem_optin = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev_start = nullptr, ev_k0 = nullptr, ev_k1 = nullptr, ev_end = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_k0 = nullptr, ev_k1 = nullptr, ev_k2 = nullptr, ev_end = nullptr;
     std::string err;
-    DevBuf hist, tabs, aux, stats, flush, trace;
+    DevBuf hist, tabs, aux, stats, flush, trace, idx;
     uint64_t tabs_gen = 0;
     int tabs_prec = -1;
     DevTables<float> tf{};
@@ -54,6 +54,7 @@ struct rtmc_context {
     double last_kernel_ms = 0;
     int last_launches = 0;
     int cache_tables = 1;
+    int opt_block = 0, opt_ring = 0, opt_index_mb = 0;
 };
 
 namespace {
@@ -91,9 +92,11 @@ template <typename R> int upload_tables(rtmc_context *ctx, const rtmc_tables *t,
         std::memcpy(host.data() + off[i][0], c.data(), n * sizeof(double));
         R *rt = reinterpret_cast<R *>(host.data() + off[i][1]);
         R *rs = reinterpret_cast<R *>(host.data() + off[i][2]);
+        // angles are staged as theta / pi, the argument of sincospi in the kernel
+        const double ip = 1.0 / M_PI;
         for (size_t k = 0; k < n; ++k) {
-            rt[k] = (R)th[k];
-            rs[k] = (k + 1 < n) ? (R)((th[k + 1] - th[k]) / (c[k + 1] - c[k])) : (R)0;
+            rt[k] = (R)(th[k] * ip);
+            rs[k] = (k + 1 < n) ? (R)((th[k + 1] - th[k]) * ip / (c[k + 1] - c[k])) : (R)0;
         }
         int32_t *g = reinterpret_cast<int32_t *>(host.data() + off[i][3]);
         size_t k = 0;
@@ -169,6 +172,10 @@ int check_problem(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t
     if (tot_edges > kMaxEdges) return fail(e, RTMC_ERR_ARG, "too many bin edges (4096 at most over all axes)");
     if (P->time_stride < 0 || P->mode_stride < 0 || maxidx >= P->hist_len)
         return fail(e, RTMC_ERR_ARG, "histogram strides exceed hist_len");
+    int64_t in_slice = 0;
+    for (int a = 0; a < 4; ++a)
+        if (P->axis_mode[a] == RTMC_AXIS_BINNED) in_slice += (int64_t)(P->axis_nedges[a] - 2) * P->axis_stride[a];
+    if (in_slice >= ((int64_t)1 << 31) - 1) return fail(e, RTMC_ERR_ARG, "one time slice must hold fewer than 2^31 bins");
     return RTMC_OK;
 }
 
@@ -203,8 +210,10 @@ void fill_params(rtmc_context *ctx, const rtmc_problem *P, const DevTables<R> &t
     }
     p->cos_half_pi = (R)std::cos(M_PI / 2);
     edges->clear();
+    bool finite_uniform[4] = {true, true, true, true};
     for (int a = 0; a < 4; ++a) {
         p->ax_mode[a] = P->axis_mode[a];
+        p->ax_nbe[a] = 1;
         if (P->axis_mode[a] == RTMC_AXIS_IGNORED) continue;
         const int ne = P->axis_nedges[a];
         const double *E = P->axis_edges[a];
@@ -214,12 +223,29 @@ void fill_params(rtmc_context *ctx, const rtmc_problem *P, const DevTables<R> &t
         p->ax_lo[a] = (R)E[0];
         p->ax_hi[a] = (R)E[ne - 1];
         p->ax_stride[a] = P->axis_stride[a];
+        p->ax_stride32[a] = (int32_t)P->axis_stride[a];
         const double w = (E[ne - 1] - E[0]) / (ne - 1);
         bool uni = true;
         for (int k = 1; k < ne; ++k)
             if (std::fabs((E[k] - E[k - 1]) - w) > 1e-6 * std::fabs(w)) uni = false;
         p->ax_uniform[a] = uni ? 1 : 0;
         p->ax_inv_w[a] = (R)(1.0 / w);
+        if (P->axis_mode[a] == RTMC_AXIS_BINNED) p->ax_nbe[a] = ne - 1;
+        else p->ax_stride32[a] = 0;
+        finite_uniform[a] = uni && std::isfinite(E[0]) && std::isfinite(E[ne - 1]);
+    }
+    // observation path (see obs_offset in transport.cu)
+    p->obs_kind = 0;
+    if (P->frame == RTMC_FRAME_CARTESIAN) {
+        bool ok = true;
+        for (int a = 0; a < 3; ++a) ok = ok && (P->axis_mode[a] == RTMC_AXIS_IGNORED || finite_uniform[a]);
+        if (ok) p->obs_kind = 1;
+    } else if (P->axis_mode[1] == RTMC_AXIS_IGNORED && P->axis_mode[2] == RTMC_AXIS_IGNORED &&
+               P->axis_mode[0] != RTMC_AXIS_IGNORED && finite_uniform[0]) {
+        p->obs_kind = 2;
+        p->radial_3d = (P->frame == RTMC_FRAME_SPHERICAL && P->d == 3) ? 1 : 0;
+        p->ax_a0 = (R)(-P->axis_edges[0][0] * (double)(P->axis_nedges[0] - 1) /
+                       (P->axis_edges[0][P->axis_nedges[0] - 1] - P->axis_edges[0][0]));
     }
     p->time_stride = P->time_stride; p->mode_stride = P->mode_stride; p->hist_len = P->hist_len;
     *n_edges_out = (int)edges->size();
@@ -286,40 +312,108 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         p.trace = static_cast<double *>(ctx->trace.p);
     }
 
-    // launch shape: whole histogram in shared memory when it fits, else global atomics
+    // Sink: the whole histogram in shared memory when it fits beside a segment ring of at
+    // least 2 slots per lane at 512 threads; otherwise a dense index array folded slice
+    // by slice (rt_bin_slices), or plain global 64-bit atomics when the index array is
+    // switched off or does not fit.
     const size_t edge_smem = align_up((size_t)n_edges * sizeof(R), 16);
-    const size_t hist_smem = (size_t)P->hist_len * sizeof(uint32_t);
-    int smem_mode = (edge_smem + hist_smem + 1024 <= (size_t)ctx->max_smem_optin) ? 1 : 0;
-    int block = smem_mode ? 1024 : 256;
-    size_t smem = edge_smem + (smem_mode ? hist_smem : 0);
-    int bps = 0;
-    if (transport_set_smem(prec, smem_mode, smem) != 0) return fail(&ctx->err, RTMC_ERR_CUDA, "cudaFuncSetAttribute failed");
-    if (smem_mode) {
-        // the largest block that fits the register file, one block per SM
-        for (; block >= 128; block /= 2) {
-            bps = 0;
-            if (transport_occupancy(prec, 1, block, smem, &bps) == 0 && bps >= 1) break;
+    const size_t hist_smem = align_up((size_t)P->hist_len * sizeof(uint32_t), 16);
+    const size_t seg_bytes = 6 * sizeof(R) + 2 * sizeof(int32_t);
+    const size_t budget = (size_t)ctx->max_smem_optin - 1024;
+    const int nm = P->acoustics ? 1 : 2;
+    int sink = kSinkGlobal, block = ctx->opt_block ? ctx->opt_block : 256;
+    int cap = ctx->opt_ring ? ctx->opt_ring : (sizeof(R) == 4 ? 8 : 6);
+    {
+        const int sb = ctx->opt_block ? ctx->opt_block : 512;
+        if (edge_smem + hist_smem + (size_t)sb * 2 * seg_bytes <= budget) {
+            sink = kSinkSmem;
+            block = sb;
+            const int fit = (int)((budget - edge_smem - hist_smem) / ((size_t)sb * seg_bytes));
+            cap = std::min(ctx->opt_ring ? ctx->opt_ring : 8, fit);
         }
-        if (bps < 1) { smem_mode = 0; block = 256; smem = edge_smem; transport_set_smem(prec, 0, smem); }
     }
-    p.hist_smem = smem_mode;
-    if (!smem_mode) {
-        if (transport_occupancy(prec, 0, block, smem, &bps) != 0 || bps < 1)
-            return fail(&ctx->err, RTMC_ERR_CUDA, "transport kernel does not fit on the device");
+    int64_t chunk = P->n_particles; // particles per transport launch
+    if (sink != kSinkSmem && ctx->opt_index_mb >= 0 && P->time_stride < ((int64_t)1 << 30)) {
+        const int64_t mb = ctx->opt_index_mb ? ctx->opt_index_mb : 12288; // default index budget: 12 GB
+        const int64_t rows = std::max<int64_t>(32, ((mb << 20) / (4 * (int64_t)P->n_obs)) / 32 * 32);
+        chunk = std::min<int64_t>(P->n_particles, rows);
+        if (chunk > 0 && ctx->idx.grow((size_t)chunk * P->n_obs * sizeof(int32_t)) == 0) sink = kSinkIndex;
+        else chunk = P->n_particles;
     }
+    size_t smem = edge_smem + (sink == kSinkSmem ? hist_smem : 0) + (size_t)block * cap * seg_bytes;
+    int bps = 0;
+    if (transport_set_smem(prec, sink, p.obs_kind, smem) != 0) return fail(&ctx->err, RTMC_ERR_CUDA, "cudaFuncSetAttribute failed");
+    if (transport_occupancy(prec, sink, p.obs_kind, block, smem, &bps) != 0 || bps < 1)
+        return fail(&ctx->err, RTMC_ERR_CUDA, "transport kernel does not fit on the device");
+    p.sink = sink;
+    p.ring_cap = cap;
     int64_t grid = (int64_t)ctx->num_sms * bps;
-    const int64_t need = (P->n_particles + block - 1) / block;
+    const int64_t need = (std::max<int64_t>(chunk, 1) + block - 1) / block;
     grid = std::max<int64_t>(1, std::min<int64_t>(grid, need));
-    if (smem_mode && P->n_particles / grid >= ((int64_t)1 << 32) - 1)
+    if (sink == kSinkSmem && P->n_particles / grid >= ((int64_t)1 << 32) - 1)
         return fail(&ctx->err, RTMC_ERR_ARG, "too many particles per block for 32-bit shared-memory counts");
-    CK(cudaEventRecord(ctx->ev_k0, ctx->stream), "event");
-    int le = 0;
-    if (P->n_particles > 0) {
-        if constexpr (sizeof(R) == 4) le = launch_transport_f32(p, (int)grid, block, smem, ctx->stream);
-        else le = launch_transport_f64(p, (int)grid, block, smem, ctx->stream);
+    // slice fold: privatise groups of slices in shared memory when 8 or more fit
+    BinParams bp{};
+    size_t fold_smem = 0;
+    int fold_grid = 1;
+    if (sink == kSinkIndex) {
+        bp.idx = static_cast<const int32_t *>(ctx->idx.p);
+        bp.rows = chunk;
+        bp.n_obs = P->n_obs;
+        bp.n_modes = nm;
+        bp.slice_bins = (int32_t)P->time_stride;
+        bp.time_stride = P->time_stride;
+        bp.mode_stride = P->mode_stride;
+        bp.hist_shift = P->hist_shift;
+        bp.hist = static_cast<unsigned long long *>(ctx->hist.p);
+        const size_t slice_bytes = (size_t)P->time_stride * nm * sizeof(uint32_t);
+        const int group = (int)std::min<size_t>((size_t)P->n_obs, (size_t)(200 << 10) / std::max<size_t>(slice_bytes, 1));
+        if (group >= 8) {
+            bp.group = group;
+            fold_smem = (size_t)group * slice_bytes;
+            if (bin_slices_set_smem(fold_smem) != 0) return fail(&ctx->err, RTMC_ERR_CUDA, "cudaFuncSetAttribute failed");
+            const int ngroups = (P->n_obs + group - 1) / group;
+            // enough particle ranges to fill the GPU twice over
+            const int64_t ranges = std::max<int64_t>(1, (2 * ctx->num_sms + ngroups - 1) / ngroups);
+            bp.part_per_block = (chunk + ranges - 1) / ranges;
+            fold_grid = (int)ranges;
+        } else {
+            bp.group = 0;
+            fold_grid = (int)std::max<int64_t>(1, std::min<int64_t>((chunk + 255) / 256, 2 * ctx->num_sms));
+        }
+        p.obs_idx = static_cast<int32_t *>(ctx->idx.p);
+        p.obs_rows = chunk;
+    }
+    int le = 0, launches = 0;
+    double kms = 0, fms = 0;
+    for (int64_t base = 0; base < P->n_particles && !le; base += chunk) {
+        DevParams<R> q = p;
+        q.pid0 = P->pid0 + base;
+        q.n_particles = std::min<int64_t>(chunk, P->n_particles - base);
+        if (p.trace) q.trace = p.trace + 16 * base;
+        CK(cudaEventRecord(ctx->ev_k0, ctx->stream), "event");
+        if constexpr (sizeof(R) == 4) le = launch_transport_f32(q, (int)grid, block, smem, ctx->stream);
+        else le = launch_transport_f64(q, (int)grid, block, smem, ctx->stream);
+        CK(cudaEventRecord(ctx->ev_k1, ctx->stream), "event");
+        ++launches;
+        if (!le && sink == kSinkIndex) {
+            BinParams b = bp;
+            b.n = q.n_particles;
+            if (b.group) b.part_per_block = (b.n + fold_grid - 1) / fold_grid;
+            le = launch_bin_slices(b, fold_grid, fold_smem, ctx->stream);
+            CK(cudaEventRecord(ctx->ev_k2, ctx->stream), "event");
+            ++launches;
+        }
+        CK(cudaEventSynchronize(sink == kSinkIndex ? ctx->ev_k2 : ctx->ev_k1), "transport");
+        float a = 0, b = 0;
+        cudaEventElapsedTime(&a, ctx->ev_k0, ctx->ev_k1);
+        kms += a;
+        if (sink == kSinkIndex) {
+            cudaEventElapsedTime(&b, ctx->ev_k1, ctx->ev_k2);
+            fms += b;
+        }
     }
     if (le) return cuda_fail(ctx, (cudaError_t)le, "transport launch");
-    CK(cudaEventRecord(ctx->ev_k1, ctx->stream), "event");
     int64_t dstats[32];
     CK(cudaMemcpyAsync(dstats, ctx->stats.p, 256, cudaMemcpyDeviceToHost, ctx->stream), "counters");
     if (host_out) {
@@ -332,11 +426,10 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
     }
     CK(cudaEventRecord(ctx->ev_end, ctx->stream), "event");
     CK(cudaStreamSynchronize(ctx->stream), "transport");
-    float kms = 0, tms = 0;
-    cudaEventElapsedTime(&kms, ctx->ev_k0, ctx->ev_k1);
+    float tms = 0;
     cudaEventElapsedTime(&tms, ctx->ev_start, ctx->ev_end);
-    ctx->last_kernel_ms = kms;
-    ctx->last_launches = P->n_particles > 0 ? 1 : 0;
+    ctx->last_kernel_ms = kms + fms;
+    ctx->last_launches = launches;
     const int32_t status = (int32_t)(dstats[16] & 0xffffffff);
     if (st) {
         std::memset(st, 0, sizeof *st);
@@ -348,6 +441,9 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         st->conversions = dstats[5];
         st->device_status = status;
         st->kernel_ms = kms;
+        st->fold_ms = fms;
+        st->launches = launches;
+        st->sink = sink;
         st->total_ms = tms;
         st->h2d_bytes = h2d;
         st->d2h_bytes = d2h + 256;
@@ -398,6 +494,7 @@ extern "C" int rtmc_create(int32_t device, rtmc_context **out)
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_start);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_k0);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_k1);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_k2);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_end);
     if (e != cudaSuccess) {
         rtmc_destroy(ctx);
@@ -418,9 +515,11 @@ extern "C" void rtmc_destroy(rtmc_context *ctx)
     ctx->stats.release();
     ctx->flush.release();
     ctx->trace.release();
+    ctx->idx.release();
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
     if (ctx->ev_k0) cudaEventDestroy(ctx->ev_k0);
     if (ctx->ev_k1) cudaEventDestroy(ctx->ev_k1);
+    if (ctx->ev_k2) cudaEventDestroy(ctx->ev_k2);
     if (ctx->ev_end) cudaEventDestroy(ctx->ev_end);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -473,6 +572,18 @@ extern "C" int rtmc_host_alloc(int64_t bytes, void **out)
 extern "C" int rtmc_host_free(void *p)
 {
     if (p && cudaFreeHost(p) != cudaSuccess) return fail(nullptr, RTMC_ERR_CUDA, "cudaFreeHost failed");
+    return RTMC_OK;
+}
+
+extern "C" int rtmc_set_launch(rtmc_context *ctx, int32_t block, int32_t ring_cap, int32_t index_mb)
+{
+    if (!ctx) return fail(nullptr, RTMC_ERR_ARG, "rtmc_set_launch: NULL context");
+    if (block < 0 || block > 1024 || block % 32) return fail(&ctx->err, RTMC_ERR_ARG, "block must be 0 or a multiple of 32 up to 1024");
+    if (ring_cap < 0 || ring_cap == 1 || ring_cap > 64) return fail(&ctx->err, RTMC_ERR_ARG, "ring_cap must be 0 or in [2, 64]");
+    if (index_mb < -1) return fail(&ctx->err, RTMC_ERR_ARG, "index_mb must be -1, 0 or a size in MB");
+    ctx->opt_block = block;
+    ctx->opt_ring = ring_cap;
+    ctx->opt_index_mb = index_mb;
     return RTMC_OK;
 }
 

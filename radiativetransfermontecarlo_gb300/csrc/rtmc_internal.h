@@ -36,8 +36,8 @@ constexpr int kGuideN = 1 << kGuideBits;
 // Device-side view of one precision's tables; R = float or double.
 template <typename R> struct DevTables {
     const double *cdf[4];   // knots of u, FP64 in both precisions (search + interpolation offset)
-    const R *theta[4];      // knot angles
-    const R *slope[4];      // (theta[i+1]-theta[i]) / (cdf[i+1]-cdf[i]), built in FP64
+    const R *theta[4];      // knot angles divided by pi
+    const R *slope[4];      // (theta[i+1]-theta[i]) / (pi (cdf[i+1]-cdf[i])), built in FP64
     const int32_t *guide[4];
     int32_t n[4];
 };
@@ -45,7 +45,12 @@ template <typename R> struct DevTables {
 template <typename R> struct DevParams {
     int32_t d, frame, acoustics, src_dir;
     int32_t polarization, n_sub, n_obs, n_bnd;
-    int32_t hist_shift, hist_smem, s_end, max_events;
+    int32_t hist_shift, sink, s_end, max_events;
+    int32_t ring_cap;  // trajectory segments per lane in the shared-memory ring
+    int32_t obs_kind;  // 0 general, 1 cartesian linear, 2 radius only
+    int32_t radial_3d; // radius-only path: 1 = |x|, 0 = |(x, y)|
+    int32_t ax_nbe[4]; // bins of a binned axis, 1 for a range-checked or ignored axis
+    R ax_a0;           // -lo / width of axis 0 (radius-only path)
     int64_t n_particles, pid0;
     uint32_t key0, key1;
     R src_pos[3];
@@ -61,6 +66,7 @@ template <typename R> struct DevParams {
     int32_t ax_mode[4], ax_n[4], ax_off[4], ax_uniform[4];
     R ax_lo[4], ax_hi[4], ax_inv_w[4];
     int64_t ax_stride[4];
+    int32_t ax_stride32[4];  // in-slice strides (a time slice holds < 2^31 bins)
     int64_t time_stride, mode_stride, hist_len;
     int32_t n_edges;
     int32_t bnd_dir[RTMC_MAX_BND], bnd_absorb[RTMC_MAX_BND];
@@ -72,12 +78,28 @@ template <typename R> struct DevParams {
     unsigned long long *stats;  // [8]
     int32_t *status;
     double *trace;  // optional [n_particles][16] final particle states
+    int32_t *obs_idx;  // index sink: [n_obs][obs_rows] in-slice bin | mode << 30, or -1
+    int64_t obs_rows;
+};
+
+// Parameters of the slice fold (rt_bin_slices*).
+struct BinParams {
+    const int32_t *idx;
+    int64_t rows;          // row length of the index array
+    int64_t n;             // particles in this chunk
+    int32_t n_obs, n_modes, slice_bins, group;
+    int64_t time_stride, mode_stride, part_per_block;
+    int32_t hist_shift;
+    unsigned long long *hist;
 };
 
 // Launch wrappers (transport.cu).  Return a cudaError_t value.
 int launch_transport_f32(const DevParams<float> &p, int grid, int block, size_t smem, void *stream);
 int launch_transport_f64(const DevParams<double> &p, int grid, int block, size_t smem, void *stream);
-int transport_occupancy(int precision, int smem_hist, int block, size_t smem, int *blocks_per_sm);
-int transport_set_smem(int precision, int smem_hist, size_t smem);
+int transport_occupancy(int precision, int sink, int obs, int block, size_t smem, int *blocks_per_sm);
+int transport_set_smem(int precision, int sink, int obs, size_t smem);
+int launch_bin_slices(const BinParams &b, int grid_x, size_t smem, void *stream);
+int bin_slices_set_smem(size_t smem);
+enum { kSinkSmem = 0, kSinkGlobal = 1, kSinkIndex = 2 };
 
 } // namespace rtmc

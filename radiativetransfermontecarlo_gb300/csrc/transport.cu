@@ -48,10 +48,6 @@ __device__ __forceinline__ float m_atan2(float y, float x) { return atan2f(y, x)
 __device__ __forceinline__ double m_atan2(double y, double x) { return atan2(y, x); }
 __device__ __forceinline__ float m_hypot(float x, float y) { return hypotf(x, y); }
 __device__ __forceinline__ double m_hypot(double x, double y) { return hypot(x, y); }
-__device__ __forceinline__ float m_sin(float x) { return sinf(x); }
-__device__ __forceinline__ double m_sin(double x) { return sin(x); }
-__device__ __forceinline__ void m_sincos(float x, float *s, float *c) { sincosf(x, s, c); }
-__device__ __forceinline__ void m_sincos(double x, double *s, double *c) { sincos(x, s, c); }
 __device__ __forceinline__ void m_sincospi(float x, float *s, float *c) { sincospif(x, s, c); }
 __device__ __forceinline__ void m_sincospi(double x, double *s, double *c) { sincospi(x, s, c); }
 __device__ __forceinline__ float m_cospi(float x) { return cospif(x); }
@@ -119,7 +115,8 @@ template <typename R> __device__ __forceinline__ R invcdf(const DevTables<R> &t,
 }
 
 // ----------------------------------------------------------------------------------
-// particle state
+// particle state (registers only: every component access below uses a static index or a
+// select, so nothing is spilled to local memory)
 // ----------------------------------------------------------------------------------
 template <typename R> struct Part {
     R x[3], d[3], q[3];
@@ -128,6 +125,23 @@ template <typename R> struct Part {
     int s_death;
     uint32_t k;
 };
+
+template <typename R> __device__ __forceinline__ R sel3(const R a[3], int k)
+{
+    return k == 0 ? a[0] : (k == 1 ? a[1] : a[2]);
+}
+
+template <typename R> __device__ __forceinline__ void put3(R a[3], int k, R v)
+{
+    a[0] = k == 0 ? v : a[0];
+    a[1] = k == 1 ? v : a[1];
+    a[2] = k == 2 ? v : a[2];
+}
+
+template <typename T> __device__ __forceinline__ T by_mode(const T v[2], int m) { return m ? v[1] : v[0]; }
+
+__device__ __forceinline__ float m_rnorm(float x) { return rsqrtf(x); }
+__device__ __forceinline__ double m_rnorm(double x) { return 1.0 / sqrt(x); }
 
 template <typename R> __device__ __forceinline__ void cross3(const R a[3], const R b[3], R o[3])
 {
@@ -143,7 +157,7 @@ template <typename R> __device__ __forceinline__ R dot3(const R a[3], const R b[
 
 template <typename R> __device__ __forceinline__ void normalize3(R a[3])
 {
-    const R s = (R)1 / m_sqrt(dot3(a, a));
+    const R s = m_rnorm(dot3(a, a));
     a[0] *= s; a[1] *= s; a[2] *= s;
 }
 
@@ -152,11 +166,13 @@ template <typename R> __device__ __forceinline__ void next_boundary(const DevPar
 {
     const int cap = p.s_end + 1;
     s.sB = cap;
-    const R step = p.step[s.mode];
-    for (int b = 0; b < p.n_bnd; ++b) {
+    const R step = by_mode(p.step, s.mode);
+#pragma unroll
+    for (int b = 0; b < RTMC_MAX_BND; ++b) {
+        if (b >= p.n_bnd) break;
         const int k = p.bnd_dir[b] - 1;
-        const R a = s.x[k] - p.bnd_val[b];
-        const R bs = step * s.d[k];
+        const R a = sel3(s.x, k) - p.bnd_val[b];
+        const R bs = step * sel3(s.d, k);
         if (a == (R)0 || bs == (R)0 || ((a > (R)0) == (bs > (R)0))) continue;
         const R j = m_floor(m_abs(a) / m_abs(bs)) + (R)1;
         if (j < (R)(cap - s.s0)) {
@@ -171,7 +187,6 @@ template <typename R> __device__ void init_particle(const DevParams<R> &p, uint6
 {
     const U4<R> a = draw(p, pid, 0u, 0u);  // r1, r2, phi0, theta0
     const U4<R> b = draw(p, pid, 0u, 1u);  // phi, theta, alpha, first scattering
-    const U4<R> c = draw(p, pid, 0u, 2u);  // Q-kill
     const R r = m_abs(m_sqrt((R)-2 * m_log(a.a)) * m_cospi((R)2 * a.b)) * p.src_lambda;
     R cphi0, sphi0, cphi, sphi;
     if (p.d == 2) {
@@ -205,8 +220,12 @@ template <typename R> __device__ void init_particle(const DevParams<R> &p, uint6
     s.s0 = 0;
     s.s_death = -1;
     const int cap = p.s_end + 1;
-    s.sS = geom_steps(b.d, p.inv_lam[s.mode], p.scat_on[s.mode], cap);
-    s.sK = geom_steps(c.a, p.inv_q[s.mode], p.kill_on[s.mode], cap);
+    s.sS = geom_steps(b.d, by_mode(p.inv_lam, s.mode), by_mode(p.scat_on, s.mode), cap);
+    s.sK = cap;
+    if (by_mode(p.kill_on, s.mode)) {
+        const U4<R> c = draw(p, pid, 0u, 2u);  // Q-kill
+        s.sK = geom_steps(c.a, by_mode(p.inv_q, s.mode), 1, cap);
+    }
     next_boundary(p, s);
 }
 
@@ -228,27 +247,26 @@ template <typename R>
 __device__ int elastic_reflect(const DevParams<R> &p, Part<R> &s, int k, R u_split, R u_coin)
 {
     const R eps = (R)2.220446049250313e-16;
-    R n[3] = {(R)0, (R)0, (R)0};
-    n[k] = (R)1;
+    const R n[3] = {k == 0 ? (R)1 : (R)0, k == 1 ? (R)1 : (R)0, k == 2 ? (R)1 : (R)0};
     const int m0 = s.mode;
-    R adn = m_abs(s.d[k]);
+    const R dk = sel3(s.d, k);
+    R adn = m_abs(dk);
     adn = adn > (R)1 ? (R)1 : adn;
     const R ang = m_acos(adn) * (R)57.295779513082320876798154814105;
     if (s.mode == 0) {
         const R rpp = zoe_lookup(p.zoe, ang);
         if (u_coin <= rpp) {
-            s.d[k] = -s.d[k];
-            s.q[k] = -s.q[k];
+            put3(s.d, k, -dk);
+            put3(s.q, k, -sel3(s.q, k));
         } else { // P -> SV, propagateParticleSmallDt.m:212-248
             s.mode = 1;
             const R ratio = p.vs_over_vp;
-            const R dn = s.d[k];
             R nd[3] = {s.d[0] * ratio, s.d[1] * ratio, s.d[2] * ratio};
-            nd[k] = (R)0;
+            put3(nd, k, (R)0);
             const R sin2 = dot3(nd, nd);
             const R cv = m_sqrt(m_max((R)0, (R)1 - sin2));
-            const R sg = (R)((dn > (R)0) - (dn < (R)0));
-            nd[k] = -sg * cv;
+            const R sg = (R)((dk > (R)0) - (dk < (R)0));
+            put3(nd, k, -sg * cv);
             normalize3(nd);
             s.d[0] = nd[0]; s.d[1] = nd[1]; s.d[2] = nd[2];
             R ax[3];
@@ -261,11 +279,9 @@ __device__ int elastic_reflect(const DevParams<R> &p, Part<R> &s, int k, R u_spl
         cross3(s.d, n, eSH);
         R nsh = m_sqrt(dot3(eSH, eSH));
         if (nsh < eps) {
-            R t[3] = {(R)1, (R)0, (R)0};
-            const R tn = t[k];
-            t[k] -= tn;
-            eSH[0] = t[0]; eSH[1] = t[1]; eSH[2] = t[2];
-            nsh = m_sqrt(dot3(t, t));
+            // arbitrary tangent [1 0 0] projected on the plane (MaterialClass.m:1618-1625)
+            eSH[0] = k == 0 ? (R)0 : (R)1; eSH[1] = (R)0; eSH[2] = (R)0;
+            nsh = m_sqrt(dot3(eSH, eSH));
         }
         const R inv = (R)1 / nsh;
         eSH[0] *= inv; eSH[1] *= inv; eSH[2] *= inv;
@@ -276,27 +292,26 @@ __device__ int elastic_reflect(const DevParams<R> &p, Part<R> &s, int k, R u_spl
         const R Esv = aSV * aSV, Esh = aSH * aSH;
         const R probSV = Esv / (Esv + Esh + eps);
         if (!(u_split < probSV)) { // SH -> SH
-            s.d[k] = -s.d[k];
-            s.q[k] = -s.q[k];
+            put3(s.d, k, -dk);
+            put3(s.q, k, -sel3(s.q, k));
         } else {
             const R rsv = zoe_lookup(p.zoe + RTMC_ZOE_N, ang);
             if (u_coin <= rsv) { // SV -> SV
-                s.d[k] = -s.d[k];
-                s.q[k] = -s.q[k];
+                put3(s.d, k, -dk);
+                put3(s.q, k, -sel3(s.q, k));
             } else { // SV -> P, :274-321
                 const R ratio = p.vp_over_vs;
-                const R dn = s.d[k];
                 R nd[3] = {s.d[0] * ratio, s.d[1] * ratio, s.d[2] * ratio};
-                nd[k] = (R)0;
+                put3(nd, k, (R)0);
                 const R sin2 = dot3(nd, nd);
                 if (sin2 <= (R)1) {
                     s.mode = 0;
-                    const R sg = (R)((dn > (R)0) - (dn < (R)0));
-                    nd[k] = -sg * m_sqrt((R)1 - sin2);
+                    const R sg = (R)((dk > (R)0) - (dk < (R)0));
+                    put3(nd, k, -sg * m_sqrt((R)1 - sin2));
                     normalize3(nd);
                     s.d[0] = nd[0]; s.d[1] = nd[1]; s.d[2] = nd[2];
                 } else {
-                    s.d[k] = -s.d[k]; // total internal reflection: SV, dir mirrored only
+                    put3(s.d, k, -dk); // total internal reflection: SV, dir mirrored only
                 }
             }
         }
@@ -324,9 +339,9 @@ __device__ __forceinline__ void scatter(const DevParams<R> &p, Part<R> &s, R u_p
         else if (m == 1 && u_mode > p.s2s) m2 = 0;
     }
     const int ti = p.acoustics ? 0 : m * 2 + m2;
-    const R th = invcdf(p.tab, ti, u_theta);
+    const R th_pi = invcdf(p.tab, ti, u_theta); // tables hold theta / pi
     R st, ct;
-    m_sincos(th, &st, &ct);
+    m_sincospi(th_pi, &st, &ct);
     R nd[3], nq[3];
 #pragma unroll
     for (int i = 0; i < 3; ++i) {
@@ -359,7 +374,7 @@ __device__ void process_event(const DevParams<R> &p, uint64_t pid, Part<R> &s, C
         return;
     }
     s.k++;
-    const R step = p.step[s.mode];
+    const R step = by_mode(p.step, s.mode);
     const R dt = step * (R)(e - s.s0);
     R xe[3] = {s.x[0] + dt * s.d[0], s.x[1] + dt * s.d[1], s.x[2] + dt * s.d[2]};
     if (kind == 1) {
@@ -367,10 +382,13 @@ __device__ void process_event(const DevParams<R> &p, uint64_t pid, Part<R> &s, C
         const R x1[3] = {s.x[0] + dt1 * s.d[0], s.x[1] + dt1 * s.d[1], s.x[2] + dt1 * s.d[2]};
         s.x[0] = xe[0]; s.x[1] = xe[1]; s.x[2] = xe[2];
         int changed = 0;
-        for (int b = 0; b < p.n_bnd; ++b) {
+#pragma unroll
+        for (int b = 0; b < RTMC_MAX_BND; ++b) {
+            if (b >= p.n_bnd) break;
             const int k = p.bnd_dir[b] - 1;
             const R val = p.bnd_val[b];
-            if (!((s.x[k] - val) * (x1[k] - val) < (R)0)) continue;
+            const R xk = sel3(s.x, k);
+            if (!((xk - val) * (sel3(x1, k) - val) < (R)0)) continue;
             cnt.bnd++;
             if (p.bnd_absorb[b]) {
                 s.alive = 0;
@@ -379,9 +397,9 @@ __device__ void process_event(const DevParams<R> &p, uint64_t pid, Part<R> &s, C
                 cnt.absorb++;
                 return;
             }
-            s.x[k] = (R)2 * val - s.x[k];
+            put3(s.x, k, (R)2 * val - xk);
             if (p.acoustics) {
-                s.d[k] = -s.d[k];
+                put3(s.d, k, -sel3(s.d, k));
             } else {
                 const U4<R> bb = draw(p, pid, s.k, 1u + (uint32_t)b);
                 const int ch = elastic_reflect(p, s, k, bb.a, bb.b);
@@ -392,9 +410,9 @@ __device__ void process_event(const DevParams<R> &p, uint64_t pid, Part<R> &s, C
         s.s0 = e;
         if (changed) {
             const U4<R> r0 = draw(p, pid, s.k, 0u);
-            const int js = geom_steps(r0.a, p.inv_lam[s.mode], p.scat_on[s.mode], cap);
+            const int js = geom_steps(r0.a, by_mode(p.inv_lam, s.mode), by_mode(p.scat_on, s.mode), cap);
             s.sS = js >= cap ? cap : e - 1 + js;
-            const int jk = geom_steps(r0.b, p.inv_q[s.mode], p.kill_on[s.mode], cap);
+            const int jk = geom_steps(r0.b, by_mode(p.inv_q, s.mode), by_mode(p.kill_on, s.mode), cap);
             s.sK = jk >= cap ? cap : e + jk;
         }
     } else {
@@ -404,12 +422,14 @@ __device__ void process_event(const DevParams<R> &p, uint64_t pid, Part<R> &s, C
         scatter(p, s, r0.b, r0.c, r0.d);
         cnt.scat++;
         s.s0 = e;
-        const int js = geom_steps(r0.a, p.inv_lam[s.mode], p.scat_on[s.mode], cap);
+        const int js = geom_steps(r0.a, by_mode(p.inv_lam, s.mode), by_mode(p.scat_on, s.mode), cap);
         s.sS = js >= cap ? cap : e + js;
-        if (s.mode != m0) {
+        if (s.mode != m0 && by_mode(p.kill_on, s.mode)) {
             const U4<R> r1 = draw(p, pid, s.k, 1u);
-            const int jk = geom_steps(r1.a, p.inv_q[s.mode], p.kill_on[s.mode], cap);
+            const int jk = geom_steps(r1.a, by_mode(p.inv_q, s.mode), 1, cap);
             s.sK = jk >= cap ? cap : e + jk;
+        } else if (s.mode != m0) {
+            s.sK = cap;
         }
     }
     if (s.sS > cap) s.sS = cap;
@@ -428,8 +448,8 @@ __device__ __forceinline__ int bin_of(const DevParams<R> &p, const R *sedges, in
     if (p.ax_uniform[a]) {
         b = (int)((c - p.ax_lo[a]) * p.ax_inv_w[a]);
         b = b < 0 ? 0 : (b > nb - 1 ? nb - 1 : b);
-        while (b > 0 && c < e[b]) --b;
-        while (b < nb - 1 && c >= e[b + 1]) ++b;
+        // the arithmetic guess is off by at most one near an edge: settle it on the edges
+        b = b - (c < e[b] ? 1 : 0) + ((b < nb - 1 && c >= e[b + 1]) ? 1 : 0);
     } else {
         int lo = 0, hi = nb - 1;
         while (hi > lo) {
@@ -441,11 +461,31 @@ __device__ __forceinline__ int bin_of(const DevParams<R> &p, const R *sedges, in
     return b;
 }
 
-// observeTime.m:14-144 for one particle at observation j; returns the histogram index or -1
+// observeTime.m:24-32: the direction axis depends on the direction only, so its bin
+// offset is computed once per trajectory segment (-1: outside its range)
 template <typename R>
-__device__ __forceinline__ int64_t obs_index(const DevParams<R> &p, const R *sedges, const R x[3], R dz, int mode, int j)
+__device__ __forceinline__ int dir_offset(const DevParams<R> &p, const R *sedges, R dz)
 {
-    R c[4];
+    const int am = p.ax_mode[3];
+    if (am == RTMC_AXIS_IGNORED) return 0;
+    const R cz = dz > (R)1 ? (R)1 : (dz < (R)-1 ? (R)-1 : dz);
+    const R c = (p.d == 3) ? cz : m_acos(cz);
+    if (am == RTMC_AXIS_RANGE) return (c >= p.ax_lo[3] && c <= p.ax_hi[3]) ? 0 : -1;
+    const int b = bin_of(p, sedges, 3, c);
+    return b < 0 ? -1 : b * p.ax_stride32[3];
+}
+
+__device__ __forceinline__ float m_fast_sqrt(float x) { return x > 0.f ? x * rsqrtf(x) : 0.f; }
+__device__ __forceinline__ double m_fast_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ int m_floor_int(float x) { return __float2int_rd(x); }
+__device__ __forceinline__ int m_floor_int(double x) { return __double2int_rd(x); }
+
+// observeTime.m:14-144 for the position axes X, Y, Z of one observation in any frame:
+// offset of the bin inside the time slice (direction part excluded), or -1
+template <typename R>
+__device__ __forceinline__ int pos_offset(const DevParams<R> &p, const R *sedges, const R x[3])
+{
+    R c[3];
     if (p.frame == RTMC_FRAME_CARTESIAN) {
         c[0] = x[0]; c[1] = x[1]; c[2] = x[2];
     } else {
@@ -456,71 +496,281 @@ __device__ __forceinline__ int64_t obs_index(const DevParams<R> &p, const R *sed
         } else {
             const R r = m_hypot(rxy, x[2]);
             c[0] = r;
-            c[2] = (p.ax_mode[2] != RTMC_AXIS_IGNORED) ? m_sin(m_atan2(x[2], rxy)) : (R)0;
+            c[2] = (p.ax_mode[2] != RTMC_AXIS_IGNORED && r > (R)0) ? x[2] / r : (R)0; // sin(elevation)
         }
     }
-    if (p.ax_mode[3] != RTMC_AXIS_IGNORED) {
-        R cz = dz > (R)1 ? (R)1 : (dz < (R)-1 ? (R)-1 : dz);
-        c[3] = (p.d == 3) ? cz : m_acos(cz);
-    } else {
-        c[3] = (R)0;
-    }
-    int64_t idx = (int64_t)j * p.time_stride + (int64_t)mode * p.mode_stride;
+    int idx = 0;
 #pragma unroll
-    for (int a = 0; a < 4; ++a) {
+    for (int a = 0; a < 3; ++a) {
         const int am = p.ax_mode[a];
         if (am == RTMC_AXIS_RANGE) {
             if (!(c[a] >= p.ax_lo[a] && c[a] <= p.ax_hi[a])) return -1;
         } else if (am == RTMC_AXIS_BINNED) {
             const int b = bin_of(p, sedges, a, c[a]);
             if (b < 0) return -1;
-            idx += (int64_t)b * p.ax_stride[a];
+            idx += b * p.ax_stride32[a];
         }
     }
     return idx;
 }
 
-template <typename R, bool SMEM>
-__global__ void __launch_bounds__(SMEM ? 1024 : 256) rt_transport(const DevParams<R> p)
+// Observation paths, fixed at compile time from the observation grid:
+//   OBS_CART    cartesian frame, uniform finite axes: a coordinate is linear in the
+//               sub-step along a segment, so its bin position is t = A + B * (so - s0)
+//               with A, B set once per segment (one FMA and a floor per axis);
+//   OBS_RADIAL  radius-only frames (the other position axes integrate over their whole
+//               range): r = |x0 + D (so - s0)|;
+//   OBS_GENERAL anything else (angles, non-uniform edges).
+// The fast paths place a coordinate sitting on a bin edge to within rounding by
+// arithmetic rather than by comparing with the edge table.
+enum { OBS_GENERAL = 0, OBS_CART = 1, OBS_RADIAL = 2 };
+
+// A straight piece of trajectory: position x at sub-step s0, direction d, mode, plus the
+// per-segment binning terms of the observation path.
+template <typename R> struct Seg {
+    R x[3], d[3];
+    R A[3], B[3];
+    int s0, mode, doff;
+};
+
+template <typename R, int OBS>
+__device__ __forceinline__ void seg_prepare(const DevParams<R> &p, const R *sedges, Seg<R> &g)
 {
+    g.doff = dir_offset(p, sedges, g.d[2]);
+    const R step = by_mode(p.step, g.mode);
+    if (OBS == OBS_CART) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            g.A[a] = (g.x[a] - p.ax_lo[a]) * p.ax_inv_w[a];
+            g.B[a] = step * g.d[a] * p.ax_inv_w[a];
+        }
+    } else if (OBS == OBS_RADIAL) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) g.B[a] = step * g.d[a];
+    }
+}
+
+// bin offset inside the time slice of an observation at sub-step so, or -1
+template <typename R, int OBS>
+__device__ __forceinline__ int obs_offset(const DevParams<R> &p, const R *sedges, const Seg<R> &g, int so)
+{
+    if (g.doff < 0) return -1;
+    const R dl = (R)(so - g.s0);
+    if (OBS == OBS_CART) {
+        int idx = g.doff;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            const int b = m_floor_int(g.A[a] + g.B[a] * dl);
+            if ((unsigned)b >= (unsigned)p.ax_nbe[a]) return -1;
+            idx += b * p.ax_stride32[a];
+        }
+        return idx;
+    } else if (OBS == OBS_RADIAL) {
+        const R x0 = g.x[0] + g.B[0] * dl, x1 = g.x[1] + g.B[1] * dl;
+        R r2 = x0 * x0 + x1 * x1;
+        if (p.radial_3d) {
+            const R x2 = g.x[2] + g.B[2] * dl;
+            r2 += x2 * x2;
+        }
+        const int b = m_floor_int(m_fast_sqrt(r2) * p.ax_inv_w[0] + p.ax_a0);
+        if ((unsigned)b >= (unsigned)p.ax_nbe[0]) return -1;
+        return g.doff + b * p.ax_stride32[0];
+    } else {
+        const R dt = by_mode(p.step, g.mode) * dl;
+        const R xo[3] = {g.x[0] + dt * g.d[0], g.x[1] + dt * g.d[1], g.x[2] + dt * g.d[2]};
+        const int po = pos_offset(p, sedges, xo);
+        return po < 0 ? -1 : po + g.doff;
+    }
+}
+
+// Per-lane ring of segments in shared memory, field-major so that lane t of every
+// slot sits in bank t % 32.
+template <typename R> struct Ring {
+    R *x0, *x1, *x2, *d0, *d1, *d2;
+    int *s0, *mode;
+    int cap, stride;
+    __device__ __forceinline__ void put(int slot, const Part<R> &s) const
+    {
+        const int k = slot * stride + threadIdx.x;
+        x0[k] = s.x[0]; x1[k] = s.x[1]; x2[k] = s.x[2];
+        d0[k] = s.d[0]; d1[k] = s.d[1]; d2[k] = s.d[2];
+        s0[k] = s.s0; mode[k] = s.mode;
+    }
+    __device__ __forceinline__ void get(int slot, Seg<R> &g) const
+    {
+        const int k = slot * stride + threadIdx.x;
+        g.x[0] = x0[k]; g.x[1] = x1[k]; g.x[2] = x2[k];
+        g.d[0] = d0[k]; g.d[1] = d1[k]; g.d[2] = d2[k];
+        g.s0 = s0[k]; g.mode = mode[k];
+    }
+    __device__ __forceinline__ int start(int slot) const { return s0[slot * stride + threadIdx.x]; }
+};
+
+template <typename R> __device__ __forceinline__ void seg_from(const Part<R> &s, Seg<R> &g)
+{
+#pragma unroll
+    for (int c = 0; c < 3; ++c) { g.x[c] = s.x[c]; g.d[c] = s.d[c]; }
+    g.s0 = s.s0;
+    g.mode = s.mode;
+}
+
+template <typename R> __device__ __forceinline__ int next_event(const Part<R> &s) { return min(min(s.sK, s.sB), s.sS); }
+
+// Where observations go: a block-private u32 histogram in shared memory (the whole
+// histogram fits), 64-bit global atomics, or a dense time-major array of 32-bit bin
+// indices that rt_bin_slices folds into the histogram one time slice at a time.
+enum { SINK_SMEM = 0, SINK_GLOBAL = 1, SINK_INDEX = 2 };
+
+template <typename R, int SINK> struct Bounds {
+    static constexpr int threads = SINK == SINK_SMEM ? 512 : 256;
+    static constexpr int min_blocks = SINK == SINK_SMEM ? 1 : 2;
+};
+
+// The transport kernel.  A warp takes 32 consecutive particles at a time and walks the
+// observation instants in lockstep.  Each lane keeps two cursors on its particle's
+// trajectory: the event state s (phase 1, runs ahead and pushes one segment per event
+// into the lane's ring) and the observation cursor (phase 2, bins observation instants
+// with the segment in force).  Phase 1 runs with every lane that has room in its ring
+// taking part, so events execute converged; phase 2 then bins the number of
+// observations that every live lane has covered, fully converged.
+template <typename R, int SINK, int OBS>
+__global__ void __launch_bounds__(Bounds<R, SINK>::threads, Bounds<R, SINK>::min_blocks) rt_transport(const DevParams<R> p)
+{
+    constexpr bool SMEM = SINK == SINK_SMEM;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R *sedges = reinterpret_cast<R *>(smem_raw);
-    const int edge_bytes = ((p.n_edges * (int)sizeof(R) + 15) / 16) * 16;
-    unsigned *shist = reinterpret_cast<unsigned *>(smem_raw + edge_bytes);
+    size_t off = (((size_t)p.n_edges * sizeof(R) + 15) / 16) * 16;
+    unsigned *shist = reinterpret_cast<unsigned *>(smem_raw + off);
+    if (SMEM) off += (((size_t)p.hist_len * 4 + 15) / 16) * 16;
+    const int T = blockDim.x, C = p.ring_cap;
+    Ring<R> ring;
+    ring.cap = C;
+    ring.stride = T;
+    {
+        R *r = reinterpret_cast<R *>(smem_raw + off);
+        ring.x0 = r; ring.x1 = r + C * T; ring.x2 = r + 2 * C * T;
+        ring.d0 = r + 3 * C * T; ring.d1 = r + 4 * C * T; ring.d2 = r + 5 * C * T;
+        int *ri = reinterpret_cast<int *>(r + 6 * C * T);
+        ring.s0 = ri; ring.mode = ri + C * T;
+    }
 
-    for (int i = threadIdx.x; i < p.n_edges; i += blockDim.x) sedges[i] = p.edges[i];
+    for (int k = threadIdx.x; k < p.n_edges; k += T) sedges[k] = p.edges[k];
     if (SMEM)
-        for (int64_t i = threadIdx.x; i < p.hist_len; i += blockDim.x) shist[i] = 0u;
+        for (int64_t k = threadIdx.x; k < p.hist_len; k += T) shist[k] = 0u;
     __syncthreads();
 
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
     Counters cnt = {0u, 0u, 0u, 0u, 0u, 0u};
     bool bad = false;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     const unsigned long long inc = 1ull << p.hist_shift;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.n_particles; i += stride) {
+    const int s_end = p.s_end;
+    const int64_t warps = ((int64_t)gridDim.x * T) >> 5;
+
+    for (int64_t base = (((int64_t)blockIdx.x * T + threadIdx.x) >> 5) << 5; base < p.n_particles; base += warps * 32) {
+        const int64_t i = base + lane;
+        const bool have = i < p.n_particles;
         const uint64_t pid = (uint64_t)(p.pid0 + i);
         Part<R> s;
-        init_particle(p, pid, s);
+        Seg<R> cur;
+        int head = 0, count = 0;
         const unsigned scat0 = cnt.scat, bnd0 = cnt.bnd;
-        int guard = 0;
-        for (int j = 1; j <= p.n_obs; ++j) {
-            const int so = j * p.n_sub;
-            while (s.alive && min(min(s.sK, s.sB), s.sS) <= so) {
-                process_event(p, pid, s, cnt);
-                if (++guard > p.max_events) { s.alive = 0; bad = true; }
+        if (have) {
+            init_particle(p, pid, s);
+        } else {
+            s.alive = 0; s.s_death = 0; s.s0 = 0; s.sS = s.sK = s.sB = s_end + 1; s.k = 0; s.mode = 0;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) { s.x[c] = (R)0; s.d[c] = (R)0; s.q[c] = (R)0; }
+        }
+        seg_from(s, cur);
+        seg_prepare<R, OBS>(p, sedges, cur);
+        int32_t *optr = (SINK == SINK_INDEX && have) ? p.obs_idx + i : nullptr;
+        int jn = 1; // warp-uniform
+        while (jn <= p.n_obs) {
+            // ---- phase 1: refill the rings (events of all lanes with room run together)
+            const int so_next = jn * p.n_sub;
+            for (;;) {
+                // segments starting at or before the next observation supersede the
+                // current one: consume them, so the ring only holds later segments
+                while (count > 0 && ring.start(head) <= so_next) {
+                    ring.get(head, cur);
+                    seg_prepare<R, OBS>(p, sedges, cur);
+                    head = (head + 1) % C;
+                    --count;
+                }
+                const bool need = s.alive && count < C && next_event(s) <= s_end;
+                if (!__any_sync(full, need)) break;
+                if (need) {
+                    process_event(p, pid, s, cnt);
+                    if ((int)s.k > p.max_events) { s.alive = 0; s.s_death = s.s0; bad = true; }
+                    if (s.alive) {
+                        if (count == 0 && s.s0 <= so_next) {
+                            seg_from(s, cur);
+                            seg_prepare<R, OBS>(p, sedges, cur);
+                        } else {
+                            ring.put((head + count) % C, s);
+                            ++count;
+                        }
+                    }
+                }
             }
-            if (!s.alive) break;
-            const R dt = p.step[s.mode] * (R)(so - s.s0);
-            const R xo[3] = {s.x[0] + dt * s.d[0], s.x[1] + dt * s.d[1], s.x[2] + dt * s.d[2]};
-            const int64_t idx = obs_index(p, sedges, xo, s.d[2], s.mode, j);
-            if (idx >= 0) {
-                if (idx >= p.hist_len) { bad = true; continue; }
-                cnt.obs++;
-                if (SMEM) atomicAdd(shist + idx, 1u);
-                else atomicAdd(p.hist + idx, inc);
+            // ---- window: observations every live lane has covered (dead lanes never limit)
+            unsigned avail = 0x7fffffffu;
+            if (s.alive) {
+                const int limit = next_event(s) <= s_end ? next_event(s) : s_end + 1;
+                int last = (limit - 1) / p.n_sub;
+                last = last < p.n_obs ? last : p.n_obs;
+                avail = (unsigned)(last - jn + 1);
+            }
+            unsigned nw = __reduce_min_sync(full, avail);
+            if (nw > (unsigned)(p.n_obs - jn + 1)) {
+                if (SINK == SINK_INDEX) {
+                    nw = (unsigned)(p.n_obs - jn + 1); // no live lane left: write the rest
+                } else {
+                    // no live lane left: bin what the dead lanes observed before dying
+                    int rem = 0;
+                    if (have && s.s_death > jn * p.n_sub) rem = min(p.n_obs, (s.s_death - 1) / p.n_sub) - jn + 1;
+                    nw = __reduce_max_sync(full, (unsigned)(rem > 0 ? rem : 0));
+                    if (nw == 0) break;
+                }
+            }
+            // ---- phase 2: nw observations per lane
+            const int obs_limit = s.alive ? 0x7fffffff : s.s_death;
+            int next_start = count > 0 ? ring.start(head) : 0x7fffffff;
+            int so = jn * p.n_sub;
+            for (unsigned w = 0; w < nw; ++w, ++jn, so += p.n_sub) {
+                int v = -1;
+                if (so < obs_limit) {
+                    if (so >= next_start) {
+                        do {
+                            ring.get(head, cur);
+                            head = (head + 1) % C;
+                            --count;
+                        } while (count > 0 && ring.start(head) <= so);
+                        seg_prepare<R, OBS>(p, sedges, cur);
+                        next_start = count > 0 ? ring.start(head) : 0x7fffffff;
+                    }
+                    v = obs_offset<R, OBS>(p, sedges, cur, so);
+                }
+                if (SINK == SINK_INDEX) {
+                    if (have) {
+                        *optr = v < 0 ? -1 : (v | (cur.mode << 30));
+                        optr += p.obs_rows;
+                    }
+                    if (v >= 0) cnt.obs++;
+                } else if (v >= 0) {
+                    const int64_t idx = (int64_t)jn * p.time_stride + (cur.mode ? p.mode_stride : 0) + v;
+                    if (idx < p.hist_len) {
+                        cnt.obs++;
+                        if (SMEM) atomicAdd(shist + idx, 1u);
+                        else atomicAdd(p.hist + idx, inc);
+                    } else {
+                        bad = true;
+                    }
+                }
             }
         }
-        if (p.trace) { // final state of the particle, the oracle's layout
+        if (have && p.trace) { // final state of the particle, the oracle's layout
             double *f = p.trace + 16 * i;
 #pragma unroll
             for (int c = 0; c < 3; ++c) { f[c] = s.x[c]; f[3 + c] = s.d[c]; f[6 + c] = s.q[c]; }
@@ -530,34 +780,107 @@ __global__ void __launch_bounds__(SMEM ? 1024 : 256) rt_transport(const DevParam
     }
 
     // counters: warp reduction, one global atomic per warp
-    const unsigned full = 0xffffffffu;
     unsigned v[6] = {cnt.scat, cnt.bnd, cnt.kill, cnt.absorb, cnt.obs, cnt.conv};
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
         const unsigned t = __reduce_add_sync(full, v[c]);
-        if ((threadIdx.x & 31) == 0 && t) atomicAdd(p.stats + c, (unsigned long long)t);
+        if (lane == 0 && t) atomicAdd(p.stats + c, (unsigned long long)t);
     }
     if (bad) atomicExch(p.status, 1);
     if (SMEM) {
         __syncthreads();
-        for (int64_t i = threadIdx.x; i < p.hist_len; i += blockDim.x) {
-            const unsigned c = shist[i];
-            if (c) atomicAdd(p.hist + i, (unsigned long long)c << p.hist_shift);
+        for (int64_t k = threadIdx.x; k < p.hist_len; k += T) {
+            const unsigned c = shist[k];
+            if (c) atomicAdd(p.hist + k, (unsigned long long)c << p.hist_shift);
         }
     }
 }
 
-template <typename R, bool SMEM> void *kernel_ptr() { return (void *)rt_transport<R, SMEM>; }
+// Fold the dense index array into the histogram, one time slice at a time: blockIdx.y
+// is the slice (so the L2 holds the slice being written), blockIdx.x strides over the
+// particles of the chunk.
+__global__ void __launch_bounds__(256) rt_bin_slices(const BinParams b)
+{
+    const int j = blockIdx.y + 1;
+    const int32_t *row = b.idx + (int64_t)(j - 1) * b.rows; // rows is a multiple of 32: 16-byte aligned
+    unsigned long long *slice = b.hist + (int64_t)j * b.time_stride;
+    const unsigned long long inc = 1ull << b.hist_shift;
+    const int64_t n4 = (b.n + 3) >> 2;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int4 *row4 = reinterpret_cast<const int4 *>(row);
+    // two 16-byte loads in flight per thread before their atomics
+    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n4; k += 2 * stride) {
+        const int64_t k2 = k + stride;
+        const int4 a = __ldcs(row4 + k);
+        const int4 c = k2 < n4 ? __ldcs(row4 + k2) : make_int4(-1, -1, -1, -1);
+        const int va[8] = {a.x, a.y, a.z, a.w, c.x, c.y, c.z, c.w};
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+            const int64_t e = (u < 4 ? k : k2) * 4 + (u & 3);
+            const int v = va[u];
+            if (v >= 0 && e < b.n) atomicAdd(slice + ((v >> 30) ? b.mode_stride : 0) + (v & 0x3fffffff), inc);
+        }
+    }
+}
+
+// Same fold with a group of slices privatised in shared memory (u32 counts), flushed
+// with one 64-bit atomic per touched bin: blockIdx.y is the slice group, blockIdx.x a
+// contiguous particle range.
+__global__ void __launch_bounds__(512) rt_bin_slices_smem(const BinParams b)
+{
+    extern __shared__ __align__(16) unsigned sh[];
+    const int j0 = 1 + blockIdx.y * b.group;
+    const int j1 = min(b.n_obs, j0 + b.group - 1);
+    const int per = b.slice_bins * b.n_modes; // bins of one slice, all modes
+    const int nb = (j1 - j0 + 1) * per;
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) sh[k] = 0u;
+    __syncthreads();
+    const int64_t p0 = (int64_t)blockIdx.x * b.part_per_block;
+    const int64_t p1 = min(b.n, p0 + b.part_per_block);
+    for (int j = j0; j <= j1; ++j) {
+        const int32_t *row = b.idx + (int64_t)(j - 1) * b.rows;
+        unsigned *sj = sh + (j - j0) * per;
+        for (int64_t k = p0 + threadIdx.x; k < p1; k += blockDim.x) {
+            const int v = __ldcs(row + k);
+            if (v >= 0) atomicAdd(sj + ((v >> 30) ? b.slice_bins : 0) + (v & 0x3fffffff), 1u);
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) {
+        const unsigned c = sh[k];
+        if (!c) continue;
+        const int jj = j0 + k / per, r = k % per;
+        const int m = r / b.slice_bins, o = r % b.slice_bins;
+        atomicAdd(b.hist + (int64_t)jj * b.time_stride + (m ? b.mode_stride : 0) + o, (unsigned long long)c << b.hist_shift);
+    }
+}
+
+template <typename R, int SINK, int OBS> void *kernel_ptr() { return (void *)rt_transport<R, SINK, OBS>; }
+
+template <typename R, int SINK> void *pick_obs(int obs)
+{
+    return obs == OBS_CART ? kernel_ptr<R, SINK, OBS_CART>()
+                           : (obs == OBS_RADIAL ? kernel_ptr<R, SINK, OBS_RADIAL>() : kernel_ptr<R, SINK, OBS_GENERAL>());
+}
+
+template <typename R> void *pick_t(int sink, int obs)
+{
+    return sink == SINK_SMEM ? pick_obs<R, SINK_SMEM>(obs)
+                             : (sink == SINK_GLOBAL ? pick_obs<R, SINK_GLOBAL>(obs) : pick_obs<R, SINK_INDEX>(obs));
+}
 
 } // namespace
 
+static void *pick(int precision, int sink, int obs)
+{
+    return precision == RTMC_FP64 ? pick_t<double>(sink, obs) : pick_t<float>(sink, obs);
+}
+
 template <typename R> static int launch(const DevParams<R> &p, int grid, int block, size_t smem, void *stream)
 {
-    if (p.hist_smem)
-        rt_transport<R, true><<<grid, block, smem, (cudaStream_t)stream>>>(p);
-    else
-        rt_transport<R, false><<<grid, block, smem, (cudaStream_t)stream>>>(p);
-    return (int)cudaGetLastError();
+    void *fn = pick(sizeof(R) == 8 ? RTMC_FP64 : RTMC_FP32, p.sink, p.obs_kind);
+    void *args[] = {(void *)&p};
+    return (int)cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, (cudaStream_t)stream);
 }
 
 int launch_transport_f32(const DevParams<float> &p, int grid, int block, size_t smem, void *stream)
@@ -570,20 +893,31 @@ int launch_transport_f64(const DevParams<double> &p, int grid, int block, size_t
     return launch(p, grid, block, smem, stream);
 }
 
-static void *pick(int precision, int smem_hist)
+int launch_bin_slices(const BinParams &b, int grid_x, size_t smem, void *stream)
 {
-    if (precision == RTMC_FP64) return smem_hist ? kernel_ptr<double, true>() : kernel_ptr<double, false>();
-    return smem_hist ? kernel_ptr<float, true>() : kernel_ptr<float, false>();
+    if (b.group > 0) {
+        dim3 g(grid_x, (b.n_obs + b.group - 1) / b.group);
+        rt_bin_slices_smem<<<g, 512, smem, (cudaStream_t)stream>>>(b);
+    } else {
+        dim3 g(grid_x, b.n_obs);
+        rt_bin_slices<<<g, 256, 0, (cudaStream_t)stream>>>(b);
+    }
+    return (int)cudaGetLastError();
 }
 
-int transport_set_smem(int precision, int smem_hist, size_t smem)
+int bin_slices_set_smem(size_t smem)
 {
-    return (int)cudaFuncSetAttribute(pick(precision, smem_hist), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    return (int)cudaFuncSetAttribute((const void *)rt_bin_slices_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
-int transport_occupancy(int precision, int smem_hist, int block, size_t smem, int *blocks_per_sm)
+int transport_set_smem(int precision, int sink, int obs, size_t smem)
 {
-    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pick(precision, smem_hist), block, smem);
+    return (int)cudaFuncSetAttribute(pick(precision, sink, obs), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+int transport_occupancy(int precision, int sink, int obs, int block, size_t smem, int *blocks_per_sm)
+{
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pick(precision, sink, obs), block, smem);
 }
 
 } // namespace rtmc

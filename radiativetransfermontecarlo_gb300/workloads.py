@@ -27,13 +27,13 @@ def c1_acoustic3d(n: int = 1_000_000, precision: str = "fp64"):
     return geo, src, mat, obs, {"precision": precision, "seed": 0}
 
 
-def c2_elastic3d(n: int = 10_000_000, precision: str = "fp32"):
+def c2_elastic3d(n: int = 10_000_000, precision: str = "fp32", t_end: float = 5.0):
     """3D elastic isotropic unbounded, cartesian 60^3 x 8 directions x 251 times x 2 modes."""
     geo = {"dimension": 3, "frame": "cartesian"}
     mat = MaterialClass(geo, 5, False, [2, 1.155], [0.1, 0.1, 0.1], [0, 0, 0], "gauss", 0.2)
     src = {"numberParticles": n, "position": [0, 0, 0], "lambda": 0.05, "polarization": "P"}
     e = colon(-5, 1 / 6, 5)
-    obs = {"x": e, "y": e, "z": e, "directions": colon(0, math.pi / 8, math.pi), "time": colon(0, 0.02, 5)}
+    obs = {"x": e, "y": e, "z": e, "directions": colon(0, math.pi / 8, math.pi), "time": colon(0, 0.02, t_end)}
     return geo, src, mat, obs, {"precision": precision, "seed": 1, "histogram": "extended", "hist_shift": 40}
 
 

@@ -143,3 +143,41 @@ def test_determinism_bit_identical():
     b, sb = get_context(0).forward(P, prob.tables)
     assert np.array_equal(a, b)
     assert sa["observations"] == (a >> prob.hist_shift).sum()
+
+
+@pytest.mark.parametrize("index_mb", [0, -1, 8])
+def test_large_histogram_paths_match_oracle(index_mb):
+    """Histograms too big for shared memory: index array + slice fold (0: default budget,
+    8: a budget that forces several particle chunks) and the global-atomics path (-1)."""
+    geo, src, mat, obs, opts = W.c3_halfspace2d()  # 200 r x 401 t x 2 modes: 641 KB as u32
+    ctx = get_context(0)
+    ctx.set_launch(0, 0, index_mb)
+    try:
+        prob, grid, N, hist, states, stats, ref_hist, ref_states, ref_stats = _run_both(
+            geo, src, mat, obs, opts, 6000, "fp64")
+    finally:
+        ctx.set_launch(0, 0, 0)
+    assert stats["device_status"] == 0
+    assert stats["sink"] == (1 if index_mb == -1 else 2)
+    if index_mb == 8:
+        assert stats["launches"] >= 4  # two particle chunks, each transport + fold
+    assert _path_match(states, ref_states, 1e-9).mean() == 1.0
+    assert stats["observations"] == ref_stats["observations"]
+    assert _l1_diff(hist, ref_hist) <= max(4, 1e-6 * stats["observations"])
+
+
+@pytest.mark.parametrize("frame,extra", [("spherical", {"y": colon(-math.pi, math.pi / 4, math.pi)}),
+                                         ("cylindrical", {"z": colon(-2, 0.5, 2)})])
+def test_general_observation_path(frame, extra):
+    """Angle or z binning takes the general observation path (edge-table binning)."""
+    geo = {"dimension": 3, "frame": frame}
+    mat = MaterialClass(geo, 10, True, 1, [0.1, 0.1], 0, "exp", 0.1)
+    src = {"lambda": 0.05}
+    obs = dict({"x": colon(0, 0.1, 3), "time": colon(0, 0.05, 2)}, **extra)
+    for precision, tol, need in (("fp64", 1e-9, 1.0), ("fp32", 1e-3, 0.99)):
+        prob, grid, N, hist, states, stats, ref_hist, ref_states, ref_stats = _run_both(
+            geo, src, mat, obs, {"seed": 9}, 8000, precision)
+        assert stats["device_status"] == 0
+        assert _path_match(states, ref_states, tol).mean() >= need
+        if precision == "fp64":
+            assert _l1_diff(hist, ref_hist) <= max(4, 1e-6 * stats["observations"])
