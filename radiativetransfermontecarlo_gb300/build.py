@@ -51,7 +51,8 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     objs = []
     for cu in sorted(CSRC.glob("*.cu")):
         o = BUILD / (cu.stem + ".o")
-        cmd = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", *inc, "-c", str(cu), "-o", str(o)]
+        extra = os.environ.get("RTMC_NVCC_EXTRA", "").split()  # e.g. -DRTMC_TRANSPORT_MIN_BLOCKS=3
+        cmd = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", *extra, *inc, "-c", str(cu), "-o", str(o)]
         if ptxas_info:
             cmd.insert(2, "-Xptxas=-v")
         jobs.append(cmd)

@@ -340,6 +340,11 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         if (chunk > 0 && ctx->idx.grow((size_t)chunk * P->n_obs * sizeof(int32_t)) == 0) sink = kSinkIndex;
         else chunk = P->n_particles;
     }
+    {
+        // the variant's launch bound caps the block (fill_params chose the observation path)
+        const int mt = transport_max_threads(prec, sink, p.obs_kind);
+        if (mt > 0 && block > mt) block = mt - mt % 32;
+    }
     size_t smem = edge_smem + (sink == kSinkSmem ? hist_smem : 0) + (size_t)block * cap * seg_bytes;
     int bps = 0;
     if (transport_set_smem(prec, sink, p.obs_kind, smem) != 0) return fail(&ctx->err, RTMC_ERR_CUDA, "cudaFuncSetAttribute failed");

@@ -98,6 +98,7 @@ int launch_transport_f32(const DevParams<float> &p, int grid, int block, size_t 
 int launch_transport_f64(const DevParams<double> &p, int grid, int block, size_t smem, void *stream);
 int transport_occupancy(int precision, int sink, int obs, int block, size_t smem, int *blocks_per_sm);
 int transport_set_smem(int precision, int sink, int obs, size_t smem);
+int transport_max_threads(int precision, int sink, int obs);
 int launch_bin_slices(const BinParams &b, int grid_x, size_t smem, void *stream);
 int bin_slices_set_smem(size_t smem);
 enum { kSinkSmem = 0, kSinkGlobal = 1, kSinkIndex = 2 };

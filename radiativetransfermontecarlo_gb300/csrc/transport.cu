@@ -621,9 +621,16 @@ template <typename R> __device__ __forceinline__ int next_event(const Part<R> &s
 // indices that rt_bin_slices folds into the histogram one time slice at a time.
 enum { SINK_SMEM = 0, SINK_GLOBAL = 1, SINK_INDEX = 2 };
 
+// launch bounds of the transport variants (build-time knobs for the index/global sinks)
+#ifndef RTMC_TRANSPORT_THREADS
+#define RTMC_TRANSPORT_THREADS 256
+#endif
+#ifndef RTMC_TRANSPORT_MIN_BLOCKS
+#define RTMC_TRANSPORT_MIN_BLOCKS 3 // FP32: 3 x 256 threads per SM measured fastest (85 registers)
+#endif
 template <typename R, int SINK> struct Bounds {
-    static constexpr int threads = SINK == SINK_SMEM ? 512 : 256;
-    static constexpr int min_blocks = SINK == SINK_SMEM ? 1 : 2;
+    static constexpr int threads = SINK == SINK_SMEM ? 512 : RTMC_TRANSPORT_THREADS;
+    static constexpr int min_blocks = SINK == SINK_SMEM ? 1 : (sizeof(R) == 4 ? RTMC_TRANSPORT_MIN_BLOCKS : 2);
 };
 
 // The transport kernel.  A warp takes 32 consecutive particles at a time and walks the
@@ -913,6 +920,13 @@ int bin_slices_set_smem(size_t smem)
 int transport_set_smem(int precision, int sink, int obs, size_t smem)
 {
     return (int)cudaFuncSetAttribute(pick(precision, sink, obs), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+int transport_max_threads(int precision, int sink, int obs)
+{
+    cudaFuncAttributes a;
+    if (cudaFuncGetAttributes(&a, pick(precision, sink, obs)) != cudaSuccess) return 0;
+    return a.maxThreadsPerBlock;
 }
 
 int transport_occupancy(int precision, int sink, int obs, int block, size_t smem, int *blocks_per_sm)
