@@ -201,6 +201,34 @@ int rtmc_copy_histogram(rtmc_context *ctx, int64_t *hist_out, int64_t n);
 int rtmc_forward_trace(rtmc_context *ctx, const rtmc_problem *problem, const rtmc_tables *tables,
                        int64_t *hist_out, double *state_out, rtmc_stats *stats);
 
+/* Size of the static device scratch of rtmc_forward_noalloc (96 MB per GPU). */
+#define RTMC_STATIC_SCRATCH_BYTES (96u << 20)
+
+/* rtmc_forward for callers that cannot allocate device memory: code running where a
+ * cudaMalloc is not allowed or not wanted, such as inside a host application whose
+ * allocator owns the whole device, or a host that hands over only pre-allocated
+ * buffers.  No counterpart in the reference (whose MATLAB loop allocates as it goes).
+ *
+ * The call allocates nothing: no cudaMalloc / cudaFree, no pinned host memory, no
+ * streams or events, no heap memory on the host.  The caller passes the inputs
+ * (problem, host tables) and the output: hist_device, a DEVICE buffer of
+ * problem->hist_len int64 on the current device, which the call zeroes and fills.  The
+ * staged tables, edges, counters and the time-major observation-index array (the
+ * scratch of the index path, folded slice by slice as in rtmc_forward) live in one
+ * file-scope __device__ array of RTMC_STATIC_SCRATCH_BYTES that every GPU loading the
+ * library holds until exit; particles run in as many chunks as that array requires.
+ * Problems whose tables, edges and one chunk of 32 particles do not fit are rejected
+ * with RTMC_ERR_ARG and a message giving the sizes.
+ *
+ * The first call on a device looks the array up (cudaGetSymbolAddress with that device
+ * current); make that first call before any stream capture.  stream may be NULL (the
+ * legacy default stream); the call returns after the stream has finished its work.
+ * All calls share the one array and it keeps the last call's contents (the call clears
+ * what must start at zero): calls that overlap on the GPU, from several host threads or
+ * streams, race and must be serialised by the caller. */
+int rtmc_forward_noalloc(const rtmc_problem *problem, const rtmc_tables *tables, int64_t *hist_device,
+                         void *stream, rtmc_stats *stats);
+
 /* pinned host memory for fast copies (cudaMallocHost); free with rtmc_host_free */
 int rtmc_host_alloc(int64_t bytes, void **out);
 int rtmc_host_free(void *p);

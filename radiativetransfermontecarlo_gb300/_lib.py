@@ -83,6 +83,7 @@ SIGNATURES = {
                                      C.POINTER(RtmcStats)]),
     "rtmc_forward_device": (C.c_int, [_P, C.POINTER(RtmcProblem), _P, C.POINTER(RtmcStats)]),
     "rtmc_copy_histogram": (C.c_int, [_P, C.POINTER(C.c_int64), C.c_int64]),
+    "rtmc_forward_noalloc": (C.c_int, [C.POINTER(RtmcProblem), _P, C.c_void_p, C.c_void_p, C.POINTER(RtmcStats)]),
     "rtmc_host_alloc": (C.c_int, [C.c_int64, C.POINTER(_P)]),
     "rtmc_host_free": (C.c_int, [_P]),
     "rtmc_flush_l2": (C.c_int, [_P]),

@@ -179,9 +179,9 @@ int check_problem(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t
     return RTMC_OK;
 }
 
-template <typename R>
+template <typename R, typename Vec>
 void fill_params(rtmc_context *ctx, const rtmc_problem *P, const DevTables<R> &tab, DevParams<R> *p, int *n_edges_out,
-                 std::vector<R> *edges, std::vector<R> *zoe)
+                 Vec *edges, Vec *zoe)
 {
     std::memset(p, 0, sizeof *p);
     p->d = P->d; p->frame = P->frame; p->acoustics = P->acoustics; p->src_dir = P->src_dir;
@@ -467,6 +467,212 @@ int forward(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int6
                                      : run<float>(ctx, P, t, host_out, st, trace_out);
 }
 
+// ---- rtmc_forward_noalloc: everything staged in the static device scratch ----------
+
+// fixed-capacity vector on the stack (fill_params' edge and Zoeppritz lists)
+template <typename R, int N> struct StackVec {
+    R v[N];
+    size_t n = 0;
+    void clear() { n = 0; }
+    void push_back(R x) { if (n < (size_t)N) v[n++] = x; }
+    void resize(size_t k) { n = k < (size_t)N ? k : (size_t)N; }
+    size_t size() const { return n; }
+    R &operator[](size_t i) { return v[i]; }
+    R *data() { return v; }
+};
+
+// host -> device copy from a stack buffer that is reused right after
+template <typename T> int copy_chunk(unsigned char *dst, const T *src, size_t count, cudaStream_t st)
+{
+    cudaError_t e = cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    return (int)e;
+}
+
+// same layout as upload_tables (knots, angle/pi, slope/pi, guide), written in chunks
+template <typename R>
+int stage_tables_static(const rtmc_tables *t, unsigned char *base, size_t cap, size_t *used, DevTables<R> *dt,
+                        cudaStream_t st, std::string *err)
+{
+    const int G = kGuideN;
+    size_t off[4][4], total = 0;
+    for (int i = 0; i < t->n_tables; ++i) {
+        const size_t n = t->cdf[i].size();
+        off[i][0] = total; total = align_up(total + n * sizeof(double), 256);
+        off[i][1] = total; total = align_up(total + n * sizeof(R), 256);
+        off[i][2] = total; total = align_up(total + n * sizeof(R), 256);
+        off[i][3] = total; total = align_up(total + (size_t)(G + 1) * sizeof(int32_t), 256);
+    }
+    if (total > cap)
+        return fail(err, RTMC_ERR_ARG, "rtmc_forward_noalloc: the tables need " + std::to_string(total) +
+                                            " bytes, more than the static scratch of " + std::to_string(cap) + " bytes");
+    constexpr size_t B = 4096; // staging chunk on the stack
+    R buf[B];
+    int32_t gbuf[B];
+    const double ip = 1.0 / M_PI;
+    for (int i = 0; i < t->n_tables; ++i) {
+        const std::vector<double> &c = t->cdf[i], &th = t->theta[i];
+        const size_t n = c.size();
+        int e = (int)cudaMemcpyAsync(base + off[i][0], c.data(), n * sizeof(double), cudaMemcpyHostToDevice, st);
+        if (e) return e;
+        for (size_t k0 = 0; k0 < n; k0 += B) {
+            const size_t m = std::min(B, n - k0);
+            for (size_t k = 0; k < m; ++k) buf[k] = (R)(th[k0 + k] * ip);
+            if ((e = copy_chunk(base + off[i][1] + k0 * sizeof(R), buf, m, st))) return e;
+            for (size_t k = 0; k < m; ++k) {
+                const size_t q = k0 + k;
+                buf[k] = (q + 1 < n) ? (R)((th[q + 1] - th[q]) * ip / (c[q + 1] - c[q])) : (R)0;
+            }
+            if ((e = copy_chunk(base + off[i][2] + k0 * sizeof(R), buf, m, st))) return e;
+        }
+        size_t k = 0;
+        for (int j0 = 0; j0 <= G; j0 += (int)B) {
+            const int m = std::min((int)B, G + 1 - j0);
+            for (int jj = 0; jj < m; ++jj) {
+                const double target = (double)(j0 + jj) / (double)G;
+                while (k + 1 <= n - 2 && c[k + 1] <= target) ++k;
+                gbuf[jj] = (int32_t)k;
+            }
+            if ((e = copy_chunk(base + off[i][3] + (size_t)j0 * sizeof(int32_t), gbuf, (size_t)m, st))) return e;
+        }
+        dt->cdf[i] = reinterpret_cast<const double *>(base + off[i][0]);
+        dt->theta[i] = reinterpret_cast<const R *>(base + off[i][1]);
+        dt->slope[i] = reinterpret_cast<const R *>(base + off[i][2]);
+        dt->guide[i] = reinterpret_cast<const int32_t *>(base + off[i][3]);
+        dt->n[i] = (int32_t)n;
+    }
+    *used = total;
+    return RTMC_OK;
+}
+
+template <typename R>
+int forward_noalloc(const rtmc_problem *P, const rtmc_tables *t, int64_t *d_hist, cudaStream_t st, rtmc_stats *stats)
+{
+    rtmc_context slot; // error slot for check_problem; owns no device resources
+    int s = check_problem(&slot, P, t);
+    if (s) return fail(nullptr, s, slot.err);
+    std::string err;
+    int dev = 0, sms = 0, smem_optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess) return fail(nullptr, RTMC_ERR_CUDA, std::string("rtmc_forward_noalloc: ") + cudaGetErrorString(e));
+    unsigned char *base = nullptr;
+    size_t cap = 0;
+    if ((s = static_scratch(dev, &base, &cap)) != 0)
+        return fail(nullptr, RTMC_ERR_CUDA, std::string("rtmc_forward_noalloc: static scratch lookup: ") +
+                                                cudaGetErrorString((cudaError_t)s));
+    const int prec = sizeof(R) == 4 ? RTMC_FP32 : RTMC_FP64;
+    DevTables<R> dt{};
+    size_t used = 0;
+    if ((s = stage_tables_static<R>(t, base, cap, &used, &dt, st, &err)) != 0)
+        return s == RTMC_ERR_ARG ? fail(nullptr, s, err) : fail(nullptr, RTMC_ERR_CUDA, "rtmc_forward_noalloc: table staging");
+    DevParams<R> p;
+    StackVec<R, kMaxEdges> edges;
+    StackVec<R, kMaxEdges> zoe; // same type as the edge list (2 x 181 values used)
+    int n_edges = 0;
+    fill_params<R>(&slot, P, dt, &p, &n_edges, &edges, &zoe);
+    const size_t e_off = align_up(used, 256);
+    const size_t z_off = align_up(e_off + std::max<size_t>(1, edges.size()) * sizeof(R), 256);
+    const size_t c_off = align_up(z_off + zoe.size() * sizeof(R), 256);
+    const size_t i_off = align_up(c_off + 256, 256);
+    const int64_t rows = i_off < cap ? (int64_t)((cap - i_off) / (4 * (size_t)P->n_obs)) / 32 * 32 : 0;
+    if (rows < 32)
+        return fail(nullptr, RTMC_ERR_ARG, "rtmc_forward_noalloc: tables, edges and 32 particles x " +
+                                               std::to_string(P->n_obs) + " observations need more than the static scratch of " +
+                                               std::to_string(cap) + " bytes");
+    if (P->time_stride >= ((int64_t)1 << 30))
+        return fail(nullptr, RTMC_ERR_ARG, "rtmc_forward_noalloc: a time slice must hold fewer than 2^30 bins");
+    if (edges.size() && (s = copy_chunk(base + e_off, edges.data(), edges.size(), st)) != 0)
+        return fail(nullptr, RTMC_ERR_CUDA, "rtmc_forward_noalloc: edge staging");
+    if ((s = copy_chunk(base + z_off, zoe.data(), zoe.size(), st)) != 0)
+        return fail(nullptr, RTMC_ERR_CUDA, "rtmc_forward_noalloc: Zoeppritz staging");
+    e = cudaMemsetAsync(d_hist, 0, (size_t)P->hist_len * sizeof(int64_t), st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(base + c_off, 0, 256, st);
+    if (e != cudaSuccess) return fail(nullptr, RTMC_ERR_CUDA, std::string("rtmc_forward_noalloc: ") + cudaGetErrorString(e));
+    p.edges = reinterpret_cast<const R *>(base + e_off);
+    p.zoe = reinterpret_cast<const R *>(base + z_off);
+    p.hist = reinterpret_cast<unsigned long long *>(d_hist);
+    p.stats = reinterpret_cast<unsigned long long *>(base + c_off);
+    p.status = reinterpret_cast<int32_t *>(base + c_off + 128);
+    p.trace = nullptr;
+    p.sink = kSinkIndex;
+    p.ring_cap = sizeof(R) == 4 ? 8 : 6;
+    p.obs_idx = reinterpret_cast<int32_t *>(base + i_off);
+    const int64_t chunk = std::min<int64_t>(std::max<int64_t>(P->n_particles, 1), rows);
+    p.obs_rows = chunk;
+    int block = 256;
+    const int mt = transport_max_threads(prec, kSinkIndex, p.obs_kind);
+    if (mt > 0 && block > mt) block = mt - mt % 32;
+    const size_t seg_bytes = 6 * sizeof(R) + 2 * sizeof(int32_t);
+    const size_t smem = align_up((size_t)n_edges * sizeof(R), 16) + (size_t)block * p.ring_cap * seg_bytes;
+    int bps = 0;
+    if (transport_set_smem(prec, kSinkIndex, p.obs_kind, smem) != 0 ||
+        transport_occupancy(prec, kSinkIndex, p.obs_kind, block, smem, &bps) != 0 || bps < 1)
+        return fail(nullptr, RTMC_ERR_CUDA, "rtmc_forward_noalloc: transport kernel does not fit on the device");
+    const int64_t grid = std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * bps, (chunk + block - 1) / block));
+    BinParams bp{};
+    bp.idx = p.obs_idx;
+    bp.rows = chunk;
+    bp.n_obs = P->n_obs;
+    bp.n_modes = P->acoustics ? 1 : 2;
+    bp.slice_bins = (int32_t)P->time_stride;
+    bp.time_stride = P->time_stride;
+    bp.mode_stride = P->mode_stride;
+    bp.hist_shift = P->hist_shift;
+    bp.hist = p.hist;
+    const size_t slice_bytes = (size_t)P->time_stride * bp.n_modes * sizeof(uint32_t);
+    const int group = (int)std::min<size_t>((size_t)P->n_obs, (size_t)(200 << 10) / std::max<size_t>(slice_bytes, 1));
+    size_t fold_smem = 0;
+    int fold_grid = 1;
+    if (group >= 8) {
+        bp.group = group;
+        fold_smem = (size_t)group * slice_bytes;
+        if (bin_slices_set_smem(fold_smem) != 0) return fail(nullptr, RTMC_ERR_CUDA, "rtmc_forward_noalloc: fold attributes");
+        const int ngroups = (P->n_obs + group - 1) / group;
+        fold_grid = (int)std::max<int64_t>(1, (2 * sms + ngroups - 1) / ngroups);
+    } else {
+        fold_grid = (int)std::max<int64_t>(1, std::min<int64_t>((chunk + 255) / 256, 2 * sms));
+    }
+    int launches = 0;
+    for (int64_t b0 = 0; b0 < P->n_particles; b0 += chunk) {
+        DevParams<R> q = p;
+        q.pid0 = P->pid0 + b0;
+        q.n_particles = std::min<int64_t>(chunk, P->n_particles - b0);
+        int le;
+        if constexpr (sizeof(R) == 4) le = launch_transport_f32(q, (int)grid, block, smem, st);
+        else le = launch_transport_f64(q, (int)grid, block, smem, st);
+        if (le) return fail(nullptr, RTMC_ERR_CUDA, std::string("rtmc_forward_noalloc: ") + cudaGetErrorString((cudaError_t)le));
+        BinParams b = bp;
+        b.n = q.n_particles;
+        if (b.group) b.part_per_block = (b.n + fold_grid - 1) / fold_grid;
+        if ((le = launch_bin_slices(b, fold_grid, fold_smem, st)) != 0)
+            return fail(nullptr, RTMC_ERR_CUDA, std::string("rtmc_forward_noalloc: ") + cudaGetErrorString((cudaError_t)le));
+        launches += 2;
+    }
+    int64_t dstats[32];
+    e = cudaMemcpyAsync(dstats, base + c_off, 256, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return fail(nullptr, RTMC_ERR_CUDA, std::string("rtmc_forward_noalloc: ") + cudaGetErrorString(e));
+    const int32_t status = (int32_t)(dstats[16] & 0xffffffff);
+    if (stats) {
+        std::memset(stats, 0, sizeof *stats);
+        stats->scatter_events = dstats[0];
+        stats->boundary_hits = dstats[1];
+        stats->kills = dstats[2];
+        stats->absorbed = dstats[3];
+        stats->observations = dstats[4];
+        stats->conversions = dstats[5];
+        stats->device_status = status;
+        stats->launches = launches;
+        stats->sink = kSinkIndex;
+        stats->h2d_bytes = (double)used + (double)(edges.size() + zoe.size()) * sizeof(R);
+        stats->d2h_bytes = 256;
+    }
+    if (status) return fail(nullptr, RTMC_ERR_DEVICE, "rtmc_forward_noalloc: a transport guard tripped");
+    return RTMC_OK;
+}
+
 } // namespace
 
 extern "C" int32_t rtmc_abi_version(void) { return RTMC_ABI_VERSION; }
@@ -564,6 +770,15 @@ extern "C" int rtmc_copy_histogram(rtmc_context *ctx, int64_t *hist_out, int64_t
     CK(cudaMemcpyAsync(hist_out, ctx->hist.p, (size_t)n * 8, cudaMemcpyDeviceToHost, ctx->stream), "histogram copy");
     CK(cudaStreamSynchronize(ctx->stream), "histogram copy");
     return RTMC_OK;
+}
+
+extern "C" int rtmc_forward_noalloc(const rtmc_problem *P, const rtmc_tables *t, int64_t *hist_device, void *stream,
+                                    rtmc_stats *stats)
+{
+    if (!P || !t || !hist_device) return fail(nullptr, RTMC_ERR_ARG, "rtmc_forward_noalloc: NULL argument");
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    return P->precision == RTMC_FP64 ? forward_noalloc<double>(P, t, hist_device, st, stats)
+                                     : forward_noalloc<float>(P, t, hist_device, st, stats);
 }
 
 extern "C" int rtmc_host_alloc(int64_t bytes, void **out)

@@ -101,6 +101,8 @@ int transport_set_smem(int precision, int sink, int obs, size_t smem);
 int transport_max_threads(int precision, int sink, int obs);
 int launch_bin_slices(const BinParams &b, int grid_x, size_t smem, void *stream);
 int bin_slices_set_smem(size_t smem);
+// device address of the static scratch of rtmc_forward_noalloc (noalloc.cu); device current
+int static_scratch(int device, unsigned char **ptr, size_t *bytes);
 enum { kSinkSmem = 0, kSinkGlobal = 1, kSinkIndex = 2 };
 
 } // namespace rtmc
