@@ -63,6 +63,10 @@ def load():
         lib.oracle_invcdf.restype = C.c_double
         lib.oracle_invcdf.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int64, C.c_double]
         lib.oracle_max_threads.restype = C.c_int
+        lib.oracle_reflect.restype = C.c_int
+        lib.oracle_reflect.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_double, C.c_double, C.c_int,
+                                       C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                       C.POINTER(C.c_int32), C.POINTER(C.c_double)]
         _lib = lib
     return _lib
 
@@ -140,6 +144,21 @@ def run(prob, knots, scheme: str = "event", u24: bool | None = None, nthreads: i
     if rc:
         raise RuntimeError(f"oracle_run failed ({rc})")
     return hist, dict(zip(ST_NAMES, map(int, stats[:6]))), fs
+
+
+def reflect(zoe_rpp, zoe_rsvsv, vp, vs, k, d, q, mode, u):
+    """Elastic reflection of n particles at the plane normal to e_k (test entry of the oracle)."""
+    d = np.ascontiguousarray(d, dtype=np.float64).copy()
+    q = np.ascontiguousarray(q, dtype=np.float64).copy()
+    mode = np.ascontiguousarray(mode, dtype=np.int32).copy()
+    zr = np.ascontiguousarray(zoe_rpp, dtype=np.float64)
+    zs = np.ascontiguousarray(zoe_rsvsv, dtype=np.float64)
+    u = np.ascontiguousarray(u, dtype=np.float64)
+    rc = load().oracle_reflect(_dp(zr), _dp(zs), vp, vs, k, len(mode), _dp(d), _dp(q),
+                               mode.ctypes.data_as(C.POINTER(C.c_int32)), _dp(u))
+    if rc:
+        raise RuntimeError("oracle_reflect failed")
+    return d, q, mode
 
 
 def table_knots(tables) -> list:

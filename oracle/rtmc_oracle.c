@@ -677,3 +677,33 @@ int oracle_max_threads(void)
     return 1;
 #endif
 }
+
+/* Test entry: the elastic plane reflection (MaterialInterface decisions + the updates of
+ * propagateParticleSmallDt.m:197-321) applied to n particles at the plane normal to
+ * e_k, with draws u[2i] (SV/SH split) and u[2i+1] (reflection coin).  d, q are n x 3,
+ * updated in place with mode.  Restates the energy-partition experiment of
+ * Examples/BoundaryReflectionEnergyTests.m:110-193 without volume scattering. */
+int oracle_reflect(const double *zoe_rpp, const double *zoe_rsvsv, double vp, double vs, int k, int64_t n,
+                   double *d, double *q, int32_t *mode, const double *u)
+{
+    if (k < 0 || k > 2 || n < 0) return 1;
+    oracle_problem P;
+    memset(&P, 0, sizeof P);
+    P.v[0] = vp;
+    P.v[1] = vs;
+    P.zoe_rpp = zoe_rpp;
+    P.zoe_rsvsv = zoe_rsvsv;
+    int64_t stats[ST_N];
+    for (int64_t i = 0; i < n; ++i) {
+        particle_t pt;
+        memcpy(pt.d, d + 3 * i, sizeof pt.d);
+        memcpy(pt.q, q + 3 * i, sizeof pt.q);
+        pt.mode = mode[i];
+        pt.alive = 1;
+        elastic_plane_reflect(&P, &pt, k, u[2 * i], u[2 * i + 1], stats);
+        memcpy(d + 3 * i, pt.d, sizeof pt.d);
+        memcpy(q + 3 * i, pt.q, sizeof pt.q);
+        mode[i] = pt.mode;
+    }
+    return 0;
+}

@@ -71,7 +71,8 @@ def initialize_observation(geometry: dict, acoustics: bool, observation: dict, N
     t = np.concatenate([[0.0], np.setdiff1d(time, [0.0])])
     Nt = t.size
     binX = np.atleast_1d(np.asarray(observation["x"], dtype=float))
-    x = (binX[:-1] + binX[1:]) / 2
+    with np.errstate(invalid="ignore"):  # centres of [-Inf Inf] are NaN, as in MATLAB
+        x = (binX[:-1] + binX[1:]) / 2
     Nx = x.size
     dx = np.diff(binX)
     if frame == "cartesian":
@@ -85,14 +86,16 @@ def initialize_observation(geometry: dict, acoustics: bool, observation: dict, N
         binZ = np.array([-np.pi / 2, np.pi / 2])
     if observation.get("y") is not None and np.size(observation["y"]) > 0:
         binY = np.atleast_1d(np.asarray(observation["y"], dtype=float))
-    y = (binY[:-1] + binY[1:]) / 2
+    with np.errstate(invalid="ignore"):
+        y = (binY[:-1] + binY[1:]) / 2
     Ny = y.size
     dy = np.diff(binY)
     if d == 3 and observation.get("z") is not None and np.size(observation["z"]) > 0:
         binZ = np.atleast_1d(np.asarray(observation["z"], dtype=float))
     if d == 3 and frame == "spherical":
         binZ = np.sin(binZ)
-    z = (binZ[:-1] + binZ[1:]) / 2
+    with np.errstate(invalid="ignore"):
+        z = (binZ[:-1] + binZ[1:]) / 2
     Nz = z.size
     dz = np.diff(binZ)
     if observation.get("directions") is not None and np.size(observation["directions"]) > 0:

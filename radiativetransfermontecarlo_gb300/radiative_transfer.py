@@ -172,10 +172,10 @@ def build_problem(geometry: dict, source: dict, material: MaterialClass, observa
     frame = geometry["frame"]
     modes = list(grid.axis_mode)
     for a in range(4):
-        if modes[a] == _lib.AXIS_RANGE:
-            e = grid.edges[a]
-            if natural_range_covered(frame, d, a, float(e[0]), float(e[-1])):
-                modes[a] = _lib.AXIS_IGNORED
+        e = grid.edges[a]
+        one_bin = modes[a] == _lib.AXIS_BINNED and e.size == 2  # a single bin: index 0 always
+        if (modes[a] == _lib.AXIS_RANGE or one_bin) and natural_range_covered(frame, d, a, float(e[0]), float(e[-1])):
+            modes[a] = _lib.AXIS_IGNORED
     prob = TransportProblem(
         d=d, frame=_lib.FRAME[frame], acoustics=acoustics,
         precision=_lib.FP64 if opt["precision"] == "fp64" else _lib.FP32,
