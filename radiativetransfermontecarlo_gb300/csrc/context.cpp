@@ -384,7 +384,8 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
             fold_grid = (int)ranges;
         } else {
             bp.group = 0;
-            fold_grid = (int)std::max<int64_t>(1, std::min<int64_t>((chunk + 255) / 256, 2 * ctx->num_sms));
+            // chunks of at least 8 vectors per thread of a 512-thread block, up to one block per SM per slice
+            fold_grid = (int)std::max<int64_t>(1, std::min<int64_t>((chunk + 16383) / 16384, ctx->num_sms));
         }
         p.obs_idx = static_cast<int32_t *>(ctx->idx.p);
         p.obs_rows = chunk;
@@ -632,7 +633,7 @@ int forward_noalloc(const rtmc_problem *P, const rtmc_tables *t, int64_t *d_hist
         const int ngroups = (P->n_obs + group - 1) / group;
         fold_grid = (int)std::max<int64_t>(1, (2 * sms + ngroups - 1) / ngroups);
     } else {
-        fold_grid = (int)std::max<int64_t>(1, std::min<int64_t>((chunk + 255) / 256, 2 * sms));
+        fold_grid = (int)std::max<int64_t>(1, std::min<int64_t>((chunk + 16383) / 16384, sms));
     }
     int launches = 0;
     for (int64_t b0 = 0; b0 < P->n_particles; b0 += chunk) {

@@ -804,29 +804,106 @@ __global__ void __launch_bounds__(Bounds<R, SINK>::threads, Bounds<R, SINK>::min
 }
 
 // Fold the dense index array into the histogram, one time slice at a time: blockIdx.y
-// is the slice (so the L2 holds the slice being written), blockIdx.x strides over the
-// particles of the chunk.
-__global__ void __launch_bounds__(256) rt_bin_slices(const BinParams b)
+// is the slice (so the L2 holds the slice being written), blockIdx.x a contiguous chunk
+// of the slice's entries.  While particles crowd a few bins (early times) many entries
+// of a chunk share a bin, and 64-bit reductions on the same L2 lines serialise; entries
+// therefore go into a shared-memory hash table (bin -> count) of the block, which sends
+// one atomic per distinct bin to the L2 at the end.  A probe window decides: unless its
+// entries crowd into few bins (at most a quarter of the table, each hit twice on
+// average) the rest of the chunk goes straight to the L2; a crowded chunk keeps using
+// the table until it is three quarters full.
+constexpr int kFoldThreads = 512;
+constexpr int kHashSlots = 4096;
+
+__device__ __forceinline__ bool hash_insert(int *keys, unsigned *cnts, int *used, int v)
 {
+    unsigned h = ((unsigned)v * 2654435761u) >> (32 - 12); // 12 = log2(kHashSlots)
+#pragma unroll 1
+    for (int probe = 0; probe < 8; ++probe) {
+        int k = *((volatile int *)keys + h);
+        if (k == -1) {
+            k = atomicCAS(keys + h, -1, v);
+            if (k == -1) atomicAdd(used, 1);
+        }
+        if (k == -1 || k == v) {
+            atomicAdd(cnts + h, 1u);
+            return true;
+        }
+        h = (h + 1) & (kHashSlots - 1);
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(kFoldThreads) rt_bin_slices(const BinParams b)
+{
+    __shared__ int keys[kHashSlots];
+    __shared__ unsigned cnts[kHashSlots];
+    __shared__ int used, valid, dense;
     const int j = blockIdx.y + 1;
     const int32_t *row = b.idx + (int64_t)(j - 1) * b.rows; // rows is a multiple of 32: 16-byte aligned
     unsigned long long *slice = b.hist + (int64_t)j * b.time_stride;
     const unsigned long long inc = 1ull << b.hist_shift;
+    for (int k = threadIdx.x; k < kHashSlots; k += blockDim.x) { keys[k] = -1; cnts[k] = 0u; }
+    if (threadIdx.x == 0) { used = 0; valid = 0; }
+    // this block's chunk of the slice, in 16-byte vectors
     const int64_t n4 = (b.n + 3) >> 2;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t per = (n4 + gridDim.x - 1) / gridDim.x;
+    const int64_t q0 = (int64_t)blockIdx.x * per, q1 = min(n4, q0 + per);
     const int4 *row4 = reinterpret_cast<const int4 *>(row);
-    // two 16-byte loads in flight per thread before their atomics
-    for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n4; k += 2 * stride) {
-        const int64_t k2 = k + stride;
-        const int4 a = __ldcs(row4 + k);
-        const int4 c = k2 < n4 ? __ldcs(row4 + k2) : make_int4(-1, -1, -1, -1);
-        const int va[8] = {a.x, a.y, a.z, a.w, c.x, c.y, c.z, c.w};
+    __syncthreads();
+    // probe window: one vector per thread through the table
+    int64_t q = q0 + threadIdx.x;
+    if (q < q1) {
+        const int4 a = __ldcs(row4 + q);
+        const int va[4] = {a.x, a.y, a.z, a.w};
+        int nv = 0;
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-            const int64_t e = (u < 4 ? k : k2) * 4 + (u & 3);
+        for (int u = 0; u < 4; ++u) {
             const int v = va[u];
-            if (v >= 0 && e < b.n) atomicAdd(slice + ((v >> 30) ? b.mode_stride : 0) + (v & 0x3fffffff), inc);
+            if (v < 0 || q * 4 + u >= b.n) continue;
+            ++nv;
+            if (!hash_insert(keys, cnts, &used, v))
+                atomicAdd(slice + ((v >> 30) ? b.mode_stride : 0) + (v & 0x3fffffff), inc);
         }
+        if (nv) atomicAdd(&valid, nv);
+    }
+    __syncthreads();
+    // crowded: the window's entries fell in at most a quarter of the table, with every
+    // bin hit twice on average
+    if (threadIdx.x == 0) dense = valid >= 64 && used * 4 <= kHashSlots && used * 2 <= valid;
+    __syncthreads();
+    if (dense) {
+        for (q += blockDim.x; q < q1; q += blockDim.x) {
+            const int4 a = __ldcs(row4 + q);
+            const int va[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int v = va[u];
+                if (v < 0 || q * 4 + u >= b.n) continue;
+                // a table three-quarters full takes no new bins
+                if (*((volatile int *)&used) >= 3 * kHashSlots / 4 || !hash_insert(keys, cnts, &used, v))
+                    atomicAdd(slice + ((v >> 30) ? b.mode_stride : 0) + (v & 0x3fffffff), inc);
+            }
+        }
+    } else {
+        // two 16-byte loads in flight per thread before their atomics
+        for (q += blockDim.x; q < q1; q += 2 * blockDim.x) {
+            const int64_t q2 = q + blockDim.x;
+            const int4 a = __ldcs(row4 + q);
+            const int4 c = q2 < q1 ? __ldcs(row4 + q2) : make_int4(-1, -1, -1, -1);
+            const int va[8] = {a.x, a.y, a.z, a.w, c.x, c.y, c.z, c.w};
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int v = va[u];
+                const int64_t e = (u < 4 ? q : q2) * 4 + (u & 3);
+                if (v >= 0 && e < b.n) atomicAdd(slice + ((v >> 30) ? b.mode_stride : 0) + (v & 0x3fffffff), inc);
+            }
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < kHashSlots; k += blockDim.x) {
+        const int v = keys[k];
+        if (v >= 0) atomicAdd(slice + ((v >> 30) ? b.mode_stride : 0) + (v & 0x3fffffff), (unsigned long long)cnts[k] << b.hist_shift);
     }
 }
 
@@ -907,7 +984,7 @@ int launch_bin_slices(const BinParams &b, int grid_x, size_t smem, void *stream)
         rt_bin_slices_smem<<<g, 512, smem, (cudaStream_t)stream>>>(b);
     } else {
         dim3 g(grid_x, b.n_obs);
-        rt_bin_slices<<<g, 256, 0, (cudaStream_t)stream>>>(b);
+        rt_bin_slices<<<g, kFoldThreads, 0, (cudaStream_t)stream>>>(b);
     }
     return (int)cudaGetLastError();
 }
