@@ -741,32 +741,29 @@ __global__ void __launch_bounds__(Bounds<R, SINK>::threads, Bounds<R, SINK>::min
                     if (nw == 0) break;
                 }
             }
-            // ---- phase 2: nw observations per lane
+            // ---- phase 2: nw observations per lane, two at a time (independent chains)
             const int obs_limit = s.alive ? 0x7fffffff : s.s_death;
             int next_start = count > 0 ? ring.start(head) : 0x7fffffff;
             int so = jn * p.n_sub;
-            for (unsigned w = 0; w < nw; ++w, ++jn, so += p.n_sub) {
-                int v = -1;
-                if (so < obs_limit) {
-                    if (so >= next_start) {
-                        do {
-                            ring.get(head, cur);
-                            head = (head + 1) % C;
-                            --count;
-                        } while (count > 0 && ring.start(head) <= so);
-                        seg_prepare<R, OBS>(p, sedges, cur);
-                        next_start = count > 0 ? ring.start(head) : 0x7fffffff;
-                    }
-                    v = obs_offset<R, OBS>(p, sedges, cur, so);
-                }
+            // make cur the segment in force at sub-step at
+            auto advance = [&](int at) {
+                do {
+                    ring.get(head, cur);
+                    head = (head + 1) % C;
+                    --count;
+                } while (count > 0 && ring.start(head) <= at);
+                seg_prepare<R, OBS>(p, sedges, cur);
+                next_start = count > 0 ? ring.start(head) : 0x7fffffff;
+            };
+            auto emit = [&](int v, int mode, int j) {
                 if (SINK == SINK_INDEX) {
                     if (have) {
-                        *optr = v < 0 ? -1 : (v | (cur.mode << 30));
+                        *optr = v < 0 ? -1 : (v | (mode << 30));
                         optr += p.obs_rows;
                     }
                     if (v >= 0) cnt.obs++;
                 } else if (v >= 0) {
-                    const int64_t idx = (int64_t)jn * p.time_stride + (cur.mode ? p.mode_stride : 0) + v;
+                    const int64_t idx = (int64_t)j * p.time_stride + (mode ? p.mode_stride : 0) + v;
                     if (idx < p.hist_len) {
                         cnt.obs++;
                         if (SMEM) atomicAdd(shist + idx, 1u);
@@ -775,6 +772,34 @@ __global__ void __launch_bounds__(Bounds<R, SINK>::threads, Bounds<R, SINK>::min
                         bad = true;
                     }
                 }
+            };
+            unsigned w = 0;
+            for (; w + 1 < nw; w += 2, jn += 2, so += 2 * p.n_sub) {
+                const int so1 = so + p.n_sub;
+                int v0 = -1, v1 = -1, m0 = cur.mode, m1 = cur.mode;
+                if (so < obs_limit) {
+                    if (so >= next_start) advance(so);
+                    m0 = m1 = cur.mode;
+                    v0 = obs_offset<R, OBS>(p, sedges, cur, so);
+                    if (so1 < obs_limit) {
+                        if (so1 >= next_start) {
+                            advance(so1);
+                            m1 = cur.mode;
+                        }
+                        v1 = obs_offset<R, OBS>(p, sedges, cur, so1);
+                    }
+                }
+                emit(v0, m0, jn);
+                emit(v1, m1, jn + 1);
+            }
+            if (w < nw) {
+                int v = -1;
+                if (so < obs_limit) {
+                    if (so >= next_start) advance(so);
+                    v = obs_offset<R, OBS>(p, sedges, cur, so);
+                }
+                emit(v, cur.mode, jn);
+                ++jn;
             }
         }
         if (have && p.trace) { // final state of the particle, the oracle's layout
