@@ -201,6 +201,35 @@ int rtmc_copy_histogram(rtmc_context *ctx, int64_t *hist_out, int64_t n);
 int rtmc_forward_trace(rtmc_context *ctx, const rtmc_problem *problem, const rtmc_tables *tables,
                        int64_t *hist_out, double *state_out, rtmc_stats *stats);
 
+/* ---------------------------------------------------------------------------------- */
+/* Batched runs: many independent problems in one persistent, CUDA-graph launch        */
+/* ---------------------------------------------------------------------------------- */
+
+typedef struct rtmc_batch rtmc_batch;
+
+/* Stage n problems that share one observation grid (dimension, frame, acoustics,
+ * precision, observation instants, axes, edges, strides, histogram length and shift;
+ * the histogram must fit in shared memory, as the spherical 120 x 251 grid does) with
+ * their own materials, tables, particle counts and seeds.  The tables and parameters go
+ * to the device once; the launch (histogram clear + persistent kernel) is captured in a
+ * CUDA graph.  Replaces n calls of radiativeTransfer (a parameter sweep driving
+ * radiativeTransfer.m in a loop). */
+int rtmc_batch_create(rtmc_context *ctx, int32_t n, const rtmc_problem *problems, const rtmc_tables *const *tables,
+                      rtmc_batch **out);
+
+/* Launch shape (0 = automatic): threads per block, ring capacity, particles per work
+ * item.  Rebuilds the work list and the graph, keeps the staged tables. */
+int rtmc_batch_set_launch(rtmc_batch *batch, int32_t block, int32_t ring_cap, int64_t chunk);
+
+/* One replay of the graph; histograms stay on the device.  stats sums all instances. */
+int rtmc_batch_run(rtmc_batch *batch, rtmc_stats *stats);
+
+/* Copies the int64 histograms of instances [first, first + count) into out (host),
+ * instance-major, hist_len each. */
+int rtmc_batch_histograms(rtmc_batch *batch, int32_t first, int32_t count, int64_t *out);
+
+void rtmc_batch_destroy(rtmc_batch *batch);
+
 /* Size of the static device scratch of rtmc_forward_noalloc (96 MB per GPU). */
 #define RTMC_STATIC_SCRATCH_BYTES (96u << 20)
 

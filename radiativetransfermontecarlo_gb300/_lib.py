@@ -89,6 +89,11 @@ SIGNATURES = {
     "rtmc_flush_l2": (C.c_int, [_P]),
     "rtmc_set_table_cache": (C.c_int, [_P, C.c_int32]),
     "rtmc_set_launch": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32]),
+    "rtmc_batch_create": (C.c_int, [_P, C.c_int32, C.POINTER(RtmcProblem), C.POINTER(_P), C.POINTER(_P)]),
+    "rtmc_batch_set_launch": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int64]),
+    "rtmc_batch_run": (C.c_int, [_P, C.POINTER(RtmcStats)]),
+    "rtmc_batch_histograms": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_int64)]),
+    "rtmc_batch_destroy": (None, [_P]),
     "rtmc_last_timing": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
 }
 

@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <numeric>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -832,4 +833,310 @@ extern "C" int rtmc_last_timing(const rtmc_context *ctx, double *kernel_ms, int3
     if (kernel_ms) *kernel_ms = ctx->last_kernel_ms;
     if (launches) *launches = ctx->last_launches;
     return RTMC_OK;
+}
+
+// ---- batched runs ----------------------------------------------------------------
+
+struct rtmc_batch {
+    rtmc_context *ctx = nullptr;
+    int n = 0, prec = RTMC_FP32, obs_kind = 0, n_obs = 0;
+    int block = 0, ring = 0, grid = 0, n_items = 0;
+    int64_t chunk = 0, hist_len = 0;
+    size_t smem = 0;
+    DevBuf params, items, tabs, edges, hists, ctl;
+    std::vector<int64_t> n_part;
+    std::vector<double> cost_per_particle;
+    int n_edges = 0;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    void *args_host = nullptr; // BatchArgs<R>, kept alive for the graph's kernel node
+};
+
+namespace {
+
+bool same_grid(const rtmc_problem &a, const rtmc_problem &b)
+{
+    if (a.d != b.d || a.frame != b.frame || a.acoustics != b.acoustics || a.precision != b.precision ||
+        a.n_obs != b.n_obs || a.time_stride != b.time_stride || a.mode_stride != b.mode_stride ||
+        a.hist_len != b.hist_len || a.hist_shift != b.hist_shift)
+        return false;
+    for (int x = 0; x < 4; ++x) {
+        if (a.axis_mode[x] != b.axis_mode[x] || a.axis_stride[x] != b.axis_stride[x]) return false;
+        if (a.axis_mode[x] == RTMC_AXIS_IGNORED) continue;
+        if (a.axis_nedges[x] != b.axis_nedges[x]) return false;
+        for (int k = 0; k < a.axis_nedges[x]; ++k)
+            if (a.axis_edges[x][k] != b.axis_edges[x][k]) return false;
+    }
+    return true;
+}
+
+// per-table layout of the staged tables (knots, angle/pi, slope/pi, guide)
+template <typename R> size_t table_bytes(size_t n)
+{
+    return align_up(n * sizeof(double), 256) + 2 * align_up(n * sizeof(R), 256) +
+           align_up((size_t)(kGuideN + 1) * sizeof(int32_t), 256);
+}
+
+template <typename R> void stage_table(const std::vector<double> &c, const std::vector<double> &th, unsigned char *host,
+                                       unsigned char *dev, DevTables<R> *dt, int i)
+{
+    const size_t n = c.size();
+    size_t o = 0;
+    std::memcpy(host + o, c.data(), n * sizeof(double));
+    dt->cdf[i] = reinterpret_cast<const double *>(dev + o);
+    o += align_up(n * sizeof(double), 256);
+    R *rt = reinterpret_cast<R *>(host + o);
+    dt->theta[i] = reinterpret_cast<const R *>(dev + o);
+    o += align_up(n * sizeof(R), 256);
+    R *rs = reinterpret_cast<R *>(host + o);
+    dt->slope[i] = reinterpret_cast<const R *>(dev + o);
+    o += align_up(n * sizeof(R), 256);
+    const double ip = 1.0 / M_PI;
+    for (size_t k = 0; k < n; ++k) {
+        rt[k] = (R)(th[k] * ip);
+        rs[k] = (k + 1 < n) ? (R)((th[k + 1] - th[k]) * ip / (c[k + 1] - c[k])) : (R)0;
+    }
+    int32_t *g = reinterpret_cast<int32_t *>(host + o);
+    dt->guide[i] = reinterpret_cast<const int32_t *>(dev + o);
+    size_t k = 0;
+    for (int j = 0; j <= kGuideN; ++j) {
+        const double target = (double)j / (double)kGuideN;
+        while (k + 1 <= n - 2 && c[k + 1] <= target) ++k;
+        g[j] = (int32_t)k;
+    }
+    dt->n[i] = (int32_t)n;
+}
+
+template <typename R> int batch_build_graph(rtmc_batch *b)
+{
+    rtmc_context *ctx = b->ctx;
+    if (b->exec) { cudaGraphExecDestroy(b->exec); b->exec = nullptr; }
+    if (b->graph) { cudaGraphDestroy(b->graph); b->graph = nullptr; }
+    // launch shape
+    const size_t seg_bytes = 6 * sizeof(R) + 2 * sizeof(int32_t);
+    const size_t fixed = align_up((size_t)b->n_edges * sizeof(R), 16) + align_up((size_t)b->hist_len * 4, 16);
+    const size_t budget = (size_t)ctx->max_smem_optin - 1024 - sizeof(DevParams<R>) - 64;
+    int block = b->block ? b->block : 512;
+    if (block > 512) block = 512;
+    if (fixed + (size_t)block * 2 * seg_bytes > budget) block = 256;
+    if (fixed + (size_t)block * 2 * seg_bytes > budget)
+        return fail(&ctx->err, RTMC_ERR_ARG, "batched runs need a histogram that fits in shared memory");
+    int ring = b->ring ? b->ring : 8;
+    ring = std::min<int>(ring, (int)((budget - fixed) / ((size_t)block * seg_bytes)));
+    b->smem = fixed + (size_t)block * ring * seg_bytes;
+    int bps = 0;
+    if (transport_batch_setup(b->prec, b->obs_kind, block, b->smem, &bps) != 0 || bps < 1)
+        return fail(&ctx->err, RTMC_ERR_CUDA, "batched transport kernel does not fit on the device");
+    b->grid = ctx->num_sms * bps;
+    // work items: chunks of each instance, largest expected cost first
+    const int64_t chunk = b->chunk ? b->chunk : 8192;
+    std::vector<BatchItem> items;
+    std::vector<double> cost;
+    for (int i = 0; i < b->n; ++i)
+        for (int64_t f = 0; f < b->n_part[i]; f += chunk) {
+            BatchItem it{};
+            it.inst = i;
+            it.first = f;
+            it.count = std::min<int64_t>(chunk, b->n_part[i] - f);
+            items.push_back(it);
+            cost.push_back(b->cost_per_particle[i] * (double)it.count);
+        }
+    std::vector<size_t> order(items.size());
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return cost[x] > cost[y]; });
+    std::vector<BatchItem> sorted(items.size());
+    for (size_t k = 0; k < order.size(); ++k) sorted[k] = items[order[k]];
+    b->n_items = (int)sorted.size();
+    if (b->items.grow(std::max<size_t>(1, sorted.size()) * sizeof(BatchItem)))
+        return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for the work list failed");
+    CK(cudaMemcpy(b->items.p, sorted.data(), sorted.size() * sizeof(BatchItem), cudaMemcpyHostToDevice), "work list");
+    // capture: clear histograms and counters, persistent launch
+    auto *a = static_cast<BatchArgs<R> *>(b->args_host);
+    a->params = static_cast<const DevParams<R> *>(b->params.p);
+    a->items = static_cast<const BatchItem *>(b->items.p);
+    a->n_items = b->n_items;
+    a->ring_cap = ring;
+    a->counter = static_cast<int32_t *>(b->ctl.p);
+    a->stats = reinterpret_cast<unsigned long long *>(static_cast<unsigned char *>(b->ctl.p) + 64);
+    a->status = reinterpret_cast<int32_t *>(static_cast<unsigned char *>(b->ctl.p) + 192);
+    a->hists = static_cast<unsigned long long *>(b->hists.p);
+    a->hist_len = b->hist_len;
+    a->edges = static_cast<const R *>(b->edges.p);
+    a->n_edges = b->n_edges;
+    a->obs_kind = b->obs_kind;
+    CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
+    cudaMemsetAsync(b->hists.p, 0, (size_t)b->n * b->hist_len * sizeof(int64_t), ctx->stream);
+    cudaMemsetAsync(b->ctl.p, 0, 256, ctx->stream);
+    int le;
+    if constexpr (sizeof(R) == 4) le = launch_transport_batch_f32(*a, b->grid, block, b->smem, ctx->stream);
+    else le = launch_transport_batch_f64(*a, b->grid, block, b->smem, ctx->stream);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &b->graph);
+    if (le) return cuda_fail(ctx, (cudaError_t)le, "batched launch capture");
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "graph capture");
+    CK(cudaGraphInstantiate(&b->exec, b->graph, 0), "graph instantiate");
+    b->block = block;
+    b->ring = ring;
+    b->chunk = chunk;
+    return RTMC_OK;
+}
+
+template <typename R>
+int batch_create(rtmc_context *ctx, int n, const rtmc_problem *P, const rtmc_tables *const *T, rtmc_batch *b)
+{
+    b->prec = sizeof(R) == 4 ? RTMC_FP32 : RTMC_FP64;
+    b->n_obs = P[0].n_obs;
+    b->hist_len = P[0].hist_len;
+    // tables and Zoeppritz tables of every instance in one device buffer
+    std::vector<size_t> toff(n);
+    size_t total = 0;
+    for (int i = 0; i < n; ++i) {
+        toff[i] = total;
+        for (int t = 0; t < T[i]->n_tables; ++t) total += table_bytes<R>(T[i]->cdf[t].size());
+        total += align_up(2 * RTMC_ZOE_N * sizeof(R), 256);
+    }
+    if (b->tabs.grow(total)) return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for batched tables failed");
+    std::vector<unsigned char> host(total, 0);
+    std::vector<DevParams<R>> params(n);
+    std::vector<R> edges, zoe;
+    int n_edges = 0;
+    unsigned char *dev = static_cast<unsigned char *>(b->tabs.p);
+    b->n_part.resize(n);
+    b->cost_per_particle.resize(n);
+    for (int i = 0; i < n; ++i) {
+        DevTables<R> dt{};
+        size_t o = toff[i];
+        for (int t = 0; t < T[i]->n_tables; ++t) {
+            stage_table<R>(T[i]->cdf[t], T[i]->theta[t], host.data() + o, dev + o, &dt, t);
+            o += table_bytes<R>(T[i]->cdf[t].size());
+        }
+        fill_params<R>(ctx, &P[i], dt, &params[i], &n_edges, &edges, &zoe);
+        std::memcpy(host.data() + o, zoe.data(), zoe.size() * sizeof(R));
+        params[i].zoe = reinterpret_cast<const R *>(dev + o);
+        params[i].sink = kSinkSmem;
+        params[i].trace = nullptr;
+        b->n_part[i] = P[i].n_particles;
+        // expected work per particle: its observations plus ~4 observation-equivalents per event
+        double rate = 0;
+        for (int m = 0; m < (P[i].acoustics ? 1 : 2); ++m)
+            if (std::isfinite(P[i].mft[m])) rate = std::max(rate, 1.0 / P[i].mft[m]);
+        b->cost_per_particle[i] = P[i].n_obs + 4.0 * rate * P[i].h * P[i].n_sub * P[i].n_obs;
+        if (i == 0) b->obs_kind = params[0].obs_kind;
+    }
+    CK(cudaMemcpy(b->tabs.p, host.data(), total, cudaMemcpyHostToDevice), "batched tables");
+    if (b->edges.grow(std::max<size_t>(1, edges.size()) * sizeof(R)) || b->params.grow((size_t)n * sizeof(DevParams<R>)) ||
+        b->hists.grow((size_t)n * b->hist_len * sizeof(int64_t)) || b->ctl.grow(256))
+        return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for a batch failed");
+    for (int i = 0; i < n; ++i) params[i].edges = static_cast<const R *>(b->edges.p);
+    if (!edges.empty())
+        CK(cudaMemcpy(b->edges.p, edges.data(), edges.size() * sizeof(R), cudaMemcpyHostToDevice), "edges");
+    CK(cudaMemcpy(b->params.p, params.data(), (size_t)n * sizeof(DevParams<R>), cudaMemcpyHostToDevice), "params");
+    b->n_edges = n_edges;
+    b->args_host = new BatchArgs<R>();
+    return batch_build_graph<R>(b);
+}
+
+} // namespace
+
+extern "C" int rtmc_batch_create(rtmc_context *ctx, int32_t n, const rtmc_problem *P, const rtmc_tables *const *T,
+                                 rtmc_batch **out)
+{
+    if (!ctx || !P || !T || !out || n < 1) return fail(ctx ? &ctx->err : nullptr, RTMC_ERR_ARG, "rtmc_batch_create: bad argument");
+    *out = nullptr;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    for (int i = 0; i < n; ++i) {
+        int s = check_problem(ctx, &P[i], T[i]);
+        if (s) return s;
+        if (i && !same_grid(P[0], P[i]))
+            return fail(&ctx->err, RTMC_ERR_ARG, "rtmc_batch_create: problem " + std::to_string(i) +
+                                                      " does not share the observation grid of problem 0");
+    }
+    auto *b = new (std::nothrow) rtmc_batch();
+    if (!b) return fail(&ctx->err, RTMC_ERR_ALLOC, "out of host memory");
+    b->ctx = ctx;
+    b->n = n;
+    int s = P[0].precision == RTMC_FP64 ? batch_create<double>(ctx, n, P, T, b) : batch_create<float>(ctx, n, P, T, b);
+    if (s) {
+        rtmc_batch_destroy(b);
+        return s;
+    }
+    *out = b;
+    return RTMC_OK;
+}
+
+extern "C" int rtmc_batch_set_launch(rtmc_batch *b, int32_t block, int32_t ring_cap, int64_t chunk)
+{
+    if (!b) return fail(nullptr, RTMC_ERR_ARG, "rtmc_batch_set_launch: NULL batch");
+    if (block < 0 || block > 512 || block % 32 || ring_cap < 0 || ring_cap == 1 || ring_cap > 64 || chunk < 0)
+        return fail(&b->ctx->err, RTMC_ERR_ARG, "rtmc_batch_set_launch: block <= 512 (multiple of 32), ring 0 or 2..64, chunk >= 0");
+    rtmc_context *ctx = b->ctx;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    b->block = block;
+    b->ring = ring_cap;
+    b->chunk = chunk;
+    return b->prec == RTMC_FP64 ? batch_build_graph<double>(b) : batch_build_graph<float>(b);
+}
+
+extern "C" int rtmc_batch_run(rtmc_batch *b, rtmc_stats *st)
+{
+    if (!b) return fail(nullptr, RTMC_ERR_ARG, "rtmc_batch_run: NULL batch");
+    rtmc_context *ctx = b->ctx;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    CK(cudaEventRecord(ctx->ev_k0, ctx->stream), "event");
+    CK(cudaGraphLaunch(b->exec, ctx->stream), "graph launch");
+    CK(cudaEventRecord(ctx->ev_k1, ctx->stream), "event");
+    int64_t d[32];
+    CK(cudaMemcpyAsync(d, static_cast<unsigned char *>(b->ctl.p) + 64, 192, cudaMemcpyDeviceToHost, ctx->stream), "counters");
+    CK(cudaStreamSynchronize(ctx->stream), "batched run");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev_k0, ctx->ev_k1);
+    ctx->last_kernel_ms = ms;
+    ctx->last_launches = 1;
+    const int32_t status = (int32_t)(d[16] & 0xffffffff);
+    if (st) {
+        std::memset(st, 0, sizeof *st);
+        st->scatter_events = d[0];
+        st->boundary_hits = d[1];
+        st->kills = d[2];
+        st->absorbed = d[3];
+        st->observations = d[4];
+        st->conversions = d[5];
+        st->device_status = status;
+        st->launches = 1;
+        st->sink = kSinkSmem;
+        st->kernel_ms = ms;
+        st->total_ms = ms;
+        st->d2h_bytes = 192;
+    }
+    if (status) return fail(&ctx->err, RTMC_ERR_DEVICE, "a transport guard tripped in a batched run");
+    return RTMC_OK;
+}
+
+extern "C" int rtmc_batch_histograms(rtmc_batch *b, int32_t first, int32_t count, int64_t *out)
+{
+    if (!b || !out || first < 0 || count < 0 || first + count > b->n)
+        return fail(b ? &b->ctx->err : nullptr, RTMC_ERR_ARG, "rtmc_batch_histograms: bad range");
+    rtmc_context *ctx = b->ctx;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    CK(cudaMemcpy(out, static_cast<int64_t *>(b->hists.p) + (int64_t)first * b->hist_len,
+                  (size_t)count * b->hist_len * sizeof(int64_t), cudaMemcpyDeviceToHost), "histogram copy");
+    return RTMC_OK;
+}
+
+extern "C" void rtmc_batch_destroy(rtmc_batch *b)
+{
+    if (!b) return;
+    if (b->ctx) cudaSetDevice(b->ctx->device);
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->params.release();
+    b->items.release();
+    b->tabs.release();
+    b->edges.release();
+    b->hists.release();
+    b->ctl.release();
+    if (b->args_host) {
+        if (b->prec == RTMC_FP64) delete static_cast<BatchArgs<double> *>(b->args_host);
+        else delete static_cast<BatchArgs<float> *>(b->args_host);
+    }
+    delete b;
 }

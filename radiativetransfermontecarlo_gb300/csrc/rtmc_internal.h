@@ -93,6 +93,25 @@ struct BinParams {
     unsigned long long *hist;
 };
 
+// One work item of a batched run: particles [first, first + count) of instance inst.
+struct BatchItem {
+    int32_t inst, pad;
+    int64_t first, count;
+};
+
+template <typename R> struct BatchArgs {
+    const DevParams<R> *params; // per instance (device)
+    const BatchItem *items;     // sorted by expected cost, largest first
+    int32_t n_items, ring_cap;
+    int32_t *counter;           // next work item
+    unsigned long long *hists;  // n x hist_len int64, instance-major
+    int64_t hist_len;
+    const R *edges;             // the grid the instances share
+    int32_t n_edges, obs_kind;
+    unsigned long long *stats;  // [8]
+    int32_t *status;
+};
+
 // Launch wrappers (transport.cu).  Return a cudaError_t value.
 int launch_transport_f32(const DevParams<float> &p, int grid, int block, size_t smem, void *stream);
 int launch_transport_f64(const DevParams<double> &p, int grid, int block, size_t smem, void *stream);
@@ -100,6 +119,9 @@ int transport_occupancy(int precision, int sink, int obs, int block, size_t smem
 int transport_set_smem(int precision, int sink, int obs, size_t smem);
 int transport_max_threads(int precision, int sink, int obs);
 int launch_bin_slices(const BinParams &b, int grid_x, size_t smem, void *stream);
+int launch_transport_batch_f32(const BatchArgs<float> &a, int grid, int block, size_t smem, void *stream);
+int launch_transport_batch_f64(const BatchArgs<double> &a, int grid, int block, size_t smem, void *stream);
+int transport_batch_setup(int precision, int obs, int block, size_t smem, int *blocks_per_sm);
 int bin_slices_set_smem(size_t smem);
 // device address of the static scratch of rtmc_forward_noalloc (noalloc.cu); device current
 int static_scratch(int device, unsigned char **ptr, size_t *bytes);

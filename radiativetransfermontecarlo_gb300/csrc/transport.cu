@@ -633,6 +633,154 @@ template <typename R, int SINK> struct Bounds {
     static constexpr int min_blocks = SINK == SINK_SMEM ? 1 : (sizeof(R) == 4 ? RTMC_TRANSPORT_MIN_BLOCKS : 2);
 };
 
+// One warp's batch of 32 consecutive particles [base, base + 32) of the problem p,
+// clipped at n_end: the two-cursor transport described at rt_transport.
+template <typename R, int SINK, int OBS>
+__device__ __forceinline__ void run_batch(const DevParams<R> &p, const R *sedges, unsigned *shist, const Ring<R> &ring,
+                                          int64_t base, int64_t n_end, Counters &cnt, bool &bad)
+{
+    constexpr bool SMEM = SINK == SINK_SMEM;
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const unsigned long long inc = 1ull << p.hist_shift;
+    const int s_end = p.s_end;
+    const int C = ring.cap;
+    const int64_t i = base + lane;
+    const bool have = i < n_end;
+    const uint64_t pid = (uint64_t)(p.pid0 + i);
+    Part<R> s;
+    Seg<R> cur;
+    int head = 0, count = 0;
+    const unsigned scat0 = cnt.scat, bnd0 = cnt.bnd;
+    if (have) {
+        init_particle(p, pid, s);
+    } else {
+        s.alive = 0; s.s_death = 0; s.s0 = 0; s.sS = s.sK = s.sB = s_end + 1; s.k = 0; s.mode = 0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) { s.x[c] = (R)0; s.d[c] = (R)0; s.q[c] = (R)0; }
+    }
+    seg_from(s, cur);
+    seg_prepare<R, OBS>(p, sedges, cur);
+    int32_t *optr = (SINK == SINK_INDEX && have) ? p.obs_idx + i : nullptr;
+    int jn = 1; // warp-uniform
+    while (jn <= p.n_obs) {
+        // ---- phase 1: refill the rings (events of all lanes with room run together)
+        const int so_next = jn * p.n_sub;
+        for (;;) {
+            // segments starting at or before the next observation supersede the
+            // current one: consume them, so the ring only holds later segments
+            while (count > 0 && ring.start(head) <= so_next) {
+                ring.get(head, cur);
+                seg_prepare<R, OBS>(p, sedges, cur);
+                head = (head + 1) % C;
+                --count;
+            }
+            const bool need = s.alive && count < C && next_event(s) <= s_end;
+            if (!__any_sync(full, need)) break;
+            if (need) {
+                process_event(p, pid, s, cnt);
+                if ((int)s.k > p.max_events) { s.alive = 0; s.s_death = s.s0; bad = true; }
+                if (s.alive) {
+                    if (count == 0 && s.s0 <= so_next) {
+                        seg_from(s, cur);
+                        seg_prepare<R, OBS>(p, sedges, cur);
+                    } else {
+                        ring.put((head + count) % C, s);
+                        ++count;
+                    }
+                }
+            }
+        }
+        // ---- window: observations every live lane has covered (dead lanes never limit)
+        unsigned avail = 0x7fffffffu;
+        if (s.alive) {
+            const int limit = next_event(s) <= s_end ? next_event(s) : s_end + 1;
+            int last = (limit - 1) / p.n_sub;
+            last = last < p.n_obs ? last : p.n_obs;
+            avail = (unsigned)(last - jn + 1);
+        }
+        unsigned nw = __reduce_min_sync(full, avail);
+        if (nw > (unsigned)(p.n_obs - jn + 1)) {
+            if (SINK == SINK_INDEX) {
+                nw = (unsigned)(p.n_obs - jn + 1); // no live lane left: write the rest
+            } else {
+                // no live lane left: bin what the dead lanes observed before dying
+                int rem = 0;
+                if (have && s.s_death > jn * p.n_sub) rem = min(p.n_obs, (s.s_death - 1) / p.n_sub) - jn + 1;
+                nw = __reduce_max_sync(full, (unsigned)(rem > 0 ? rem : 0));
+                if (nw == 0) break;
+            }
+        }
+        // ---- phase 2: nw observations per lane, two at a time (independent chains)
+        const int obs_limit = s.alive ? 0x7fffffff : s.s_death;
+        int next_start = count > 0 ? ring.start(head) : 0x7fffffff;
+        int so = jn * p.n_sub;
+        // make cur the segment in force at sub-step at
+        auto advance = [&](int at) {
+            do {
+                ring.get(head, cur);
+                head = (head + 1) % C;
+                --count;
+            } while (count > 0 && ring.start(head) <= at);
+            seg_prepare<R, OBS>(p, sedges, cur);
+            next_start = count > 0 ? ring.start(head) : 0x7fffffff;
+        };
+        auto emit = [&](int v, int mode, int j) {
+            if (SINK == SINK_INDEX) {
+                if (have) {
+                    *optr = v < 0 ? -1 : (v | (mode << 30));
+                    optr += p.obs_rows;
+                }
+                if (v >= 0) cnt.obs++;
+            } else if (v >= 0) {
+                const int64_t idx = (int64_t)j * p.time_stride + (mode ? p.mode_stride : 0) + v;
+                if (idx < p.hist_len) {
+                    cnt.obs++;
+                    if (SMEM) atomicAdd(shist + idx, 1u);
+                    else atomicAdd(p.hist + idx, inc);
+                } else {
+                    bad = true;
+                }
+            }
+        };
+        unsigned w = 0;
+        for (; w + 1 < nw; w += 2, jn += 2, so += 2 * p.n_sub) {
+            const int so1 = so + p.n_sub;
+            int v0 = -1, v1 = -1, m0 = cur.mode, m1 = cur.mode;
+            if (so < obs_limit) {
+                if (so >= next_start) advance(so);
+                m0 = m1 = cur.mode;
+                v0 = obs_offset<R, OBS>(p, sedges, cur, so);
+                if (so1 < obs_limit) {
+                    if (so1 >= next_start) {
+                        advance(so1);
+                        m1 = cur.mode;
+                    }
+                    v1 = obs_offset<R, OBS>(p, sedges, cur, so1);
+                }
+            }
+            emit(v0, m0, jn);
+            emit(v1, m1, jn + 1);
+        }
+        if (w < nw) {
+            int v = -1;
+            if (so < obs_limit) {
+                if (so >= next_start) advance(so);
+                v = obs_offset<R, OBS>(p, sedges, cur, so);
+            }
+            emit(v, cur.mode, jn);
+            ++jn;
+        }
+    }
+    if (have && p.trace) { // final state of the particle, the oracle's layout
+        double *f = p.trace + 16 * i;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) { f[c] = s.x[c]; f[3 + c] = s.d[c]; f[6 + c] = s.q[c]; }
+        f[9] = s.mode; f[10] = s.alive; f[11] = cnt.scat - scat0; f[12] = cnt.bnd - bnd0;
+        f[13] = s.s0; f[14] = s.s_death; f[15] = s.k;
+    }
+}
+
 // The transport kernel.  A warp takes 32 consecutive particles at a time and walks the
 // observation instants in lockstep.  Each lane keeps two cursors on its particle's
 // trajectory: the event state s (phase 1, runs ahead and pushes one segment per event
@@ -670,145 +818,10 @@ __global__ void __launch_bounds__(Bounds<R, SINK>::threads, Bounds<R, SINK>::min
     const int lane = threadIdx.x & 31;
     Counters cnt = {0u, 0u, 0u, 0u, 0u, 0u};
     bool bad = false;
-    const unsigned long long inc = 1ull << p.hist_shift;
-    const int s_end = p.s_end;
     const int64_t warps = ((int64_t)gridDim.x * T) >> 5;
 
     for (int64_t base = (((int64_t)blockIdx.x * T + threadIdx.x) >> 5) << 5; base < p.n_particles; base += warps * 32) {
-        const int64_t i = base + lane;
-        const bool have = i < p.n_particles;
-        const uint64_t pid = (uint64_t)(p.pid0 + i);
-        Part<R> s;
-        Seg<R> cur;
-        int head = 0, count = 0;
-        const unsigned scat0 = cnt.scat, bnd0 = cnt.bnd;
-        if (have) {
-            init_particle(p, pid, s);
-        } else {
-            s.alive = 0; s.s_death = 0; s.s0 = 0; s.sS = s.sK = s.sB = s_end + 1; s.k = 0; s.mode = 0;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) { s.x[c] = (R)0; s.d[c] = (R)0; s.q[c] = (R)0; }
-        }
-        seg_from(s, cur);
-        seg_prepare<R, OBS>(p, sedges, cur);
-        int32_t *optr = (SINK == SINK_INDEX && have) ? p.obs_idx + i : nullptr;
-        int jn = 1; // warp-uniform
-        while (jn <= p.n_obs) {
-            // ---- phase 1: refill the rings (events of all lanes with room run together)
-            const int so_next = jn * p.n_sub;
-            for (;;) {
-                // segments starting at or before the next observation supersede the
-                // current one: consume them, so the ring only holds later segments
-                while (count > 0 && ring.start(head) <= so_next) {
-                    ring.get(head, cur);
-                    seg_prepare<R, OBS>(p, sedges, cur);
-                    head = (head + 1) % C;
-                    --count;
-                }
-                const bool need = s.alive && count < C && next_event(s) <= s_end;
-                if (!__any_sync(full, need)) break;
-                if (need) {
-                    process_event(p, pid, s, cnt);
-                    if ((int)s.k > p.max_events) { s.alive = 0; s.s_death = s.s0; bad = true; }
-                    if (s.alive) {
-                        if (count == 0 && s.s0 <= so_next) {
-                            seg_from(s, cur);
-                            seg_prepare<R, OBS>(p, sedges, cur);
-                        } else {
-                            ring.put((head + count) % C, s);
-                            ++count;
-                        }
-                    }
-                }
-            }
-            // ---- window: observations every live lane has covered (dead lanes never limit)
-            unsigned avail = 0x7fffffffu;
-            if (s.alive) {
-                const int limit = next_event(s) <= s_end ? next_event(s) : s_end + 1;
-                int last = (limit - 1) / p.n_sub;
-                last = last < p.n_obs ? last : p.n_obs;
-                avail = (unsigned)(last - jn + 1);
-            }
-            unsigned nw = __reduce_min_sync(full, avail);
-            if (nw > (unsigned)(p.n_obs - jn + 1)) {
-                if (SINK == SINK_INDEX) {
-                    nw = (unsigned)(p.n_obs - jn + 1); // no live lane left: write the rest
-                } else {
-                    // no live lane left: bin what the dead lanes observed before dying
-                    int rem = 0;
-                    if (have && s.s_death > jn * p.n_sub) rem = min(p.n_obs, (s.s_death - 1) / p.n_sub) - jn + 1;
-                    nw = __reduce_max_sync(full, (unsigned)(rem > 0 ? rem : 0));
-                    if (nw == 0) break;
-                }
-            }
-            // ---- phase 2: nw observations per lane, two at a time (independent chains)
-            const int obs_limit = s.alive ? 0x7fffffff : s.s_death;
-            int next_start = count > 0 ? ring.start(head) : 0x7fffffff;
-            int so = jn * p.n_sub;
-            // make cur the segment in force at sub-step at
-            auto advance = [&](int at) {
-                do {
-                    ring.get(head, cur);
-                    head = (head + 1) % C;
-                    --count;
-                } while (count > 0 && ring.start(head) <= at);
-                seg_prepare<R, OBS>(p, sedges, cur);
-                next_start = count > 0 ? ring.start(head) : 0x7fffffff;
-            };
-            auto emit = [&](int v, int mode, int j) {
-                if (SINK == SINK_INDEX) {
-                    if (have) {
-                        *optr = v < 0 ? -1 : (v | (mode << 30));
-                        optr += p.obs_rows;
-                    }
-                    if (v >= 0) cnt.obs++;
-                } else if (v >= 0) {
-                    const int64_t idx = (int64_t)j * p.time_stride + (mode ? p.mode_stride : 0) + v;
-                    if (idx < p.hist_len) {
-                        cnt.obs++;
-                        if (SMEM) atomicAdd(shist + idx, 1u);
-                        else atomicAdd(p.hist + idx, inc);
-                    } else {
-                        bad = true;
-                    }
-                }
-            };
-            unsigned w = 0;
-            for (; w + 1 < nw; w += 2, jn += 2, so += 2 * p.n_sub) {
-                const int so1 = so + p.n_sub;
-                int v0 = -1, v1 = -1, m0 = cur.mode, m1 = cur.mode;
-                if (so < obs_limit) {
-                    if (so >= next_start) advance(so);
-                    m0 = m1 = cur.mode;
-                    v0 = obs_offset<R, OBS>(p, sedges, cur, so);
-                    if (so1 < obs_limit) {
-                        if (so1 >= next_start) {
-                            advance(so1);
-                            m1 = cur.mode;
-                        }
-                        v1 = obs_offset<R, OBS>(p, sedges, cur, so1);
-                    }
-                }
-                emit(v0, m0, jn);
-                emit(v1, m1, jn + 1);
-            }
-            if (w < nw) {
-                int v = -1;
-                if (so < obs_limit) {
-                    if (so >= next_start) advance(so);
-                    v = obs_offset<R, OBS>(p, sedges, cur, so);
-                }
-                emit(v, cur.mode, jn);
-                ++jn;
-            }
-        }
-        if (have && p.trace) { // final state of the particle, the oracle's layout
-            double *f = p.trace + 16 * i;
-#pragma unroll
-            for (int c = 0; c < 3; ++c) { f[c] = s.x[c]; f[3 + c] = s.d[c]; f[6 + c] = s.q[c]; }
-            f[9] = s.mode; f[10] = s.alive; f[11] = cnt.scat - scat0; f[12] = cnt.bnd - bnd0;
-            f[13] = s.s0; f[14] = s.s_death; f[15] = s.k;
-        }
+        run_batch<R, SINK, OBS>(p, sedges, shist, ring, base, p.n_particles, cnt, bad);
     }
 
     // counters: warp reduction, one global atomic per warp
@@ -826,6 +839,80 @@ __global__ void __launch_bounds__(Bounds<R, SINK>::threads, Bounds<R, SINK>::min
             if (c) atomicAdd(p.hist + k, (unsigned long long)c << p.hist_shift);
         }
     }
+}
+
+// Batched transport: many independent problems (instances) sharing one observation
+// grid, in one persistent launch.  Blocks pull (instance, particle range) work items,
+// largest expected cost first, from a global counter; the instance's parameters are
+// copied into shared memory and its histogram accumulates in the block's shared-memory
+// copy, flushed to the instance's output whenever the block moves to another instance.
+template <typename R, int OBS>
+__global__ void __launch_bounds__(512, 1) rt_transport_batch(const BatchArgs<R> a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ DevParams<R> sp;
+    __shared__ int s_item;
+    R *sedges = reinterpret_cast<R *>(smem_raw);
+    size_t off = (((size_t)a.n_edges * sizeof(R) + 15) / 16) * 16;
+    unsigned *shist = reinterpret_cast<unsigned *>(smem_raw + off);
+    off += (((size_t)a.hist_len * 4 + 15) / 16) * 16;
+    const int T = blockDim.x, C = a.ring_cap;
+    Ring<R> ring;
+    ring.cap = C;
+    ring.stride = T;
+    {
+        R *r = reinterpret_cast<R *>(smem_raw + off);
+        ring.x0 = r; ring.x1 = r + C * T; ring.x2 = r + 2 * C * T;
+        ring.d0 = r + 3 * C * T; ring.d1 = r + 4 * C * T; ring.d2 = r + 5 * C * T;
+        int *ri = reinterpret_cast<int *>(r + 6 * C * T);
+        ring.s0 = ri; ring.mode = ri + C * T;
+    }
+    for (int k = threadIdx.x; k < a.n_edges; k += T) sedges[k] = a.edges[k];
+    for (int64_t k = threadIdx.x; k < a.hist_len; k += T) shist[k] = 0u;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = T >> 5;
+    Counters cnt = {0u, 0u, 0u, 0u, 0u, 0u};
+    bool bad = false;
+    int cur = -1; // instance held in shared memory (the same in every thread)
+    auto flush = [&](int inst) {
+        unsigned long long *h = a.hists + (int64_t)inst * a.hist_len;
+        const int sh = sp.hist_shift;
+        for (int64_t k = threadIdx.x; k < a.hist_len; k += T) {
+            const unsigned c = shist[k];
+            if (c) {
+                atomicAdd(h + k, (unsigned long long)c << sh);
+                shist[k] = 0u;
+            }
+        }
+    };
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_item = atomicAdd(a.counter, 1);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= a.n_items) break;
+        const BatchItem bi = a.items[it];
+        if (bi.inst != cur) {
+            if (cur >= 0) flush(cur);
+            __syncthreads();
+            const uint32_t *src = reinterpret_cast<const uint32_t *>(a.params + bi.inst);
+            uint32_t *dst = reinterpret_cast<uint32_t *>(&sp);
+            for (int k = threadIdx.x; k < (int)(sizeof(DevParams<R>) / 4); k += T) dst[k] = src[k];
+            cur = bi.inst;
+            __syncthreads();
+        }
+        const int64_t end = bi.first + bi.count;
+        for (int64_t base = bi.first + 32 * warp; base < end; base += 32 * nwarps)
+            run_batch<R, SINK_SMEM, OBS>(sp, sedges, shist, ring, base, end, cnt, bad);
+    }
+    if (cur >= 0) flush(cur);
+    const unsigned full = 0xffffffffu;
+    unsigned v[6] = {cnt.scat, cnt.bnd, cnt.kill, cnt.absorb, cnt.obs, cnt.conv};
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        const unsigned t = __reduce_add_sync(full, v[c]);
+        if (lane == 0 && t) atomicAdd(a.stats + c, (unsigned long long)t);
+    }
+    if (bad) atomicExch(a.status, 1);
 }
 
 // Fold the dense index array into the histogram, one time slice at a time: blockIdx.y
@@ -1012,6 +1099,36 @@ int launch_bin_slices(const BinParams &b, int grid_x, size_t smem, void *stream)
         rt_bin_slices<<<g, kFoldThreads, 0, (cudaStream_t)stream>>>(b);
     }
     return (int)cudaGetLastError();
+}
+
+template <typename R> void *pick_batch(int obs)
+{
+    return obs == OBS_CART ? (void *)rt_transport_batch<R, OBS_CART>
+                           : (obs == OBS_RADIAL ? (void *)rt_transport_batch<R, OBS_RADIAL> : (void *)rt_transport_batch<R, OBS_GENERAL>);
+}
+
+template <typename R> static int launch_batch(const BatchArgs<R> &a, int grid, int block, size_t smem, void *stream)
+{
+    void *args[] = {(void *)&a};
+    return (int)cudaLaunchKernel(pick_batch<R>(a.obs_kind), dim3(grid), dim3(block), args, smem, (cudaStream_t)stream);
+}
+
+int launch_transport_batch_f32(const BatchArgs<float> &a, int grid, int block, size_t smem, void *stream)
+{
+    return launch_batch(a, grid, block, smem, stream);
+}
+
+int launch_transport_batch_f64(const BatchArgs<double> &a, int grid, int block, size_t smem, void *stream)
+{
+    return launch_batch(a, grid, block, smem, stream);
+}
+
+int transport_batch_setup(int precision, int obs, int block, size_t smem, int *blocks_per_sm)
+{
+    void *fn = precision == RTMC_FP64 ? pick_batch<double>(obs) : pick_batch<float>(obs);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, block, smem);
+    return (int)e;
 }
 
 int bin_slices_set_smem(size_t smem)

@@ -1,0 +1,64 @@
+"""Batched runs (rtmc_batch_*): one persistent, graph-captured launch over many instances
+sharing an observation grid.  Each instance must give exactly the histogram of its own
+single run (same seed and particle ids: the same trajectories, integer counts)."""
+import numpy as np
+import pytest
+
+from radiativetransfermontecarlo_gb300 import build_problem, get_context
+from radiativetransfermontecarlo_gb300 import workloads as W
+from radiativetransfermontecarlo_gb300.batch import Batch, autotune
+
+pytestmark = pytest.mark.gpu
+
+
+def _instances(k, n_cap):
+    out = []
+    for i in range(k):
+        geo, src, mat, obs, opts = W.c4_instance(i)
+        src = dict(src, numberParticles=min(src["numberParticles"], n_cap))
+        out.append((geo, src, mat, obs, dict(opts, exact_count=True, seed=100 + i)))
+    return out
+
+
+def test_c4_parameter_ranges():
+    lcs, cvs, fs, qs, ns = [], [], [], [], []
+    for i in range(256):
+        geo, src, mat, obs, opts = W.c4_instance(i)
+        lcs.append(mat.CorrelationLength); cvs.append(mat.coefficients_of_variation[0])
+        fs.append(mat.Frequency); qs.append(mat.Q); ns.append(src["numberParticles"])
+    assert 0.02 <= min(lcs) and max(lcs) <= 1 and 0.01 <= min(cvs) and max(cvs) <= 0.2
+    assert 1 <= min(fs) and max(fs) <= 20 and set(qs) <= {float("inf"), 100.0, 500.0}
+    assert 1e4 <= min(ns) and max(ns) <= 1e7 and len(set(qs)) == 3
+
+
+def test_batch_equals_single_runs():
+    inst = _instances(12, 6000)
+    b = Batch(inst)
+    st = b.run()
+    assert st["device_status"] == 0
+    H = b.histograms()
+    ctx = get_context(0)
+    total = 0
+    for i, (geo, src, mat, obs, opts) in enumerate(inst):
+        prob, grid, N = build_problem(geo, src, mat, obs, dict(opts, precision="fp32"))
+        P, keep = prob.to_ctypes()
+        ref, s = ctx.forward(P, prob.tables)
+        assert np.array_equal(H[i], ref), i
+        total += s["scatter_events"]
+    assert st["scatter_events"] == total
+    # a second replay of the graph gives the same result
+    b.run()
+    assert np.array_equal(b.histograms(), H)
+    b.close()
+
+
+def test_batch_autotune_keeps_results():
+    inst = _instances(6, 4000)
+    b = Batch(inst)
+    b.run()
+    H = b.histograms()
+    shape, times = autotune(b, blocks=(256, 512), rings=(4, 8), chunks=(2048, 16384), repeats=1)
+    assert shape in times and len(times) >= 4
+    b.run()
+    assert np.array_equal(b.histograms(), H)
+    b.close()
