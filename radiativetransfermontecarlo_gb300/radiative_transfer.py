@@ -120,21 +120,30 @@ def build_problem(geometry: dict, source: dict, material: MaterialClass, observa
     grid = initialize_observation(geometry, acoustics, observation, N, extended=opt["histogram"] == "extended")
     if material.invcdf is None:
         MaterialClass.prepareSigma(material, d)
-    if material.timeSteps not in (0, None):
-        raise NotImplementedError("timeSteps = 1 (propagateParticle) is served by the same event-driven kernel; "
-                                  "set timeSteps = 0")
-    # sub-step of propagateParticleSmallDt.m:4-7 (uniform observation times)
+    large_dt = material.timeSteps == 1
+    if material.timeSteps not in (0, 1, None):
+        raise ValueError("timeSteps must be 0 (small time steps) or 1 (large time steps)")
     t = grid.t
     T = float(np.mean(np.diff(t)))
     mft = np.atleast_1d(np.asarray(material.meanFreeTime, dtype=float)).ravel()
     if mft.size == 1:
         mft = np.array([mft[0], mft[0]])
-    dt = min(0.01 * float(np.min(mft)), T)
-    n_sub = int(math.ceil(T / dt))
+    if large_dt:
+        # propagateParticle.m: exponential flights in continuous time (Poisson jumps per
+        # interval, next jump at the minimum of uniform times), no Q and no boundaries.
+        # Served by the event kernel on a grid of 2^20 sub-steps per interval (fewer when
+        # the run has more than 1023 intervals), where geometric draws are exponential.
+        n_sub = 1 << 20
+        while n_sub > 1 and n_sub * (grid.Nt - 1) >= (1 << 30):
+            n_sub >>= 1
+    else:
+        # sub-step of propagateParticleSmallDt.m:4-7 (uniform observation times)
+        dt = min(0.01 * float(np.min(mft)), T)
+        n_sub = int(math.ceil(T / dt))
     h = T / n_sub
     QP, QS = _q_values(material)
     qrate = [0.0, 0.0]
-    if math.isfinite(QP) or math.isfinite(QS):
+    if not large_dt and (math.isfinite(QP) or math.isfinite(QS)):
         if material.Frequency is None or np.size(material.Frequency) == 0:
             raise ValueError("A finite quality factor Q was provided, but mat.Frequency is empty. Please define "
                              "mat.Frequency before using Q-based attenuation.")
@@ -154,7 +163,7 @@ def build_problem(geometry: dict, source: dict, material: MaterialClass, observa
     pol = 1 if (not acoustics and source.get("polarization", "P") == "S") else 0
     # boundaries (propagateParticleSmallDt.m:146-166)
     bnd = []
-    for b in geometry.get("bnd", []) or []:
+    for b in ([] if large_dt else geometry.get("bnd", []) or []):
         btype = (b.get("type") or "reflective").lower()
         if btype not in ("reflective", "absorbing"):
             raise ValueError(f'Unknown boundary type "{btype}". Use "reflective" or "absorbing".')

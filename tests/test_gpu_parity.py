@@ -181,3 +181,19 @@ def test_general_observation_path(frame, extra):
         assert _path_match(states, ref_states, tol).mean() >= need
         if precision == "fp64":
             assert _l1_diff(hist, ref_hist) <= max(4, 1e-6 * stats["observations"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_large_time_steps_scheme_matches_oracle(precision):
+    """timeSteps = 1 (propagateParticle.m) through the event kernel on the fine grid."""
+    geo, src, mat, obs, opts = W.c2_elastic3d(t_end=2.0)
+    mat.timeSteps = 1
+    prob, grid, N, hist, states, stats, ref_hist, ref_states, ref_stats = _run_both(geo, src, mat, obs, opts, 5000,
+                                                                                    precision)
+    assert prob.n_sub == 1 << 20 and stats["device_status"] == 0
+    if precision == "fp64":
+        assert stats["scatter_events"] == ref_stats["scatter_events"]
+        assert _path_match(states, ref_states, 1e-9).mean() == 1.0
+        assert _l1_diff(hist, ref_hist) >> prob.hist_shift <= max(4, 1e-6 * stats["observations"])
+    else:
+        assert _path_match(states, ref_states, 1e-3).mean() >= 0.99

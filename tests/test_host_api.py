@@ -105,3 +105,13 @@ def test_shard_partitions_particle_ids():
         for f, c in parts:
             assert f == first
             first += c
+
+
+def test_large_time_steps_scheme_set_up():
+    """timeSteps = 1 (propagateParticle.m): continuous-time flights on a 2^20 grid per
+    interval, no Q and no boundaries, as the reference's large-dt scheme has none."""
+    geo, src, mat, obs, opts = W.c3_halfspace2d(t_end=1.0)
+    mat.timeSteps = 1
+    prob, grid, N = build_problem(geo, src, mat, obs, opts)
+    assert prob.n_sub == 1 << 20 and prob.qrate == (0.0, 0.0) and prob.bnd == []
+    assert prob.n_sub * prob.n_obs < 1 << 30

@@ -116,3 +116,105 @@ def test_boundary_energy_partition(mode, angle):
     if conv.any():
         s_out = np.hypot(d2[conv, 0], d2[conv, 1])
         assert np.allclose(s_out, math.sin(a) * vs / vp, atol=1e-12)
+
+
+def _invcdf(u, cdf, th):
+    """Piecewise-linear inverse CDF with linear extrapolation past the end knots
+    (griddedInterpolant 'linear', MaterialClass.m:2462)."""
+    out = np.interp(u, cdf, th)
+    lo, hi = u < cdf[0], u > cdf[-1]
+    out[lo] = th[0] + (u[lo] - cdf[0]) * (th[1] - th[0]) / (cdf[1] - cdf[0])
+    out[hi] = th[-1] + (u[hi] - cdf[-1]) * (th[-1] - th[-2]) / (cdf[-1] - cdf[-2])
+    return out
+
+
+def _continuous_time_flights(prob, knots, t, n, rng):
+    """numpy restatement of propagateParticle.m (timeSteps = 1) for 3D acoustics: Poisson
+    jumps per interval are exponential flights; isotropic start on a Gaussian-radius ball
+    (initializeParticle.m); returns radii at each observation time (column j = t[j])."""
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    q = np.cross(d, rng.normal(size=(n, 3)))
+    q /= np.linalg.norm(q, axis=1, keepdims=True)
+    x0 = rng.normal(size=(n, 3))
+    x0 /= np.linalg.norm(x0, axis=1, keepdims=True)
+    x = x0 * (np.abs(rng.normal(size=(n, 1))) * prob.src_lambda)
+    cdf, th = knots[0]
+    v, mft = prob.v[0], prob.mft[0]
+    invcdf = lambda u: _invcdf(u, cdf, th)
+    radii = np.zeros((n, t.size))
+    for j in range(1, t.size):
+        dt = np.full(n, t[j] - t[j - 1])
+        live = dt > 0
+        while live.any():
+            tau = rng.exponential(mft, n)
+            jump = live & (tau < dt)
+            fly = np.where(jump, tau, np.where(live, dt, 0.0))
+            x += (v * fly)[:, None] * d
+            dt = np.where(jump, dt - tau, 0.0)
+            k = np.flatnonzero(jump)
+            if k.size:
+                phi = 2 * np.pi * rng.random(k.size)
+                qk = np.cos(phi)[:, None] * q[k] + np.sin(phi)[:, None] * np.cross(d[k], q[k])
+                theta = invcdf(rng.random(k.size))
+                dk = np.cos(theta)[:, None] * d[k] + np.sin(theta)[:, None] * qk
+                qk = -np.sin(theta)[:, None] * d[k] + np.cos(theta)[:, None] * qk
+                d[k] = dk / np.linalg.norm(dk, axis=1, keepdims=True)
+                q[k] = qk / np.linalg.norm(qk, axis=1, keepdims=True)
+            live = dt > 0
+        radii[:, j] = np.linalg.norm(x, axis=1)
+    return radii
+
+
+def test_large_time_steps_match_continuous_time_flights():
+    """timeSteps = 1 runs the event scheme on 2^20 sub-steps per interval; its radial
+    energy agrees with independent continuous-time flights within Monte Carlo error."""
+    geo, src, mat, obs, opts = W.c1_acoustic3d()
+    mat = MaterialClass(geo, 10, True, 1, [0.2, 0.2], 0, "exp", 0.1)  # mean free time 0.13
+    obs = dict(obs, time=colon(0, 0.05, 1.5))
+    mat.timeSteps = 1
+    n = 100_000
+    prob, grid, N = build_problem(geo, dict(src, numberParticles=n), mat, obs,
+                                  dict(opts, exact_count=True, precision="fp64"))
+    assert prob.n_sub == 1 << 20
+    kn = O.table_knots(prob.tables)
+    he, se, _ = O.run(prob, kn, scheme="event")
+    he = he.reshape(grid.shape, order="F")[:, 0, :, 0]
+    radii = _continuous_time_flights(prob, kn, grid.t, n, np.random.default_rng(5))
+    edges = grid.edges[0]
+    ref = np.stack([np.histogram(radii[:, j], bins=edges)[0] for j in range(grid.t.size)], axis=1)
+    assert he[:, 0].sum() == 0 and ref[:, 1:].sum() > 0.99 * n * (grid.t.size - 1)
+    # bins share particles across time slices, so only per-bin statistics are tested
+    z = (he[:, 1:] - ref[:, 1:]) / np.sqrt(np.maximum(he[:, 1:] + ref[:, 1:], 1))
+    m = (he[:, 1:] + ref[:, 1:]) > 50
+    assert np.mean(np.abs(z[m]) < 3) > 0.99 and np.mean(z[m] ** 2) < 1.3
+    # scattering count: Poisson with mean n * T / mft
+    expect = n * (grid.t[-1] - grid.t[0]) / prob.mft[0]
+    assert abs(se["scatter_events"] - expect) < 5 * math.sqrt(expect)
+
+
+def test_large_time_steps_mean_square_displacement():
+    """Exponential flights with mean cosine g per scattering have the closed-form
+    <|x(t)|^2> = lambda^2 + 2 v^2 tau (t - tau (1 - exp(-t / tau))), tau = mft / (1 - g);
+    the event scheme on the timeSteps = 1 grid reproduces it from exact final positions."""
+    geo, src, mat, obs, opts = W.c1_acoustic3d()
+    mat = MaterialClass(geo, 10, True, 1, [0.2, 0.2], 0, "exp", 0.1)
+    mat.timeSteps = 1
+    n = 200_000
+    obs = dict(obs, time=colon(0, 0.1, 3.0))
+    prob, grid, N = build_problem(geo, dict(src, numberParticles=n), mat, obs,
+                                  dict(opts, exact_count=True, precision="fp64"))
+    kn = O.table_knots(prob.tables)
+    _, se, fs = O.run(prob, kn, scheme="event", want_state=True)
+    # final states hold the segment start (position at the last event, sub-step fs[:, 13])
+    cap = prob.n_sub * prob.n_obs
+    x = fs[:, :3] + (prob.v[0] * prob.h * (cap - fs[:, 13]))[:, None] * fs[:, 3:6]
+    r2 = np.sum(x ** 2, axis=1)
+    cdf, th = kn[0]
+    u = (np.arange(1 << 22) + 0.5) / (1 << 22)
+    g = float(np.mean(np.cos(_invcdf(u, cdf, th))))
+    tau = prob.mft[0] / (1 - g)
+    t, v = grid.t[-1], prob.v[0]
+    expect = prob.src_lambda ** 2 + 2 * v * v * tau * (t - tau * (1 - math.exp(-t / tau)))
+    assert 0.2 < g < 0.95 and t > tau  # forward scattering, past the ballistic regime
+    assert abs(r2.mean() - expect) < 4 * r2.std() / math.sqrt(n), (r2.mean(), expect)
