@@ -18,9 +18,10 @@
 extern "C" {
 #endif
 
-#define RTMC_ABI_VERSION 1
+#define RTMC_ABI_VERSION 2
 #define RTMC_MAX_BND 4
 #define RTMC_ZOE_N 181 /* Zoeppritz table on 0:0.5:90 degrees (MaterialClass.m:1809) */
+#define RTMC_MAX_RADIAL 65536 /* knots of a radial source profile */
 
 enum rtmc_status {
     RTMC_OK = 0,
@@ -44,6 +45,8 @@ enum rtmc_psdf {
 enum rtmc_frame { RTMC_FRAME_CARTESIAN = 0, RTMC_FRAME_CYLINDRICAL = 1, RTMC_FRAME_SPHERICAL = 2 };
 enum rtmc_axis_mode { RTMC_AXIS_IGNORED = 0, RTMC_AXIS_RANGE = 1, RTMC_AXIS_BINNED = 2 };
 enum rtmc_precision { RTMC_FP32 = 0, RTMC_FP64 = 1 };
+enum rtmc_source { RTMC_SOURCE_POINT = 0, RTMC_SOURCE_PLANE = 1 };
+enum rtmc_aperture { RTMC_APERTURE_RECTANGLE = 0, RTMC_APERTURE_CIRCLE = 1 };
 
 /* ---------------------------------------------------------------------------------- */
 /* Host FP64 table builders                                                            */
@@ -143,11 +146,22 @@ typedef struct {
     int64_t time_stride;
     int64_t mode_stride;
     int64_t hist_len;        /* int64 elements of the histogram */
-    int32_t bnd_dir[RTMC_MAX_BND];    /* 1, 2, 3: plane normal to x, y, z */
+    int32_t bnd_dir[RTMC_MAX_BND];    /* 1, 2, 3: plane x_dir = val; 4: cylinder sqrt(x^2 + y^2) = val */
     int32_t bnd_absorb[RTMC_MAX_BND]; /* 1 'absorbing', 0 'reflective' */
     double bnd_val[RTMC_MAX_BND];
-    double zoe_rpp[RTMC_ZOE_N];       /* E_Rpp on 0:0.5:90 deg (elastic reflective plane) */
+    double zoe_rpp[RTMC_ZOE_N];       /* E_Rpp on 0:0.5:90 deg (elastic reflective boundary) */
     double zoe_rsvsv[RTMC_ZOE_N];     /* E_Rsvsv on 0:0.5:90 deg */
+    /* source shape, initializeParticle.m:14-148; all zero is the Gaussian point source */
+    int32_t src_type;       /* enum rtmc_source: point or plane (3D only) */
+    int32_t src_aperture;   /* plane: enum rtmc_aperture */
+    int32_t src_radial_n;   /* point: knots of the radial inverse CDF (0: Gaussian radius), <= RTMC_MAX_RADIAL */
+    int32_t reserved2;
+    const double *src_radial_cdf; /* [src_radial_n] strictly increasing CDF values (initializeParticle.m:175-203) */
+    const double *src_radial_r;   /* [src_radial_n] radii at those CDF values */
+    double src_normal[3];   /* plane: unit propagation direction n */
+    double src_u[3];        /* plane: orthonormal basis (u, v) of the aperture plane, null(n) */
+    double src_v[3];
+    double src_extent[2];   /* plane: rectangle sides along u and v, or the circle radius in [0] */
 } rtmc_problem;
 
 typedef struct {

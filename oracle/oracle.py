@@ -45,7 +45,10 @@ class OracleProblem(C.Structure):
                 ("bnd_dir", C.c_int32 * 4), ("bnd_absorb", C.c_int32 * 4), ("bnd_val", C.c_double * 4),
                 ("zoe_rpp", C.POINTER(C.c_double)), ("zoe_rsvsv", C.POINTER(C.c_double)),
                 ("tab_n", C.c_int64 * 4), ("tab_cdf", C.POINTER(C.c_double) * 4),
-                ("tab_theta", C.POINTER(C.c_double) * 4)]
+                ("tab_theta", C.POINTER(C.c_double) * 4), ("src_type", C.c_int32), ("src_aperture", C.c_int32),
+                ("src_radial_n", C.c_int64), ("src_radial_cdf", C.POINTER(C.c_double)),
+                ("src_radial_r", C.POINTER(C.c_double)), ("src_normal", C.c_double * 3), ("src_u", C.c_double * 3),
+                ("src_v", C.c_double * 3), ("src_extent", C.c_double * 2)]
 
 
 _lib = None
@@ -129,6 +132,20 @@ def run(prob, knots, scheme: str = "event", u24: bool | None = None, nthreads: i
         zs = np.ascontiguousarray(prob.zoe_rsvsv, dtype=np.float64)
         keep += [zr, zs]
         P.zoe_rpp, P.zoe_rsvsv = _dp(zr), _dp(zs)
+    P.src_type = getattr(prob, "src_type", 0)
+    P.src_aperture = getattr(prob, "src_aperture", 0)
+    for i in range(3):
+        P.src_normal[i] = getattr(prob, "src_normal", (0.0, 0.0, 1.0))[i]
+        P.src_u[i] = getattr(prob, "src_u", (1.0, 0.0, 0.0))[i]
+        P.src_v[i] = getattr(prob, "src_v", (0.0, 1.0, 0.0))[i]
+    P.src_extent[0], P.src_extent[1] = getattr(prob, "src_extent", (0.0, 0.0))
+    radial = getattr(prob, "src_radial", None)
+    if radial is not None:
+        rc = np.ascontiguousarray(radial[0], dtype=np.float64)
+        rr = np.ascontiguousarray(radial[1], dtype=np.float64)
+        keep += [rc, rr]
+        P.src_radial_n = rc.size
+        P.src_radial_cdf, P.src_radial_r = _dp(rc), _dp(rr)
     for i, (c, t) in enumerate(knots):
         c = np.ascontiguousarray(c, dtype=np.float64)
         t = np.ascontiguousarray(t, dtype=np.float64)
@@ -147,7 +164,8 @@ def run(prob, knots, scheme: str = "event", u24: bool | None = None, nthreads: i
 
 
 def reflect(zoe_rpp, zoe_rsvsv, vp, vs, k, d, q, mode, u):
-    """Elastic reflection of n particles at the plane normal to e_k (test entry of the oracle)."""
+    """Elastic reflection of n particles at the plane normal to e_k (k = 0, 1, 2), or at a
+    cylinder wall with outward normal e_x (k = 3); test entry of the oracle."""
     d = np.ascontiguousarray(d, dtype=np.float64).copy()
     q = np.ascontiguousarray(q, dtype=np.float64).copy()
     mode = np.ascontiguousarray(mode, dtype=np.int32).copy()

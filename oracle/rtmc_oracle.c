@@ -77,8 +77,8 @@ typedef struct {
     int64_t time_stride;
     int64_t mode_stride;
     int64_t hist_len;
-    /* plane boundaries */
-    int32_t bnd_dir[OR_MAX_BND]; /* 1,2,3 */
+    /* boundaries */
+    int32_t bnd_dir[OR_MAX_BND]; /* 1,2,3: planes x_dir = val; 4: cylinder sqrt(x^2+y^2) = val */
     int32_t bnd_absorb[OR_MAX_BND];
     double bnd_val[OR_MAX_BND];
     const double *zoe_rpp;   /* 181 values, 0:0.5:90 deg */
@@ -87,6 +87,14 @@ typedef struct {
     int64_t tab_n[4];
     const double *tab_cdf[4];
     const double *tab_theta[4];
+    /* source shape (initializeParticle.m:14-148) */
+    int32_t src_type;     /* 0 point, 1 plane */
+    int32_t src_aperture; /* plane: 0 rectangle, 1 circle */
+    int64_t src_radial_n; /* point: knots of the radial inverse CDF, 0 = Gaussian radius */
+    const double *src_radial_cdf;
+    const double *src_radial_r;
+    double src_normal[3], src_u[3], src_v[3];
+    double src_extent[2];
 } oracle_problem;
 
 enum { ST_SCATTER = 0, ST_BOUNDARY, ST_KILL, ST_ABSORB, ST_OBS, ST_CONVERT, ST_N };
@@ -195,14 +203,53 @@ typedef struct {
     int alive;
 } particle_t;
 
-/* initializeParticle.m:14-58,151-170 (point source).  Slots: step 0, block 0 =
- * [r1, r2, phi0, theta0], block 1 = [phi, theta, alpha, next-scatter], block 2 = [kill]. */
+/* griddedInterpolant(cdf, r, 'linear', 'nearest') of initializeParticle.m:201 */
+static double radial_invcdf(const double *c, const double *r, int64_t n, double u)
+{
+    if (!(u > c[0])) return r[0];
+    if (!(u < c[n - 1])) return r[n - 1];
+    int64_t lo = 0, hi = n - 1;
+    while (hi - lo > 1) {
+        int64_t mid = (lo + hi) >> 1;
+        if (c[mid] <= u) lo = mid; else hi = mid;
+    }
+    return r[lo] + (u - c[lo]) / (c[hi] - c[lo]) * (r[hi] - r[lo]);
+}
+
+/* initializeParticle.m:14-148,151-170.  Slots: step 0, block 0 = [r1, r2, phi0, theta0]
+ * (plane source: [r1, r2, aperture 1, aperture 2]), block 1 = [phi, theta, alpha,
+ * next-scatter], block 2 = [kill]. */
 static void init_particle(const oracle_problem *P, const rng_t *g, particle_t *pt, double ub1[4])
 {
     double a[4];
     rng_block(g, 0, 0, a);
     rng_block(g, 0, 1, ub1);
-    double r = fabs(sqrt(-2.0 * log(a[0])) * cos(2.0 * M_PI * a[1])) * P->src_lambda;
+    if (P->src_type == 1) {
+        /* plane wave (:61-148): Gaussian offset lambda/2 along n, aperture offsets along u, v */
+        double c_long = sqrt(-2.0 * log(a[0])) * cos(2.0 * M_PI * a[1]) * P->src_lambda * 0.5;
+        double c1, c2;
+        if (P->src_aperture == 1) {
+            double rho = P->src_extent[0] * sqrt(a[2]);
+            double al = 2.0 * M_PI * a[3];
+            c1 = rho * cos(al);
+            c2 = rho * sin(al);
+        } else {
+            c1 = (a[2] - 0.5) * P->src_extent[0];
+            c2 = (a[3] - 0.5) * P->src_extent[1];
+        }
+        double th = 2.0 * M_PI * ub1[1];
+        double ct = cos(th), st = sin(th);
+        for (int i = 0; i < 3; ++i) {
+            pt->x[i] = P->src_pos[i] + c_long * P->src_normal[i] + c1 * P->src_u[i] + c2 * P->src_v[i];
+            pt->d[i] = P->src_normal[i];
+            pt->q[i] = ct * P->src_u[i] + st * P->src_v[i];
+        }
+        pt->mode = (!P->acoustics && P->polarization == 1) ? 1 : 0;
+        pt->alive = 1;
+        return;
+    }
+    double r = P->src_radial_n > 0 ? radial_invcdf(P->src_radial_cdf, P->src_radial_r, P->src_radial_n, a[0])
+                                   : fabs(sqrt(-2.0 * log(a[0])) * cos(2.0 * M_PI * a[1])) * P->src_lambda;
     double cphi0, sphi0, cphi, sphi;
     double theta0 = 2.0 * M_PI * a[3];
     double theta = 2.0 * M_PI * ub1[1];
@@ -329,6 +376,100 @@ static int elastic_plane_reflect(const oracle_problem *P, particle_t *pt, int k,
     return pt->mode != mode0;
 }
 
+static inline void mirror3(double v[3], const double n[3])
+{
+    double vn = 2.0 * dot3(v, n);
+    for (int i = 0; i < 3; ++i) v[i] -= vn * n[i];
+}
+
+/* Elastic reflection at the cylinder wall with outward unit normal n,
+ * propagateParticleSmallDt.m:356-571 (coefficients through griddedInterpolant 'linear',
+ * 'nearest' on 0:0.5:90 degrees).  Returns 1 when the mode changed. */
+static int elastic_cylinder_reflect(const oracle_problem *P, particle_t *pt, const double n[3], double u_split,
+                                    double u_coin, int64_t *stats)
+{
+    int mode0 = pt->mode;
+    double dn = dot3(pt->d, n);
+    double ang = acos(fmin(1.0, fmax(-1.0, dn))) * (180.0 / M_PI);
+    if (ang > 90.0) ang = 90.0;
+    if (pt->mode == 0) {
+        if (u_coin <= zoe_lookup(P->zoe_rpp, ang)) { /* P -> P, :392-405 */
+            mirror3(pt->d, n);
+            mirror3(pt->q, n);
+        } else {                                     /* P -> SV, :409-451 */
+            pt->mode = 1;
+            double eta = P->v[1] / P->v[0];
+            double nd[3];
+            for (int i = 0; i < 3; ++i) nd[i] = eta * (pt->d[i] - dn * n[i]);
+            double cv = sqrt(fmax(0.0, 1.0 - dot3(nd, nd)));
+            for (int i = 0; i < 3; ++i) nd[i] -= cv * n[i];
+            scale3(nd, 1.0 / norm3(nd));
+            memcpy(pt->d, nd, sizeof nd);
+            double ax[3];
+            cross3(pt->d, n, ax);
+            if (norm3(ax) < 1e-6) {
+                const double ex[3] = {1.0, 0.0, 0.0};
+                cross3(pt->d, ex, ax);
+            }
+            scale3(ax, 1.0 / norm3(ax));
+            cross3(ax, pt->d, pt->q);
+        }
+    } else {
+        double ax[3];
+        cross3(pt->d, n, ax);
+        double a2 = dot3(ax, ax);
+        double sh = dot3(pt->q, ax);
+        double prob_sh = a2 > 0 ? sh * sh / a2 : -1.0; /* NaN in the reference: never SH */
+        if (u_split < prob_sh) {                                   /* SH, :474-485 */
+            mirror3(pt->d, n);
+            mirror3(pt->q, n);
+        } else if (u_coin <= zoe_lookup(P->zoe_rsvsv, ang)) {      /* SV -> SV, :508-521 */
+            mirror3(pt->d, n);
+            mirror3(pt->q, n);
+        } else {                                                   /* SV -> P, :523-566 */
+            double eta = P->v[0] / P->v[1];
+            double nd[3];
+            for (int i = 0; i < 3; ++i) nd[i] = eta * (pt->d[i] - dn * n[i]);
+            double sin2 = dot3(nd, nd);
+            if (sin2 <= 1.0) {
+                pt->mode = 0;
+                double cv = sqrt(1.0 - sin2);
+                for (int i = 0; i < 3; ++i) nd[i] -= cv * n[i];
+                scale3(nd, 1.0 / norm3(nd));
+                memcpy(pt->d, nd, sizeof nd); /* polarisation kept */
+            } else {                          /* total internal reflection: SV mirror */
+                mirror3(pt->d, n);
+                mirror3(pt->q, n);
+            }
+        }
+    }
+    if (pt->mode != mode0) stats[ST_CONVERT]++;
+    return pt->mode != mode0;
+}
+
+/* Cylinder test and update of one boundary pass (propagateParticleSmallDt.m:325-352):
+ * 0 inside, 1 reflected, 2 absorbed. */
+static int cylinder_hit(const oracle_problem *P, const rng_t *g, uint32_t step, uint32_t block, int b,
+                        particle_t *pt, int *changed, int64_t *stats)
+{
+    double r = sqrt(pt->x[0] * pt->x[0] + pt->x[1] * pt->x[1]);
+    double over = r - P->bnd_val[b];
+    if (!(over > 0)) return 0;
+    stats[ST_BOUNDARY]++;
+    if (P->bnd_absorb[b]) { pt->alive = 0; stats[ST_ABSORB]++; return 2; }
+    double n[3] = {pt->x[0] / r, pt->x[1] / r, 0.0};
+    pt->x[0] -= 2.0 * over * n[0];
+    pt->x[1] -= 2.0 * over * n[1];
+    if (P->acoustics) {
+        mirror3(pt->d, n);
+    } else {
+        double bb[4];
+        rng_block(g, step, block, bb);
+        *changed |= elastic_cylinder_reflect(P, pt, n, bb[0], bb[1], stats);
+    }
+    return 1;
+}
+
 /* Scattering: azimuth (:604-611), mode conversion (:619-623), theta (:614-632),
  * rotation and renormalisation (:635-639).  Returns the new mode. */
 static void scatter(const oracle_problem *P, particle_t *pt, double u_phi, double u_mode, double u_theta)
@@ -452,6 +593,11 @@ static void run_substep(const oracle_problem *P, int64_t pid, int64_t *hist, int
             double step = P->v[m] * P->h;
             for (int i = 0; i < 3; ++i) pt.x[i] += step * pt.d[i];
             for (int b = 0; b < P->n_bnd && pt.alive; ++b) {
+                if (P->bnd_dir[b] == 4) {
+                    int ch = 0;
+                    if (cylinder_hit(P, &g, sg, 2 + b, b, &pt, &ch, stats) == 2) break;
+                    continue;
+                }
                 int k = P->bnd_dir[b] - 1;
                 double val = P->bnd_val[b];
                 if (!((pt.x[k] - val) * (x1[k] - val) < 0)) continue;
@@ -504,6 +650,33 @@ static inline int64_t geom_steps(double u, double rate, int64_t cap)
     return (int64_t)k;
 }
 
+/* outside the cylinder after j sub-steps of the segment, placed as the event step does */
+static inline int cyl_outside(const particle_t *pt, double step, int64_t j, double rad)
+{
+    double t = step * (double)j;
+    double x = pt->x[0] + t * pt->d[0], y = pt->x[1] + t * pt->d[1];
+    return sqrt(x * x + y * y) > rad;
+}
+
+/* first sub-step j in [1, lim) of a segment that ends outside the cylinder sqrt(x^2+y^2) =
+ * rad, or lim: the larger root of |P + j V|^2 = rad^2, settled on the exact test */
+static int64_t cyl_cross_steps(const particle_t *pt, double step, double rad, int64_t lim)
+{
+    if (cyl_outside(pt, step, 1, rad)) return 1;
+    double vx = step * pt->d[0], vy = step * pt->d[1];
+    double A = vx * vx + vy * vy;
+    if (!(A > 0)) return lim;
+    double B = pt->x[0] * vx + pt->x[1] * vy;
+    double Cc = pt->x[0] * pt->x[0] + pt->x[1] * pt->x[1] - rad * rad;
+    double sq = sqrt(fmax(0.0, B * B - A * Cc));
+    double jr = B > 0 ? -Cc / (B + sq) : (sq - B) / A;
+    if (!(jr < (double)lim)) return lim;
+    int64_t j = jr < 1.0 ? 1 : (int64_t)floor(jr);
+    for (int it = 0; it < 4 && j < lim && !cyl_outside(pt, step, j, rad); ++it) ++j;
+    for (int it = 0; it < 4 && j > 1 && cyl_outside(pt, step, j - 1, rad); ++it) --j;
+    return j < lim ? j : lim;
+}
+
 /* first sub-step j >= 1 of a segment at which the plane x_k = val is crossed */
 static inline int64_t plane_cross_steps(double a, double b, int64_t cap)
 {
@@ -543,6 +716,11 @@ static void run_event(const oracle_problem *P, int64_t pid, int64_t *hist, int u
         /* next boundary crossing on this segment */
         int64_t sB = cap;
         for (int b = 0; b < P->n_bnd; ++b) {
+            if (P->bnd_dir[b] == 4) {
+                int64_t j = cyl_cross_steps(&pt, step, P->bnd_val[b], cap - s0);
+                if (j < cap - s0 && s0 + j < sB) sB = s0 + j;
+                continue;
+            }
             int kk = P->bnd_dir[b] - 1;
             int64_t j = plane_cross_steps(pt.x[kk] - P->bnd_val[b], step * pt.d[kk], cap);
             if (j < cap && s0 + j < sB) sB = s0 + j;
@@ -571,6 +749,12 @@ static void run_event(const oracle_problem *P, int64_t pid, int64_t *hist, int u
             memcpy(pt.x, xe, sizeof xe);
             int changed = 0;
             for (int b = 0; b < P->n_bnd && pt.alive; ++b) {
+                if (P->bnd_dir[b] == 4) {
+                    int hit = cylinder_hit(P, &g, k, 1 + b, b, &pt, &changed, stats);
+                    nbnd += hit != 0;
+                    if (hit == 2) break;
+                    continue;
+                }
                 int kk = P->bnd_dir[b] - 1;
                 double val = P->bnd_val[b];
                 if (!((pt.x[kk] - val) * (x1[kk] - val) < 0)) continue;
@@ -686,7 +870,9 @@ int oracle_max_threads(void)
 int oracle_reflect(const double *zoe_rpp, const double *zoe_rsvsv, double vp, double vs, int k, int64_t n,
                    double *d, double *q, int32_t *mode, const double *u)
 {
-    if (k < 0 || k > 2 || n < 0) return 1;
+    /* k = 0, 1, 2: plane normal to e_k; k = 3: cylinder wall with outward normal e_x */
+    if (k < 0 || k > 3 || n < 0) return 1;
+    const double ex[3] = {1.0, 0.0, 0.0};
     oracle_problem P;
     memset(&P, 0, sizeof P);
     P.v[0] = vp;
@@ -700,7 +886,10 @@ int oracle_reflect(const double *zoe_rpp, const double *zoe_rsvsv, double vp, do
         memcpy(pt.q, q + 3 * i, sizeof pt.q);
         pt.mode = mode[i];
         pt.alive = 1;
-        elastic_plane_reflect(&P, &pt, k, u[2 * i], u[2 * i + 1], stats);
+        if (k == 3)
+            elastic_cylinder_reflect(&P, &pt, ex, u[2 * i], u[2 * i + 1], stats);
+        else
+            elastic_plane_reflect(&P, &pt, k, u[2 * i], u[2 * i + 1], stats);
         memcpy(d + 3 * i, pt.d, sizeof pt.d);
         memcpy(q + 3 * i, pt.q, sizeof pt.q);
         mode[i] = pt.mode;

@@ -20,6 +20,9 @@ AXIS_IGNORED, AXIS_RANGE, AXIS_BINNED = 0, 1, 2
 FP32, FP64 = 0, 1
 ZOE_N = 181
 MAX_BND = 4
+MAX_RADIAL = 65536
+SOURCE_POINT, SOURCE_PLANE = 0, 1
+APERTURE_RECTANGLE, APERTURE_CIRCLE = 0, 1
 
 
 class RtmcMaterial(C.Structure):
@@ -47,7 +50,10 @@ class RtmcProblem(C.Structure):
                 ("time_stride", C.c_int64), ("mode_stride", C.c_int64), ("hist_len", C.c_int64),
                 ("bnd_dir", C.c_int32 * MAX_BND), ("bnd_absorb", C.c_int32 * MAX_BND),
                 ("bnd_val", C.c_double * MAX_BND), ("zoe_rpp", C.c_double * ZOE_N),
-                ("zoe_rsvsv", C.c_double * ZOE_N)]
+                ("zoe_rsvsv", C.c_double * ZOE_N), ("src_type", C.c_int32), ("src_aperture", C.c_int32),
+                ("src_radial_n", C.c_int32), ("reserved2", C.c_int32), ("src_radial_cdf", C.POINTER(C.c_double)),
+                ("src_radial_r", C.POINTER(C.c_double)), ("src_normal", C.c_double * 3), ("src_u", C.c_double * 3),
+                ("src_v", C.c_double * 3), ("src_extent", C.c_double * 2)]
 
 
 class RtmcStats(C.Structure):

@@ -131,11 +131,38 @@ int check_problem(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t
         return fail(e, RTMC_ERR_ARG, "n_sub * n_obs must stay below 2^30 sub-steps");
     if (P->n_particles < 0 || P->pid0 < 0) return fail(e, RTMC_ERR_ARG, "particle count and first id must be >= 0");
     if (P->hist_shift < 0 || P->hist_shift > 62) return fail(e, RTMC_ERR_ARG, "hist_shift must be in [0, 62]");
-    if (P->n_bnd < 0 || P->n_bnd > RTMC_MAX_BND) return fail(e, RTMC_ERR_ARG, "at most 4 plane boundaries");
+    if (P->n_bnd < 0 || P->n_bnd > RTMC_MAX_BND) return fail(e, RTMC_ERR_ARG, "at most 4 boundaries");
     for (int b = 0; b < P->n_bnd; ++b) {
-        if (P->bnd_dir[b] < 1 || P->bnd_dir[b] > 3)
-            return fail(e, RTMC_ERR_ARG, "plane boundary dir must be 1, 2 or 3 (cylindrical dir 4 is not supported)");
+        if (P->bnd_dir[b] < 1 || P->bnd_dir[b] > 4)
+            return fail(e, RTMC_ERR_ARG, "boundary dir must be 1, 2, 3 (planes) or 4 (cylinder)");
         if (!std::isfinite(P->bnd_val[b])) return fail(e, RTMC_ERR_ARG, "boundary position must be finite");
+        if (P->bnd_dir[b] == 4 && !(P->bnd_val[b] > 0)) return fail(e, RTMC_ERR_ARG, "cylinder radius must be positive");
+    }
+    if (P->src_type != RTMC_SOURCE_POINT && P->src_type != RTMC_SOURCE_PLANE)
+        return fail(e, RTMC_ERR_ARG, "source type must be point or plane");
+    if (P->src_type == RTMC_SOURCE_PLANE) {
+        if (P->d != 3) return fail(e, RTMC_ERR_ARG, "plane sources are 3D only");
+        if (P->src_aperture != RTMC_APERTURE_RECTANGLE && P->src_aperture != RTMC_APERTURE_CIRCLE)
+            return fail(e, RTMC_ERR_ARG, "plane-source aperture must be rectangle or circle");
+        const double *vs[3] = {P->src_normal, P->src_u, P->src_v};
+        for (int i = 0; i < 3; ++i) {
+            const double nn = vs[i][0] * vs[i][0] + vs[i][1] * vs[i][1] + vs[i][2] * vs[i][2];
+            if (!(std::fabs(nn - 1.0) < 1e-9)) return fail(e, RTMC_ERR_ARG, "plane-source n, u, v must be unit vectors");
+        }
+        for (int i = 0; i < 2; ++i)
+            if (!std::isfinite(P->src_extent[i]) || P->src_extent[i] < 0)
+                return fail(e, RTMC_ERR_ARG, "plane-source extent must be finite and >= 0");
+    }
+    if (P->src_radial_n != 0) {
+        if (P->src_type != RTMC_SOURCE_POINT) return fail(e, RTMC_ERR_ARG, "a radial profile applies to point sources");
+        if (P->src_radial_n < 2 || P->src_radial_n > RTMC_MAX_RADIAL || !P->src_radial_cdf || !P->src_radial_r)
+            return fail(e, RTMC_ERR_ARG, "a radial source profile needs 2 to 65536 knots");
+        for (int k = 0; k < P->src_radial_n; ++k) {
+            if (!std::isfinite(P->src_radial_cdf[k]) || !std::isfinite(P->src_radial_r[k]) || P->src_radial_r[k] < 0)
+                return fail(e, RTMC_ERR_ARG, "radial source knots must be finite, radii >= 0");
+            if (k && !(P->src_radial_cdf[k] > P->src_radial_cdf[k - 1]))
+                return fail(e, RTMC_ERR_ARG, "radial source CDF knots must be strictly increasing");
+        }
     }
     const int nm = P->acoustics ? 1 : 2;
     for (int m = 0; m < nm; ++m) {
@@ -261,6 +288,19 @@ void fill_params(rtmc_context *ctx, const rtmc_problem *P, const DevTables<R> &t
         (*zoe)[k] = (R)P->zoe_rpp[k];
         (*zoe)[RTMC_ZOE_N + k] = (R)P->zoe_rsvsv[k];
     }
+    p->src_type = P->src_type;
+    p->src_aperture = P->src_aperture;
+    for (int i = 0; i < 3; ++i) {
+        p->src_n[i] = (R)P->src_normal[i];
+        p->src_u[i] = (R)P->src_u[i];
+        p->src_v[i] = (R)P->src_v[i];
+    }
+    p->src_ext[0] = (R)P->src_extent[0];
+    p->src_ext[1] = (R)P->src_extent[1];
+    // the radial source table follows the Zoeppritz tables (p->src_radial is set with p->zoe)
+    p->src_radial_n = P->src_radial_n;
+    for (int k = 0; k < P->src_radial_n; ++k) zoe->push_back((R)P->src_radial_cdf[k]);
+    for (int k = 0; k < P->src_radial_n; ++k) zoe->push_back((R)P->src_radial_r[k]);
     p->tab = tab;
     (void)ctx;
 }
@@ -298,6 +338,7 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
     h2d += (double)(edges.size() + zoe.size()) * sizeof(R);
     p.edges = reinterpret_cast<const R *>(aux);
     p.zoe = reinterpret_cast<const R *>(aux + eb);
+    p.src_radial = p.zoe + 2 * RTMC_ZOE_N;
     const size_t hist_bytes = (size_t)P->hist_len * sizeof(int64_t);
     if (ctx->hist.grow(hist_bytes)) return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for the histogram failed");
     CK(cudaMemsetAsync(ctx->hist.p, 0, hist_bytes, ctx->stream), "histogram clear");
@@ -571,8 +612,11 @@ int forward_noalloc(const rtmc_problem *P, const rtmc_tables *t, int64_t *d_hist
         return s == RTMC_ERR_ARG ? fail(nullptr, s, err) : fail(nullptr, RTMC_ERR_CUDA, "rtmc_forward_noalloc: table staging");
     DevParams<R> p;
     StackVec<R, kMaxEdges> edges;
-    StackVec<R, kMaxEdges> zoe; // same type as the edge list (2 x 181 values used)
+    StackVec<R, kMaxEdges> zoe; // same type as the edge list: 2 x 181 values and the radial table
     int n_edges = 0;
+    if (2 * RTMC_ZOE_N + 2 * P->src_radial_n > kMaxEdges)
+        return fail(nullptr, RTMC_ERR_ARG, "rtmc_forward_noalloc: a radial source profile holds at most " +
+                                               std::to_string((kMaxEdges - 2 * RTMC_ZOE_N) / 2) + " knots here");
     fill_params<R>(&slot, P, dt, &p, &n_edges, &edges, &zoe);
     const size_t e_off = align_up(used, 256);
     const size_t z_off = align_up(e_off + std::max<size_t>(1, edges.size()) * sizeof(R), 256);
@@ -594,6 +638,7 @@ int forward_noalloc(const rtmc_problem *P, const rtmc_tables *t, int64_t *d_hist
     if (e != cudaSuccess) return fail(nullptr, RTMC_ERR_CUDA, std::string("rtmc_forward_noalloc: ") + cudaGetErrorString(e));
     p.edges = reinterpret_cast<const R *>(base + e_off);
     p.zoe = reinterpret_cast<const R *>(base + z_off);
+    p.src_radial = p.zoe + 2 * RTMC_ZOE_N;
     p.hist = reinterpret_cast<unsigned long long *>(d_hist);
     p.stats = reinterpret_cast<unsigned long long *>(base + c_off);
     p.status = reinterpret_cast<int32_t *>(base + c_off + 128);
@@ -992,7 +1037,7 @@ int batch_create(rtmc_context *ctx, int n, const rtmc_problem *P, const rtmc_tab
     for (int i = 0; i < n; ++i) {
         toff[i] = total;
         for (int t = 0; t < T[i]->n_tables; ++t) total += table_bytes<R>(T[i]->cdf[t].size());
-        total += align_up(2 * RTMC_ZOE_N * sizeof(R), 256);
+        total += align_up((2 * RTMC_ZOE_N + 2 * (size_t)P[i].src_radial_n) * sizeof(R), 256);
     }
     if (b->tabs.grow(total)) return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for batched tables failed");
     std::vector<unsigned char> host(total, 0);
@@ -1012,6 +1057,7 @@ int batch_create(rtmc_context *ctx, int n, const rtmc_problem *P, const rtmc_tab
         fill_params<R>(ctx, &P[i], dt, &params[i], &n_edges, &edges, &zoe);
         std::memcpy(host.data() + o, zoe.data(), zoe.size() * sizeof(R));
         params[i].zoe = reinterpret_cast<const R *>(dev + o);
+        params[i].src_radial = params[i].zoe + 2 * RTMC_ZOE_N;
         params[i].sink = kSinkSmem;
         params[i].trace = nullptr;
         b->n_part[i] = P[i].n_particles;

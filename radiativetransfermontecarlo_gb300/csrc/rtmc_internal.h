@@ -71,8 +71,12 @@ template <typename R> struct DevParams {
     int32_t n_edges;
     int32_t bnd_dir[RTMC_MAX_BND], bnd_absorb[RTMC_MAX_BND];
     R bnd_val[RTMC_MAX_BND];
+    // source shape (initializeParticle.m:14-148)
+    int32_t src_type, src_aperture, src_radial_n, pad_src;
+    R src_n[3], src_u[3], src_v[3], src_ext[2];
     const R *edges;  // all binned/range edges, concatenated
-    const R *zoe;    // [2][RTMC_ZOE_N]: E_Rpp then E_Rsvsv
+    const R *zoe;    // [2][RTMC_ZOE_N]: E_Rpp then E_Rsvsv, then the radial source table
+    const R *src_radial;  // [2][src_radial_n]: CDF knots then radii (inside the zoe block)
     DevTables<R> tab;
     unsigned long long *hist;
     unsigned long long *stats;  // [8]

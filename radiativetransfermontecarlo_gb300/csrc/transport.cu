@@ -161,7 +161,36 @@ template <typename R> __device__ __forceinline__ void normalize3(R a[3])
     a[0] *= s; a[1] *= s; a[2] *= s;
 }
 
-// next plane crossing of the current segment (sub-step index, or cap)
+// outside the cylinder sqrt(x^2 + y^2) = rad after j sub-steps of the segment, evaluated
+// as process_event places the particle (propagateParticleSmallDt.m:327-334)
+template <typename R> __device__ __forceinline__ bool cyl_outside(const Part<R> &s, R step, int j, R rad)
+{
+    const R t = step * (R)j;
+    const R x = s.x[0] + t * s.d[0], y = s.x[1] + t * s.d[1];
+    return m_sqrt(x * x + y * y) > rad;
+}
+
+// first sub-step j in [1, lim) of the segment that ends outside the cylinder, or lim:
+// larger root of |P + j V|^2 = rad^2 (P, V the x-y position and per-sub-step move), then
+// settled on the exact test
+template <typename R> __device__ __forceinline__ int cyl_steps(const Part<R> &s, R step, R rad, int lim)
+{
+    if (cyl_outside(s, step, 1, rad)) return 1;
+    const R vx = step * s.d[0], vy = step * s.d[1];
+    const R A = vx * vx + vy * vy;
+    if (!(A > (R)0)) return lim;
+    const R B = s.x[0] * vx + s.x[1] * vy;
+    const R C = s.x[0] * s.x[0] + s.x[1] * s.x[1] - rad * rad;
+    const R sq = m_sqrt(m_max((R)0, B * B - A * C));
+    const R jr = B > (R)0 ? -C / (B + sq) : (sq - B) / A;
+    if (!(jr < (R)lim)) return lim;
+    int j = jr < (R)1 ? 1 : (int)m_floor(jr);
+    for (int it = 0; it < 4 && j < lim && !cyl_outside(s, step, j, rad); ++it) ++j;
+    for (int it = 0; it < 4 && j > 1 && cyl_outside(s, step, j - 1, rad); ++it) --j;
+    return j < lim ? j : lim;
+}
+
+// next boundary event of the current segment (sub-step index, or cap)
 template <typename R> __device__ __forceinline__ void next_boundary(const DevParams<R> &p, Part<R> &s)
 {
     const int cap = p.s_end + 1;
@@ -170,6 +199,11 @@ template <typename R> __device__ __forceinline__ void next_boundary(const DevPar
 #pragma unroll
     for (int b = 0; b < RTMC_MAX_BND; ++b) {
         if (b >= p.n_bnd) break;
+        if (p.bnd_dir[b] == 4) {
+            const int j = cyl_steps(s, step, p.bnd_val[b], cap - s.s0);
+            if (j < cap - s.s0) s.sB = s.s0 + j < s.sB ? s.s0 + j : s.sB;
+            continue;
+        }
         const int k = p.bnd_dir[b] - 1;
         const R a = sel3(s.x, k) - p.bnd_val[b];
         const R bs = step * sel3(s.d, k);
@@ -182,38 +216,78 @@ template <typename R> __device__ __forceinline__ void next_boundary(const DevPar
     }
 }
 
-// initializeParticle.m:14-58,151-170 (point source); step 0 of the particle's counter
+// griddedInterpolant(cdf, r, 'linear', 'nearest') of initializeParticle.m:201
+template <typename R> __device__ __forceinline__ R radial_invcdf(const R *cdf, const R *rad, int n, R u)
+{
+    if (!(u > cdf[0])) return rad[0];
+    if (!(u < cdf[n - 1])) return rad[n - 1];
+    int lo = 0, hi = n - 1; // cdf[lo] <= u < cdf[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (cdf[mid] <= u) lo = mid; else hi = mid;
+    }
+    const R w = (u - cdf[lo]) / (cdf[hi] - cdf[lo]);
+    return rad[lo] + w * (rad[hi] - rad[lo]);
+}
+
+// initializeParticle.m:14-148,151-170; step 0 of the particle's counter
 template <typename R> __device__ void init_particle(const DevParams<R> &p, uint64_t pid, Part<R> &s)
 {
-    const U4<R> a = draw(p, pid, 0u, 0u);  // r1, r2, phi0, theta0
+    const U4<R> a = draw(p, pid, 0u, 0u);  // r1, r2, phi0, theta0 (plane: r1, r2, aperture 1, 2)
     const U4<R> b = draw(p, pid, 0u, 1u);  // phi, theta, alpha, first scattering
-    const R r = m_abs(m_sqrt((R)-2 * m_log(a.a)) * m_cospi((R)2 * a.b)) * p.src_lambda;
-    R cphi0, sphi0, cphi, sphi;
-    if (p.d == 2) {
-        cphi0 = p.cos_half_pi; sphi0 = (R)1;
-        cphi = cphi0; sphi = sphi0;
-    } else {
-        cphi0 = (R)-1 + (R)2 * a.c;
-        sphi0 = m_sqrt(m_max((R)0, ((R)1 - cphi0) * ((R)1 + cphi0)));
-        cphi = (p.src_dir == 2) ? b.a : (R)-1 + (R)2 * b.a;
-        sphi = m_sqrt(m_max((R)0, ((R)1 - cphi) * ((R)1 + cphi)));
-    }
-    R st0, ct0, st, ct;
-    m_sincospi((R)2 * a.d, &st0, &ct0);
-    m_sincospi((R)2 * b.b, &st, &ct);
-    if (p.src_dir == 1) { st = st0; ct = ct0; cphi = cphi0; sphi = sphi0; }
-    s.d[0] = ct * sphi; s.d[1] = st * sphi; s.d[2] = cphi;
-    s.q[0] = -st; s.q[1] = ct; s.q[2] = (R)0;
-    if (p.d == 3) {
-        R sa, ca, cr[3];
-        m_sincospi((R)2 * b.c, &sa, &ca);
-        cross3(s.d, s.q, cr);
+    if (p.src_type == RTMC_SOURCE_PLANE) {
+        // plane wave (:61-148): Gaussian offset along n, aperture offsets along u and v
+        const R c_long = m_sqrt((R)-2 * m_log(a.a)) * m_cospi((R)2 * a.b) * p.src_lambda * (R)0.5;
+        R c1, c2;
+        if (p.src_aperture == RTMC_APERTURE_CIRCLE) {
+            const R rho = p.src_ext[0] * m_sqrt(a.c);
+            R sa, ca;
+            m_sincospi((R)2 * a.d, &sa, &ca);
+            c1 = rho * ca; c2 = rho * sa;
+        } else {
+            c1 = (a.c - (R)0.5) * p.src_ext[0];
+            c2 = (a.d - (R)0.5) * p.src_ext[1];
+        }
+        R st, ct;
+        m_sincospi((R)2 * b.b, &st, &ct);
 #pragma unroll
-        for (int i = 0; i < 3; ++i) s.q[i] = s.q[i] * ca + cr[i] * sa;
+        for (int i = 0; i < 3; ++i) {
+            s.x[i] = p.src_pos[i] + c_long * p.src_n[i] + c1 * p.src_u[i] + c2 * p.src_v[i];
+            s.d[i] = p.src_n[i];
+            s.q[i] = ct * p.src_u[i] + st * p.src_v[i];
+        }
+    } else {
+        // point source (:18-58): Gaussian radius, or the radial profile's inverse CDF
+        const R r = p.src_radial_n > 0
+                        ? radial_invcdf(p.src_radial, p.src_radial + p.src_radial_n, p.src_radial_n, a.a)
+                        : m_abs(m_sqrt((R)-2 * m_log(a.a)) * m_cospi((R)2 * a.b)) * p.src_lambda;
+        R cphi0, sphi0, cphi, sphi;
+        if (p.d == 2) {
+            cphi0 = p.cos_half_pi; sphi0 = (R)1;
+            cphi = cphi0; sphi = sphi0;
+        } else {
+            cphi0 = (R)-1 + (R)2 * a.c;
+            sphi0 = m_sqrt(m_max((R)0, ((R)1 - cphi0) * ((R)1 + cphi0)));
+            cphi = (p.src_dir == 2) ? b.a : (R)-1 + (R)2 * b.a;
+            sphi = m_sqrt(m_max((R)0, ((R)1 - cphi) * ((R)1 + cphi)));
+        }
+        R st0, ct0, st, ct;
+        m_sincospi((R)2 * a.d, &st0, &ct0);
+        m_sincospi((R)2 * b.b, &st, &ct);
+        if (p.src_dir == 1) { st = st0; ct = ct0; cphi = cphi0; sphi = sphi0; }
+        s.d[0] = ct * sphi; s.d[1] = st * sphi; s.d[2] = cphi;
+        s.q[0] = -st; s.q[1] = ct; s.q[2] = (R)0;
+        if (p.d == 3) {
+            R sa, ca, cr[3];
+            m_sincospi((R)2 * b.c, &sa, &ca);
+            cross3(s.d, s.q, cr);
+#pragma unroll
+            for (int i = 0; i < 3; ++i) s.q[i] = s.q[i] * ca + cr[i] * sa;
+        }
+        s.x[0] = p.src_pos[0] + r * ct0 * sphi0;
+        s.x[1] = p.src_pos[1] + r * st0 * sphi0;
+        s.x[2] = p.src_pos[2] + r * cphi0;
     }
-    s.x[0] = p.src_pos[0] + r * ct0 * sphi0;
-    s.x[1] = p.src_pos[1] + r * st0 * sphi0;
-    s.x[2] = p.src_pos[2] + r * cphi0;
     s.mode = (!p.acoustics && p.polarization == 1) ? 1 : 0;
     s.alive = 1;
     s.k = 0;
@@ -319,6 +393,85 @@ __device__ int elastic_reflect(const DevParams<R> &p, Part<R> &s, int k, R u_spl
     return s.mode != m0;
 }
 
+// mirror of v in the plane normal to the unit vector n: v - 2 (v.n) n
+template <typename R> __device__ __forceinline__ void mirror3(R v[3], const R n[3])
+{
+    const R vn = (R)2 * dot3(v, n);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) v[i] -= vn * n[i];
+}
+
+// elastic reflection at the cylinder wall with outward unit normal n
+// (propagateParticleSmallDt.m:356-571): P -> P or P -> SV by E_Rpp; S split into SH / SV by
+// the polarisation's component along d x n; SV -> SV or SV -> P by E_Rsvsv, with total
+// internal reflection falling back to an SV mirror.  Angles past 90 degrees take the
+// 90-degree coefficient ('nearest' extrapolation).  Returns 1 if the mode changed.
+template <typename R>
+__device__ int cylinder_reflect(const DevParams<R> &p, Part<R> &s, const R n[3], R u_split, R u_coin)
+{
+    const int m0 = s.mode;
+    const R dn = dot3(s.d, n);
+    R ang = m_acos(dn < (R)-1 ? (R)-1 : (dn > (R)1 ? (R)1 : dn)) * (R)57.295779513082320876798154814105;
+    ang = ang > (R)90 ? (R)90 : ang;
+    if (s.mode == 0) {
+        if (u_coin <= zoe_lookup(p.zoe, ang)) { // P -> P
+            mirror3(s.d, n);
+            mirror3(s.q, n);
+        } else { // P -> SV (:409-451)
+            s.mode = 1;
+            const R eta = p.vs_over_vp;
+            R nd[3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) nd[i] = eta * (s.d[i] - dn * n[i]);
+            const R cv = m_sqrt(m_max((R)0, (R)1 - dot3(nd, nd)));
+#pragma unroll
+            for (int i = 0; i < 3; ++i) nd[i] -= cv * n[i];
+            normalize3(nd);
+            s.d[0] = nd[0]; s.d[1] = nd[1]; s.d[2] = nd[2];
+            R ax[3];
+            cross3(s.d, n, ax);
+            if (m_sqrt(dot3(ax, ax)) < (R)1e-6) { // normal incidence: axis d x e_x
+                const R ex[3] = {(R)1, (R)0, (R)0};
+                cross3(s.d, ex, ax);
+            }
+            normalize3(ax);
+            cross3(ax, s.d, s.q);
+        }
+    } else {
+        R ax[3];
+        cross3(s.d, n, ax);
+        const R a2 = dot3(ax, ax);
+        const R sh = dot3(s.q, ax);
+        // (q . (d x n) / |d x n|)^2; d parallel to n leaves it undefined and the particle SV
+        const R prob_sh = a2 > (R)0 ? sh * sh / a2 : (R)-1;
+        if (u_split < prob_sh) { // SH -> SH
+            mirror3(s.d, n);
+            mirror3(s.q, n);
+        } else if (u_coin <= zoe_lookup(p.zoe + RTMC_ZOE_N, ang)) { // SV -> SV
+            mirror3(s.d, n);
+            mirror3(s.q, n);
+        } else { // SV -> P (:523-566)
+            const R eta = p.vp_over_vs;
+            R nd[3];
+#pragma unroll
+            for (int i = 0; i < 3; ++i) nd[i] = eta * (s.d[i] - dn * n[i]);
+            const R sin2 = dot3(nd, nd);
+            if (sin2 <= (R)1) {
+                s.mode = 0;
+                const R cv = m_sqrt((R)1 - sin2);
+#pragma unroll
+                for (int i = 0; i < 3; ++i) nd[i] -= cv * n[i];
+                normalize3(nd);
+                s.d[0] = nd[0]; s.d[1] = nd[1]; s.d[2] = nd[2]; // polarisation kept
+            } else { // total internal reflection: SV mirror
+                mirror3(s.d, n);
+                mirror3(s.q, n);
+            }
+        }
+    }
+    return s.mode != m0;
+}
+
 // azimuth, mode conversion, polar angle, rotation (propagateParticleSmallDt.m:603-639)
 template <typename R>
 __device__ __forceinline__ void scatter(const DevParams<R> &p, Part<R> &s, R u_phi, R u_mode, R u_theta)
@@ -385,8 +538,33 @@ __device__ void process_event(const DevParams<R> &p, uint64_t pid, Part<R> &s, C
 #pragma unroll
         for (int b = 0; b < RTMC_MAX_BND; ++b) {
             if (b >= p.n_bnd) break;
-            const int k = p.bnd_dir[b] - 1;
             const R val = p.bnd_val[b];
+            if (p.bnd_dir[b] == 4) { // cylinder (propagateParticleSmallDt.m:325-348)
+                const R r = m_sqrt(s.x[0] * s.x[0] + s.x[1] * s.x[1]);
+                const R over = r - val;
+                if (!(over > (R)0)) continue;
+                cnt.bnd++;
+                if (p.bnd_absorb[b]) {
+                    s.alive = 0;
+                    s.s0 = e;
+                    s.s_death = e;
+                    cnt.absorb++;
+                    return;
+                }
+                const R n[3] = {s.x[0] / r, s.x[1] / r, (R)0};
+                s.x[0] -= (R)2 * over * n[0];
+                s.x[1] -= (R)2 * over * n[1];
+                if (p.acoustics) {
+                    mirror3(s.d, n);
+                } else {
+                    const U4<R> bb = draw(p, pid, s.k, 1u + (uint32_t)b);
+                    const int ch = cylinder_reflect(p, s, n, bb.a, bb.b);
+                    cnt.conv += ch;
+                    changed |= ch;
+                }
+                continue;
+            }
+            const int k = p.bnd_dir[b] - 1;
             const R xk = sel3(s.x, k);
             if (!((xk - val) * (sel3(x1, k) - val) < (R)0)) continue;
             cnt.bnd++;

@@ -59,6 +59,13 @@ class TransportProblem:
     bnd: list = field(default_factory=list)     # [(dir, val, absorbing)]
     zoe_rpp: np.ndarray | None = None
     zoe_rsvsv: np.ndarray | None = None
+    src_type: int = 0                            # _lib.SOURCE_POINT / SOURCE_PLANE
+    src_aperture: int = 0                        # _lib.APERTURE_RECTANGLE / APERTURE_CIRCLE
+    src_normal: tuple = (0.0, 0.0, 1.0)
+    src_u: tuple = (1.0, 0.0, 0.0)
+    src_v: tuple = (0.0, 1.0, 0.0)
+    src_extent: tuple = (0.0, 0.0)
+    src_radial: tuple | None = None              # (cdf knots, radii) of a radial point source
 
     def to_ctypes(self):
         """Return (RtmcProblem, keep-alive list of the arrays it points into)."""
@@ -89,6 +96,16 @@ class TransportProblem:
             for k in range(_lib.ZOE_N):
                 P.zoe_rpp[k] = self.zoe_rpp[k]
                 P.zoe_rsvsv[k] = self.zoe_rsvsv[k]
+        P.src_type, P.src_aperture = self.src_type, self.src_aperture
+        for i in range(3):
+            P.src_normal[i], P.src_u[i], P.src_v[i] = self.src_normal[i], self.src_u[i], self.src_v[i]
+        P.src_extent[0], P.src_extent[1] = self.src_extent
+        if self.src_radial is not None:
+            c = np.ascontiguousarray(self.src_radial[0], dtype=np.float64)
+            r = np.ascontiguousarray(self.src_radial[1], dtype=np.float64)
+            keep += [c, r]
+            P.src_radial_n = c.size
+            P.src_radial_cdf, P.src_radial_r = _lib.dptr(c), _lib.dptr(r)
         return P, keep
 
 
@@ -101,6 +118,80 @@ def _q_values(material: MaterialClass):
     if material.acoustics:
         return Qv[0], Qv[0]
     return (Qv[0], Qv[0]) if Qv.size == 1 else (Qv[0], Qv[1])
+
+
+def radial_source_table(f, d: int, rmax: float, n: int = 10000) -> tuple[np.ndarray, np.ndarray]:
+    """Inverse CDF of a radial source profile f(r) in dimension d (initializeParticle.m:175-203):
+    pdf ~ r^(d-1) f(r) on linspace(0, rmax, n), cumulative sum, end values pinned to 0 and 1,
+    flat stretches dropped.  Returns the (cdf, r) knots of the linear interpolant."""
+    x = np.linspace(0.0, rmax, n)
+    w = x ** (d - 1) * np.asarray(f(x), dtype=float)
+    pdf = w / (0.5 * np.sum((w[1:] + w[:-1]) * np.diff(x)))  # trapz
+    cdf = np.cumsum(pdf) * np.mean(np.diff(x))
+    cdf[0], cdf[-1] = 0.0, 1.0
+    i = np.flatnonzero(np.diff(cdf) > 0)
+    ind = np.unique(np.concatenate([i, i + 1]))
+    c, first = np.unique(np.sort(cdf[ind]), return_index=True)
+    r = np.sort(x[ind])[first]
+    return c, r
+
+
+def _radial_profile(source: dict, d: int):
+    """source['radial']: a (grid, values) pair read as griddedInterpolant(grid, values) (linear,
+    linear extrapolation; Rmax = grid[-1]), or a callable f with source['radialMax']."""
+    rad = source["radial"]
+    if callable(rad):
+        if source.get("radialMax") is None:
+            raise ValueError("a callable radial profile needs source['radialMax']")
+        return radial_source_table(rad, d, float(source["radialMax"]))
+    g, v = (np.asarray(a, dtype=float).ravel() for a in rad)
+    if g.size < 2 or g.size != v.size or np.any(np.diff(g) <= 0):
+        raise ValueError("radial profile grid must be increasing and match its values")
+
+    def f(x):
+        y = np.interp(x, g, v)
+        lo, hi = x < g[0], x > g[-1]
+        y[lo] = v[0] + (x[lo] - g[0]) * (v[1] - v[0]) / (g[1] - g[0])
+        y[hi] = v[-1] + (x[hi] - g[-1]) * (v[-1] - v[-2]) / (g[-1] - g[-2])
+        return y
+    return radial_source_table(f, d, float(g[-1]))
+
+
+def _plane_source(source: dict):
+    """Plane-wave source geometry (initializeParticle.m:61-148): unit normal n, an orthonormal
+    basis (u, v) of the plane normal to n from the SVD of n (as MATLAB's null), the aperture
+    and its extent."""
+    sd = source.get("direction")
+    if sd is None:
+        raise ValueError("a plane source needs source['direction'] (+-1, +-2, +-3 or a 3-vector)")
+    sd = np.atleast_1d(np.asarray(sd, dtype=float)).ravel()
+    if sd.size == 1:
+        k = int(sd[0])
+        if k != sd[0] or abs(k) not in (1, 2, 3):
+            raise ValueError("For a scalar plane-source direction, use +-1, +-2, or +-3.")
+        n = np.zeros(3)
+        n[abs(k) - 1] = math.copysign(1.0, k)
+    elif sd.size == 3:
+        n = sd
+    else:
+        raise ValueError("For a plane source, source.direction must be a 3-component vector or a scalar axis "
+                         "+-1, +-2, or +-3.")
+    n = n / np.linalg.norm(n)
+    vh = np.linalg.svd(n.reshape(1, 3))[2]
+    u, v = vh[1], vh[2]
+    aperture = str(source.get("aperture") or "rectangle").lower()
+    ext = np.atleast_1d(np.asarray(source.get("extent", 0.0), dtype=float)).ravel()
+    if aperture == "rectangle":
+        ap = _lib.APERTURE_RECTANGLE
+        extent = (float(ext[0]), float(ext[0])) if ext.size == 1 else (float(ext[0]), float(ext[1]))
+    elif aperture == "circle":
+        if ext.size != 1:
+            raise ValueError("For source.aperture = 'circle', source.extent must be a scalar radius.")
+        ap = _lib.APERTURE_CIRCLE
+        extent = (float(ext[0]), 0.0)
+    else:
+        raise ValueError("Unknown plane-wave aperture: use 'rectangle' or 'circle'.")
+    return ap, tuple(n), tuple(u), tuple(v), extent
 
 
 def build_problem(geometry: dict, source: dict, material: MaterialClass, observation: dict,
@@ -149,17 +240,26 @@ def build_problem(geometry: dict, source: dict, material: MaterialClass, observa
                              "mat.Frequency before using Q-based attenuation.")
         omega = 2 * math.pi * float(np.atleast_1d(material.Frequency)[0])
         qrate = [omega * h / QP if math.isfinite(QP) else 0.0, omega * h / QS if math.isfinite(QS) else 0.0]
-    # source (initializeParticle.m:3-12, 157-160)
+    # source (initializeParticle.m:3-148, 157-160)
     stype = source.get("type", "point")
-    if stype != "point":
-        raise NotImplementedError("only point sources are supported")
-    if source.get("radial") is not None:
-        raise NotImplementedError("radial source profiles are not supported")
     pos = list(np.atleast_1d(np.asarray(source.get("position", [0.0, 0.0, 0.0]), dtype=float)))
     if len(pos) == 2:
         pos.append(0.0)
-    sdir = source.get("direction", "uniform")
-    src_dir = {"uniform": 0, "outgoing": 1, "upper": 2}.get(sdir if isinstance(sdir, str) else "uniform", 0)
+    src_dir = 0
+    plane = dict(src_type=_lib.SOURCE_POINT)
+    radial = None
+    if stype == "point":
+        sdir = source.get("direction", "uniform")
+        src_dir = {"uniform": 0, "outgoing": 1, "upper": 2}.get(sdir if isinstance(sdir, str) else "uniform", 0)
+        if source.get("radial") is not None and np.size(source["radial"]) > 0:
+            radial = _radial_profile(source, d)
+    elif stype == "plane":
+        if d != 3:
+            raise ValueError("plane sources are 3D only")
+        ap, n, u, v, extent = _plane_source(source)
+        plane = dict(src_type=_lib.SOURCE_PLANE, src_aperture=ap, src_normal=n, src_u=u, src_v=v, src_extent=extent)
+    else:
+        raise ValueError(f"unknown source type '{stype}' (point or plane)")
     pol = 1 if (not acoustics and source.get("polarization", "P") == "S") else 0
     # boundaries (propagateParticleSmallDt.m:146-166)
     bnd = []
@@ -167,11 +267,11 @@ def build_problem(geometry: dict, source: dict, material: MaterialClass, observa
         btype = (b.get("type") or "reflective").lower()
         if btype not in ("reflective", "absorbing"):
             raise ValueError(f'Unknown boundary type "{btype}". Use "reflective" or "absorbing".')
-        if int(b["dir"]) == 4:
-            raise NotImplementedError("cylindrical boundaries (dir = 4) are not supported")
+        if int(b["dir"]) not in (1, 2, 3, 4):
+            raise ValueError("boundary dir must be 1, 2, 3 (planes) or 4 (cylinder)")
         bnd.append((int(b["dir"]), float(b["val"]), btype == "absorbing"))
     if len(bnd) > _lib.MAX_BND:
-        raise ValueError("at most 4 plane boundaries")
+        raise ValueError("at most 4 boundaries")
     zr = zs = None
     if not acoustics and any(not ab for _, _, ab in bnd):
         z = MaterialClass.Zoeppritz(material)
@@ -194,7 +294,7 @@ def build_problem(geometry: dict, source: dict, material: MaterialClass, observa
         qrate=tuple(qrate), h=h, axis_mode=modes, axis_edges=list(grid.edges), axis_stride=list(grid.axis_stride),
         time_stride=grid.time_stride, mode_stride=grid.mode_stride, hist_len=grid.hist_len, shape=grid.shape,
         tables=material.invcdf, pid0=int(opt["pid0"]), hist_shift=int(opt["hist_shift"]), bnd=bnd,
-        zoe_rpp=zr, zoe_rsvsv=zs)
+        zoe_rpp=zr, zoe_rsvsv=zs, src_radial=radial, **plane)
     return prob, grid, N
 
 

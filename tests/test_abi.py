@@ -31,7 +31,7 @@ def test_struct_layout_matches_binding():
     assert lib.rtmc_abi_sizes(sizes) == 0
     assert list(sizes) == [C.sizeof(_lib.RtmcMaterial), C.sizeof(_lib.RtmcTablesInfo),
                            C.sizeof(_lib.RtmcProblem), C.sizeof(_lib.RtmcStats)]
-    assert lib.rtmc_abi_version() == 1
+    assert lib.rtmc_abi_version() == 2
 
 
 def test_host_functions_report_errors():

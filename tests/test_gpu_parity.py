@@ -197,3 +197,57 @@ def test_large_time_steps_scheme_matches_oracle(precision):
         assert _l1_diff(hist, ref_hist) >> prob.hist_shift <= max(4, 1e-6 * stats["observations"])
     else:
         assert _path_match(states, ref_states, 1e-3).mean() >= 0.99
+
+
+def _feature_cases():
+    cyl_geo = {"dimension": 3, "frame": "cylindrical", "bnd": [{"dir": 4, "val": 1.0}]}
+    ac = MaterialClass(cyl_geo, 10, True, 1, [0.2, 0.2], 0, "exp", 0.1)
+    el = MaterialClass(cyl_geo, 5, False, [2, 1.155], [0.2, 0.2, 0.2], [0, 0, 0], "exp", 0.2)
+    el.rho = 1000.0
+    cyl_obs = {"x": colon(0, 0.05, 1.0), "time": colon(0, 0.05, 2.0)}
+    cart = {"dimension": 3, "frame": "cartesian"}
+    cart_obs = {"x": colon(-2, 0.1, 3), "y": colon(-2, 0.25, 2), "time": colon(0, 0.05, 2.0)}
+    two_d = {"dimension": 2, "frame": "cylindrical", "bnd": [{"dir": 4, "val": 1.5}, {"dir": 2, "val": -1.0}]}
+    el2 = MaterialClass(two_d, 8, False, [2, 1.155], [0.2, 0.2, 0.2], [0, 0, 0], "exp", 0.5)
+    el2.rho = 1000.0
+    return {
+        "cylinder_acoustic": (cyl_geo, {"lambda": 0.05, "position": [0.3, 0, 0]}, ac, cyl_obs, {"seed": 7}),
+        "cylinder_elastic": (cyl_geo, {"lambda": 0.05, "position": [0.3, 0, 0], "polarization": "S"}, el, cyl_obs,
+                             {"seed": 8}),
+        "cylinder_and_plane_2d": (two_d, {"lambda": 0.05, "position": [0.2, 0.0]}, el2,
+                                  {"x": colon(0, 0.05, 1.5), "time": colon(0, 0.05, 1.0)}, {"seed": 9}),
+        "absorbing_cylinder": (dict(cyl_geo, bnd=[{"dir": 4, "val": 1.0, "type": "absorbing"}]),
+                               {"lambda": 0.05}, ac, cyl_obs, {"seed": 10}),
+        "plane_rectangle": (cart, {"type": "plane", "direction": [1, 1, 0], "extent": [1.0, 0.5], "lambda": 0.1},
+                            MaterialClass(cart, 10, True, 1, [0.2, 0.2], 0, "exp", 0.1), cart_obs, {"seed": 11}),
+        "plane_circle": (cart, {"type": "plane", "direction": -3, "aperture": "circle", "extent": 0.7,
+                                "lambda": 0.1}, MaterialClass(cart, 10, True, 1, [0.2, 0.2], 0, "exp", 0.1),
+                         dict(cart_obs, x=colon(-1, 0.1, 1), y=None, z=colon(-3, 0.1, 1)), {"seed": 12}),
+        "radial_source": ({"dimension": 3}, {"lambda": 0.05, "radial": ([0.0, 0.2, 0.4], [1.0, 0.5, 0.0])},
+                          MaterialClass({"dimension": 3}, 10, True, 1, [0.2, 0.2], 0, "exp", 0.1),
+                          {"x": colon(0, 0.05, 3), "time": colon(0, 0.05, 2.0)}, {"seed": 13}),
+    }
+
+
+@pytest.mark.parametrize("name", sorted(_feature_cases()))
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_boundaries_and_sources_match_oracle(name, precision):
+    """Cylinder boundaries (dir 4, reflective and absorbing, acoustic and elastic, alone and
+    beside a plane), plane-wave and radial sources: GPU traces against the event oracle."""
+    geo, src, mat, obs, opts = _feature_cases()[name]
+    obs = {k: v for k, v in obs.items() if v is not None}
+    prob, grid, N, hist, states, stats, ref_hist, ref_states, ref_stats = _run_both(geo, src, mat, obs, opts, 8000,
+                                                                                    precision)
+    assert stats["device_status"] == 0
+    if precision == "fp64":
+        ok = _path_match(states, ref_states, 1e-9)
+        assert ok.mean() == 1.0, f"{(~ok).sum()} particles left the oracle's trajectory"
+        for k in ("scatter_events", "boundary_hits", "kills", "absorbed", "conversions"):
+            assert stats[k] == ref_stats[k], k
+        assert _l1_diff(hist, ref_hist) >> prob.hist_shift <= max(4, 1e-6 * stats["observations"])
+    else:
+        assert _path_match(states, ref_states, 1e-3).mean() >= 0.99
+        rel = abs(stats["boundary_hits"] - ref_stats["boundary_hits"]) / max(1, ref_stats["boundary_hits"])
+        assert rel < 0.02
+    if "cylinder" in name:
+        assert stats["boundary_hits"] > 0

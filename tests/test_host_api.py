@@ -73,8 +73,17 @@ def test_problem_set_up_errors_like_the_reference():
     m.Q = 100  # finite Q needs a frequency (propagateParticleSmallDt.m:59-62)
     with pytest.raises(ValueError, match="Frequency"):
         build_problem(geo, src, m, obs, opts)
-    with pytest.raises(NotImplementedError):
-        build_problem(dict(geo, bnd=[{"dir": 4, "val": 1}]), src, mat, obs, opts)
+    with pytest.raises(ValueError, match="boundary dir"):
+        build_problem(dict(geo, bnd=[{"dir": 5, "val": 1}]), src, mat, obs, opts)
+    with pytest.raises(ValueError, match="plane sources are 3D only"):
+        g2, s2, m2, o2, p2 = W.c3_halfspace2d()
+        build_problem(g2, dict(s2, type="plane", direction=1, extent=1), m2, o2, p2)
+    with pytest.raises(ValueError, match="use \\+-1"):
+        build_problem(geo, dict(src, type="plane", direction=4, extent=1), mat, obs, opts)
+    with pytest.raises(ValueError, match="scalar radius"):
+        build_problem(geo, dict(src, type="plane", direction=3, aperture="circle", extent=[1, 2]), mat, obs, opts)
+    with pytest.raises(ValueError, match="Unknown plane-wave aperture"):
+        build_problem(geo, dict(src, type="plane", direction=3, aperture="hexagon", extent=1), mat, obs, opts)
     with pytest.raises(ValueError, match="density"):
         geo3, src3, mat3, obs3, opts3 = W.c3_halfspace2d()
         mat3.rho = None

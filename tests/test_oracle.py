@@ -218,3 +218,158 @@ def test_large_time_steps_mean_square_displacement():
     expect = prob.src_lambda ** 2 + 2 * v * v * tau * (t - tau * (1 - math.exp(-t / tau)))
     assert 0.2 < g < 0.95 and t > tau  # forward scattering, past the ballistic regime
     assert abs(r2.mean() - expect) < 4 * r2.std() / math.sqrt(n), (r2.mean(), expect)
+
+
+@pytest.mark.parametrize("mode,angle", [("P", 15), ("P", 45), ("P", 70), ("SV", 10), ("SV", 25), ("SV", 50),
+                                        ("SH", 30)])
+def test_cylinder_wall_energy_partition(mode, angle):
+    """propagateParticleSmallDt.m:356-571: at the cylinder wall (outward normal n = e_x) a P
+    packet ends as P with probability E_Rpp, an SV packet converts to P with probability
+    1 - E_Rsvsv below the critical angle and never above it (total internal reflection),
+    and an SH packet stays S; every particle heads back inside."""
+    vp, vs, rho = 2500.0, 2500.0 / math.sqrt(3), 2000.0
+    mat = MaterialClass.preset(3)
+    mat.vp, mat.vs, mat.rho = vp, vs, rho
+    z = MaterialClass.Zoeppritz(mat)
+    n = 200_000
+    a = math.radians(angle)
+    d0 = np.array([math.cos(a), 0.0, math.sin(a)])
+    eSH = np.array([0.0, 1.0, 0.0])  # d x n / |d x n|
+    eSV = np.cross(eSH, d0)
+    d = np.tile(d0, (n, 1))
+    q = np.tile(eSV if mode == "SV" else eSH, (n, 1))
+    m = np.full(n, 0 if mode == "P" else 1)
+    u = np.random.default_rng(100 + angle).random(2 * n)
+    d2, q2, m2 = O.reflect(z["E_Rpp"], z["E_Rsvsv"], vp, vs, 3, d, q, m, u)
+    frac_p = np.mean(m2 == 0)
+    crit = math.degrees(math.asin(vs / vp))
+    if mode == "P":
+        want = np.interp(angle, z["j1_deg"], z["E_Rpp"])
+    elif mode == "SV":
+        want = 1 - np.interp(angle, z["j1_deg"], z["E_Rsvsv"]) if angle < crit else 0.0
+    else:
+        want = 0.0
+    assert abs(frac_p - want) < 5 * math.sqrt(max(want * (1 - want), 1e-6) / n) + 1e-12
+    assert np.all(d2[:, 0] < 0)
+    assert np.allclose(np.linalg.norm(d2, axis=1), 1.0)
+    conv = (m == 0) & (m2 == 1)  # P -> SV: tangential slowness conserved
+    if conv.any():
+        assert np.allclose(np.hypot(d2[conv, 1], d2[conv, 2]), math.sin(a) * vs / vp, atol=1e-12)
+        assert np.allclose(np.sum(q2[conv] * d2[conv], axis=1), 0.0, atol=1e-12)
+
+
+def _cylinder_case(acoustics, n_t=1.5):
+    geo = {"dimension": 3, "frame": "cylindrical", "bnd": [{"dir": 4, "val": 1.0}]}
+    if acoustics:
+        mat = MaterialClass(geo, 10, True, 1, [0.2, 0.2], 0, "exp", 0.1)
+        src = {"lambda": 0.05, "position": [0.3, 0.0, 0.0]}
+    else:
+        mat = MaterialClass(geo, 5, False, [2, 1.155], [0.2, 0.2, 0.2], [0, 0, 0], "exp", 0.2)
+        mat.rho = 1000.0
+        src = {"lambda": 0.05, "position": [0.3, 0.0, 0.0], "polarization": "P"}
+    obs = {"x": colon(0, 0.05, 1.0), "time": colon(0, 0.05, n_t)}
+    return geo, src, mat, obs, {"seed": 3}
+
+
+@pytest.mark.parametrize("acoustics", [True, False])
+def test_cylinder_event_scheme_equals_substep_scheme(acoustics):
+    """Reflective cylinder sqrt(x^2 + y^2) = 1 (bnd.dir = 4): the event scheme's closed-form
+    crossing and the reference-order sub-step scheme give the same distribution; nothing
+    leaves the cylinder, so the radial histogram keeps every particle."""
+    geo, src, mat, obs, opts = _cylinder_case(acoustics)
+    prob, grid, N, he, hs, se, ss = _both(geo, src, mat, obs, opts, 20000)
+    assert prob.bnd == [(4, 1.0, False)]
+    assert _chi2_per_dof(he, hs) < 1.3
+    for k in ("boundary_hits", "conversions", "scatter_events"):
+        assert abs(se[k] - ss[k]) < 5 * math.sqrt(max(se[k], 1)) + 5, k
+    assert se["boundary_hits"] > 5000
+    for h in (he, hs):
+        per_t = h.sum(axis=(0, 1, 3))  # [x, y, t, mode]
+        assert per_t[0] == 0 and np.all(per_t[1:] == N)
+    _, _, fs = O.run(prob, O.table_knots(prob.tables), scheme="substep", want_state=True)
+    assert np.all(np.hypot(fs[:, 0], fs[:, 1]) <= 1.0)
+
+
+def test_absorbing_cylinder_removes_particles():
+    geo, src, mat, obs, opts = _cylinder_case(True)
+    geo = dict(geo, bnd=[{"dir": 4, "val": 1.0, "type": "absorbing"}])
+    prob, grid, N, he, hs, se, ss = _both(geo, src, mat, obs, opts, 20000)
+    assert se["absorbed"] == se["boundary_hits"] > 0
+    assert abs(se["absorbed"] - ss["absorbed"]) < 5 * math.sqrt(se["absorbed"])
+    alive = he.sum(axis=(0, 1))[:, 0]
+    assert np.all(np.diff(alive[1:]) <= 0) and alive[-1] == N - se["absorbed"]
+
+
+def _ballistic_material(geo):
+    # cv = 1e-6: mean free time ~1e10 s, so no particle scatters within the run
+    return MaterialClass(geo, 10, True, 1, [1e-6, 1e-6], 0, "exp", 0.1)
+
+
+@pytest.mark.parametrize("aperture,direction", [("rectangle", 3), ("rectangle", [1.0, 2.0, -2.0]),
+                                                ("circle", -2)])
+def test_plane_source_geometry(aperture, direction):
+    """initializeParticle.m:61-148: Gaussian offset (sd lambda/2) along n, uniform aperture
+    offsets in the plane (rectangle L1 x L2 along null(n), or a disk of radius R), direction
+    n and a polarisation uniformly oriented in the plane."""
+    geo = {"dimension": 3, "frame": "cartesian"}
+    mat = _ballistic_material(geo)
+    ext = [2.0, 0.5] if aperture == "rectangle" else 1.5
+    src = {"type": "plane", "direction": direction, "aperture": aperture, "extent": ext,
+           "lambda": 0.2, "position": [1.0, -1.0, 0.5]}
+    obs = {"x": colon(-50, 1, 50), "time": [0, 0.1]}
+    n = 100_000
+    prob, grid, N = build_problem(geo, dict(src, numberParticles=n), mat, obs,
+                                  {"exact_count": True, "precision": "fp64"})
+    _, se, fs = O.run(prob, O.table_knots(prob.tables), scheme="event", want_state=True)
+    assert se["scatter_events"] == 0
+    nv, u, v = (np.asarray(a) for a in (prob.src_normal, prob.src_u, prob.src_v))
+    assert np.allclose([nv @ u, nv @ v, u @ v], 0, atol=1e-12)
+    dd = np.asarray(direction, dtype=float)
+    want_n = dd / np.linalg.norm(dd) if dd.size == 3 else np.eye(3)[abs(int(dd)) - 1] * np.sign(dd)
+    assert np.allclose(nv, want_n)
+    assert np.allclose(fs[:, 3:6], nv)
+    q = fs[:, 6:9]
+    assert np.allclose(q @ nv, 0, atol=1e-12) and np.allclose(np.linalg.norm(q, axis=1), 1)
+    assert abs(np.mean((q @ u) ** 2) - 0.5) < 0.01
+    x = fs[:, :3] - np.asarray(src["position"])
+    cl, c1, c2 = x @ nv, x @ u, x @ v
+    assert abs(cl.mean()) < 4 * 0.1 / math.sqrt(n) and abs(cl.std() / 0.1 - 1) < 0.02
+    if aperture == "rectangle":
+        for c, L in ((c1, ext[0]), (c2, ext[1])):
+            assert c.min() >= -L / 2 and c.max() <= L / 2 and abs(c.var() / (L * L / 12) - 1) < 0.02
+    else:
+        r2 = (c1 ** 2 + c2 ** 2) / ext ** 2  # uniform over the disk: r^2 / R^2 ~ U(0, 1)
+        assert r2.max() <= 1 and abs(r2.mean() - 0.5) < 0.01 and abs(np.mean(np.arctan2(c2, c1))) < 0.03
+
+
+@pytest.mark.parametrize("d", [2, 3])
+def test_radial_source_profile(d):
+    """initializeParticle.m:22-28,175-203: r drawn from the inverse CDF of r^(d-1) f(r); a
+    constant profile on [0, R] fills the ball uniformly, so (r / R)^d ~ U(0, 1)."""
+    geo = {"dimension": d, "frame": "cartesian"}
+    mat = _ballistic_material(geo)
+    R = 0.5
+    src = {"lambda": 0.05, "radial": ([0.0, R], [1.0, 1.0])}
+    obs = {"x": colon(-5, 1, 5), "time": [0, 0.1]}
+    n = 100_000
+    prob, grid, N = build_problem(geo, dict(src, numberParticles=n), mat, obs,
+                                  {"exact_count": True, "precision": "fp64"})
+    c, r = prob.src_radial
+    assert c[0] == 0 and c[-1] == 1 and r[-1] == R and np.all(np.diff(c) > 0)
+    _, _, fs = O.run(prob, O.table_knots(prob.tables), scheme="event", want_state=True)
+    rad = np.linalg.norm(fs[:, :d], axis=1)
+    w = np.sort((rad / R) ** d)
+    assert rad.max() <= R and np.max(np.abs(w - (np.arange(n) + 0.5) / n)) < 0.01
+    # a callable profile with its radius gives the same table
+    prob2, _, _ = build_problem(geo, dict(src, radial=lambda x: np.ones_like(x), radialMax=R, numberParticles=n),
+                                mat, obs, {"exact_count": True, "precision": "fp64"})
+    assert np.array_equal(prob2.src_radial[0], c) and np.array_equal(prob2.src_radial[1], r)
+
+
+def test_plane_source_event_scheme_equals_substep_scheme():
+    geo = {"dimension": 3, "frame": "cartesian"}
+    mat = MaterialClass(geo, 10, True, 1, [0.2, 0.2], 0, "exp", 0.1)
+    src = {"type": "plane", "direction": 1, "extent": 1.0, "lambda": 0.1}
+    obs = {"x": colon(-1, 0.1, 3), "time": colon(0, 0.1, 2.0)}
+    prob, grid, N, he, hs, se, ss = _both(geo, src, mat, obs, {}, 20000)
+    assert _chi2_per_dof(he, hs) < 1.3
