@@ -104,6 +104,13 @@ int rtmc_tables_eval(const rtmc_tables *tables, int32_t t, int64_t n, const doub
 
 void rtmc_tables_free(rtmc_tables *tables);
 
+/* sigma(theta) of table `table` of a material (calcSigmaIsotropic, MaterialClass.m:172-359),
+ * at n angles; and the totals Sigma, Sigma' of every table (prepareSigmaOne,
+ * MaterialClass.m:2447-2452; 1 value for acoustics, 4 for elastics).  Host FP64, used to
+ * differentiate the tables with respect to material parameters. */
+int rtmc_sigma_eval(const rtmc_material *material, int32_t table, int64_t n, const double *theta, double *sigma);
+int rtmc_sigma_total(const rtmc_material *material, double *Sigma, double *Sigmapr);
+
 /* Replaces MaterialClass.Zoeppritz + ZoeppritzFluid (MaterialClass.m:1786-1885,
  * ZoeppritzFluid.m:1-244): energy coefficients of a solid/fluid interface at n angles.
  * out is row-major [7][n]: E_Rpp, E_Rpsv, E_Tpp, E_Rsvsv, E_Rsp, E_Tsp, E_Rsh. */
@@ -214,6 +221,38 @@ int rtmc_copy_histogram(rtmc_context *ctx, int64_t *hist_out, int64_t n);
  * (whose particle struct P, initializeParticle.m:163-170, is internal to the loop). */
 int rtmc_forward_trace(rtmc_context *ctx, const rtmc_problem *problem, const rtmc_tables *tables,
                        int64_t *hist_out, double *state_out, rtmc_stats *stats);
+
+/* ---------------------------------------------------------------------------------- */
+/* Gradient of a histogram misfit (score-function adjoint with Philox path replay)     */
+/* ---------------------------------------------------------------------------------- */
+
+#define RTMC_MAX_PARAMS 8
+
+/* How the path density of an acoustic problem depends on parameters p_q: the
+ * differential cross-section sigma(theta; p) of the scattering table and its total
+ * Sigma = 1 / mean free time.  The transport draws a scattering in each sub-step with
+ * probability 1 - exp(-h Sigma) and its angle from sigma(theta) sin^(d-2)(theta) / Sigma,
+ * so the score of a path up to sub-step S with scatterings at theta_1..theta_n is
+ *   sum_i d log sigma(theta_i)/dp + d log Sigma/dp [n (kappa - 1) - (S - n) h Sigma],
+ *   kappa = h Sigma / (exp(h Sigma) - 1). */
+typedef struct {
+    int32_t n_params;       /* 1 .. RTMC_MAX_PARAMS */
+    int32_t n_theta;        /* >= 2 points of a uniform grid of theta on [0, pi] */
+    const double *dlogsigma;              /* [n_params][n_theta] d log sigma(theta) / d p_q */
+    double dlogSigma[RTMC_MAX_PARAMS];    /* d log Sigma / d p_q */
+} rtmc_score;
+
+/* New entry point, no counterpart in the reference (which has no gradient).  Replays the
+ * particles of rtmc_forward (same problem, tables and Philox keys: recomputed, not
+ * stored) and returns grad[q] = sum over particles and observation instants of
+ * adjoint[bin] * score_q(path up to that instant), accumulated in FP64: the
+ * score-function estimate of d L / d p_q when adjoint[b] = d L / d (count in bin b) of
+ * the histogram rtmc_forward returns.  Acoustic problems only, with qrate = 0 (a
+ * Q-dependence is carried as exp(-omega t / Q) weights on the host); adjoint is a HOST
+ * array of hist_len doubles.  The launch shape is fixed per device, so repeated calls
+ * return identical bits. */
+int rtmc_gradient(rtmc_context *ctx, const rtmc_problem *problem, const rtmc_tables *tables,
+                  const rtmc_score *score, const double *adjoint, double *grad, rtmc_stats *stats);
 
 /* ---------------------------------------------------------------------------------- */
 /* Batched runs: many independent problems in one persistent, CUDA-graph launch        */

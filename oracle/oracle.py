@@ -66,6 +66,10 @@ def load():
         lib.oracle_invcdf.restype = C.c_double
         lib.oracle_invcdf.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_int64, C.c_double]
         lib.oracle_max_threads.restype = C.c_int
+        lib.oracle_gradient.restype = C.c_int
+        lib.oracle_gradient.argtypes = [C.POINTER(OracleProblem), C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                        C.c_int, C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                        C.POINTER(C.c_double), C.POINTER(C.c_int64)]
         lib.oracle_reflect.restype = C.c_int
         lib.oracle_reflect.argtypes = [C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_double, C.c_double, C.c_int,
                                        C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double),
@@ -91,6 +95,40 @@ def run(prob, knots, scheme: str = "event", u24: bool | None = None, nthreads: i
     """Run the oracle on a TransportProblem-like object with the given table knots
     [(cdf, theta), ...].  scheme 'substep' (reference order) or 'event' (snap, GPU stream).
     Returns (int64 histogram, stats dict, final states [N,16] or None)."""
+    lib = load()
+    P, keep = _problem(prob, knots, scheme, u24, nthreads, n_particles, pid0)
+    hist = np.zeros(prob.hist_len, dtype=np.int64)
+    stats = np.zeros(8, dtype=np.int64)
+    fs = np.zeros((P.n_particles, 16)) if want_state else None
+    rc = lib.oracle_run(C.byref(P), hist.ctypes.data_as(C.POINTER(C.c_int64)),
+                        stats.ctypes.data_as(C.POINTER(C.c_int64)), _dp(fs) if want_state else None)
+    if rc:
+        raise RuntimeError(f"oracle_run failed ({rc})")
+    return hist, dict(zip(ST_NAMES, map(int, stats[:6]))), fs
+
+
+def gradient(prob, knots, dlogsigma, dlogSigma, adjoint, u24: bool | None = None, nthreads: int | None = None):
+    """Score-function gradient by the event scheme (the restatement of rtmc_gradient):
+    returns (grad [n_params], stats).  prob must be acoustic with qrate = 0."""
+    lib = load()
+    P, keep = _problem(prob, knots, "event", u24, nthreads, None, None)
+    dls = np.ascontiguousarray(dlogsigma, dtype=np.float64)
+    adj = np.ascontiguousarray(adjoint, dtype=np.float64).ravel()
+    hS = prob.h / prob.mft[0] if math.isfinite(prob.mft[0]) else 0.0
+    kappa = hS / math.expm1(hS) if hS > 0 else 1.0
+    dlS = np.asarray(dlogSigma, dtype=np.float64)
+    a_inc = np.ascontiguousarray(dlS * (kappa - 1.0 + hS))
+    b_obs = np.ascontiguousarray(-dlS * hS * prob.n_sub)
+    grad = np.zeros(dls.shape[0])
+    stats = np.zeros(8, dtype=np.int64)
+    rc = lib.oracle_gradient(C.byref(P), _dp(adj), _dp(dls), dls.shape[0], dls.shape[1], _dp(a_inc), _dp(b_obs),
+                             _dp(grad), stats.ctypes.data_as(C.POINTER(C.c_int64)))
+    if rc:
+        raise RuntimeError(f"oracle_gradient failed ({rc})")
+    return grad, dict(zip(ST_NAMES, map(int, stats[:6])))
+
+
+def _problem(prob, knots, scheme, u24, nthreads, n_particles, pid0):
     lib = load()
     P = OracleProblem()
     P.d, P.frame, P.acoustics = prob.d, prob.frame, int(prob.acoustics)
@@ -153,14 +191,7 @@ def run(prob, knots, scheme: str = "event", u24: bool | None = None, nthreads: i
         P.tab_n[i] = c.size
         P.tab_cdf[i] = _dp(c)
         P.tab_theta[i] = _dp(t)
-    hist = np.zeros(prob.hist_len, dtype=np.int64)
-    stats = np.zeros(8, dtype=np.int64)
-    fs = np.zeros((P.n_particles, 16)) if want_state else None
-    rc = lib.oracle_run(C.byref(P), hist.ctypes.data_as(C.POINTER(C.c_int64)),
-                        stats.ctypes.data_as(C.POINTER(C.c_int64)), _dp(fs) if want_state else None)
-    if rc:
-        raise RuntimeError(f"oracle_run failed ({rc})")
-    return hist, dict(zip(ST_NAMES, map(int, stats[:6]))), fs
+    return P, keep
 
 
 def reflect(zoe_rpp, zoe_rsvsv, vp, vs, k, d, q, mode, u):

@@ -472,7 +472,7 @@ static int cylinder_hit(const oracle_problem *P, const rng_t *g, uint32_t step, 
 
 /* Scattering: azimuth (:604-611), mode conversion (:619-623), theta (:614-632),
  * rotation and renormalisation (:635-639).  Returns the new mode. */
-static void scatter(const oracle_problem *P, particle_t *pt, double u_phi, double u_mode, double u_theta)
+static double scatter(const oracle_problem *P, particle_t *pt, double u_phi, double u_mode, double u_theta)
 {
     if (P->d == 2) {
         if (u_phi >= 0.5) scale3(pt->q, -1.0);
@@ -501,6 +501,7 @@ static void scatter(const oracle_problem *P, particle_t *pt, double u_phi, doubl
     memcpy(pt->d, nd, sizeof nd);
     memcpy(pt->q, nq, sizeof nq);
     pt->mode = m2;
+    return th;
 }
 
 /* ------------------------------------------------------------------------- */
@@ -519,8 +520,21 @@ static int64_t bin_index(const double *e, int ne, double v)
     return lo;
 }
 
+static int64_t obs_index(const oracle_problem *P, const double x[3], const double dir[3], int mode, int it);
+
 static void observe(const oracle_problem *P, const double x[3], const double dir[3], int mode, int it,
                     int64_t *hist, int use_atomic, int64_t *stats)
+{
+    int64_t idx = obs_index(P, x, dir, mode, it);
+    if (idx < 0) return;
+    int64_t inc = (int64_t)1 << P->hist_shift;
+    if (use_atomic) __atomic_fetch_add(&hist[idx], inc, __ATOMIC_RELAXED);
+    else hist[idx] += inc;
+    stats[ST_OBS]++;
+}
+
+/* histogram index of an observation (observeTime.m:14-144), -1 outside the grid */
+static int64_t obs_index(const oracle_problem *P, const double x[3], const double dir[3], int mode, int it)
 {
     double c[4];
     double cz = dir[2];
@@ -548,19 +562,27 @@ static void observe(const oracle_problem *P, const double x[3], const double dir
         const double *e = P->axis_edges[a];
         int ne = P->axis_nedges[a];
         if (am == 1) {
-            if (!(c[a] >= e[0] && c[a] <= e[ne - 1])) return;
+            if (!(c[a] >= e[0] && c[a] <= e[ne - 1])) return -1;
         } else {
             int64_t b = bin_index(e, ne, c[a]);
-            if (b < 0) return;
+            if (b < 0) return -1;
             idx += b * P->axis_stride[a];
         }
     }
-    idx += (int64_t)it * P->time_stride + (int64_t)mode * P->mode_stride;
-    int64_t inc = (int64_t)1 << P->hist_shift;
-    if (use_atomic) __atomic_fetch_add(&hist[idx], inc, __ATOMIC_RELAXED);
-    else hist[idx] += inc;
-    stats[ST_OBS]++;
+    return idx + (int64_t)it * P->time_stride + (int64_t)mode * P->mode_stride;
 }
+
+/* Score-function adjoint of an acoustic problem (see oracle_gradient): the score of
+ * parameter q at observation j is A[q] + b_obs[q] j; a scattering at angle theta adds
+ * dlogsigma_q(theta) (linear interpolation on a uniform grid of theta / pi) + a_inc[q]. */
+typedef struct {
+    const double *adjoint;
+    const double *dlogsigma;
+    int n_params, n_theta;
+    const double *a_inc, *b_obs;
+    double A[8];
+    double g[8]; /* this thread's sums */
+} adj_t;
 
 /* ------------------------------------------------------------------------- */
 /* Scheme 0: literal sub-step restatement                                     */
@@ -688,8 +710,10 @@ static inline int64_t plane_cross_steps(double a, double b, int64_t cap)
 }
 
 static void run_event(const oracle_problem *P, int64_t pid, int64_t *hist, int use_atomic, int64_t *stats,
-                      double *fstate)
+                      double *fstate, adj_t *adj)
 {
+    if (adj)
+        for (int q = 0; q < adj->n_params; ++q) adj->A[q] = 0.0;
     rng_t g;
     g.key[0] = (uint32_t)P->seed;
     g.key[1] = (uint32_t)(P->seed >> 32);
@@ -735,7 +759,17 @@ static void run_event(const oracle_problem *P, int64_t pid, int64_t *hist, int u
             int64_t so = (int64_t)next_obs * P->n_sub;
             double dt = step * (double)(so - s0);
             double xo[3] = {pt.x[0] + dt * pt.d[0], pt.x[1] + dt * pt.d[1], pt.x[2] + dt * pt.d[2]};
-            observe(P, xo, pt.d, m, next_obs, hist, use_atomic, stats);
+            if (adj) {
+                int64_t idx = obs_index(P, xo, pt.d, m, next_obs);
+                if (idx >= 0) {
+                    double w = adj->adjoint[idx];
+                    for (int q = 0; q < adj->n_params; ++q)
+                        adj->g[q] += w * (adj->A[q] + adj->b_obs[q] * (double)next_obs);
+                    stats[ST_OBS]++;
+                }
+            } else {
+                observe(P, xo, pt.d, m, next_obs, hist, use_atomic, stats);
+            }
             next_obs++;
         }
         if (kind < 0) break;
@@ -785,8 +819,20 @@ static void run_event(const oracle_problem *P, int64_t pid, int64_t *hist, int u
             rng_block(&g, k, 0, r0); /* [next, azimuth, mode, theta] */
             memcpy(pt.x, xe, sizeof xe);
             int m0 = pt.mode;
-            scatter(P, &pt, r0[1], r0[2], r0[3]);
+            double th = scatter(P, &pt, r0[1], r0[2], r0[3]);
             stats[ST_SCATTER]++;
+            if (adj) {
+                double f = th / M_PI;
+                f = f < 0 ? 0 : (f > 1 ? 1 : f);
+                f *= (double)(adj->n_theta - 1);
+                int kk = (int)f;
+                if (kk > adj->n_theta - 2) kk = adj->n_theta - 2;
+                double w = f - (double)kk;
+                for (int q = 0; q < adj->n_params; ++q) {
+                    const double *t = adj->dlogsigma + (int64_t)q * adj->n_theta + kk;
+                    adj->A[q] += t[0] + w * (t[1] - t[0]) + adj->a_inc[q];
+                }
+            }
             nscat++;
             s0 = e;
             int64_t js = geom_steps(r0[0], lam[pt.mode], cap);
@@ -835,7 +881,7 @@ int oracle_run(const oracle_problem *P, int64_t *hist, int64_t *stats_out, doubl
         for (int64_t i = 0; i < P->n_particles; ++i) {
             double *fs = fstate ? fstate + 16 * i : NULL;
             if (P->scheme == 0) run_substep(P, P->pid0 + i, h, !(priv) && nth > 1, ls, fs);
-            else run_event(P, P->pid0 + i, h, !(priv) && nth > 1, ls, fs);
+            else run_event(P, P->pid0 + i, h, !(priv) && nth > 1, ls, fs, NULL);
         }
         if (h != hist) {
 #ifdef _OPENMP
@@ -848,6 +894,47 @@ int oracle_run(const oracle_problem *P, int64_t *hist, int64_t *stats_out, doubl
 #pragma omp critical
 #endif
         for (int j = 0; j < ST_N; ++j) stats[j] += ls[j];
+    }
+    if (stats_out) memcpy(stats_out, stats, sizeof stats);
+    return 0;
+}
+
+/* Score-function gradient of an acoustic problem (qrate = 0) by the event scheme:
+ * grad[q] = sum over particles and observations of adjoint[bin] * (A_q + b_obs[q] j),
+ * the replay that the GPU's rt_adjoint performs. */
+int oracle_gradient(const oracle_problem *P, const double *adjoint, const double *dlogsigma, int n_params,
+                    int n_theta, const double *a_inc, const double *b_obs, double *grad, int64_t *stats_out)
+{
+    if (!P || !adjoint || !dlogsigma || !grad || n_params < 1 || n_params > 8 || n_theta < 2 || !P->acoustics) return 1;
+    int nth = P->nthreads > 0 ? P->nthreads : 1;
+    int64_t stats[ST_N];
+    memset(stats, 0, sizeof stats);
+    for (int q = 0; q < n_params; ++q) grad[q] = 0.0;
+#ifdef _OPENMP
+#pragma omp parallel num_threads(nth)
+#endif
+    {
+        int64_t ls[ST_N];
+        memset(ls, 0, sizeof ls);
+        adj_t a;
+        memset(&a, 0, sizeof a);
+        a.adjoint = adjoint;
+        a.dlogsigma = dlogsigma;
+        a.n_params = n_params;
+        a.n_theta = n_theta;
+        a.a_inc = a_inc;
+        a.b_obs = b_obs;
+#ifdef _OPENMP
+#pragma omp for schedule(dynamic, 256)
+#endif
+        for (int64_t i = 0; i < P->n_particles; ++i) run_event(P, P->pid0 + i, NULL, 0, ls, NULL, &a);
+#ifdef _OPENMP
+#pragma omp critical
+#endif
+        {
+            for (int q = 0; q < n_params; ++q) grad[q] += a.g[q];
+            for (int j = 0; j < ST_N; ++j) stats[j] += ls[j];
+        }
     }
     if (stats_out) memcpy(stats_out, stats, sizeof stats);
     return 0;

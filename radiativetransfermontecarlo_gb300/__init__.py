@@ -5,10 +5,11 @@ Drop-in for the hot path of cottereau/RadiativeTransferMonteCarlo:
 (initializeParticle + propagateParticleSmallDt + observeTime) on sm_103a CUDA kernels
 behind the C ABI of librtmc (include/rtmc.h).
 """
+from .adjoint import radiativeTransferGradient
 from .material import MaterialClass
 from .observation import colon, initialize_observation
 from .radiative_transfer import (TransportProblem, build_problem, get_context, normalise, radiativeTransfer,
                                  run_transport)
 
-__all__ = ["MaterialClass", "radiativeTransfer", "build_problem", "run_transport", "normalise",
+__all__ = ["MaterialClass", "radiativeTransfer", "radiativeTransferGradient", "build_problem", "run_transport", "normalise",
            "initialize_observation", "colon", "TransportProblem", "get_context"]

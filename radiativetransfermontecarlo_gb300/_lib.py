@@ -67,6 +67,14 @@ class RtmcStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}
 
 
+MAX_PARAMS = 8
+
+
+class RtmcScore(C.Structure):
+    _fields_ = [("n_params", C.c_int32), ("n_theta", C.c_int32), ("dlogsigma", C.POINTER(C.c_double)),
+                ("dlogSigma", C.c_double * MAX_PARAMS)]
+
+
 # every function declared in include/rtmc.h: name -> (restype, argtypes)
 _P = C.c_void_p
 SIGNATURES = {
@@ -77,6 +85,11 @@ SIGNATURES = {
     "rtmc_tables_get_knots": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "rtmc_tables_eval": (C.c_int, [_P, C.c_int32, C.c_int64, C.POINTER(C.c_double), C.POINTER(C.c_double)]),
     "rtmc_tables_free": (None, [_P]),
+    "rtmc_sigma_eval": (C.c_int, [C.POINTER(RtmcMaterial), C.c_int32, C.c_int64, C.POINTER(C.c_double),
+                                  C.POINTER(C.c_double)]),
+    "rtmc_sigma_total": (C.c_int, [C.POINTER(RtmcMaterial), C.POINTER(C.c_double), C.POINTER(C.c_double)]),
+    "rtmc_gradient": (C.c_int, [_P, C.POINTER(RtmcProblem), _P, C.POINTER(RtmcScore), C.POINTER(C.c_double),
+                                C.POINTER(C.c_double), C.POINTER(RtmcStats)]),
     "rtmc_zoeppritz_fluid": (C.c_int, [C.c_int32, C.POINTER(C.c_double), C.c_double, C.c_double, C.c_double,
                                        C.c_double, C.c_double, C.c_double, C.POINTER(C.c_double)]),
     "rtmc_create": (C.c_int, [C.c_int32, C.POINTER(_P)]),
@@ -243,6 +256,24 @@ class Context:
                                           out.ctypes.data_as(C.POINTER(C.c_int64)), dptr(states), C.byref(st)),
               self.handle)
         return out, states, st.as_dict()
+
+    def gradient(self, problem: RtmcProblem, tables: Tables, dlogsigma: np.ndarray, dlogSigma, adjoint: np.ndarray):
+        """rtmc_gradient: score-function adjoint replay.  dlogsigma [n_params, n_theta] on a
+        uniform theta grid of [0, pi], dlogSigma [n_params], adjoint [hist_len] (d L / d count).
+        Returns (grad [n_params], stats)."""
+        dls = np.ascontiguousarray(dlogsigma, dtype=np.float64)
+        adj = np.ascontiguousarray(adjoint, dtype=np.float64).ravel()
+        assert dls.ndim == 2 and adj.size == problem.hist_len
+        sc = RtmcScore()
+        sc.n_params, sc.n_theta = dls.shape
+        sc.dlogsigma = dptr(dls)
+        for q, v in enumerate(dlogSigma):
+            sc.dlogSigma[q] = float(v)
+        grad = np.zeros(dls.shape[0], dtype=np.float64)
+        st = RtmcStats()
+        check(self.lib.rtmc_gradient(self.handle, C.byref(problem), tables.handle, C.byref(sc), dptr(adj), dptr(grad),
+                                     C.byref(st)), self.handle)
+        return grad, st.as_dict()
 
     def forward_device(self, problem: RtmcProblem, tables: Tables) -> dict:
         st = RtmcStats()

@@ -46,7 +46,7 @@ struct rtmc_context {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_start = nullptr, ev_k0 = nullptr, ev_k1 = nullptr, ev_k2 = nullptr, ev_end = nullptr;
     std::string err;
-    DevBuf hist, tabs, aux, stats, flush, trace, idx;
+    DevBuf hist, tabs, aux, stats, flush, trace, idx, adj, partial;
     uint64_t tabs_gen = 0;
     int tabs_prec = -1;
     DevTables<float> tf{};
@@ -510,6 +510,131 @@ int forward(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int6
                                      : run<float>(ctx, P, t, host_out, st, trace_out);
 }
 
+// ---- rtmc_gradient: score-function adjoint replay ----------------------------------
+
+int check_score(rtmc_context *ctx, const rtmc_problem *P, const rtmc_score *sc, const double *adjoint, double *grad)
+{
+    std::string *e = &ctx->err;
+    if (!sc || !adjoint || !grad) return fail(e, RTMC_ERR_ARG, "rtmc_gradient: NULL argument");
+    if (!P->acoustics) return fail(e, RTMC_ERR_ARG, "rtmc_gradient: acoustic problems only");
+    if (P->qrate[0] != 0)
+        return fail(e, RTMC_ERR_ARG, "rtmc_gradient: set qrate = 0 and weight the histogram by exp(-omega t / Q)");
+    if (sc->n_params < 1 || sc->n_params > RTMC_MAX_PARAMS)
+        return fail(e, RTMC_ERR_ARG, "rtmc_gradient: n_params must be in [1, 8]");
+    if (sc->n_theta < 2 || sc->n_theta > (1 << 24) || !sc->dlogsigma)
+        return fail(e, RTMC_ERR_ARG, "rtmc_gradient: the d log sigma table needs 2 to 2^24 angles");
+    for (int64_t k = 0; k < (int64_t)sc->n_params * sc->n_theta; ++k)
+        if (!std::isfinite(sc->dlogsigma[k])) return fail(e, RTMC_ERR_ARG, "rtmc_gradient: d log sigma must be finite");
+    for (int q = 0; q < sc->n_params; ++q)
+        if (!std::isfinite(sc->dlogSigma[q])) return fail(e, RTMC_ERR_ARG, "rtmc_gradient: d log Sigma must be finite");
+    return RTMC_OK;
+}
+
+template <typename R>
+int gradient_run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, const rtmc_score *sc,
+                 const double *adjoint, double *grad, rtmc_stats *st)
+{
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    CK(cudaEventRecord(ctx->ev_start, ctx->stream), "event");
+    DevTables<R> *dt;
+    if constexpr (sizeof(R) == 4) dt = &ctx->tf; else dt = &ctx->td;
+    const int prec = sizeof(R) == 4 ? RTMC_FP32 : RTMC_FP64;
+    if (!ctx->cache_tables || ctx->tabs_gen != t->gen || ctx->tabs_prec != prec) {
+        int s = upload_tables<R>(ctx, t, dt);
+        if (s) { ctx->tabs_gen = 0; return s; }
+        ctx->tabs_gen = t->gen;
+        ctx->tabs_prec = prec;
+    }
+    DevParams<R> p;
+    std::vector<R> edges, zoe;
+    int n_edges = 0;
+    fill_params<R>(ctx, P, *dt, &p, &n_edges, &edges, &zoe);
+    const size_t eb = align_up(std::max<size_t>(1, edges.size()) * sizeof(R), 256);
+    const size_t zb = align_up(zoe.size() * sizeof(R), 256);
+    const size_t hb = (size_t)P->hist_len * sizeof(double);
+    const size_t sb = (size_t)sc->n_params * sc->n_theta * sizeof(double);
+    if (ctx->aux.grow(eb + zb) || ctx->stats.grow(256) || ctx->adj.grow(align_up(hb, 256) + sb))
+        return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for the gradient failed");
+    unsigned char *aux = static_cast<unsigned char *>(ctx->aux.p);
+    if (!edges.empty())
+        CK(cudaMemcpyAsync(aux, edges.data(), edges.size() * sizeof(R), cudaMemcpyHostToDevice, ctx->stream), "edges");
+    CK(cudaMemcpyAsync(aux + eb, zoe.data(), zoe.size() * sizeof(R), cudaMemcpyHostToDevice, ctx->stream), "zoeppritz");
+    unsigned char *ab = static_cast<unsigned char *>(ctx->adj.p);
+    CK(cudaMemcpyAsync(ab, adjoint, hb, cudaMemcpyHostToDevice, ctx->stream), "adjoint weights");
+    CK(cudaMemcpyAsync(ab + align_up(hb, 256), sc->dlogsigma, sb, cudaMemcpyHostToDevice, ctx->stream), "score table");
+    CK(cudaMemsetAsync(ctx->stats.p, 0, 256, ctx->stream), "counter clear");
+    p.edges = reinterpret_cast<const R *>(aux);
+    p.zoe = reinterpret_cast<const R *>(aux + eb);
+    p.src_radial = p.zoe + 2 * RTMC_ZOE_N;
+    p.hist = nullptr;
+    p.stats = static_cast<unsigned long long *>(ctx->stats.p);
+    p.status = reinterpret_cast<int32_t *>(static_cast<unsigned char *>(ctx->stats.p) + 128);
+    p.trace = nullptr;
+    AdjointArgs a{};
+    a.adjoint = reinterpret_cast<const double *>(ab);
+    a.dlogsigma = reinterpret_cast<const double *>(ab + align_up(hb, 256));
+    a.n_params = sc->n_params;
+    a.n_theta = sc->n_theta;
+    // per-sub-step scattering probability 1 - exp(-h Sigma), Sigma = 1 / mean free time
+    const double hS = std::isfinite(P->mft[0]) ? P->h / P->mft[0] : 0.0;
+    const double kappa = hS > 0 ? hS / std::expm1(hS) : 1.0;
+    for (int q = 0; q < sc->n_params; ++q) {
+        a.a_inc[q] = sc->dlogSigma[q] * (kappa - 1.0 + hS);
+        a.b_obs[q] = -sc->dlogSigma[q] * hS * (double)P->n_sub;
+    }
+    const int block = kAdjointThreads;
+    const size_t smem = align_up((size_t)n_edges * sizeof(R), 16);
+    int bps = 0;
+    if (adjoint_occupancy(prec, p.obs_kind, block, smem, &bps) != 0 || bps < 1)
+        return fail(&ctx->err, RTMC_ERR_CUDA, "adjoint kernel does not fit on the device");
+    const int64_t need = (std::max<int64_t>(P->n_particles, 1) + block - 1) / block;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->num_sms * bps, need));
+    if (ctx->partial.grow((size_t)grid * sc->n_params * sizeof(double)))
+        return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for the gradient failed");
+    a.partial = static_cast<double *>(ctx->partial.p);
+    CK(cudaEventRecord(ctx->ev_k0, ctx->stream), "event");
+    int le;
+    if constexpr (sizeof(R) == 4) le = launch_adjoint_f32(p, a, grid, block, smem, ctx->stream);
+    else le = launch_adjoint_f64(p, a, grid, block, smem, ctx->stream);
+    if (le) return cuda_fail(ctx, (cudaError_t)le, "adjoint launch");
+    CK(cudaEventRecord(ctx->ev_k1, ctx->stream), "event");
+    std::vector<double> part((size_t)grid * sc->n_params);
+    int64_t dstats[32];
+    CK(cudaMemcpyAsync(part.data(), a.partial, part.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
+       "partial sums");
+    CK(cudaMemcpyAsync(dstats, ctx->stats.p, 256, cudaMemcpyDeviceToHost, ctx->stream), "counters");
+    CK(cudaEventRecord(ctx->ev_end, ctx->stream), "event");
+    CK(cudaStreamSynchronize(ctx->stream), "adjoint");
+    for (int q = 0; q < sc->n_params; ++q) {
+        double acc = 0.0;
+        for (int b = 0; b < grid; ++b) acc += part[(size_t)b * sc->n_params + q];
+        grad[q] = acc;
+    }
+    float kms = 0, tms = 0;
+    cudaEventElapsedTime(&kms, ctx->ev_k0, ctx->ev_k1);
+    cudaEventElapsedTime(&tms, ctx->ev_start, ctx->ev_end);
+    ctx->last_kernel_ms = kms;
+    ctx->last_launches = 1;
+    const int32_t status = (int32_t)(dstats[16] & 0xffffffff);
+    if (st) {
+        std::memset(st, 0, sizeof *st);
+        st->scatter_events = dstats[0];
+        st->boundary_hits = dstats[1];
+        st->kills = dstats[2];
+        st->absorbed = dstats[3];
+        st->observations = dstats[4];
+        st->conversions = dstats[5];
+        st->device_status = status;
+        st->kernel_ms = kms;
+        st->launches = 1;
+        st->total_ms = tms;
+        st->h2d_bytes = (double)(hb + sb + (edges.size() + zoe.size()) * sizeof(R));
+        st->d2h_bytes = (double)(part.size() * sizeof(double) + 256);
+    }
+    if (status) return fail(&ctx->err, RTMC_ERR_DEVICE, "an adjoint guard tripped (event cap or histogram index)");
+    return RTMC_OK;
+}
+
 // ---- rtmc_forward_noalloc: everything staged in the static device scratch ----------
 
 // fixed-capacity vector on the stack (fill_params' edge and Zoeppritz lists)
@@ -774,6 +899,8 @@ extern "C" void rtmc_destroy(rtmc_context *ctx)
     ctx->flush.release();
     ctx->trace.release();
     ctx->idx.release();
+    ctx->adj.release();
+    ctx->partial.release();
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
     if (ctx->ev_k0) cudaEventDestroy(ctx->ev_k0);
     if (ctx->ev_k1) cudaEventDestroy(ctx->ev_k1);
@@ -807,6 +934,17 @@ extern "C" int rtmc_forward_trace(rtmc_context *ctx, const rtmc_problem *P, cons
     if (!hist_out || !state_out)
         return fail(ctx ? &ctx->err : nullptr, RTMC_ERR_ARG, "rtmc_forward_trace: NULL output buffer");
     return forward(ctx, P, t, hist_out, st, state_out);
+}
+
+extern "C" int rtmc_gradient(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, const rtmc_score *score,
+                             const double *adjoint, double *grad, rtmc_stats *st)
+{
+    if (!ctx || !P) return fail(ctx ? &ctx->err : nullptr, RTMC_ERR_ARG, "rtmc_gradient: NULL argument");
+    int s = check_problem(ctx, P, t);
+    if (s) return s;
+    if ((s = check_score(ctx, P, score, adjoint, grad)) != 0) return s;
+    return P->precision == RTMC_FP64 ? gradient_run<double>(ctx, P, t, score, adjoint, grad, st)
+                                     : gradient_run<float>(ctx, P, t, score, adjoint, grad, st);
 }
 
 extern "C" int rtmc_copy_histogram(rtmc_context *ctx, int64_t *hist_out, int64_t n)

@@ -116,10 +116,26 @@ template <typename R> struct BatchArgs {
     int32_t *status;
 };
 
+// Score-function adjoint replay (rt_adjoint): the per-particle score of parameter q up to
+// observation j is A_q(j) + b_obs[q] * j, where A_q gains dlogsigma_q(theta_i) + a_inc[q]
+// at each scattering; grad_q = sum over particles and j of adjoint[bin] * score_q(j).
+struct AdjointArgs {
+    const double *adjoint;    // [hist_len] d L / d count
+    const double *dlogsigma;  // [n_params][n_theta] on a uniform grid of theta / pi in [0, 1]
+    int32_t n_params, n_theta;
+    double a_inc[RTMC_MAX_PARAMS];
+    double b_obs[RTMC_MAX_PARAMS];
+    double *partial;          // [gridDim.x][n_params] block sums
+};
+
 // Launch wrappers (transport.cu).  Return a cudaError_t value.
 int launch_transport_f32(const DevParams<float> &p, int grid, int block, size_t smem, void *stream);
 int launch_transport_f64(const DevParams<double> &p, int grid, int block, size_t smem, void *stream);
 int transport_occupancy(int precision, int sink, int obs, int block, size_t smem, int *blocks_per_sm);
+int launch_adjoint_f32(const DevParams<float> &p, const AdjointArgs &a, int grid, int block, size_t smem, void *stream);
+int launch_adjoint_f64(const DevParams<double> &p, const AdjointArgs &a, int grid, int block, size_t smem, void *stream);
+int adjoint_occupancy(int precision, int obs, int block, size_t smem, int *blocks_per_sm);
+constexpr int kAdjointThreads = 256;
 int transport_set_smem(int precision, int sink, int obs, size_t smem);
 int transport_max_threads(int precision, int sink, int obs);
 int launch_bin_slices(const BinParams &b, int grid_x, size_t smem, void *stream);

@@ -222,6 +222,20 @@ double integrate(const std::function<double(double)> &f, double a, double b)
     return s;
 }
 
+// total and momentum-transfer cross-sections (prepareSigmaOne, MaterialClass.m:2447-2452)
+void sigma_totals(const Sigma &s, int d, double *S, double *Sp)
+{
+    const double pi = kPi;
+    std::function<double(double)> f = [&](double t) { return s(t); };
+    if (d == 2) {
+        *S = 2 * integrate(f, 0, pi);
+        *Sp = 2 * integrate([&](double t) { return s(t) * std::cos(t); }, 0, pi);
+    } else {
+        *S = 2 * pi * integrate([&](double t) { return s(t) * std::sin(t); }, 0, pi);
+        *Sp = 2 * pi * integrate([&](double t) { return s(t) * std::sin(t) * std::cos(t); }, 0, pi);
+    }
+}
+
 struct OneTable {
     double Sigma = 0, Sigmapr = 0;
     std::vector<double> cdf, theta;
@@ -231,15 +245,8 @@ struct OneTable {
 void prepare_one(const Sigma &s, int d, int64_t nth, OneTable *out)
 {
     const double pi = kPi;
-    std::function<double(double)> f = [&](double t) { return s(t); };
     double S, Sp;
-    if (d == 2) {
-        S = 2 * integrate(f, 0, pi);
-        Sp = 2 * integrate([&](double t) { return s(t) * std::cos(t); }, 0, pi);
-    } else {
-        S = 2 * pi * integrate([&](double t) { return s(t) * std::sin(t); }, 0, pi);
-        Sp = 2 * pi * integrate([&](double t) { return s(t) * std::sin(t) * std::cos(t); }, 0, pi);
-    }
+    sigma_totals(s, d, &S, &Sp);
     out->Sigma = S;
     out->Sigmapr = Sp;
     const double dx = pi / (double)(nth - 1);
@@ -287,6 +294,81 @@ int validate_tables(const rtmc_tables *t, std::string *err)
 
 using namespace rtmc;
 
+namespace rtmc {
+namespace {
+
+// the cross-section of table i (0 for acoustics; PP, PS, SP, SS for elastics) of material m
+int material_sigma(const rtmc_material *m, int i, Sigma *out)
+{
+    if (m->d != 2 && m->d != 3) return fail(nullptr, RTMC_ERR_ARG, "dimension must be 2 or 3");
+    const bool ac = m->acoustics != 0;
+    if (i < 0 || i >= (ac ? 1 : 4)) return fail(nullptr, RTMC_ERR_ARG, "table index out of range");
+    Sigma base;
+    base.d = m->d;
+    if (m->psdf == RTMC_PSDF_CONST) {
+        base.which = 5;
+        base.cst = m->sigma_const[i];
+        *out = base;
+        return RTMC_OK;
+    }
+    if (!(m->freq > 0) || !(m->lc > 0)) return fail(nullptr, RTMC_ERR_ARG, "frequency and lc must be positive");
+    int st = make_psdf(*m, &base.phi, nullptr);
+    if (st) return st;
+    base.omega = 2 * kPi * m->freq;
+    if (ac) {
+        if (!(m->v[0] > 0)) return fail(nullptr, RTMC_ERR_ARG, "acoustic speed must be positive");
+        if (std::fabs(m->corr[0]) > 1)
+            return fail(nullptr, RTMC_ERR_ARG, "Absolute value of corr(kappa,rho) should be less than 1!");
+        base.zeta = base.omega / m->v[0] * m->lc;
+        base.c1 = m->cv[0];
+        base.c2 = m->cv[1];
+        base.c3 = m->corr[0];
+    } else {
+        if (!(m->v[0] > 0) || !(m->v[1] > 0)) return fail(nullptr, RTMC_ERR_ARG, "vp and vs must be positive");
+        for (int k = 0; k < 3; ++k)
+            if (std::fabs(m->corr[k]) > 1)
+                return fail(nullptr, RTMC_ERR_ARG, "Absolute values of correlation coefficients should be less than 1!");
+        base.K = m->v[0] / m->v[1];
+        base.zP = base.omega / m->v[0] * m->lc;
+        base.zS = base.K * base.zP;
+        base.dll = m->cv[0];
+        base.dmm = m->cv[1];
+        base.drr = m->cv[2];
+        base.rlm = m->corr[0];
+        base.rlr = m->corr[1];
+        base.rmr = m->corr[2];
+    }
+    base.which = ac ? 0 : 1 + i;
+    *out = base;
+    return RTMC_OK;
+}
+
+} // namespace
+} // namespace rtmc
+
+extern "C" int rtmc_sigma_eval(const rtmc_material *m, int32_t table, int64_t n, const double *theta, double *sigma)
+{
+    if (!m || (n > 0 && (!theta || !sigma)) || n < 0) return fail(nullptr, RTMC_ERR_ARG, "rtmc_sigma_eval: bad argument");
+    Sigma s;
+    int st = material_sigma(m, table, &s);
+    if (st) return st;
+    for (int64_t k = 0; k < n; ++k) sigma[k] = s(theta[k]);
+    return RTMC_OK;
+}
+
+extern "C" int rtmc_sigma_total(const rtmc_material *m, double *Sigma_out, double *Sigmapr_out)
+{
+    if (!m || !Sigma_out || !Sigmapr_out) return fail(nullptr, RTMC_ERR_ARG, "rtmc_sigma_total: NULL argument");
+    const int nt = m->acoustics ? 1 : 4;
+    for (int i = 0; i < nt; ++i) {
+        Sigma s;
+        int st = material_sigma(m, i, &s);
+        if (st) return st;
+        sigma_totals(s, m->d, Sigma_out + i, Sigmapr_out + i);
+    }
+    return RTMC_OK;
+}
+
 extern "C" int rtmc_tables_build(const rtmc_material *m, rtmc_tables **out)
 {
     if (!m || !out) return fail(nullptr, RTMC_ERR_ARG, "rtmc_tables_build: NULL argument");
@@ -295,53 +377,18 @@ extern "C" int rtmc_tables_build(const rtmc_material *m, rtmc_tables **out)
     int64_t nth = m->n_theta > 0 ? m->n_theta : 1000000;
     if (nth < 16) return fail(nullptr, RTMC_ERR_ARG, "n_theta must be at least 16");
     const bool ac = m->acoustics != 0;
-    Sigma base;
-    base.d = m->d;
-    if (m->psdf != RTMC_PSDF_CONST) {
-        if (!(m->freq > 0) || !(m->lc > 0)) return fail(nullptr, RTMC_ERR_ARG, "frequency and lc must be positive");
-        int st = make_psdf(*m, &base.phi, nullptr);
+    Sigma sig[4];
+    for (int i = 0; i < (ac ? 1 : 4); ++i) {
+        int st = material_sigma(m, i, &sig[i]);
         if (st) return st;
-        base.omega = 2 * kPi * m->freq;
-        if (ac) {
-            if (!(m->v[0] > 0)) return fail(nullptr, RTMC_ERR_ARG, "acoustic speed must be positive");
-            if (std::fabs(m->corr[0]) > 1)
-                return fail(nullptr, RTMC_ERR_ARG, "Absolute value of corr(kappa,rho) should be less than 1!");
-            base.zeta = base.omega / m->v[0] * m->lc;
-            base.c1 = m->cv[0];
-            base.c2 = m->cv[1];
-            base.c3 = m->corr[0];
-        } else {
-            if (!(m->v[0] > 0) || !(m->v[1] > 0)) return fail(nullptr, RTMC_ERR_ARG, "vp and vs must be positive");
-            for (int i = 0; i < 3; ++i)
-                if (std::fabs(m->corr[i]) > 1)
-                    return fail(nullptr, RTMC_ERR_ARG,
-                                "Absolute values of correlation coefficients should be less than 1!");
-            base.K = m->v[0] / m->v[1];
-            base.zP = base.omega / m->v[0] * m->lc;
-            base.zS = base.K * base.zP;
-            base.dll = m->cv[0];
-            base.dmm = m->cv[1];
-            base.drr = m->cv[2];
-            base.rlm = m->corr[0];
-            base.rlr = m->corr[1];
-            base.rmr = m->corr[2];
-        }
     }
     auto *t = new (std::nothrow) rtmc_tables();
     if (!t) return fail(nullptr, RTMC_ERR_ALLOC, "out of host memory");
     t->n_tables = ac ? 1 : 4;
     OneTable one[4];
     std::vector<std::thread> th;
-    for (int i = 0; i < t->n_tables; ++i) {
-        Sigma s = base;
-        if (m->psdf == RTMC_PSDF_CONST) {
-            s.which = 5;
-            s.cst = m->sigma_const[i];
-        } else {
-            s.which = ac ? 0 : 1 + i;
-        }
-        th.emplace_back([s, &one, i, d = m->d, nth]() { prepare_one(s, d, nth, &one[i]); });
-    }
+    for (int i = 0; i < t->n_tables; ++i)
+        th.emplace_back([s = sig[i], &one, i, d = m->d, nth]() { prepare_one(s, d, nth, &one[i]); });
     for (auto &x : th) x.join();
     for (int i = 0; i < t->n_tables; ++i) {
         t->cdf[i] = std::move(one[i].cdf);

@@ -120,6 +120,7 @@ template <typename R> __device__ __forceinline__ R invcdf(const DevTables<R> &t,
 // ----------------------------------------------------------------------------------
 template <typename R> struct Part {
     R x[3], d[3], q[3];
+    R th; // polar angle / pi of the last scattering (read by the adjoint replay only)
     int mode, alive;
     int s0, sS, sK, sB;
     int s_death;
@@ -493,6 +494,7 @@ __device__ __forceinline__ void scatter(const DevParams<R> &p, Part<R> &s, R u_p
     }
     const int ti = p.acoustics ? 0 : m * 2 + m2;
     const R th_pi = invcdf(p.tab, ti, u_theta); // tables hold theta / pi
+    s.th = th_pi;
     R st, ct;
     m_sincospi(th_pi, &st, &ct);
     R nd[3], nq[3];
@@ -512,9 +514,10 @@ struct Counters {
     unsigned scat, bnd, kill, absorb, obs, conv;
 };
 
-// one event: the earliest of kill / boundary / scattering (ties in that order)
+// one event: the earliest of kill / boundary / scattering (ties in that order); returns
+// its kind (2 kill, 1 boundary, 0 scattering)
 template <typename R>
-__device__ void process_event(const DevParams<R> &p, uint64_t pid, Part<R> &s, Counters &cnt)
+__device__ int process_event(const DevParams<R> &p, uint64_t pid, Part<R> &s, Counters &cnt)
 {
     const int cap = p.s_end + 1;
     int e = s.sK, kind = 2;
@@ -524,7 +527,7 @@ __device__ void process_event(const DevParams<R> &p, uint64_t pid, Part<R> &s, C
         s.alive = 0;
         s.s_death = e;
         cnt.kill++;
-        return;
+        return kind;
     }
     s.k++;
     const R step = by_mode(p.step, s.mode);
@@ -549,7 +552,7 @@ __device__ void process_event(const DevParams<R> &p, uint64_t pid, Part<R> &s, C
                     s.s0 = e;
                     s.s_death = e;
                     cnt.absorb++;
-                    return;
+                    return kind;
                 }
                 const R n[3] = {s.x[0] / r, s.x[1] / r, (R)0};
                 s.x[0] -= (R)2 * over * n[0];
@@ -573,7 +576,7 @@ __device__ void process_event(const DevParams<R> &p, uint64_t pid, Part<R> &s, C
                 s.s0 = e;
                 s.s_death = e;
                 cnt.absorb++;
-                return;
+                return kind;
             }
             put3(s.x, k, (R)2 * val - xk);
             if (p.acoustics) {
@@ -613,6 +616,7 @@ __device__ void process_event(const DevParams<R> &p, uint64_t pid, Part<R> &s, C
     if (s.sS > cap) s.sS = cap;
     if (s.sK > cap) s.sK = cap;
     next_boundary(p, s);
+    return kind;
 }
 
 // histcounts bin of c on a binned axis (edges staged in shared memory), -1 outside
@@ -1237,6 +1241,106 @@ template <typename R, int SINK> void *pick_obs(int obs)
                            : (obs == OBS_RADIAL ? kernel_ptr<R, SINK, OBS_RADIAL>() : kernel_ptr<R, SINK, OBS_GENERAL>());
 }
 
+// Score-function adjoint: replays each particle of rt_transport from its Philox key
+// (one particle per thread; the path is recomputed, never stored) and accumulates, in
+// FP64, adjoint[bin] * score over every observation instant.  Between two events the
+// score is A + b_obs * j, so a segment only sums adjoint[bin] and j * adjoint[bin]; the
+// scattering that ends it adds d log sigma(theta) / dp (table lookup) + a_inc to A.
+// Block sums go to a.partial in a fixed order, so the result is reproducible.
+template <typename R, int OBS>
+__global__ void __launch_bounds__(kAdjointThreads) rt_adjoint(const DevParams<R> p, const AdjointArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R *sedges = reinterpret_cast<R *>(smem_raw);
+    __shared__ double red[kAdjointThreads / 32][RTMC_MAX_PARAMS];
+    for (int k = threadIdx.x; k < p.n_edges; k += blockDim.x) sedges[k] = p.edges[k];
+    __syncthreads();
+    const int np = a.n_params;
+    double g[RTMC_MAX_PARAMS];
+#pragma unroll
+    for (int q = 0; q < RTMC_MAX_PARAMS; ++q) g[q] = 0.0;
+    Counters cnt = {0u, 0u, 0u, 0u, 0u, 0u};
+    bool bad = false;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    const R tmax = (R)(a.n_theta - 1);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.n_particles; i += stride) {
+        const uint64_t pid = (uint64_t)(p.pid0 + i);
+        Part<R> s;
+        init_particle(p, pid, s);
+        double A[RTMC_MAX_PARAMS];
+#pragma unroll
+        for (int q = 0; q < RTMC_MAX_PARAMS; ++q) A[q] = 0.0;
+        int j = 1;
+        for (;;) {
+            const int e = next_event(s);
+            const int lim = e <= p.s_end ? e : p.s_end + 1;
+            Seg<R> sg;
+            seg_from(s, sg);
+            seg_prepare<R, OBS>(p, sedges, sg);
+            double sa = 0.0, saj = 0.0;
+            for (; j <= p.n_obs && j * p.n_sub < lim; ++j) { // observations strictly before the event
+                const int v = obs_offset<R, OBS>(p, sedges, sg, j * p.n_sub);
+                if (v < 0) continue;
+                const int64_t idx = (int64_t)j * p.time_stride + (sg.mode ? p.mode_stride : 0) + v;
+                if (idx >= p.hist_len) { bad = true; continue; }
+                const double w = __ldg(a.adjoint + idx);
+                sa += w;
+                saj = fma(w, (double)j, saj);
+                cnt.obs++;
+            }
+#pragma unroll
+            for (int q = 0; q < RTMC_MAX_PARAMS; ++q)
+                if (q < np) g[q] = fma(A[q], sa, fma(a.b_obs[q], saj, g[q]));
+            if (j > p.n_obs || e > p.s_end) break;
+            const int kind = process_event(p, pid, s, cnt);
+            if ((int)s.k > p.max_events) { bad = true; break; }
+            if (!s.alive) break;
+            if (kind == 0) {
+                R f = s.th < (R)0 ? (R)0 : (s.th > (R)1 ? (R)1 : s.th);
+                f *= tmax;
+                int k = (int)f;
+                k = k > a.n_theta - 2 ? a.n_theta - 2 : k;
+                const double w = (double)(f - (R)k);
+#pragma unroll
+                for (int q = 0; q < RTMC_MAX_PARAMS; ++q) {
+                    if (q < np) {
+                        const double *t = a.dlogsigma + (size_t)q * a.n_theta + k;
+                        A[q] += fma(w, __ldg(t + 1) - __ldg(t), __ldg(t)) + a.a_inc[q];
+                    }
+                }
+            }
+        }
+    }
+    // block reduction in a fixed order: warp shuffles, then warp 0 over the warps
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < RTMC_MAX_PARAMS; ++q) {
+        double v = g[q];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[warp][q] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < RTMC_MAX_PARAMS && threadIdx.x < np) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w][threadIdx.x];
+        a.partial[(size_t)blockIdx.x * np + threadIdx.x] = v;
+    }
+    const unsigned full = 0xffffffffu;
+    unsigned cv[6] = {cnt.scat, cnt.bnd, cnt.kill, cnt.absorb, cnt.obs, cnt.conv};
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        const unsigned t = __reduce_add_sync(full, cv[c]);
+        if (lane == 0 && t) atomicAdd(p.stats + c, (unsigned long long)t);
+    }
+    if (bad) atomicExch(p.status, 1);
+}
+
+template <typename R> void *pick_adjoint(int obs)
+{
+    return obs == OBS_CART ? (void *)rt_adjoint<R, OBS_CART>
+                           : (obs == OBS_RADIAL ? (void *)rt_adjoint<R, OBS_RADIAL> : (void *)rt_adjoint<R, OBS_GENERAL>);
+}
+
 template <typename R> void *pick_t(int sink, int obs)
 {
     return sink == SINK_SMEM ? pick_obs<R, SINK_SMEM>(obs)
@@ -1324,6 +1428,31 @@ int transport_max_threads(int precision, int sink, int obs)
     cudaFuncAttributes a;
     if (cudaFuncGetAttributes(&a, pick(precision, sink, obs)) != cudaSuccess) return 0;
     return a.maxThreadsPerBlock;
+}
+
+template <typename R>
+static int launch_adj(const DevParams<R> &p, const AdjointArgs &a, int grid, int block, size_t smem, void *stream)
+{
+    void *args[] = {(void *)&p, (void *)&a};
+    return (int)cudaLaunchKernel(pick_adjoint<R>(p.obs_kind), dim3(grid), dim3(block), args, smem, (cudaStream_t)stream);
+}
+
+int launch_adjoint_f32(const DevParams<float> &p, const AdjointArgs &a, int grid, int block, size_t smem, void *stream)
+{
+    return launch_adj(p, a, grid, block, smem, stream);
+}
+
+int launch_adjoint_f64(const DevParams<double> &p, const AdjointArgs &a, int grid, int block, size_t smem, void *stream)
+{
+    return launch_adj(p, a, grid, block, smem, stream);
+}
+
+int adjoint_occupancy(int precision, int obs, int block, size_t smem, int *blocks_per_sm)
+{
+    void *fn = precision == RTMC_FP64 ? pick_adjoint<double>(obs) : pick_adjoint<float>(obs);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, block, smem);
+    return (int)e;
 }
 
 int transport_occupancy(int precision, int sink, int obs, int block, size_t smem, int *blocks_per_sm)

@@ -255,3 +255,59 @@ def test_boundaries_and_sources_match_oracle(name, precision):
         assert rel < 0.02
     if "cylinder" in name:
         assert stats["boundary_hits"] > 0
+
+
+def _gradient_case(n):
+    from radiativetransfermontecarlo_gb300 import adjoint as A
+    geo, src, mat, obs, opts = W.c1_acoustic3d()
+    obs = dict(obs, time=colon(0, 0.05, 3))
+    tgt = MaterialClass(geo, 10, True, 1, [0.06, 0.04], 0, "exp", 0.12)
+    tgt.Q = 300
+    Et = A.forward_weighted(geo, dict(src, numberParticles=n), tgt, obs, dict(opts, exact_count=True, seed=77,
+                                                                               precision="fp64"))[0]
+    mat = MaterialClass(geo, 10, True, 1, [0.05, 0.05], 0, "exp", 0.1)
+    mat.Q = 400
+    return geo, src, mat, obs, opts, Et
+
+
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_gradient_replay_matches_oracle(precision):
+    """rtmc_gradient replays the forward's paths and accumulates the same score as the
+    event oracle's restatement (FP64: to rounding; FP32: the oracle fed 24-bit uniforms)."""
+    from radiativetransfermontecarlo_gb300 import adjoint as A
+    geo, src, mat, obs, opts, Et = _gradient_case(20000)
+    E, prob, grid, N, counts, _ = A.forward_weighted(geo, dict(src, numberParticles=20000), mat, obs,
+                                                     dict(opts, exact_count=True, precision=precision))
+    L, dLdE = A.misfit(E, Et)
+    unit = normalise(np.ones(prob.hist_len), grid, N)[0]
+    adj = (dLdE * unit).ravel(order="F")
+    params = ["lc", "cv_kappa", "cv_rho", "mfp"]
+    dls, dlS = A.score_tables(mat, 3, params)
+    P, keep = prob.to_ctypes()
+    g, st = get_context(0).gradient(P, prob.tables, dls, dlS, adj)
+    go, sto = O.gradient(prob, O.table_knots(prob.tables), dls, dlS, adj)
+    assert st["device_status"] == 0 and st["scatter_events"] > 0
+    scale = np.abs(go) + 1e-3 * np.max(np.abs(go))
+    if precision == "fp64":
+        assert st["scatter_events"] == sto["scatter_events"] and st["observations"] == sto["observations"]
+        assert np.all(np.abs(g - go) <= 1e-8 * scale), (g, go)
+    else:
+        assert np.all(np.abs(g - go) <= 0.05 * scale), (g, go)
+    g2, _ = get_context(0).gradient(P, prob.tables, dls, dlS, adj)
+    assert np.array_equal(g, g2)  # fixed launch shape: reproducible bits
+
+
+def test_gradient_against_central_differences():
+    """Score-function gradient vs central differences with common random numbers (same
+    seed) for lc, cv_kappa, cv_rho, Q and the mean free path, FP32 transport."""
+    from radiativetransfermontecarlo_gb300 import adjoint as A
+    n = 2_000_000
+    geo, src, mat, obs, opts, Et = _gradient_case(n)
+    src = dict(src, numberParticles=n)
+    o = dict(opts, exact_count=True, precision="fp32", seed=5)
+    params = ("lc", "cv_kappa", "cv_rho", "Q", "mfp")
+    res = A.radiativeTransferGradient(geo, src, mat, obs, Et, params, o)
+    for p in params:
+        fd = A.finite_difference(geo, src, mat, obs, Et, p, 1e-2 if p != "Q" else 1e-3, o)
+        tol = 1e-6 if p == "Q" else 0.1
+        assert abs(res["grad"][p] - fd) <= tol * abs(fd), (p, res["grad"][p], fd)
