@@ -19,7 +19,10 @@ score-function estimates accumulated by the rt_adjoint kernel, which replays eac
 from its Philox key.  Q only rescales the survival probability exp(-omega t / Q) of every
 particle (the kill draw is independent of the path), so it is carried as a weight of each
 time slice ("weight mode": the transport runs with qrate = 0) and differentiated exactly.
-Bins with E_target = 0 are left out of L.
+Bins where the target holds fewer than min_target_count particles (default 1000, so a
+relative Monte Carlo error of the target below about 3%; 0 keeps every bin with
+E_target > 0) are left out of L: a few-particle bin carries a weight 1 / E_target that
+is mostly noise.
 """
 from __future__ import annotations
 
@@ -34,6 +37,16 @@ from .radiative_transfer import DEFAULT_OPTIONS, build_problem, get_context, nor
 
 PARAMS = ("lc", "cv_kappa", "cv_rho", "Q", "mfp")
 N_THETA = 4097  # grid of the d log sigma tables on [0, pi]
+
+
+def target_mask(E_target: np.ndarray, grid, n_target: int, min_count: float) -> np.ndarray:
+    """Bins kept in L: E_target > 0 and at least min_count target particles, counted as
+    E_target x n_target x bin volume (the normalisation of radiativeTransfer.m:161-188)."""
+    keep = E_target > 0
+    if min_count > 0:
+        one = normalise(np.ones(grid.hist_len), grid, 1)[0]  # density of one particle per bin
+        keep &= E_target * n_target / one >= min_count - 1e-9
+    return keep
 
 
 def misfit(E: np.ndarray, E_target: np.ndarray) -> tuple[float, np.ndarray]:
@@ -168,6 +181,8 @@ def radiativeTransferGradient(geometry: dict, source: dict, material: MaterialCl
             raise ValueError(f"unknown parameter '{p}' (one of {PARAMS})")
     E, prob, grid, N, counts, st_f = forward_weighted(geometry, source, material, observation, opt)
     E_target = np.asarray(E_target, dtype=float).reshape(E.shape)
+    kept = target_mask(E_target, grid, int(opt.get("target_particles", N)), float(opt.get("min_target_count", 1000)))
+    E_target = np.where(kept, E_target, 0.0)
     L, dLdE = misfit(E, E_target)
     w, omega, Q = _weights(material, grid)
     # d E_b / d count_b: the (linear) normalisation times the slice weight
@@ -185,19 +200,28 @@ def radiativeTransferGradient(geometry: dict, source: dict, material: MaterialCl
     st_a = None
     if scat:
         dls, dlS = score_tables(material, prob.d, scat)
-        P, keep = prob.to_ctypes()
+        P, _keep = prob.to_ctypes()
         g, st_a = get_context(int(opt["device"])).gradient(P, prob.tables, dls, dlS, adjoint)
+        del _keep
         grad.update({p: float(v) for p, v in zip(scat, g)})
     if "Q" in params:
         tq = (omega * grid.t / Q ** 2) if math.isfinite(Q) else np.zeros(grid.Nt)
         grad["Q"] = float(np.sum(dLdE * E * _slice(tq, E)))
-    return {"L": L, "grad": grad, "energyDensity": E, "N": N, "forward_stats": st_f, "adjoint_stats": st_a}
+    return {"L": L, "grad": grad, "energyDensity": E, "N": N, "bins": int(kept.sum()), "forward_stats": st_f,
+            "adjoint_stats": st_a}
 
 
 def finite_difference(geometry, source, material, observation, E_target, name: str, rel: float = 1e-3,
                       options: dict | None = None) -> float:
     """Central difference of L in parameter `name` with common random numbers (the same
-    seed, so the same Philox keys, on both sides), step rel * |p|."""
+    seed, so the same Philox keys, on both sides), step rel * |p|, over the bins that
+    radiativeTransferGradient keeps."""
+    opt = dict(DEFAULT_OPTIONS)
+    opt.update(options or {})
+    _, grid, N = build_problem(geometry, source, material, observation, opt)
+    E_target = np.asarray(E_target, dtype=float).reshape(grid.shape)
+    keep = target_mask(E_target, grid, int(opt.get("target_particles", N)), float(opt.get("min_target_count", 1000)))
+    E_target = np.where(keep, E_target, 0.0)
     if name == "mfp":
         mfp = material.meanFreePath if material.meanFreePath is not None else None
         if mfp is None:
