@@ -551,7 +551,7 @@ int gradient_run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t,
     fill_params<R>(ctx, P, *dt, &p, &n_edges, &edges, &zoe);
     const size_t eb = align_up(std::max<size_t>(1, edges.size()) * sizeof(R), 256);
     const size_t zb = align_up(zoe.size() * sizeof(R), 256);
-    const size_t hb = (size_t)P->hist_len * sizeof(double);
+    const size_t hb = (size_t)P->hist_len * sizeof(R);
     const size_t sb = (size_t)sc->n_params * sc->n_theta * sizeof(double);
     if (ctx->aux.grow(eb + zb) || ctx->stats.grow(256) || ctx->adj.grow(align_up(hb, 256) + sb))
         return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for the gradient failed");
@@ -560,7 +560,14 @@ int gradient_run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t,
         CK(cudaMemcpyAsync(aux, edges.data(), edges.size() * sizeof(R), cudaMemcpyHostToDevice, ctx->stream), "edges");
     CK(cudaMemcpyAsync(aux + eb, zoe.data(), zoe.size() * sizeof(R), cudaMemcpyHostToDevice, ctx->stream), "zoeppritz");
     unsigned char *ab = static_cast<unsigned char *>(ctx->adj.p);
-    CK(cudaMemcpyAsync(ab, adjoint, hb, cudaMemcpyHostToDevice, ctx->stream), "adjoint weights");
+    if constexpr (sizeof(R) == 8) {
+        CK(cudaMemcpyAsync(ab, adjoint, hb, cudaMemcpyHostToDevice, ctx->stream), "adjoint weights");
+    } else {
+        std::vector<R> wr((size_t)P->hist_len);
+        for (size_t k = 0; k < wr.size(); ++k) wr[k] = (R)adjoint[k];
+        CK(cudaMemcpyAsync(ab, wr.data(), hb, cudaMemcpyHostToDevice, ctx->stream), "adjoint weights");
+        CK(cudaStreamSynchronize(ctx->stream), "adjoint weights"); // wr is released on return
+    }
     CK(cudaMemcpyAsync(ab + align_up(hb, 256), sc->dlogsigma, sb, cudaMemcpyHostToDevice, ctx->stream), "score table");
     CK(cudaMemsetAsync(ctx->stats.p, 0, 256, ctx->stream), "counter clear");
     p.edges = reinterpret_cast<const R *>(aux);
@@ -571,7 +578,7 @@ int gradient_run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t,
     p.status = reinterpret_cast<int32_t *>(static_cast<unsigned char *>(ctx->stats.p) + 128);
     p.trace = nullptr;
     AdjointArgs a{};
-    a.adjoint = reinterpret_cast<const double *>(ab);
+    a.adjoint = ab;
     a.dlogsigma = reinterpret_cast<const double *>(ab + align_up(hb, 256));
     a.n_params = sc->n_params;
     a.n_theta = sc->n_theta;

@@ -119,8 +119,10 @@ template <typename R> struct BatchArgs {
 // Score-function adjoint replay (rt_adjoint): the per-particle score of parameter q up to
 // observation j is A_q(j) + b_obs[q] * j, where A_q gains dlogsigma_q(theta_i) + a_inc[q]
 // at each scattering; grad_q = sum over particles and j of adjoint[bin] * score_q(j).
+// The weights, the per-particle score and the per-segment sums use the transport's
+// precision; grad accumulates in FP64.
 struct AdjointArgs {
-    const double *adjoint;    // [hist_len] d L / d count
+    const void *adjoint;      // [hist_len] d L / d count, in the transport's precision
     const double *dlogsigma;  // [n_params][n_theta] on a uniform grid of theta / pi in [0, 1]
     int32_t n_params, n_theta;
     double a_inc[RTMC_MAX_PARAMS];

@@ -1248,13 +1248,14 @@ template <typename R, int SINK> void *pick_obs(int obs)
 // scattering that ends it adds d log sigma(theta) / dp (table lookup) + a_inc to A.
 // Block sums go to a.partial in a fixed order, so the result is reproducible.
 template <typename R, int OBS>
-__global__ void __launch_bounds__(kAdjointThreads) rt_adjoint(const DevParams<R> p, const AdjointArgs a)
+__global__ void __launch_bounds__(kAdjointThreads, sizeof(R) == 4 ? 3 : 2) rt_adjoint(const DevParams<R> p, const AdjointArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     R *sedges = reinterpret_cast<R *>(smem_raw);
     __shared__ double red[kAdjointThreads / 32][RTMC_MAX_PARAMS];
     for (int k = threadIdx.x; k < p.n_edges; k += blockDim.x) sedges[k] = p.edges[k];
     __syncthreads();
+    const R *wts = static_cast<const R *>(a.adjoint);
     const int np = a.n_params;
     double g[RTMC_MAX_PARAMS];
 #pragma unroll
@@ -1267,9 +1268,9 @@ __global__ void __launch_bounds__(kAdjointThreads) rt_adjoint(const DevParams<R>
         const uint64_t pid = (uint64_t)(p.pid0 + i);
         Part<R> s;
         init_particle(p, pid, s);
-        double A[RTMC_MAX_PARAMS];
+        R A[RTMC_MAX_PARAMS]; // this particle's score, scattering part
 #pragma unroll
-        for (int q = 0; q < RTMC_MAX_PARAMS; ++q) A[q] = 0.0;
+        for (int q = 0; q < RTMC_MAX_PARAMS; ++q) A[q] = (R)0;
         int j = 1;
         for (;;) {
             const int e = next_event(s);
@@ -1277,20 +1278,21 @@ __global__ void __launch_bounds__(kAdjointThreads) rt_adjoint(const DevParams<R>
             Seg<R> sg;
             seg_from(s, sg);
             seg_prepare<R, OBS>(p, sedges, sg);
-            double sa = 0.0, saj = 0.0;
+            R sa = (R)0, saj = (R)0;
             for (; j <= p.n_obs && j * p.n_sub < lim; ++j) { // observations strictly before the event
                 const int v = obs_offset<R, OBS>(p, sedges, sg, j * p.n_sub);
                 if (v < 0) continue;
                 const int64_t idx = (int64_t)j * p.time_stride + (sg.mode ? p.mode_stride : 0) + v;
                 if (idx >= p.hist_len) { bad = true; continue; }
-                const double w = __ldg(a.adjoint + idx);
+                const R w = __ldg(wts + idx);
                 sa += w;
-                saj = fma(w, (double)j, saj);
+                saj += w * (R)j;
                 cnt.obs++;
             }
+            const double sad = (double)sa, sajd = (double)saj;
 #pragma unroll
             for (int q = 0; q < RTMC_MAX_PARAMS; ++q)
-                if (q < np) g[q] = fma(A[q], sa, fma(a.b_obs[q], saj, g[q]));
+                if (q < np) g[q] = fma((double)A[q], sad, fma(a.b_obs[q], sajd, g[q]));
             if (j > p.n_obs || e > p.s_end) break;
             const int kind = process_event(p, pid, s, cnt);
             if ((int)s.k > p.max_events) { bad = true; break; }
@@ -1305,7 +1307,7 @@ __global__ void __launch_bounds__(kAdjointThreads) rt_adjoint(const DevParams<R>
                 for (int q = 0; q < RTMC_MAX_PARAMS; ++q) {
                     if (q < np) {
                         const double *t = a.dlogsigma + (size_t)q * a.n_theta + k;
-                        A[q] += fma(w, __ldg(t + 1) - __ldg(t), __ldg(t)) + a.a_inc[q];
+                        A[q] += (R)(fma(w, __ldg(t + 1) - __ldg(t), __ldg(t)) + a.a_inc[q]);
                     }
                 }
             }
