@@ -7,6 +7,7 @@ int64 fixed-point histogram (2^-40).  One step = one whole simulation of that wo
 (histogram clear + particle init + transport + binning) with the tables resident.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+  python bench.py --workload c4|c5      (batched sweep / gradient; one extra JSON line)
 
 Prints one JSON line.  `value` is device time (CUDA events on the library's stream);
 `e2e` times rtmc_forward through the C ABI with host buffers (tables uploaded and the
@@ -324,6 +325,109 @@ def run_our_arm(args, rank, world, dist):
     return result
 
 
+def run_c4(args):
+    """256 independent 3D acoustic instances (lc, cv, f, Q, N drawn per instance), shared
+    spherical 120 x 251 grid, one persistent CUDA-graph launch per step."""
+    from oracle import oracle as O
+    from radiativetransfermontecarlo_gb300 import workloads as W
+    from radiativetransfermontecarlo_gb300.batch import Batch, autotune
+    t0 = time.perf_counter()
+    batch = Batch([W.c4_instance(i) for i in range(256)])
+    setup_s = time.perf_counter() - t0
+    shape, tune = autotune(batch, repeats=1)
+    for _ in range(args.warmup):
+        batch.run()
+    ms, ev = [], 0
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            batch.ctx.flush_l2()
+            st = batch.run()
+            ms.append(st["kernel_ms"])
+            ev += st["scatter_events"]
+    value = ev / (sum(ms) / 1000.0)
+    # end to end: launch + every instance's histogram back to the host
+    times, ev2 = [], 0
+    for _ in range(max(3, args.steps // 4)):
+        t1 = time.perf_counter()
+        st = batch.run()
+        H = batch.histograms()
+        times.append(time.perf_counter() - t1)
+        ev2 += st["scatter_events"]
+    n_total = int(sum(batch.N))
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": float(np.mean(ms)), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "256-instance 3D acoustic sweep: lc log-U[0.02,1], cv U[0.01,0.2], f log-U[1,20], "
+                                   "Q in {Inf,100,500}, N log-U[1e4,1e7]; spherical 120 x 251 grid",
+                       "particles_total": n_total, "launch_shape": list(shape), "table_setup_s": setup_s,
+                       "l2": "512 MB device write between steps"},
+            "gpu_launches": args.steps, "clocks": clk.summary(),
+            "events_per_step": ev / args.steps,
+            "e2e": {"value": ev2 / sum(times), "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": int(H.nbytes), "ms_per_step": 1000 * float(np.mean(times))},
+            "autotune_ms": {f"{b}x{r}x{c}": t for (b, r, c), t in tune.items()}}
+    if not args.no_cpu:
+        prob = batch.problems[int(np.argmax(batch.N))]
+        line["cpu_baseline"] = {k: v for k, v in cpu_sample(prob, O.table_knots(prob.tables)).items()
+                                if k not in ("events", "seconds")}
+        line["cpu_baseline"]["sample"] = "the largest instance, " + line["cpu_baseline"]["sample"]
+    batch.close()
+    return line
+
+
+def run_c5(args):
+    """Gradient of L = sum (E - E_t)^2 / E_t over (lc, cv_kappa, cv_rho, Q) at lc 0.1,
+    cv [0.05 0.05], Q 400 against a target at lc 0.12, cv [0.06 0.04], Q 300, 3D acoustic,
+    1e7 particles, C1's grid; checked against central differences with common random numbers."""
+    from radiativetransfermontecarlo_gb300 import MaterialClass
+    from radiativetransfermontecarlo_gb300 import adjoint as A
+    from radiativetransfermontecarlo_gb300 import workloads as W
+    n = 10_000_000
+    geo, src, mat0, obs, opts = W.c1_acoustic3d(n=n, precision="fp32")
+    tgt = MaterialClass(geo, 10, True, 1, [0.06, 0.04], 0, "exp", 0.12)
+    tgt.Q = 300
+    o = dict(opts, exact_count=True, precision="fp32")
+    Et = A.forward_weighted(geo, src, tgt, obs, dict(o, seed=77))[0]
+    mat = MaterialClass(geo, 10, True, 1, [0.05, 0.05], 0, "exp", 0.1)
+    mat.Q = 400
+    params = ("lc", "cv_kappa", "cv_rho", "Q", "mfp")
+    o = dict(o, seed=5)
+    for _ in range(args.warmup):
+        A.radiativeTransferGradient(geo, src, mat, obs, Et, params, o)
+    fwd, adj, wall, ev = [], [], [], 0
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            res = A.radiativeTransferGradient(geo, src, mat, obs, Et, params, o)
+            wall.append(time.perf_counter() - t0)
+            fwd.append(res["forward_stats"]["total_ms"])
+            adj.append(res["adjoint_stats"]["total_ms"])
+            ev += res["forward_stats"]["scatter_events"] + res["adjoint_stats"]["scatter_events"]
+    dev_s = (sum(fwd) + sum(adj)) / 1000.0
+    scale = {"lc": 0.1, "cv_kappa": 0.05, "cv_rho": 0.05, "Q": 400.0, "mfp": float(mat.meanFreePath)}
+    fd = {p: A.finite_difference(geo, src, mat, obs, Et, p, 1e-3, o) for p in params}
+    fd2 = {p: A.finite_difference(geo, src, mat, obs, Et, p, 1e-2, o) for p in params if p != "Q"}
+    g = np.array([res["grad"][p] * scale[p] for p in params])
+    f = np.array([fd[p] * scale[p] for p in params])
+    f2 = np.array([(fd2[p] if p != "Q" else fd[p]) * scale[p] for p in params])
+    line = {"metric": "gradient evaluations/s (forward + adjoint replay), " + UNIT + " alongside",
+            "value": args.steps / dev_s, "unit": "gradients/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000 * dev_s / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (FP64 gradient accumulation)", "data": "synthetic",
+            "config": {"workload": "3D acoustic exp lc=0.1 cv=[.05 .05] f=10 Q=400, 1e7 particles, spherical 120 x 251, "
+                                   "target lc=0.12 cv=[.06 .04] Q=300 (1e7 particles, another seed)",
+                       "bins_in_misfit": res["bins"], "min_target_count": 1000},
+            "scattering_events_per_s": ev / dev_s, "forward_ms": float(np.mean(fwd)), "adjoint_ms": float(np.mean(adj)),
+            "wall_ms": 1000 * float(np.mean(wall)), "gpu_launches": 2 * args.steps, "clocks": clk.summary(),
+            "L": res["L"], "gradient": res["grad"],
+            "finite_differences_1e-3": fd, "finite_differences_1e-2": fd2,
+            "rel_error_scaled_vector_1e-3": float(np.linalg.norm(g - f) / np.linalg.norm(f)),
+            "rel_error_scaled_vector_1e-2": float(np.linalg.norm(g - f2) / np.linalg.norm(f2)),
+            "rel_error_per_param_1e-2": {p: abs(res["grad"][p] - (fd2.get(p, fd[p]))) / abs(fd2.get(p, fd[p]))
+                                         for p in params}}
+    return line
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -339,11 +443,18 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c4", "c5"],
+                    help="c2: the headline line (default); c4: batched sweep; c5: gradient")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     import __graft_entry__
     __graft_entry__.build()
+    if args.workload != "c2":
+        if rank == 0:
+            line = run_c4(args) if args.workload == "c4" else run_c5(args)
+            print(json.dumps(line), flush=True)
+        return
     if args.impl == "reference":
         line = run_reference_arm(args, rank, world)
         if line is not None:

@@ -9,11 +9,14 @@ largest expected cost first.
 from __future__ import annotations
 
 import ctypes as C
+import os
 import time
+from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
 
 from . import _lib
+from .material import MaterialClass
 from .radiative_transfer import build_problem, get_context, normalise
 
 
@@ -22,6 +25,11 @@ class Batch:
         """instances: list of (geometry, source, material, observation, options)."""
         self.ctx = get_context(device)
         self.problems, self.grids, self.N = [], [], []
+        # tables first, on host threads (the FP64 builder releases the GIL)
+        todo = [(mat, int(geo["dimension"])) for geo, src, mat, obs, opt in instances if mat.invcdf is None]
+        if todo:
+            with ThreadPoolExecutor(max_workers=min(len(todo), os.cpu_count() or 1)) as ex:
+                list(ex.map(lambda md: MaterialClass.prepareSigma(*md), todo))
         for geo, src, mat, obs, opt in instances:
             prob, grid, n = build_problem(geo, src, mat, obs, opt)
             self.problems.append(prob)
