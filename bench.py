@@ -204,6 +204,8 @@ def run_our_arm(args, rank, world, dist):
     ctx = get_context(device)
     if args.block or args.ring or args.index_mb:
         ctx.set_launch(args.block, args.ring, args.index_mb)
+    if args.chunks or args.k1_bps:
+        ctx.set_pipeline(args.chunks, args.k1_bps)
     P32, keep32 = prob.to_ctypes()
 
     def barrier():
@@ -439,6 +441,8 @@ def main():
     ap.add_argument("--block", type=int, default=0, help="threads per block (0: automatic)")
     ap.add_argument("--ring", type=int, default=0, help="segments per lane (0: automatic)")
     ap.add_argument("--index-mb", type=int, default=0, help="index-array budget in MB (0: automatic, -1: global atomics)")
+    ap.add_argument("--chunks", type=int, default=0, help="transport/fold pipeline chunks (0: automatic, 1: off)")
+    ap.add_argument("--k1-bps", type=int, default=0, help="transport blocks per SM while pipelined (0: automatic)")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")

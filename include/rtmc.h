@@ -321,6 +321,13 @@ int rtmc_host_free(void *p);
  * array, observations go straight to the histogram with 64-bit global atomics). */
 int rtmc_set_launch(rtmc_context *ctx, int32_t block, int32_t ring_cap, int32_t index_mb);
 
+/* Pipelining of large histograms (index-array path): the particles run in `chunks`
+ * launches over two index slots, and the fold of one chunk (bound by L2 atomics) runs on
+ * a second stream while the transport of the next (bound by instruction issue) runs with
+ * at most `transport_blocks_per_sm` blocks per SM, leaving room for the fold's blocks.
+ * 0 = automatic (4 chunks from 2e6 particles up, 2 blocks per SM); chunks = 1: off. */
+int rtmc_set_pipeline(rtmc_context *ctx, int32_t chunks, int32_t transport_blocks_per_sm);
+
 /* enable (1, default) or disable (0) reuse of the device copy of a tables handle across
  * calls; with 0 every call uploads its tables again (end-to-end timing) */
 int rtmc_set_table_cache(rtmc_context *ctx, int32_t enable);

@@ -108,6 +108,7 @@ SIGNATURES = {
     "rtmc_flush_l2": (C.c_int, [_P]),
     "rtmc_set_table_cache": (C.c_int, [_P, C.c_int32]),
     "rtmc_set_launch": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32]),
+    "rtmc_set_pipeline": (C.c_int, [_P, C.c_int32, C.c_int32]),
     "rtmc_batch_create": (C.c_int, [_P, C.c_int32, C.POINTER(RtmcProblem), C.POINTER(_P), C.POINTER(_P)]),
     "rtmc_batch_set_launch": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int64]),
     "rtmc_batch_run": (C.c_int, [_P, C.POINTER(RtmcStats)]),
@@ -287,6 +288,10 @@ class Context:
 
     def set_launch(self, block: int = 0, ring_cap: int = 0, index_mb: int = 0):
         check(self.lib.rtmc_set_launch(self.handle, block, ring_cap, index_mb), self.handle)
+
+    def set_pipeline(self, chunks: int = 0, transport_blocks_per_sm: int = 0):
+        """rtmc_set_pipeline: 0 = automatic; chunks = 1 turns the transport/fold overlap off."""
+        check(self.lib.rtmc_set_pipeline(self.handle, chunks, transport_blocks_per_sm), self.handle)
 
     def last_timing(self):
         ms = C.c_double()

@@ -56,6 +56,12 @@ struct rtmc_context {
     int last_launches = 0;
     int cache_tables = 1;
     int opt_block = 0, opt_ring = 0, opt_index_mb = 0;
+    // transport / fold pipeline over particle chunks (index sink): a second stream and
+    // per-chunk events, created on first use
+    int opt_chunks = 0, opt_k1_bps = 0;
+    static constexpr int kPipe = 32;
+    cudaStream_t fold_stream = nullptr;
+    cudaEvent_t ev_a0[kPipe] = {}, ev_a1[kPipe] = {}, ev_b0[kPipe] = {}, ev_b1[kPipe] = {};
 };
 
 namespace {
@@ -305,6 +311,19 @@ void fill_params(rtmc_context *ctx, const rtmc_problem *P, const DevTables<R> &t
     (void)ctx;
 }
 
+int ensure_pipeline(rtmc_context *ctx)
+{
+    cudaError_t e = cudaSuccess;
+    if (!ctx->fold_stream) e = cudaStreamCreateWithFlags(&ctx->fold_stream, cudaStreamNonBlocking);
+    for (int i = 0; i < rtmc_context::kPipe && e == cudaSuccess; ++i) {
+        if (!ctx->ev_a0[i]) e = cudaEventCreate(&ctx->ev_a0[i]);
+        if (e == cudaSuccess && !ctx->ev_a1[i]) e = cudaEventCreate(&ctx->ev_a1[i]);
+        if (e == cudaSuccess && !ctx->ev_b0[i]) e = cudaEventCreate(&ctx->ev_b0[i]);
+        if (e == cudaSuccess && !ctx->ev_b1[i]) e = cudaEventCreate(&ctx->ev_b1[i]);
+    }
+    return (int)e;
+}
+
 template <typename R>
 int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t *host_out, rtmc_stats *st,
         double *trace_out)
@@ -375,12 +394,32 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         }
     }
     int64_t chunk = P->n_particles; // particles per transport launch
+    int n_pipe = 0;                 // > 0: chunks pipelined over two index slots
     if (sink != kSinkSmem && ctx->opt_index_mb >= 0 && P->time_stride < ((int64_t)1 << 30)) {
         const int64_t mb = ctx->opt_index_mb ? ctx->opt_index_mb : 12288; // default index budget: 12 GB
         const int64_t rows = std::max<int64_t>(32, ((mb << 20) / (4 * (int64_t)P->n_obs)) / 32 * 32);
-        chunk = std::min<int64_t>(P->n_particles, rows);
-        if (chunk > 0 && ctx->idx.grow((size_t)chunk * P->n_obs * sizeof(int32_t)) == 0) sink = kSinkIndex;
-        else chunk = P->n_particles;
+        // pipeline: the fold of chunk c overlaps the transport of chunk c + 1 (the fold is
+        // bound by L2 atomics, the transport by instruction issue), two index slots
+        const int want = ctx->opt_chunks ? ctx->opt_chunks : (P->n_particles >= 2000000 ? 4 : 1);
+        if (want >= 2) {
+            int nc = want;
+            int64_t per = ((P->n_particles + nc - 1) / nc + 31) / 32 * 32;
+            while (2 * per > rows && nc < rtmc_context::kPipe) {
+                ++nc;
+                per = ((P->n_particles + nc - 1) / nc + 31) / 32 * 32;
+            }
+            if (2 * per <= rows && nc >= 2 && ensure_pipeline(ctx) == 0 &&
+                ctx->idx.grow((size_t)2 * per * P->n_obs * sizeof(int32_t)) == 0) {
+                sink = kSinkIndex;
+                chunk = per;
+                n_pipe = nc;
+            }
+        }
+        if (!n_pipe) {
+            chunk = std::min<int64_t>(P->n_particles, rows);
+            if (chunk > 0 && ctx->idx.grow((size_t)chunk * P->n_obs * sizeof(int32_t)) == 0) sink = kSinkIndex;
+            else chunk = P->n_particles;
+        }
     }
     {
         // the variant's launch bound caps the block (fill_params chose the observation path)
@@ -394,6 +433,8 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         return fail(&ctx->err, RTMC_ERR_CUDA, "transport kernel does not fit on the device");
     p.sink = sink;
     p.ring_cap = cap;
+    // pipelined transport keeps room on every SM for the fold's blocks
+    if (n_pipe) bps = std::min(bps, ctx->opt_k1_bps ? ctx->opt_k1_bps : 2);
     int64_t grid = (int64_t)ctx->num_sms * bps;
     const int64_t need = (std::max<int64_t>(chunk, 1) + block - 1) / block;
     grid = std::max<int64_t>(1, std::min<int64_t>(grid, need));
@@ -434,7 +475,50 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
     }
     int le = 0, launches = 0;
     double kms = 0, fms = 0;
-    for (int64_t base = 0; base < P->n_particles && !le; base += chunk) {
+    if (n_pipe) {
+        const size_t slot_elems = (size_t)chunk * P->n_obs;
+        int32_t *idx0 = static_cast<int32_t *>(ctx->idx.p);
+        int c = 0;
+        for (int64_t base = 0; base < P->n_particles && !le; base += chunk, ++c) {
+            DevParams<R> q = p;
+            q.pid0 = P->pid0 + base;
+            q.n_particles = std::min<int64_t>(chunk, P->n_particles - base);
+            q.obs_idx = idx0 + (c & 1) * slot_elems;
+            q.obs_rows = chunk;
+            if (p.trace) q.trace = p.trace + 16 * base;
+            if (c >= 2) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_b1[c - 2], 0), "pipeline wait");
+            CK(cudaEventRecord(ctx->ev_a0[c], ctx->stream), "event");
+            if constexpr (sizeof(R) == 4) le = launch_transport_f32(q, (int)grid, block, smem, ctx->stream);
+            else le = launch_transport_f64(q, (int)grid, block, smem, ctx->stream);
+            if (le) break;
+            CK(cudaEventRecord(ctx->ev_a1[c], ctx->stream), "event");
+            CK(cudaStreamWaitEvent(ctx->fold_stream, ctx->ev_a1[c], 0), "pipeline wait");
+            BinParams b = bp;
+            b.idx = q.obs_idx;
+            b.rows = chunk;
+            b.n = q.n_particles;
+            if (b.group) b.part_per_block = (b.n + fold_grid - 1) / fold_grid;
+            CK(cudaEventRecord(ctx->ev_b0[c], ctx->fold_stream), "event");
+            le = launch_bin_slices(b, fold_grid, fold_smem, ctx->fold_stream);
+            if (le) break;
+            CK(cudaEventRecord(ctx->ev_b1[c], ctx->fold_stream), "event");
+            launches += 2;
+        }
+        if (!le) {
+            CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_b1[c - 1], 0), "pipeline join");
+            CK(cudaStreamSynchronize(ctx->stream), "transport");
+            for (int k = 0; k < c; ++k) {
+                float a = 0, b = 0;
+                cudaEventElapsedTime(&a, ctx->ev_a0[k], ctx->ev_a1[k]);
+                cudaEventElapsedTime(&b, ctx->ev_b0[k], ctx->ev_b1[k]);
+                kms += a;
+                fms += b;
+            }
+        } else {
+            cudaStreamSynchronize(ctx->fold_stream);
+        }
+    }
+    for (int64_t base = 0; !n_pipe && base < P->n_particles && !le; base += chunk) {
         DevParams<R> q = p;
         q.pid0 = P->pid0 + base;
         q.n_particles = std::min<int64_t>(chunk, P->n_particles - base);
@@ -913,6 +997,14 @@ extern "C" void rtmc_destroy(rtmc_context *ctx)
     if (ctx->ev_k1) cudaEventDestroy(ctx->ev_k1);
     if (ctx->ev_k2) cudaEventDestroy(ctx->ev_k2);
     if (ctx->ev_end) cudaEventDestroy(ctx->ev_end);
+    if (ctx->fold_stream) cudaStreamSynchronize(ctx->fold_stream);
+    for (int i = 0; i < rtmc_context::kPipe; ++i) {
+        if (ctx->ev_a0[i]) cudaEventDestroy(ctx->ev_a0[i]);
+        if (ctx->ev_a1[i]) cudaEventDestroy(ctx->ev_a1[i]);
+        if (ctx->ev_b0[i]) cudaEventDestroy(ctx->ev_b0[i]);
+        if (ctx->ev_b1[i]) cudaEventDestroy(ctx->ev_b1[i]);
+    }
+    if (ctx->fold_stream) cudaStreamDestroy(ctx->fold_stream);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -996,6 +1088,17 @@ extern "C" int rtmc_set_launch(rtmc_context *ctx, int32_t block, int32_t ring_ca
     ctx->opt_block = block;
     ctx->opt_ring = ring_cap;
     ctx->opt_index_mb = index_mb;
+    return RTMC_OK;
+}
+
+extern "C" int rtmc_set_pipeline(rtmc_context *ctx, int32_t chunks, int32_t transport_blocks_per_sm)
+{
+    if (!ctx) return fail(nullptr, RTMC_ERR_ARG, "rtmc_set_pipeline: NULL context");
+    if (chunks < 0 || chunks > rtmc_context::kPipe) return fail(&ctx->err, RTMC_ERR_ARG, "chunks must be in [0, 32]");
+    if (transport_blocks_per_sm < 0 || transport_blocks_per_sm > 16)
+        return fail(&ctx->err, RTMC_ERR_ARG, "transport_blocks_per_sm must be in [0, 16]");
+    ctx->opt_chunks = chunks;
+    ctx->opt_k1_bps = transport_blocks_per_sm;
     return RTMC_OK;
 }
 

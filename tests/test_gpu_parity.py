@@ -166,6 +166,30 @@ def test_large_histogram_paths_match_oracle(index_mb):
     assert _l1_diff(hist, ref_hist) <= max(4, 1e-6 * stats["observations"])
 
 
+@pytest.mark.parametrize("chunks,bps,index_mb", [(3, 2, 0), (5, 1, 0), (2, 2, 8), (32, 3, 0)])
+def test_pipelined_transport_and_fold_match_oracle(chunks, bps, index_mb):
+    """The fold of a chunk on the second stream overlapping the transport of the next one,
+    over two index slots (the budget of 8 MB forces more chunks than asked for)."""
+    geo, src, mat, obs, opts = W.c3_halfspace2d()
+    ctx = get_context(0)
+    ctx.set_launch(0, 0, index_mb)
+    ctx.set_pipeline(chunks, bps)
+    try:
+        prob, grid, N, hist, states, stats, ref_hist, ref_states, ref_stats = _run_both(
+            geo, src, mat, obs, opts, 6000, "fp64")
+        P, keep = prob.to_ctypes()
+        h2, _ = ctx.forward(P, prob.tables)
+    finally:
+        ctx.set_launch(0, 0, 0)
+        ctx.set_pipeline(0, 0)
+    assert stats["device_status"] == 0 and stats["sink"] == 2
+    assert stats["launches"] >= 2 * min(chunks, 6000 // 32)
+    assert _path_match(states, ref_states, 1e-9).mean() == 1.0
+    assert stats["observations"] == ref_stats["observations"]
+    assert _l1_diff(hist, ref_hist) <= max(4, 1e-6 * stats["observations"])
+    assert np.array_equal(hist, h2)  # integer adds: the same histogram in any order
+
+
 @pytest.mark.parametrize("frame,extra", [("spherical", {"y": colon(-math.pi, math.pi / 4, math.pi)}),
                                          ("cylindrical", {"z": colon(-2, 0.5, 2)})])
 def test_general_observation_path(frame, extra):
