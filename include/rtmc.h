@@ -325,7 +325,8 @@ int rtmc_set_launch(rtmc_context *ctx, int32_t block, int32_t ring_cap, int32_t 
  * launches over two index slots, and the fold of one chunk (bound by L2 atomics) runs on
  * a second stream while the transport of the next (bound by instruction issue) runs with
  * at most `transport_blocks_per_sm` blocks per SM, leaving room for the fold's blocks.
- * 0 = automatic (4 chunks from 2e6 particles up, 2 blocks per SM); chunks = 1: off. */
+ * It also halves the index scratch.  0 = automatic (off; 2 blocks per SM when on);
+ * chunks = 1: off. */
 int rtmc_set_pipeline(rtmc_context *ctx, int32_t chunks, int32_t transport_blocks_per_sm);
 
 /* enable (1, default) or disable (0) reuse of the device copy of a tables handle across

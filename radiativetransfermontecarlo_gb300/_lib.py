@@ -290,7 +290,8 @@ class Context:
         check(self.lib.rtmc_set_launch(self.handle, block, ring_cap, index_mb), self.handle)
 
     def set_pipeline(self, chunks: int = 0, transport_blocks_per_sm: int = 0):
-        """rtmc_set_pipeline: 0 = automatic; chunks = 1 turns the transport/fold overlap off."""
+        """rtmc_set_pipeline: chunks >= 2 overlaps the fold of a chunk with the next chunk's
+        transport; 0 = automatic (off), 1 = off."""
         check(self.lib.rtmc_set_pipeline(self.handle, chunks, transport_blocks_per_sm), self.handle)
 
     def last_timing(self):

@@ -400,7 +400,9 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         const int64_t rows = std::max<int64_t>(32, ((mb << 20) / (4 * (int64_t)P->n_obs)) / 32 * 32);
         // pipeline: the fold of chunk c overlaps the transport of chunk c + 1 (the fold is
         // bound by L2 atomics, the transport by instruction issue), two index slots
-        const int want = ctx->opt_chunks ? ctx->opt_chunks : (P->n_particles >= 2000000 ? 4 : 1);
+        // off unless asked for: on C2 it measured 25.5 ms against 25.9 ms sequential (the
+        // transport at 2 blocks per SM loses what the overlap gains)
+        const int want = ctx->opt_chunks ? ctx->opt_chunks : 1;
         if (want >= 2) {
             int nc = want;
             int64_t per = ((P->n_particles + nc - 1) / nc + 31) / 32 * 32;
