@@ -79,47 +79,72 @@ int cuda_fail(rtmc_context *c, cudaError_t e, const char *what)
 
 size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
-// Stage the tables in precision R: FP64 knots of u, R angles, R slopes, int32 guide.
+// ---- device layout of one inverse-CDF table: interleaved knots, then the guide ----------
+
+// bytes of one staged table: n knots (256-aligned), then 2^b + 1 guide entries
+template <typename R> size_t table_bytes(size_t n)
+{
+    return align_up(n * sizeof(Knot<R>), 256) + align_up((((size_t)1 << guide_bits(n)) + 1) * sizeof(int32_t), 256);
+}
+
+// knots [k0, k0 + m) of table (c, th): u, theta / pi and the slope, built in FP64
+template <typename R> void fill_knots(const std::vector<double> &c, const std::vector<double> &th, size_t k0, size_t m,
+                                      Knot<R> *out)
+{
+    const double ip = 1.0 / M_PI;
+    const size_t n = c.size();
+    for (size_t k = 0; k < m; ++k) {
+        const size_t q = k0 + k;
+        out[k].c = c[q];
+        out[k].th = (R)(th[q] * ip);
+        out[k].sl = (q + 1 < n) ? (R)((th[q + 1] - th[q]) * ip / (c[q + 1] - c[q])) : (R)0;
+    }
+}
+
+// guide entries [j0, j0 + m): the last knot index with c <= j / 2^b (a walk that resumes at *k)
+inline void fill_guide(const std::vector<double> &c, int bits, int64_t j0, int64_t m, size_t *k, int32_t *out)
+{
+    const size_t n = c.size();
+    const double G = (double)((int64_t)1 << bits);
+    for (int64_t jj = 0; jj < m; ++jj) {
+        const double target = (double)(j0 + jj) / G;
+        while (*k + 1 <= n - 2 && c[*k + 1] <= target) ++*k;
+        out[jj] = (int32_t)*k;
+    }
+}
+
+// table i into a host image at `host` whose device copy starts at `dev`
+template <typename R> void stage_table(const std::vector<double> &c, const std::vector<double> &th, unsigned char *host,
+                                       unsigned char *dev, DevTables<R> *dt, int i)
+{
+    const size_t n = c.size();
+    const int bits = guide_bits(n);
+    fill_knots<R>(c, th, 0, n, reinterpret_cast<Knot<R> *>(host));
+    const size_t go = align_up(n * sizeof(Knot<R>), 256);
+    size_t k = 0;
+    fill_guide(c, bits, 0, ((int64_t)1 << bits) + 1, &k, reinterpret_cast<int32_t *>(host + go));
+    dt->knot[i] = reinterpret_cast<const Knot<R> *>(dev);
+    dt->guide[i] = reinterpret_cast<const int32_t *>(dev + go);
+    dt->n[i] = (int32_t)n;
+    dt->gbits[i] = bits;
+}
+
+// Stage the tables in precision R (knots, guide) in the context's table buffer.
 template <typename R> int upload_tables(rtmc_context *ctx, const rtmc_tables *t, DevTables<R> *dt)
 {
-    const int G = kGuideN;
-    size_t off[4][4], total = 0;
+    size_t off[4], total = 0;
     for (int i = 0; i < t->n_tables; ++i) {
-        const size_t n = t->cdf[i].size();
-        off[i][0] = total; total = align_up(total + n * sizeof(double), 256);
-        off[i][1] = total; total = align_up(total + n * sizeof(R), 256);
-        off[i][2] = total; total = align_up(total + n * sizeof(R), 256);
-        off[i][3] = total; total = align_up(total + (size_t)(G + 1) * sizeof(int32_t), 256);
+        off[i] = total;
+        total += table_bytes<R>(t->cdf[i].size());
     }
     if (ctx->tabs.grow(total)) return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for tables failed");
     std::vector<unsigned char> host(total, 0);
-    for (int i = 0; i < t->n_tables; ++i) {
-        const std::vector<double> &c = t->cdf[i], &th = t->theta[i];
-        const size_t n = c.size();
-        std::memcpy(host.data() + off[i][0], c.data(), n * sizeof(double));
-        R *rt = reinterpret_cast<R *>(host.data() + off[i][1]);
-        R *rs = reinterpret_cast<R *>(host.data() + off[i][2]);
-        // angles are staged as theta / pi, the argument of sincospi in the kernel
-        const double ip = 1.0 / M_PI;
-        for (size_t k = 0; k < n; ++k) {
-            rt[k] = (R)(th[k] * ip);
-            rs[k] = (k + 1 < n) ? (R)((th[k + 1] - th[k]) * ip / (c[k + 1] - c[k])) : (R)0;
-        }
-        int32_t *g = reinterpret_cast<int32_t *>(host.data() + off[i][3]);
-        size_t k = 0;
-        for (int j = 0; j <= G; ++j) {
-            const double target = (double)j / (double)G;
-            while (k + 1 <= n - 2 && c[k + 1] <= target) ++k;
-            g[j] = (int32_t)k;
-        }
-        unsigned char *base = static_cast<unsigned char *>(ctx->tabs.p);
-        dt->cdf[i] = reinterpret_cast<const double *>(base + off[i][0]);
-        dt->theta[i] = reinterpret_cast<const R *>(base + off[i][1]);
-        dt->slope[i] = reinterpret_cast<const R *>(base + off[i][2]);
-        dt->guide[i] = reinterpret_cast<const int32_t *>(base + off[i][3]);
-        dt->n[i] = (int32_t)n;
+    unsigned char *base = static_cast<unsigned char *>(ctx->tabs.p);
+    for (int i = 0; i < t->n_tables; ++i) stage_table<R>(t->cdf[i], t->theta[i], host.data() + off[i], base + off[i], dt, i);
+    for (int i = t->n_tables; i < 4; ++i) {
+        dt->knot[i] = nullptr;
+        dt->guide[i] = nullptr;
     }
-    for (int i = t->n_tables; i < 4; ++i) *(&dt->cdf[0] + i) = nullptr;
     CK(cudaMemcpyAsync(ctx->tabs.p, host.data(), total, cudaMemcpyHostToDevice, ctx->stream), "table upload");
     CK(cudaStreamSynchronize(ctx->stream), "table upload");
     return RTMC_OK;
@@ -339,7 +364,7 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         if (s) { ctx->tabs_gen = 0; return s; }
         ctx->tabs_gen = t->gen;
         ctx->tabs_prec = prec;
-        for (int i = 0; i < t->n_tables; ++i) h2d += (double)t->cdf[i].size() * (8 + 2 * sizeof(R)) + (kGuideN + 1) * 4.0;
+        for (int i = 0; i < t->n_tables; ++i) h2d += (double)table_bytes<R>(t->cdf[i].size());
     }
     DevParams<R> p;
     std::vector<R> edges, zoe;
@@ -750,57 +775,45 @@ template <typename T> int copy_chunk(unsigned char *dst, const T *src, size_t co
     return (int)e;
 }
 
-// same layout as upload_tables (knots, angle/pi, slope/pi, guide), written in chunks
+// same layout as upload_tables, written through stack buffers in chunks
 template <typename R>
 int stage_tables_static(const rtmc_tables *t, unsigned char *base, size_t cap, size_t *used, DevTables<R> *dt,
                         cudaStream_t st, std::string *err)
 {
-    const int G = kGuideN;
-    size_t off[4][4], total = 0;
+    size_t off[4], total = 0;
     for (int i = 0; i < t->n_tables; ++i) {
-        const size_t n = t->cdf[i].size();
-        off[i][0] = total; total = align_up(total + n * sizeof(double), 256);
-        off[i][1] = total; total = align_up(total + n * sizeof(R), 256);
-        off[i][2] = total; total = align_up(total + n * sizeof(R), 256);
-        off[i][3] = total; total = align_up(total + (size_t)(G + 1) * sizeof(int32_t), 256);
+        off[i] = total;
+        total += table_bytes<R>(t->cdf[i].size());
     }
     if (total > cap)
         return fail(err, RTMC_ERR_ARG, "rtmc_forward_noalloc: the tables need " + std::to_string(total) +
                                             " bytes, more than the static scratch of " + std::to_string(cap) + " bytes");
     constexpr size_t B = 4096; // staging chunk on the stack
-    R buf[B];
+    Knot<R> kbuf[B];
     int32_t gbuf[B];
-    const double ip = 1.0 / M_PI;
     for (int i = 0; i < t->n_tables; ++i) {
         const std::vector<double> &c = t->cdf[i], &th = t->theta[i];
         const size_t n = c.size();
-        int e = (int)cudaMemcpyAsync(base + off[i][0], c.data(), n * sizeof(double), cudaMemcpyHostToDevice, st);
-        if (e) return e;
+        const int bits = guide_bits(n);
+        unsigned char *kd = base + off[i];
+        unsigned char *gd = kd + align_up(n * sizeof(Knot<R>), 256);
+        int e;
         for (size_t k0 = 0; k0 < n; k0 += B) {
             const size_t m = std::min(B, n - k0);
-            for (size_t k = 0; k < m; ++k) buf[k] = (R)(th[k0 + k] * ip);
-            if ((e = copy_chunk(base + off[i][1] + k0 * sizeof(R), buf, m, st))) return e;
-            for (size_t k = 0; k < m; ++k) {
-                const size_t q = k0 + k;
-                buf[k] = (q + 1 < n) ? (R)((th[q + 1] - th[q]) * ip / (c[q + 1] - c[q])) : (R)0;
-            }
-            if ((e = copy_chunk(base + off[i][2] + k0 * sizeof(R), buf, m, st))) return e;
+            fill_knots<R>(c, th, k0, m, kbuf);
+            if ((e = copy_chunk(kd + k0 * sizeof(Knot<R>), kbuf, m, st))) return e;
         }
+        const int64_t ng = ((int64_t)1 << bits) + 1;
         size_t k = 0;
-        for (int j0 = 0; j0 <= G; j0 += (int)B) {
-            const int m = std::min((int)B, G + 1 - j0);
-            for (int jj = 0; jj < m; ++jj) {
-                const double target = (double)(j0 + jj) / (double)G;
-                while (k + 1 <= n - 2 && c[k + 1] <= target) ++k;
-                gbuf[jj] = (int32_t)k;
-            }
-            if ((e = copy_chunk(base + off[i][3] + (size_t)j0 * sizeof(int32_t), gbuf, (size_t)m, st))) return e;
+        for (int64_t j0 = 0; j0 < ng; j0 += (int64_t)B) {
+            const int64_t m = std::min<int64_t>((int64_t)B, ng - j0);
+            fill_guide(c, bits, j0, m, &k, gbuf);
+            if ((e = copy_chunk(gd + (size_t)j0 * sizeof(int32_t), gbuf, (size_t)m, st))) return e;
         }
-        dt->cdf[i] = reinterpret_cast<const double *>(base + off[i][0]);
-        dt->theta[i] = reinterpret_cast<const R *>(base + off[i][1]);
-        dt->slope[i] = reinterpret_cast<const R *>(base + off[i][2]);
-        dt->guide[i] = reinterpret_cast<const int32_t *>(base + off[i][3]);
+        dt->knot[i] = reinterpret_cast<const Knot<R> *>(kd);
+        dt->guide[i] = reinterpret_cast<const int32_t *>(gd);
         dt->n[i] = (int32_t)n;
+        dt->gbits[i] = bits;
     }
     *used = total;
     return RTMC_OK;
@@ -1163,43 +1176,6 @@ bool same_grid(const rtmc_problem &a, const rtmc_problem &b)
             if (a.axis_edges[x][k] != b.axis_edges[x][k]) return false;
     }
     return true;
-}
-
-// per-table layout of the staged tables (knots, angle/pi, slope/pi, guide)
-template <typename R> size_t table_bytes(size_t n)
-{
-    return align_up(n * sizeof(double), 256) + 2 * align_up(n * sizeof(R), 256) +
-           align_up((size_t)(kGuideN + 1) * sizeof(int32_t), 256);
-}
-
-template <typename R> void stage_table(const std::vector<double> &c, const std::vector<double> &th, unsigned char *host,
-                                       unsigned char *dev, DevTables<R> *dt, int i)
-{
-    const size_t n = c.size();
-    size_t o = 0;
-    std::memcpy(host + o, c.data(), n * sizeof(double));
-    dt->cdf[i] = reinterpret_cast<const double *>(dev + o);
-    o += align_up(n * sizeof(double), 256);
-    R *rt = reinterpret_cast<R *>(host + o);
-    dt->theta[i] = reinterpret_cast<const R *>(dev + o);
-    o += align_up(n * sizeof(R), 256);
-    R *rs = reinterpret_cast<R *>(host + o);
-    dt->slope[i] = reinterpret_cast<const R *>(dev + o);
-    o += align_up(n * sizeof(R), 256);
-    const double ip = 1.0 / M_PI;
-    for (size_t k = 0; k < n; ++k) {
-        rt[k] = (R)(th[k] * ip);
-        rs[k] = (k + 1 < n) ? (R)((th[k + 1] - th[k]) * ip / (c[k + 1] - c[k])) : (R)0;
-    }
-    int32_t *g = reinterpret_cast<int32_t *>(host + o);
-    dt->guide[i] = reinterpret_cast<const int32_t *>(dev + o);
-    size_t k = 0;
-    for (int j = 0; j <= kGuideN; ++j) {
-        const double target = (double)j / (double)kGuideN;
-        while (k + 1 <= n - 2 && c[k + 1] <= target) ++k;
-        g[j] = (int32_t)k;
-    }
-    dt->n[i] = (int32_t)n;
 }
 
 template <typename R> int batch_build_graph(rtmc_batch *b)

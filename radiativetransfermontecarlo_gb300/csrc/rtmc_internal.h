@@ -30,16 +30,30 @@ inline uint64_t next_generation()
 }
 
 constexpr int kMaxEdges = 4096;  // all axes together, staged in shared memory
-constexpr int kGuideBits = 16;   // Chen-Asau guide table of 2^16 + 1 entries per table
-constexpr int kGuideN = 1 << kGuideBits;
+// Chen-Asau guide table of 2^b + 1 entries per table, b = ceil(log2(knots)) in [16, 20]:
+// about one knot per guide cell, so the search is a guide load and at most a step or two
+constexpr int kGuideMinBits = 16, kGuideMaxBits = 20;
+inline int guide_bits(size_t n_knots)
+{
+    int b = kGuideMinBits;
+    while (b < kGuideMaxBits && ((size_t)1 << b) < n_knots) ++b;
+    return b;
+}
+
+// One knot of an inverse-CDF table: u (FP64 in both precisions: search and interpolation
+// offset), theta / pi and (theta[i+1] - theta[i]) / (pi (u[i+1] - u[i])), built in FP64.
+// 16 bytes for FP32, so the interpolation reads one vector.
+template <typename R> struct alignas(sizeof(R) == 4 ? 16 : 8) Knot {
+    double c;
+    R th, sl;
+};
 
 // Device-side view of one precision's tables; R = float or double.
 template <typename R> struct DevTables {
-    const double *cdf[4];   // knots of u, FP64 in both precisions (search + interpolation offset)
-    const R *theta[4];      // knot angles divided by pi
-    const R *slope[4];      // (theta[i+1]-theta[i]) / (pi (cdf[i+1]-cdf[i])), built in FP64
+    const Knot<R> *knot[4];
     const int32_t *guide[4];
     int32_t n[4];
+    int32_t gbits[4];
 };
 
 template <typename R> struct DevParams {

@@ -98,20 +98,38 @@ template <typename R> __device__ __forceinline__ int geom_steps(R u, R inv_rate,
 // ----------------------------------------------------------------------------------
 // inverse CDF: guide-table start, binary search, linear (extrapolating) interpolation
 // ----------------------------------------------------------------------------------
+template <typename R> __device__ __forceinline__ Knot<R> load_knot(const Knot<R> *k)
+{
+    Knot<R> r;
+    if constexpr (sizeof(R) == 4) {
+        const float4 v = __ldg(reinterpret_cast<const float4 *>(k));
+        r.c = __hiloint2double(__float_as_int(v.y), __float_as_int(v.x));
+        r.th = v.z;
+        r.sl = v.w;
+    } else {
+        r.c = __ldg(&k->c);
+        r.th = __ldg(&k->th);
+        r.sl = __ldg(&k->sl);
+    }
+    return r;
+}
+
 template <typename R> __device__ __forceinline__ R invcdf(const DevTables<R> &t, int ti, R u)
 {
     const double ud = (double)u;
-    int g = (int)(ud * (double)kGuideN);
-    g = g < 0 ? 0 : (g > kGuideN - 1 ? kGuideN - 1 : g);
+    const int G = 1 << t.gbits[ti];
+    int g = (int)(ud * (double)G);
+    g = g < 0 ? 0 : (g > G - 1 ? G - 1 : g);
     const int32_t *guide = t.guide[ti];
-    const double *c = t.cdf[ti];
+    const Knot<R> *kn = t.knot[ti];
     int lo = __ldg(guide + g), hi = __ldg(guide + g + 1);
     while (hi > lo) { // largest i in [lo, hi] with c[i] <= u (lo itself when none)
         int mid = (lo + hi + 1) >> 1;
-        if (__ldg(c + mid) <= ud) lo = mid; else hi = mid - 1;
+        if (__ldg(&kn[mid].c) <= ud) lo = mid; else hi = mid - 1;
     }
-    const R off = (R)(ud - __ldg(c + lo));
-    return __ldg(t.theta[ti] + lo) + off * __ldg(t.slope[ti] + lo);
+    const Knot<R> k = load_knot(kn + lo);
+    const R off = (R)(ud - k.c);
+    return k.th + off * k.sl;
 }
 
 // ----------------------------------------------------------------------------------
