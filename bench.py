@@ -7,7 +7,7 @@ int64 fixed-point histogram (2^-40).  One step = one whole simulation of that wo
 (histogram clear + particle init + transport + binning) with the tables resident.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-  python bench.py --workload c4|c5      (batched sweep / gradient; one extra JSON line)
+  python bench.py --workload c3|c4|c5   (half-space / batched sweep / gradient; one extra JSON line)
 
 Prints one JSON line.  `value` is device time (CUDA events on the library's stream);
 `e2e` times rtmc_forward through the C ABI with host buffers (tables uploaded and the
@@ -377,6 +377,69 @@ def run_c4(args):
     return line
 
 
+def run_c3(args):
+    """2D elastic P-SV half-space, free surface with Zoeppritz reflection, Q = 200, 1e8
+    particles, cylindrical 200 r x 401 t; FP32 vs FP64 (1e7 particles, the same ids)."""
+    from oracle import oracle as O
+    from radiativetransfermontecarlo_gb300 import build_problem, get_context, normalise
+    from radiativetransfermontecarlo_gb300 import workloads as W
+    import warnings
+    n = args.particles if args.particles != 10_000_000 else 100_000_000
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        geo, src, mat, obs, opts = W.c3_halfspace2d(n=n, precision="fp32")
+        prob, grid, N = build_problem(geo, src, mat, obs, dict(opts, exact_count=True))
+        n64 = min(n, 10_000_000)
+        geo, src, mat, obs, opts = W.c3_halfspace2d(n=n64, precision="fp64")
+        prob64, _, _ = build_problem(geo, src, mat, obs, dict(opts, exact_count=True))
+    prob64.tables = prob.tables
+    ctx = get_context(0)
+    if args.block or args.ring or args.index_mb:
+        ctx.set_launch(args.block, args.ring, args.index_mb)
+    P32, k32 = prob.to_ctypes()
+    for _ in range(args.warmup):
+        ctx.forward_device(P32, prob.tables)
+    ms, ev = [], 0
+    with ClockSampler(0) as clk:
+        for _ in range(args.steps):
+            ctx.flush_l2()
+            st = ctx.forward_device(P32, prob.tables)
+            ms.append(st["total_ms"])
+            ev += st["scatter_events"]
+    value = ev / (sum(ms) / 1000.0)
+    # FP64 and FP32 on the same 1e7 particle ids: speed ratio and the per-bin error
+    P64, k64 = prob64.to_ctypes()
+    h64, s64 = ctx.forward(P64, prob.tables)
+    P32s, k32s = prob.to_ctypes()
+    P32s.n_particles = n64
+    h32, s32 = ctx.forward(P32s, prob.tables)
+    e32 = normalise(h32, grid, n64)[0]
+    e64 = normalise(h64, grid, n64)[0]
+    m = e64 > 0
+    rel = np.abs(e32[m] - e64[m]) / e64[m]
+    sig = np.sqrt(np.maximum(h64.reshape(grid.shape, order="F")[m], 1))  # Monte Carlo error of a bin, in counts
+    z = (h32.reshape(grid.shape, order="F")[m] - h64.reshape(grid.shape, order="F")[m]) / sig
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": float(np.mean(ms)), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "2D elastic P-SV half-space, free surface y=0 (Zoeppritz), source at depth 1, "
+                                   "exp lc=0.5 f=8 cv=0.2x3, vp=2 vs=1.155 rho=1000, Q=200, cylindrical 200 r x 401 t",
+                       "particles": n, "l2": "512 MB device write between steps"},
+            "gpu_launches": args.steps, "clocks": clk.summary(), "events_per_step": ev / args.steps,
+            "boundary_hits_per_step": st["boundary_hits"], "kills_per_step": st["kills"], "sink": st["sink"],
+            "fp64_vs_fp32_same_1e7_ids": {"fp64_ms": s64["kernel_ms"], "fp32_ms": s32["kernel_ms"],
+                                          "fp32_over_fp64": s64["kernel_ms"] / s32["kernel_ms"],
+                                          "rel_l2_energy_density": float(np.linalg.norm(e32 - e64) / np.linalg.norm(e64)),
+                                          "per_bin_rel_error_median": float(np.median(rel)),
+                                          "per_bin_rel_error_p99": float(np.quantile(rel, 0.99)),
+                                          "per_bin_diff_over_sqrt_count_p99": float(np.quantile(np.abs(z), 0.99)),
+                                          "bins": int(m.sum())}}
+    if not args.no_cpu:
+        line["cpu_baseline"] = {k: v for k, v in cpu_sample(prob, O.table_knots(prob.tables), target_s=12.0).items()
+                                if k not in ("events", "seconds")}
+    return line
+
+
 def run_c5(args):
     """Gradient of L = sum (E - E_t)^2 / E_t over (lc, cv_kappa, cv_rho, Q) at lc 0.1,
     cv [0.05 0.05], Q 400 against a target at lc 0.12, cv [0.06 0.04], Q 300, 3D acoustic,
@@ -447,8 +510,8 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c4", "c5"],
-                    help="c2: the headline line (default); c4: batched sweep; c5: gradient")
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"],
+                    help="c2: the headline line (default); c3: 2D half-space; c4: batched sweep; c5: gradient")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -456,7 +519,7 @@ def main():
     __graft_entry__.build()
     if args.workload != "c2":
         if rank == 0:
-            line = run_c4(args) if args.workload == "c4" else run_c5(args)
+            line = {"c3": run_c3, "c4": run_c4, "c5": run_c5}[args.workload](args)
             print(json.dumps(line), flush=True)
         return
     if args.impl == "reference":
