@@ -425,7 +425,7 @@ def run_c3(args):
             "config": {"workload": "2D elastic P-SV half-space, free surface y=0 (Zoeppritz), source at depth 1, "
                                    "exp lc=0.5 f=8 cv=0.2x3, vp=2 vs=1.155 rho=1000, Q=200, cylindrical 200 r x 401 t",
                        "particles": n, "l2": "512 MB device write between steps"},
-            "gpu_launches": args.steps, "clocks": clk.summary(), "events_per_step": ev / args.steps,
+            "gpu_launches": args.steps * int(st["launches"]), "clocks": clk.summary(), "events_per_step": ev / args.steps,
             "boundary_hits_per_step": st["boundary_hits"], "kills_per_step": st["kills"], "sink": st["sink"],
             "fp64_vs_fp32_same_1e7_ids": {"fp64_ms": s64["kernel_ms"], "fp32_ms": s32["kernel_ms"],
                                           "fp32_over_fp64": s64["kernel_ms"] / s32["kernel_ms"],
