@@ -95,7 +95,12 @@ template <typename R> void fill_knots(const std::vector<double> &c, const std::v
     const size_t n = c.size();
     for (size_t k = 0; k < m; ++k) {
         const size_t q = k0 + k;
-        out[k].c = c[q];
+        if constexpr (sizeof(R) == 4) {
+            out[k].ch = (float)c[q];
+            out[k].cl = (float)(c[q] - (double)out[k].ch);
+        } else {
+            out[k].c = c[q];
+        }
         out[k].th = (R)(th[q] * ip);
         out[k].sl = (q + 1 < n) ? (R)((th[q + 1] - th[q]) * ip / (c[q + 1] - c[q])) : (R)0;
     }

@@ -40,12 +40,18 @@ inline int guide_bits(size_t n_knots)
     return b;
 }
 
-// One knot of an inverse-CDF table: u (FP64 in both precisions: search and interpolation
-// offset), theta / pi and (theta[i+1] - theta[i]) / (pi (u[i+1] - u[i])), built in FP64.
-// 16 bytes for FP32, so the interpolation reads one vector.
-template <typename R> struct alignas(sizeof(R) == 4 ? 16 : 8) Knot {
+// One knot of an inverse-CDF table: u, theta / pi and (theta[i+1] - theta[i]) /
+// (pi (u[i+1] - u[i])), built in FP64.  FP64 tables keep u as a double; FP32 tables keep
+// it as an unevaluated float sum ch + cl, which compares with a float u and gives the
+// interpolation offset (u - ch) - cl without FP64 arithmetic.  16 bytes for FP32, so the
+// interpolation reads one vector.
+template <typename R> struct Knot {
     double c;
     R th, sl;
+};
+template <> struct alignas(16) Knot<float> {
+    float ch, cl;
+    float th, sl;
 };
 
 // Device-side view of one precision's tables; R = float or double.

@@ -98,38 +98,35 @@ template <typename R> __device__ __forceinline__ int geom_steps(R u, R inv_rate,
 // ----------------------------------------------------------------------------------
 // inverse CDF: guide-table start, binary search, linear (extrapolating) interpolation
 // ----------------------------------------------------------------------------------
-template <typename R> __device__ __forceinline__ Knot<R> load_knot(const Knot<R> *k)
+__device__ __forceinline__ double invcdf_search(const Knot<double> *kn, int lo, int hi, double u)
 {
-    Knot<R> r;
-    if constexpr (sizeof(R) == 4) {
-        const float4 v = __ldg(reinterpret_cast<const float4 *>(k));
-        r.c = __hiloint2double(__float_as_int(v.y), __float_as_int(v.x));
-        r.th = v.z;
-        r.sl = v.w;
-    } else {
-        r.c = __ldg(&k->c);
-        r.th = __ldg(&k->th);
-        r.sl = __ldg(&k->sl);
+    while (hi > lo) { // largest i in [lo, hi] with c[i] <= u (lo itself when none)
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(&kn[mid].c) <= u) lo = mid; else hi = mid - 1;
     }
-    return r;
+    return __ldg(&kn[lo].th) + (u - __ldg(&kn[lo].c)) * __ldg(&kn[lo].sl);
+}
+
+// FP32: c <= u for c = ch + cl and a float u is ch < u, or ch == u with cl <= 0; the offset
+// (u - ch) - cl is exact up to the rounding of cl.  No FP64 instruction on this path.
+__device__ __forceinline__ float invcdf_search(const Knot<float> *kn, int lo, int hi, float u)
+{
+    while (hi > lo) {
+        const int mid = (lo + hi + 1) >> 1;
+        const float2 c = __ldg(reinterpret_cast<const float2 *>(kn + mid));
+        if (c.x < u || (c.x == u && c.y <= 0.f)) lo = mid; else hi = mid - 1;
+    }
+    const float4 k = __ldg(reinterpret_cast<const float4 *>(kn + lo));
+    return k.z + ((u - k.x) - k.y) * k.w;
 }
 
 template <typename R> __device__ __forceinline__ R invcdf(const DevTables<R> &t, int ti, R u)
 {
-    const double ud = (double)u;
     const int G = 1 << t.gbits[ti];
-    int g = (int)(ud * (double)G);
+    int g = (int)(u * (R)G); // exact: G is a power of two
     g = g < 0 ? 0 : (g > G - 1 ? G - 1 : g);
     const int32_t *guide = t.guide[ti];
-    const Knot<R> *kn = t.knot[ti];
-    int lo = __ldg(guide + g), hi = __ldg(guide + g + 1);
-    while (hi > lo) { // largest i in [lo, hi] with c[i] <= u (lo itself when none)
-        int mid = (lo + hi + 1) >> 1;
-        if (__ldg(&kn[mid].c) <= ud) lo = mid; else hi = mid - 1;
-    }
-    const Knot<R> k = load_knot(kn + lo);
-    const R off = (R)(ud - k.c);
-    return k.th + off * k.sl;
+    return invcdf_search(t.knot[ti], __ldg(guide + g), __ldg(guide + g + 1), u);
 }
 
 // ----------------------------------------------------------------------------------
