@@ -712,9 +712,16 @@ int gradient_run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t,
         a.b_obs[q] = -sc->dlogSigma[q] * hS * (double)P->n_sub;
     }
     const int block = kAdjointThreads;
-    const size_t smem = align_up((size_t)n_edges * sizeof(R), 16);
+    // up to 4 parameters: the converged two-phase replay with a segment ring; more: one
+    // particle per thread
+    const bool ring = sc->n_params <= kAdjointRingParams;
+    const int cap = ctx->opt_ring ? ctx->opt_ring : (sizeof(R) == 4 ? 8 : 6);
+    size_t smem = align_up((size_t)n_edges * sizeof(R), 16);
+    if (ring) smem += (size_t)block * cap * (7 * sizeof(R) + 2 * sizeof(int32_t));
+    p.ring_cap = cap;
     int bps = 0;
-    if (adjoint_occupancy(prec, p.obs_kind, block, smem, &bps) != 0 || bps < 1)
+    if ((ring ? adjoint_ring_occupancy(prec, p.obs_kind, block, smem, &bps)
+              : adjoint_occupancy(prec, p.obs_kind, block, smem, &bps)) != 0 || bps < 1)
         return fail(&ctx->err, RTMC_ERR_CUDA, "adjoint kernel does not fit on the device");
     const int64_t need = (std::max<int64_t>(P->n_particles, 1) + block - 1) / block;
     const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->num_sms * bps, need));
@@ -723,8 +730,12 @@ int gradient_run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t,
     a.partial = static_cast<double *>(ctx->partial.p);
     CK(cudaEventRecord(ctx->ev_k0, ctx->stream), "event");
     int le;
-    if constexpr (sizeof(R) == 4) le = launch_adjoint_f32(p, a, grid, block, smem, ctx->stream);
-    else le = launch_adjoint_f64(p, a, grid, block, smem, ctx->stream);
+    if constexpr (sizeof(R) == 4)
+        le = ring ? launch_adjoint_ring_f32(p, a, grid, block, smem, ctx->stream)
+                  : launch_adjoint_f32(p, a, grid, block, smem, ctx->stream);
+    else
+        le = ring ? launch_adjoint_ring_f64(p, a, grid, block, smem, ctx->stream)
+                  : launch_adjoint_f64(p, a, grid, block, smem, ctx->stream);
     if (le) return cuda_fail(ctx, (cudaError_t)le, "adjoint launch");
     CK(cudaEventRecord(ctx->ev_k1, ctx->stream), "event");
     std::vector<double> part((size_t)grid * sc->n_params);

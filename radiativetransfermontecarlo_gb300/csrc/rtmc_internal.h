@@ -157,6 +157,10 @@ int transport_occupancy(int precision, int sink, int obs, int block, size_t smem
 int launch_adjoint_f32(const DevParams<float> &p, const AdjointArgs &a, int grid, int block, size_t smem, void *stream);
 int launch_adjoint_f64(const DevParams<double> &p, const AdjointArgs &a, int grid, int block, size_t smem, void *stream);
 int adjoint_occupancy(int precision, int obs, int block, size_t smem, int *blocks_per_sm);
+int launch_adjoint_ring_f32(const DevParams<float> &p, const AdjointArgs &a, int grid, int block, size_t smem, void *stream);
+int launch_adjoint_ring_f64(const DevParams<double> &p, const AdjointArgs &a, int grid, int block, size_t smem, void *stream);
+int adjoint_ring_occupancy(int precision, int obs, int block, size_t smem, int *blocks_per_sm);
+constexpr int kAdjointRingParams = 4; // parameters the ring-based adjoint carries
 constexpr int kAdjointThreads = 256;
 int transport_set_smem(int precision, int sink, int obs, size_t smem);
 int transport_max_threads(int precision, int sink, int obs);

@@ -728,6 +728,7 @@ template <typename R> struct Seg {
     R x[3], d[3];
     R A[3], B[3];
     int s0, mode, doff;
+    R th; // adjoint only: theta / pi of the scattering that starts the segment, or -1
 };
 
 template <typename R, int OBS>
@@ -785,20 +786,23 @@ __device__ __forceinline__ int obs_offset(const DevParams<R> &p, const R *sedges
 template <typename R> struct Ring {
     R *x0, *x1, *x2, *d0, *d1, *d2;
     int *s0, *mode;
+    R *th; // adjoint only
     int cap, stride;
-    __device__ __forceinline__ void put(int slot, const Part<R> &s) const
+    template <bool TH = false> __device__ __forceinline__ void put(int slot, const Part<R> &s, R t = (R)-1) const
     {
         const int k = slot * stride + threadIdx.x;
         x0[k] = s.x[0]; x1[k] = s.x[1]; x2[k] = s.x[2];
         d0[k] = s.d[0]; d1[k] = s.d[1]; d2[k] = s.d[2];
         s0[k] = s.s0; mode[k] = s.mode;
+        if (TH) th[k] = t;
     }
-    __device__ __forceinline__ void get(int slot, Seg<R> &g) const
+    template <bool TH = false> __device__ __forceinline__ void get(int slot, Seg<R> &g) const
     {
         const int k = slot * stride + threadIdx.x;
         g.x[0] = x0[k]; g.x[1] = x1[k]; g.x[2] = x2[k];
         g.d[0] = d0[k]; g.d[1] = d1[k]; g.d[2] = d2[k];
         g.s0 = s0[k]; g.mode = mode[k];
+        if (TH) g.th = th[k];
     }
     __device__ __forceinline__ int start(int slot) const { return s0[slot * stride + threadIdx.x]; }
 };
@@ -816,7 +820,49 @@ template <typename R> __device__ __forceinline__ int next_event(const Part<R> &s
 // Where observations go: a block-private u32 histogram in shared memory (the whole
 // histogram fits), 64-bit global atomics, or a dense time-major array of 32-bit bin
 // indices that rt_bin_slices folds into the histogram one time slice at a time.
-enum { SINK_SMEM = 0, SINK_GLOBAL = 1, SINK_INDEX = 2 };
+enum { SINK_SMEM = 0, SINK_GLOBAL = 1, SINK_INDEX = 2, SINK_ADJOINT = 3 };
+
+// Per-lane score state of the adjoint sink (at most kAdjRingParams parameters): the
+// score of the segment in force is A + b_obs * j; sa and saj sum the adjoint weights and
+// j * weights of its observations since A last changed; g accumulates in FP64.
+constexpr int kAdjRingParams = 4;
+template <typename R> struct AdjLane {
+    const AdjointArgs *a;
+    R A[kAdjRingParams];
+    R sa, saj;
+    double g[kAdjRingParams];
+    __device__ __forceinline__ void flush()
+    {
+#pragma unroll
+        for (int q = 0; q < kAdjRingParams; ++q)
+            if (q < a->n_params) g[q] = fma((double)A[q], (double)sa, fma(a->b_obs[q], (double)saj, g[q]));
+        sa = saj = (R)0;
+    }
+    // a new segment is in force; a scattering at theta / pi = th >= 0 started it
+    __device__ __forceinline__ void enter(R th)
+    {
+        if (!(th >= (R)0)) return;
+        flush();
+        R f = th > (R)1 ? (R)1 : th;
+        f *= (R)(a->n_theta - 1);
+        int k = (int)f;
+        k = k > a->n_theta - 2 ? a->n_theta - 2 : k;
+        const double w = (double)(f - (R)k);
+#pragma unroll
+        for (int q = 0; q < kAdjRingParams; ++q) {
+            if (q < a->n_params) {
+                const double *t = a->dlogsigma + (size_t)q * a->n_theta + k;
+                A[q] += (R)(fma(w, __ldg(t + 1) - __ldg(t), __ldg(t)) + a->a_inc[q]);
+            }
+        }
+    }
+    __device__ __forceinline__ void observe(int64_t idx, int j)
+    {
+        const R w = __ldg(static_cast<const R *>(a->adjoint) + idx);
+        sa += w;
+        saj += w * (R)j;
+    }
+};
 
 // launch bounds of the transport variants (build-time knobs for the index/global sinks)
 #ifndef RTMC_TRANSPORT_THREADS
@@ -831,12 +877,17 @@ template <typename R, int SINK> struct Bounds {
 };
 
 // One warp's batch of 32 consecutive particles [base, base + 32) of the problem p,
-// clipped at n_end: the two-cursor transport described at rt_transport.
+// clipped at n_end: the two-cursor transport described at rt_transport.  The adjoint
+// sink (adj non-null) accumulates adjoint weights instead of binning, and carries each
+// segment's scattering angle through the ring to update the score when the segment
+// comes into force.
 template <typename R, int SINK, int OBS>
 __device__ __forceinline__ void run_batch(const DevParams<R> &p, const R *sedges, unsigned *shist, const Ring<R> &ring,
-                                          int64_t base, int64_t n_end, Counters &cnt, bool &bad)
+                                          int64_t base, int64_t n_end, Counters &cnt, bool &bad,
+                                          AdjLane<R> *adj = nullptr)
 {
     constexpr bool SMEM = SINK == SINK_SMEM;
+    constexpr bool ADJ = SINK == SINK_ADJOINT;
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     const unsigned long long inc = 1ull << p.hist_shift;
@@ -858,6 +909,11 @@ __device__ __forceinline__ void run_batch(const DevParams<R> &p, const R *sedges
     }
     seg_from(s, cur);
     seg_prepare<R, OBS>(p, sedges, cur);
+    if (ADJ) {
+#pragma unroll
+        for (int q = 0; q < kAdjRingParams; ++q) adj->A[q] = (R)0;
+        adj->sa = adj->saj = (R)0;
+    }
     int32_t *optr = (SINK == SINK_INDEX && have) ? p.obs_idx + i : nullptr;
     int jn = 1; // warp-uniform
     while (jn <= p.n_obs) {
@@ -867,7 +923,8 @@ __device__ __forceinline__ void run_batch(const DevParams<R> &p, const R *sedges
             // segments starting at or before the next observation supersede the
             // current one: consume them, so the ring only holds later segments
             while (count > 0 && ring.start(head) <= so_next) {
-                ring.get(head, cur);
+                ring.template get<ADJ>(head, cur);
+                if (ADJ) adj->enter(cur.th);
                 seg_prepare<R, OBS>(p, sedges, cur);
                 head = (head + 1) % C;
                 --count;
@@ -875,14 +932,16 @@ __device__ __forceinline__ void run_batch(const DevParams<R> &p, const R *sedges
             const bool need = s.alive && count < C && next_event(s) <= s_end;
             if (!__any_sync(full, need)) break;
             if (need) {
-                process_event(p, pid, s, cnt);
+                const int kind = process_event(p, pid, s, cnt);
                 if ((int)s.k > p.max_events) { s.alive = 0; s.s_death = s.s0; bad = true; }
                 if (s.alive) {
+                    const R th = (ADJ && kind == 0) ? s.th : (R)-1;
                     if (count == 0 && s.s0 <= so_next) {
                         seg_from(s, cur);
+                        if (ADJ) adj->enter(th);
                         seg_prepare<R, OBS>(p, sedges, cur);
                     } else {
-                        ring.put((head + count) % C, s);
+                        ring.template put<ADJ>((head + count) % C, s, th);
                         ++count;
                     }
                 }
@@ -915,7 +974,8 @@ __device__ __forceinline__ void run_batch(const DevParams<R> &p, const R *sedges
         // make cur the segment in force at sub-step at
         auto advance = [&](int at) {
             do {
-                ring.get(head, cur);
+                ring.template get<ADJ>(head, cur);
+                if (ADJ) adj->enter(cur.th);
                 head = (head + 1) % C;
                 --count;
             } while (count > 0 && ring.start(head) <= at);
@@ -933,7 +993,8 @@ __device__ __forceinline__ void run_batch(const DevParams<R> &p, const R *sedges
                 const int64_t idx = (int64_t)j * p.time_stride + (mode ? p.mode_stride : 0) + v;
                 if (idx < p.hist_len) {
                     cnt.obs++;
-                    if (SMEM) atomicAdd(shist + idx, 1u);
+                    if (ADJ) adj->observe(idx, j);
+                    else if (SMEM) atomicAdd(shist + idx, 1u);
                     else atomicAdd(p.hist + idx, inc);
                 } else {
                     bad = true;
@@ -941,7 +1002,8 @@ __device__ __forceinline__ void run_batch(const DevParams<R> &p, const R *sedges
             }
         };
         unsigned w = 0;
-        for (; w + 1 < nw; w += 2, jn += 2, so += 2 * p.n_sub) {
+        // pairs (the adjoint goes one at a time: the score may change between the two)
+        for (; !ADJ && w + 1 < nw; w += 2, jn += 2, so += 2 * p.n_sub) {
             const int so1 = so + p.n_sub;
             int v0 = -1, v1 = -1, m0 = cur.mode, m1 = cur.mode;
             if (so < obs_limit) {
@@ -959,16 +1021,16 @@ __device__ __forceinline__ void run_batch(const DevParams<R> &p, const R *sedges
             emit(v0, m0, jn);
             emit(v1, m1, jn + 1);
         }
-        if (w < nw) {
+        for (; w < nw; ++w, ++jn, so += p.n_sub) {
             int v = -1;
             if (so < obs_limit) {
                 if (so >= next_start) advance(so);
                 v = obs_offset<R, OBS>(p, sedges, cur, so);
             }
             emit(v, cur.mode, jn);
-            ++jn;
         }
     }
+    if (ADJ) adj->flush();
     if (have && p.trace) { // final state of the particle, the oracle's layout
         double *f = p.trace + 16 * i;
 #pragma unroll
@@ -1352,6 +1414,69 @@ __global__ void __launch_bounds__(kAdjointThreads, sizeof(R) == 4 ? 3 : 2) rt_ad
     if (bad) atomicExch(p.status, 1);
 }
 
+// Adjoint replay on the converged two-phase transport (at most kAdjRingParams
+// parameters): events run together in phase 1 and carry their scattering angle through
+// the ring; phase 2 accumulates adjoint weights per observation in lockstep.
+template <typename R, int OBS>
+__global__ void __launch_bounds__(kAdjointThreads, sizeof(R) == 4 ? 2 : 1) rt_adjoint_ring(const DevParams<R> p, const AdjointArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ double red[kAdjointThreads / 32][kAdjRingParams];
+    R *sedges = reinterpret_cast<R *>(smem_raw);
+    const size_t off = (((size_t)p.n_edges * sizeof(R) + 15) / 16) * 16;
+    const int T = blockDim.x, C = p.ring_cap;
+    Ring<R> ring;
+    ring.cap = C;
+    ring.stride = T;
+    {
+        R *r = reinterpret_cast<R *>(smem_raw + off);
+        ring.x0 = r; ring.x1 = r + C * T; ring.x2 = r + 2 * C * T;
+        ring.d0 = r + 3 * C * T; ring.d1 = r + 4 * C * T; ring.d2 = r + 5 * C * T;
+        ring.th = r + 6 * C * T;
+        int *ri = reinterpret_cast<int *>(r + 7 * C * T);
+        ring.s0 = ri; ring.mode = ri + C * T;
+    }
+    for (int k = threadIdx.x; k < p.n_edges; k += T) sedges[k] = p.edges[k];
+    __syncthreads();
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    Counters cnt = {0u, 0u, 0u, 0u, 0u, 0u};
+    bool bad = false;
+    AdjLane<R> adj;
+    adj.a = &a;
+#pragma unroll
+    for (int q = 0; q < kAdjRingParams; ++q) adj.g[q] = 0.0;
+    const int64_t warps = ((int64_t)gridDim.x * T) >> 5;
+    for (int64_t base = (((int64_t)blockIdx.x * T + threadIdx.x) >> 5) << 5; base < p.n_particles; base += warps * 32)
+        run_batch<R, SINK_ADJOINT, OBS>(p, sedges, nullptr, ring, base, p.n_particles, cnt, bad, &adj);
+    // block sums in a fixed order
+#pragma unroll
+    for (int q = 0; q < kAdjRingParams; ++q) {
+        double v = adj.g[q];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(full, v, o);
+        if (lane == 0) red[warp][q] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < a.n_params) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w][threadIdx.x];
+        a.partial[(size_t)blockIdx.x * a.n_params + threadIdx.x] = v;
+    }
+    unsigned cv[6] = {cnt.scat, cnt.bnd, cnt.kill, cnt.absorb, cnt.obs, cnt.conv};
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        const unsigned t = __reduce_add_sync(full, cv[c]);
+        if (lane == 0 && t) atomicAdd(p.stats + c, (unsigned long long)t);
+    }
+    if (bad) atomicExch(p.status, 1);
+}
+
+template <typename R> void *pick_adjoint_ring(int obs)
+{
+    return obs == OBS_CART ? (void *)rt_adjoint_ring<R, OBS_CART>
+                           : (obs == OBS_RADIAL ? (void *)rt_adjoint_ring<R, OBS_RADIAL> : (void *)rt_adjoint_ring<R, OBS_GENERAL>);
+}
+
 template <typename R> void *pick_adjoint(int obs)
 {
     return obs == OBS_CART ? (void *)rt_adjoint<R, OBS_CART>
@@ -1462,6 +1587,31 @@ int launch_adjoint_f32(const DevParams<float> &p, const AdjointArgs &a, int grid
 int launch_adjoint_f64(const DevParams<double> &p, const AdjointArgs &a, int grid, int block, size_t smem, void *stream)
 {
     return launch_adj(p, a, grid, block, smem, stream);
+}
+
+template <typename R>
+static int launch_adj_ring(const DevParams<R> &p, const AdjointArgs &a, int grid, int block, size_t smem, void *stream)
+{
+    void *args[] = {(void *)&p, (void *)&a};
+    return (int)cudaLaunchKernel(pick_adjoint_ring<R>(p.obs_kind), dim3(grid), dim3(block), args, smem, (cudaStream_t)stream);
+}
+
+int launch_adjoint_ring_f32(const DevParams<float> &p, const AdjointArgs &a, int grid, int block, size_t smem, void *stream)
+{
+    return launch_adj_ring(p, a, grid, block, smem, stream);
+}
+
+int launch_adjoint_ring_f64(const DevParams<double> &p, const AdjointArgs &a, int grid, int block, size_t smem, void *stream)
+{
+    return launch_adj_ring(p, a, grid, block, smem, stream);
+}
+
+int adjoint_ring_occupancy(int precision, int obs, int block, size_t smem, int *blocks_per_sm)
+{
+    void *fn = precision == RTMC_FP64 ? pick_adjoint_ring<double>(obs) : pick_adjoint_ring<float>(obs);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, block, smem);
+    return (int)e;
 }
 
 int adjoint_occupancy(int precision, int obs, int block, size_t smem, int *blocks_per_sm)

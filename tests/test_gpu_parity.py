@@ -324,6 +324,10 @@ def test_gradient_replay_matches_oracle(precision):
         assert np.all(np.abs(g - go) <= 0.05 * scale), (g, go)
     g2, _ = get_context(0).gradient(P, prob.tables, dls, dlS, adj)
     assert np.array_equal(g, g2)  # fixed launch shape: reproducible bits
+    # five parameters take the one-particle-per-thread replay: the same numbers
+    g5, _ = get_context(0).gradient(P, prob.tables, np.vstack([dls, dls[:1]]), np.append(dlS, dlS[0]), adj)
+    tol = 1e-8 if precision == "fp64" else 1e-3
+    assert np.all(np.abs(g5[:4] - g) <= tol * scale) and abs(g5[4] - g5[0]) <= tol * scale[0], (g5, g)
 
 
 def test_gradient_against_central_differences():
