@@ -457,6 +457,9 @@ def run_c5(args):
     mat.Q = 400
     params = ("lc", "cv_kappa", "cv_rho", "Q", "mfp")
     o = dict(o, seed=5)
+    if args.block or args.ring or args.index_mb:
+        from radiativetransfermontecarlo_gb300 import get_context
+        get_context(0).set_launch(args.block, args.ring, args.index_mb)
     for _ in range(args.warmup):
         A.radiativeTransferGradient(geo, src, mat, obs, Et, params, o)
     fwd, adj, wall, ev = [], [], [], 0
