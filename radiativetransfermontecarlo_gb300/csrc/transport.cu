@@ -827,7 +827,8 @@ enum { SINK_SMEM = 0, SINK_GLOBAL = 1, SINK_INDEX = 2, SINK_ADJOINT = 3 };
 // j * weights of its observations since A last changed; g accumulates in FP64.
 constexpr int kAdjRingParams = 4;
 template <typename R> struct AdjLane {
-    const AdjointArgs *a;
+    const AdjointArgs *a; // read in the rare paths (a new scattering, the particle's end)
+    const R *wts;         // adjoint weights, read per observation
     R A[kAdjRingParams];
     R sa, saj;
     double g[kAdjRingParams];
@@ -858,7 +859,7 @@ template <typename R> struct AdjLane {
     }
     __device__ __forceinline__ void observe(int64_t idx, int j)
     {
-        const R w = __ldg(static_cast<const R *>(a->adjoint) + idx);
+        const R w = __ldg(wts + idx);
         sa += w;
         saj += w * (R)j;
     }
@@ -1444,6 +1445,7 @@ __global__ void __launch_bounds__(kAdjointThreads, sizeof(R) == 4 ? 2 : 1) rt_ad
     bool bad = false;
     AdjLane<R> adj;
     adj.a = &a;
+    adj.wts = static_cast<const R *>(a.adjoint);
 #pragma unroll
     for (int q = 0; q < kAdjRingParams; ++q) adj.g[q] = 0.0;
     const int64_t warps = ((int64_t)gridDim.x * T) >> 5;
