@@ -675,7 +675,8 @@ int gradient_run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t,
     const size_t zb = align_up(zoe.size() * sizeof(R), 256);
     const size_t hb = (size_t)P->hist_len * sizeof(R);
     const size_t sb = (size_t)sc->n_params * sc->n_theta * sizeof(double);
-    if (ctx->aux.grow(eb + zb) || ctx->stats.grow(256) || ctx->adj.grow(align_up(hb, 256) + sb))
+    const size_t sbf = (size_t)sc->n_params * sc->n_theta * sizeof(float);
+    if (ctx->aux.grow(eb + zb) || ctx->stats.grow(256) || ctx->adj.grow(align_up(hb, 256) + align_up(sb, 256) + sbf))
         return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for the gradient failed");
     unsigned char *aux = static_cast<unsigned char *>(ctx->aux.p);
     if (!edges.empty())
@@ -691,6 +692,11 @@ int gradient_run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t,
         CK(cudaStreamSynchronize(ctx->stream), "adjoint weights"); // wr is released on return
     }
     CK(cudaMemcpyAsync(ab + align_up(hb, 256), sc->dlogsigma, sb, cudaMemcpyHostToDevice, ctx->stream), "score table");
+    std::vector<float> dls_f((size_t)sc->n_params * sc->n_theta);
+    for (size_t k = 0; k < dls_f.size(); ++k) dls_f[k] = (float)sc->dlogsigma[k];
+    CK(cudaMemcpyAsync(ab + align_up(hb, 256) + align_up(sb, 256), dls_f.data(), sbf, cudaMemcpyHostToDevice,
+                       ctx->stream), "score table");
+    CK(cudaStreamSynchronize(ctx->stream), "score table"); // dls_f is released on return
     CK(cudaMemsetAsync(ctx->stats.p, 0, 256, ctx->stream), "counter clear");
     p.edges = reinterpret_cast<const R *>(aux);
     p.zoe = reinterpret_cast<const R *>(aux + eb);
@@ -702,6 +708,7 @@ int gradient_run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t,
     AdjointArgs a{};
     a.adjoint = ab;
     a.dlogsigma = reinterpret_cast<const double *>(ab + align_up(hb, 256));
+    a.dlogsigma_f = reinterpret_cast<const float *>(ab + align_up(hb, 256) + align_up(sb, 256));
     a.n_params = sc->n_params;
     a.n_theta = sc->n_theta;
     // per-sub-step scattering probability 1 - exp(-h Sigma), Sigma = 1 / mean free time
@@ -709,6 +716,7 @@ int gradient_run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t,
     const double kappa = hS > 0 ? hS / std::expm1(hS) : 1.0;
     for (int q = 0; q < sc->n_params; ++q) {
         a.a_inc[q] = sc->dlogSigma[q] * (kappa - 1.0 + hS);
+        a.a_inc_f[q] = (float)a.a_inc[q];
         a.b_obs[q] = -sc->dlogSigma[q] * hS * (double)P->n_sub;
     }
     const int block = kAdjointThreads;

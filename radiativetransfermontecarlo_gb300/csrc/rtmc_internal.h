@@ -144,9 +144,11 @@ template <typename R> struct BatchArgs {
 struct AdjointArgs {
     const void *adjoint;      // [hist_len] d L / d count, in the transport's precision
     const double *dlogsigma;  // [n_params][n_theta] on a uniform grid of theta / pi in [0, 1]
+    const float *dlogsigma_f; // the same in FP32 (FP32 replay)
     int32_t n_params, n_theta;
     double a_inc[RTMC_MAX_PARAMS];
     double b_obs[RTMC_MAX_PARAMS];
+    float a_inc_f[RTMC_MAX_PARAMS];
     double *partial;          // [gridDim.x][n_params] block sums
 };
 

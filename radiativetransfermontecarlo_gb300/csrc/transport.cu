@@ -822,46 +822,59 @@ template <typename R> __device__ __forceinline__ int next_event(const Part<R> &s
 // indices that rt_bin_slices folds into the histogram one time slice at a time.
 enum { SINK_SMEM = 0, SINK_GLOBAL = 1, SINK_INDEX = 2, SINK_ADJOINT = 3 };
 
-// Per-lane score state of the adjoint sink (at most kAdjRingParams parameters): the
-// score of the segment in force is A + b_obs * j; sa and saj sum the adjoint weights and
-// j * weights of its observations since A last changed; g accumulates in FP64.
+// Per-lane score state of the adjoint sink (at most kAdjRingParams parameters).  The
+// score of the segment in force is A + b_obs * j: sa sums the adjoint weights of the
+// segment's observations, saj the weights times j over the whole particle, and G the
+// products A * sa of the particle's finished segments, all in the transport's precision;
+// at the particle's end g += G + b_obs * saj in FP64.  FP64 instructions are slow on this
+// part, so none runs per observation or per scattering in the FP32 replay.
 constexpr int kAdjRingParams = 4;
 template <typename R> struct AdjLane {
     const AdjointArgs *a; // read in the rare paths (a new scattering, the particle's end)
     const R *wts;         // adjoint weights, read per observation
-    R A[kAdjRingParams];
+    const R *dls;         // d log sigma tables in the transport's precision
+    R A[kAdjRingParams], G[kAdjRingParams];
     R sa, saj;
     double g[kAdjRingParams];
-    __device__ __forceinline__ void flush()
+    __device__ __forceinline__ void start()
     {
 #pragma unroll
-        for (int q = 0; q < kAdjRingParams; ++q)
-            if (q < a->n_params) g[q] = fma((double)A[q], (double)sa, fma(a->b_obs[q], (double)saj, g[q]));
+        for (int q = 0; q < kAdjRingParams; ++q) { A[q] = (R)0; G[q] = (R)0; }
         sa = saj = (R)0;
     }
     // a new segment is in force; a scattering at theta / pi = th >= 0 started it
     __device__ __forceinline__ void enter(R th)
     {
         if (!(th >= (R)0)) return;
-        flush();
+        const int np = a->n_params, nt = a->n_theta;
         R f = th > (R)1 ? (R)1 : th;
-        f *= (R)(a->n_theta - 1);
+        f *= (R)(nt - 1);
         int k = (int)f;
-        k = k > a->n_theta - 2 ? a->n_theta - 2 : k;
-        const double w = (double)(f - (R)k);
+        k = k > nt - 2 ? nt - 2 : k;
+        const R w = f - (R)k;
 #pragma unroll
         for (int q = 0; q < kAdjRingParams; ++q) {
-            if (q < a->n_params) {
-                const double *t = a->dlogsigma + (size_t)q * a->n_theta + k;
-                A[q] += (R)(fma(w, __ldg(t + 1) - __ldg(t), __ldg(t)) + a->a_inc[q]);
+            if (q < np) {
+                G[q] += A[q] * sa;
+                const R *t = dls + (size_t)q * nt + k;
+                const R t0 = __ldg(t), t1 = __ldg(t + 1);
+                A[q] += t0 + w * (t1 - t0) + (sizeof(R) == 4 ? (R)a->a_inc_f[q] : (R)a->a_inc[q]);
             }
         }
+        sa = (R)0;
     }
     __device__ __forceinline__ void observe(int64_t idx, int j)
     {
         const R w = __ldg(wts + idx);
         sa += w;
         saj += w * (R)j;
+    }
+    // the particle's end
+    __device__ __forceinline__ void finish()
+    {
+#pragma unroll
+        for (int q = 0; q < kAdjRingParams; ++q)
+            if (q < a->n_params) g[q] += (double)(G[q] + A[q] * sa) + a->b_obs[q] * (double)saj;
     }
 };
 
@@ -870,7 +883,7 @@ template <typename R> struct AdjLane {
 #define RTMC_TRANSPORT_THREADS 256
 #endif
 #ifndef RTMC_TRANSPORT_MIN_BLOCKS
-#define RTMC_TRANSPORT_MIN_BLOCKS 3 // FP32: 3 x 256 threads per SM measured fastest (85 registers)
+#define RTMC_TRANSPORT_MIN_BLOCKS 3 // FP32: 3 x 256 threads per SM measured fastest
 #endif
 template <typename R, int SINK> struct Bounds {
     static constexpr int threads = SINK == SINK_SMEM ? 512 : RTMC_TRANSPORT_THREADS;
@@ -910,11 +923,7 @@ __device__ __forceinline__ void run_batch(const DevParams<R> &p, const R *sedges
     }
     seg_from(s, cur);
     seg_prepare<R, OBS>(p, sedges, cur);
-    if (ADJ) {
-#pragma unroll
-        for (int q = 0; q < kAdjRingParams; ++q) adj->A[q] = (R)0;
-        adj->sa = adj->saj = (R)0;
-    }
+    if (ADJ) adj->start();
     int32_t *optr = (SINK == SINK_INDEX && have) ? p.obs_idx + i : nullptr;
     int jn = 1; // warp-uniform
     while (jn <= p.n_obs) {
@@ -1031,7 +1040,7 @@ __device__ __forceinline__ void run_batch(const DevParams<R> &p, const R *sedges
             emit(v, cur.mode, jn);
         }
     }
-    if (ADJ) adj->flush();
+    if (ADJ) adj->finish();
     if (have && p.trace) { // final state of the particle, the oracle's layout
         double *f = p.trace + 16 * i;
 #pragma unroll
@@ -1446,6 +1455,7 @@ __global__ void __launch_bounds__(kAdjointThreads, sizeof(R) == 4 ? 2 : 1) rt_ad
     AdjLane<R> adj;
     adj.a = &a;
     adj.wts = static_cast<const R *>(a.adjoint);
+    if constexpr (sizeof(R) == 4) adj.dls = a.dlogsigma_f; else adj.dls = reinterpret_cast<const R *>(a.dlogsigma);
 #pragma unroll
     for (int q = 0; q < kAdjRingParams; ++q) adj.g[q] = 0.0;
     const int64_t warps = ((int64_t)gridDim.x * T) >> 5;
