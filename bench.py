@@ -206,6 +206,8 @@ def run_our_arm(args, rank, world, dist):
         ctx.set_launch(args.block, args.ring, args.index_mb)
     if args.chunks or args.k1_bps:
         ctx.set_pipeline(args.chunks, args.k1_bps)
+    if args.schedule >= 0:
+        ctx.set_schedule(args.schedule)
     P32, keep32 = prob.to_ctypes()
 
     def barrier():
@@ -396,6 +398,8 @@ def run_c3(args):
     ctx = get_context(0)
     if args.block or args.ring or args.index_mb:
         ctx.set_launch(args.block, args.ring, args.index_mb)
+    if args.schedule >= 0:
+        ctx.set_schedule(args.schedule)
     P32, k32 = prob.to_ctypes()
     for _ in range(args.warmup):
         ctx.forward_device(P32, prob.tables)
@@ -508,6 +512,7 @@ def main():
     ap.add_argument("--ring", type=int, default=0, help="segments per lane (0: automatic)")
     ap.add_argument("--index-mb", type=int, default=0, help="index-array budget in MB (0: automatic, -1: global atomics)")
     ap.add_argument("--chunks", type=int, default=0, help="transport/fold pipeline chunks (0: automatic, 1: off)")
+    ap.add_argument("--schedule", type=int, default=-1, help="-1 automatic, 0 lockstep warp batches, 1 particle per thread")
     ap.add_argument("--k1-bps", type=int, default=0, help="transport blocks per SM while pipelined (0: automatic)")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")

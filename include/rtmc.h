@@ -329,6 +329,14 @@ int rtmc_set_launch(rtmc_context *ctx, int32_t block, int32_t ring_cap, int32_t 
  * chunks = 1: off. */
 int rtmc_set_pipeline(rtmc_context *ctx, int32_t chunks, int32_t transport_blocks_per_sm);
 
+/* Transport schedule: 0 = warps walk 32 particles' observation instants in lockstep
+ * (events run ahead into a shared-memory ring; best when observations outnumber events);
+ * 1 = one particle per thread, each event followed by its segment's observations (best
+ * for event-heavy problems); -1 = automatic (1 when 8 x expected events per particle >=
+ * observation instants, and the histogram does not go through the index array).  Both
+ * give the same histogram. */
+int rtmc_set_schedule(rtmc_context *ctx, int32_t event_major);
+
 /* enable (1, default) or disable (0) reuse of the device copy of a tables handle across
  * calls; with 0 every call uploads its tables again (end-to-end timing) */
 int rtmc_set_table_cache(rtmc_context *ctx, int32_t enable);

@@ -59,6 +59,7 @@ struct rtmc_context {
     // transport / fold pipeline over particle chunks (index sink): a second stream and
     // per-chunk events, created on first use
     int opt_chunks = 0, opt_k1_bps = 0;
+    int opt_event_major = -1; // -1 automatic, 0 two-cursor batches, 1 one particle per thread
     static constexpr int kPipe = 32;
     cudaStream_t fold_stream = nullptr;
     cudaEvent_t ev_a0[kPipe] = {}, ev_a1[kPipe] = {}, ev_b0[kPipe] = {}, ev_b1[kPipe] = {};
@@ -312,6 +313,15 @@ void fill_params(rtmc_context *ctx, const rtmc_problem *P, const DevTables<R> &t
                        (P->axis_edges[0][P->axis_nedges[0] - 1] - P->axis_edges[0][0]));
     }
     p->time_stride = P->time_stride; p->mode_stride = P->mode_stride; p->hist_len = P->hist_len;
+    // schedule: events per particle against observations (event-heavy problems run one
+    // particle per thread; C3: ~76 events and 400 instants, C2: ~4 events and 250)
+    {
+        double rate = 0;
+        for (int m = 0; m < (P->acoustics ? 1 : 2); ++m)
+            if (std::isfinite(P->mft[m])) rate = std::max(rate, 1.0 / P->mft[m]);
+        const double events = rate * P->h * (double)P->n_sub * (double)P->n_obs;
+        p->event_major = (ctx && ctx->opt_event_major >= 0) ? ctx->opt_event_major : (events * 8.0 >= (double)P->n_obs ? 1 : 0);
+    }
     *n_edges_out = (int)edges->size();
     p->n_edges = *n_edges_out;
     for (int b = 0; b < P->n_bnd; ++b) {
@@ -471,6 +481,8 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         return fail(&ctx->err, RTMC_ERR_CUDA, "transport kernel does not fit on the device");
     p.sink = sink;
     p.ring_cap = cap;
+    // the index array wants each warp's 32 rows written together: keep the batches
+    if (sink == kSinkIndex && ctx->opt_event_major < 0) p.event_major = 0;
     // pipelined transport keeps room on every SM for the fold's blocks
     if (n_pipe) bps = std::min(bps, ctx->opt_k1_bps ? ctx->opt_k1_bps : 2);
     int64_t grid = (int64_t)ctx->num_sms * bps;
@@ -879,6 +891,7 @@ int forward_noalloc(const rtmc_problem *P, const rtmc_tables *t, int64_t *d_hist
         return fail(nullptr, RTMC_ERR_ARG, "rtmc_forward_noalloc: a radial source profile holds at most " +
                                                std::to_string((kMaxEdges - 2 * RTMC_ZOE_N) / 2) + " knots here");
     fill_params<R>(&slot, P, dt, &p, &n_edges, &edges, &zoe);
+    p.event_major = 0; // index path: each warp writes its 32 rows together
     const size_t e_off = align_up(used, 256);
     const size_t z_off = align_up(e_off + std::max<size_t>(1, edges.size()) * sizeof(R), 256);
     const size_t c_off = align_up(z_off + zoe.size() * sizeof(R), 256);
@@ -1144,6 +1157,14 @@ extern "C" int rtmc_set_pipeline(rtmc_context *ctx, int32_t chunks, int32_t tran
         return fail(&ctx->err, RTMC_ERR_ARG, "transport_blocks_per_sm must be in [0, 16]");
     ctx->opt_chunks = chunks;
     ctx->opt_k1_bps = transport_blocks_per_sm;
+    return RTMC_OK;
+}
+
+extern "C" int rtmc_set_schedule(rtmc_context *ctx, int32_t event_major)
+{
+    if (!ctx) return fail(nullptr, RTMC_ERR_ARG, "rtmc_set_schedule: NULL context");
+    if (event_major < -1 || event_major > 1) return fail(&ctx->err, RTMC_ERR_ARG, "event_major must be -1, 0 or 1");
+    ctx->opt_event_major = event_major;
     return RTMC_OK;
 }
 

@@ -67,6 +67,7 @@ template <typename R> struct DevParams {
     int32_t polarization, n_sub, n_obs, n_bnd;
     int32_t hist_shift, sink, s_end, max_events;
     int32_t ring_cap;  // trajectory segments per lane in the shared-memory ring
+    int32_t event_major; // 1: one particle per thread, events and their observations in turn
     int32_t obs_kind;  // 0 general, 1 cartesian linear, 2 radius only
     int32_t radial_3d; // radius-only path: 1 = |x|, 0 = |(x, y)|
     int32_t ax_nbe[4]; // bins of a binned axis, 1 for a range-checked or ignored axis

@@ -1050,6 +1050,60 @@ __device__ __forceinline__ void run_batch(const DevParams<R> &p, const R *sedges
     }
 }
 
+// Event-major schedule for event-heavy problems: one particle per thread, each event
+// followed by the observations of the segment it ends.  A warp then runs as many
+// iterations as its busiest lane has events (tens to hundreds, close to the mean), where
+// the two-cursor batch would refill its rings a few lanes at a time.  Same events, same
+// bins, same order of kill / boundary / scattering as run_batch.
+template <typename R, int SINK, int OBS>
+__device__ __forceinline__ void run_particle(const DevParams<R> &p, const R *sedges, unsigned *shist, int64_t i,
+                                             Counters &cnt, bool &bad)
+{
+    const unsigned long long inc = 1ull << p.hist_shift;
+    const uint64_t pid = (uint64_t)(p.pid0 + i);
+    Part<R> s;
+    init_particle(p, pid, s);
+    int32_t *optr = SINK == SINK_INDEX ? p.obs_idx + i + p.obs_rows : nullptr; // row of instant 1
+    const unsigned scat0 = cnt.scat, bnd0 = cnt.bnd;
+    int j = 1;
+    for (;;) {
+        const int e = next_event(s);
+        const int lim = s.alive ? (e <= p.s_end ? e : p.s_end + 1) : s.s_death;
+        Seg<R> g;
+        seg_from(s, g);
+        seg_prepare<R, OBS>(p, sedges, g);
+        for (; j <= p.n_obs && j * p.n_sub < lim; ++j) { // observations strictly before the event
+            const int v = obs_offset<R, OBS>(p, sedges, g, j * p.n_sub);
+            if (SINK == SINK_INDEX) {
+                *optr = v < 0 ? -1 : (v | (g.mode << 30));
+                optr += p.obs_rows;
+                if (v >= 0) cnt.obs++;
+            } else if (v >= 0) {
+                const int64_t idx = (int64_t)j * p.time_stride + (g.mode ? p.mode_stride : 0) + v;
+                if (idx < p.hist_len) {
+                    cnt.obs++;
+                    if (SINK == SINK_SMEM) atomicAdd(shist + idx, 1u);
+                    else atomicAdd(p.hist + idx, inc);
+                } else {
+                    bad = true;
+                }
+            }
+        }
+        if (j > p.n_obs || !s.alive || e > p.s_end) break;
+        process_event(p, pid, s, cnt);
+        if ((int)s.k > p.max_events) { s.alive = 0; s.s_death = s.s0; bad = true; }
+    }
+    if (SINK == SINK_INDEX)
+        for (; j <= p.n_obs; ++j, optr += p.obs_rows) *optr = -1; // after death
+    if (p.trace) { // final state of the particle, the oracle's layout
+        double *f = p.trace + 16 * i;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) { f[c] = s.x[c]; f[3 + c] = s.d[c]; f[6 + c] = s.q[c]; }
+        f[9] = s.mode; f[10] = s.alive; f[11] = cnt.scat - scat0; f[12] = cnt.bnd - bnd0;
+        f[13] = s.s0; f[14] = s.s_death; f[15] = s.k;
+    }
+}
+
 // The transport kernel.  A warp takes 32 consecutive particles at a time and walks the
 // observation instants in lockstep.  Each lane keeps two cursors on its particle's
 // trajectory: the event state s (phase 1, runs ahead and pushes one segment per event
@@ -1089,8 +1143,12 @@ __global__ void __launch_bounds__(Bounds<R, SINK>::threads, Bounds<R, SINK>::min
     bool bad = false;
     const int64_t warps = ((int64_t)gridDim.x * T) >> 5;
 
-    for (int64_t base = (((int64_t)blockIdx.x * T + threadIdx.x) >> 5) << 5; base < p.n_particles; base += warps * 32) {
-        run_batch<R, SINK, OBS>(p, sedges, shist, ring, base, p.n_particles, cnt, bad);
+    if (p.event_major) {
+        for (int64_t i = (int64_t)blockIdx.x * T + threadIdx.x; i < p.n_particles; i += (int64_t)gridDim.x * T)
+            run_particle<R, SINK, OBS>(p, sedges, shist, i, cnt, bad);
+    } else {
+        for (int64_t base = (((int64_t)blockIdx.x * T + threadIdx.x) >> 5) << 5; base < p.n_particles; base += warps * 32)
+            run_batch<R, SINK, OBS>(p, sedges, shist, ring, base, p.n_particles, cnt, bad);
     }
 
     // counters: warp reduction, one global atomic per warp
@@ -1170,8 +1228,13 @@ __global__ void __launch_bounds__(512, 1) rt_transport_batch(const BatchArgs<R> 
             __syncthreads();
         }
         const int64_t end = bi.first + bi.count;
-        for (int64_t base = bi.first + 32 * warp; base < end; base += 32 * nwarps)
-            run_batch<R, SINK_SMEM, OBS>(sp, sedges, shist, ring, base, end, cnt, bad);
+        if (sp.event_major) {
+            for (int64_t i = bi.first + threadIdx.x; i < end; i += T)
+                run_particle<R, SINK_SMEM, OBS>(sp, sedges, shist, i, cnt, bad);
+        } else {
+            for (int64_t base = bi.first + 32 * warp; base < end; base += 32 * nwarps)
+                run_batch<R, SINK_SMEM, OBS>(sp, sedges, shist, ring, base, end, cnt, bad);
+        }
     }
     if (cur >= 0) flush(cur);
     const unsigned full = 0xffffffffu;

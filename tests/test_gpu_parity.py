@@ -351,3 +351,35 @@ def test_gradient_against_central_differences():
     assert abs(res["grad"]["Q"] - fd["Q"]) <= 1e-5 * abs(fd["Q"])
     for p in ("cv_kappa", "cv_rho", "mfp"):
         assert abs(res["grad"][p] - fd[p]) <= 0.02 * abs(fd[p]), (p, res["grad"][p], fd[p])
+
+
+@pytest.mark.parametrize("name", ["c1", "c3", "c2_index", "cylinder_elastic", "plane_circle"])
+@pytest.mark.parametrize("precision", ["fp64", "fp32"])
+def test_schedules_give_identical_results(name, precision):
+    """Lockstep warp batches and one particle per thread run the same events and bins."""
+    if name == "c1":
+        geo, src, mat, obs, opts = W.c1_acoustic3d()
+    elif name == "c3":
+        geo, src, mat, obs, opts = W.c3_halfspace2d(t_end=2.0)
+    elif name == "c2_index":
+        geo, src, mat, obs, opts = W.c2_elastic3d(t_end=1.0)
+    else:
+        geo, src, mat, obs, opts = _feature_cases()[name]
+    obs = {k: v for k, v in obs.items() if v is not None}
+    prob, grid, N = build_problem(geo, dict(src, numberParticles=5000), mat, obs,
+                                  dict(opts, precision=precision, exact_count=True))
+    P, keep = prob.to_ctypes()
+    ctx = get_context(0)
+    out = []
+    try:
+        for sched in (0, 1):
+            ctx.set_schedule(sched)
+            out.append(ctx.forward_trace(P, prob.tables))
+    finally:
+        ctx.set_schedule(-1)
+    (h0, s0, st0), (h1, s1, st1) = out
+    assert st0["device_status"] == 0 and st1["device_status"] == 0 and st0["sink"] == st1["sink"]
+    assert np.array_equal(h0, h1)
+    assert np.array_equal(s0, s1)
+    for k in ("scatter_events", "boundary_hits", "kills", "absorbed", "observations", "conversions"):
+        assert st0[k] == st1[k], k
