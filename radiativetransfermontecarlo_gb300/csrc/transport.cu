@@ -1063,7 +1063,7 @@ __device__ __forceinline__ void run_particle(const DevParams<R> &p, const R *sed
     const uint64_t pid = (uint64_t)(p.pid0 + i);
     Part<R> s;
     init_particle(p, pid, s);
-    int32_t *optr = SINK == SINK_INDEX ? p.obs_idx + i + p.obs_rows : nullptr; // row of instant 1
+    int32_t *optr = SINK == SINK_INDEX ? p.obs_idx + i : nullptr; // row j - 1 holds instant j
     const unsigned scat0 = cnt.scat, bnd0 = cnt.bnd;
     int j = 1;
     for (;;) {
