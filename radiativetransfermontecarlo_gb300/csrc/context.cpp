@@ -1200,15 +1200,18 @@ struct rtmc_batch {
     rtmc_context *ctx = nullptr;
     int n = 0, prec = RTMC_FP32, obs_kind = 0, n_obs = 0;
     int block = 0, ring = 0, grid = 0, n_items = 0;
+    int grid_em = 0, n_items_em = 0; // event-heavy instances, one particle per thread
     int64_t chunk = 0, hist_len = 0;
-    size_t smem = 0;
-    DevBuf params, items, tabs, edges, hists, ctl;
+    size_t smem = 0, smem_em = 0;
+    DevBuf params, items, items_em, tabs, edges, hists, ctl;
     std::vector<int64_t> n_part;
     std::vector<double> cost_per_particle;
+    std::vector<int> event_major;
     int n_edges = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    void *args_host = nullptr; // BatchArgs<R>, kept alive for the graph's kernel node
+    void *args_host = nullptr;    // BatchArgs<R>, kept alive for the graph's kernel nodes
+    void *args_em_host = nullptr; // the same for the event-major kernel
 };
 
 namespace {
@@ -1252,26 +1255,45 @@ template <typename R> int batch_build_graph(rtmc_batch *b)
     b->grid = ctx->num_sms * bps;
     // work items: chunks of each instance, largest expected cost first
     const int64_t chunk = b->chunk ? b->chunk : 8192;
-    std::vector<BatchItem> items;
-    std::vector<double> cost;
-    for (int i = 0; i < b->n; ++i)
-        for (int64_t f = 0; f < b->n_part[i]; f += chunk) {
-            BatchItem it{};
-            it.inst = i;
-            it.first = f;
-            it.count = std::min<int64_t>(chunk, b->n_part[i] - f);
-            items.push_back(it);
-            cost.push_back(b->cost_per_particle[i] * (double)it.count);
+    // two work lists: lockstep-batch instances (shared-memory histogram kernel) and
+    // event-heavy instances (event-major kernel), each sorted by expected cost
+    std::vector<BatchItem> sorted, sorted_em;
+    for (int em = 0; em < 2; ++em) {
+        std::vector<BatchItem> items;
+        std::vector<double> cost;
+        for (int i = 0; i < b->n; ++i) {
+            if (b->event_major[i] != em) continue;
+            for (int64_t f = 0; f < b->n_part[i]; f += chunk) {
+                BatchItem it{};
+                it.inst = i;
+                it.first = f;
+                it.count = std::min<int64_t>(chunk, b->n_part[i] - f);
+                items.push_back(it);
+                cost.push_back(b->cost_per_particle[i] * (double)it.count);
+            }
         }
-    std::vector<size_t> order(items.size());
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return cost[x] > cost[y]; });
-    std::vector<BatchItem> sorted(items.size());
-    for (size_t k = 0; k < order.size(); ++k) sorted[k] = items[order[k]];
+        std::vector<size_t> order(items.size());
+        std::iota(order.begin(), order.end(), 0);
+        std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return cost[x] > cost[y]; });
+        std::vector<BatchItem> &dst = em ? sorted_em : sorted;
+        dst.resize(items.size());
+        for (size_t k = 0; k < order.size(); ++k) dst[k] = items[order[k]];
+    }
     b->n_items = (int)sorted.size();
-    if (b->items.grow(std::max<size_t>(1, sorted.size()) * sizeof(BatchItem)))
+    b->n_items_em = (int)sorted_em.size();
+    if (b->items.grow(std::max<size_t>(1, sorted.size()) * sizeof(BatchItem)) ||
+        b->items_em.grow(std::max<size_t>(1, sorted_em.size()) * sizeof(BatchItem)))
         return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for the work list failed");
-    CK(cudaMemcpy(b->items.p, sorted.data(), sorted.size() * sizeof(BatchItem), cudaMemcpyHostToDevice), "work list");
+    if (!sorted.empty())
+        CK(cudaMemcpy(b->items.p, sorted.data(), sorted.size() * sizeof(BatchItem), cudaMemcpyHostToDevice), "work list");
+    if (!sorted_em.empty())
+        CK(cudaMemcpy(b->items_em.p, sorted_em.data(), sorted_em.size() * sizeof(BatchItem), cudaMemcpyHostToDevice),
+           "work list");
+    b->smem_em = align_up((size_t)b->n_edges * sizeof(R), 16);
+    int bps_em = 0;
+    if (transport_batch_em_setup(b->prec, b->obs_kind, 256, b->smem_em, &bps_em) != 0 || bps_em < 1)
+        return fail(&ctx->err, RTMC_ERR_CUDA, "batched event-major kernel does not fit on the device");
+    b->grid_em = ctx->num_sms * bps_em;
     // capture: clear histograms and counters, persistent launch
     auto *a = static_cast<BatchArgs<R> *>(b->args_host);
     a->params = static_cast<const DevParams<R> *>(b->params.p);
@@ -1286,12 +1308,23 @@ template <typename R> int batch_build_graph(rtmc_batch *b)
     a->edges = static_cast<const R *>(b->edges.p);
     a->n_edges = b->n_edges;
     a->obs_kind = b->obs_kind;
+    auto *ae = static_cast<BatchArgs<R> *>(b->args_em_host);
+    *ae = *a;
+    ae->items = static_cast<const BatchItem *>(b->items_em.p);
+    ae->n_items = b->n_items_em;
+    ae->counter = static_cast<int32_t *>(b->ctl.p) + 2;
     CK(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal), "graph capture");
     cudaMemsetAsync(b->hists.p, 0, (size_t)b->n * b->hist_len * sizeof(int64_t), ctx->stream);
     cudaMemsetAsync(b->ctl.p, 0, 256, ctx->stream);
-    int le;
-    if constexpr (sizeof(R) == 4) le = launch_transport_batch_f32(*a, b->grid, block, b->smem, ctx->stream);
-    else le = launch_transport_batch_f64(*a, b->grid, block, b->smem, ctx->stream);
+    int le = 0;
+    if (b->n_items) {
+        if constexpr (sizeof(R) == 4) le = launch_transport_batch_f32(*a, b->grid, block, b->smem, ctx->stream);
+        else le = launch_transport_batch_f64(*a, b->grid, block, b->smem, ctx->stream);
+    }
+    if (!le && b->n_items_em) {
+        if constexpr (sizeof(R) == 4) le = launch_transport_batch_em_f32(*ae, b->grid_em, 256, b->smem_em, ctx->stream);
+        else le = launch_transport_batch_em_f64(*ae, b->grid_em, 256, b->smem_em, ctx->stream);
+    }
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &b->graph);
     if (le) return cuda_fail(ctx, (cudaError_t)le, "batched launch capture");
     if (e != cudaSuccess) return cuda_fail(ctx, e, "graph capture");
@@ -1324,6 +1357,7 @@ int batch_create(rtmc_context *ctx, int n, const rtmc_problem *P, const rtmc_tab
     unsigned char *dev = static_cast<unsigned char *>(b->tabs.p);
     b->n_part.resize(n);
     b->cost_per_particle.resize(n);
+    b->event_major.assign(n, 0);
     for (int i = 0; i < n; ++i) {
         DevTables<R> dt{};
         size_t o = toff[i];
@@ -1344,6 +1378,7 @@ int batch_create(rtmc_context *ctx, int n, const rtmc_problem *P, const rtmc_tab
             if (std::isfinite(P[i].mft[m])) rate = std::max(rate, 1.0 / P[i].mft[m]);
         b->cost_per_particle[i] = P[i].n_obs + 4.0 * rate * P[i].h * P[i].n_sub * P[i].n_obs;
         if (i == 0) b->obs_kind = params[0].obs_kind;
+        b->event_major[i] = params[i].event_major;
     }
     CK(cudaMemcpy(b->tabs.p, host.data(), total, cudaMemcpyHostToDevice), "batched tables");
     if (b->edges.grow(std::max<size_t>(1, edges.size()) * sizeof(R)) || b->params.grow((size_t)n * sizeof(DevParams<R>)) ||
@@ -1355,6 +1390,7 @@ int batch_create(rtmc_context *ctx, int n, const rtmc_problem *P, const rtmc_tab
     CK(cudaMemcpy(b->params.p, params.data(), (size_t)n * sizeof(DevParams<R>), cudaMemcpyHostToDevice), "params");
     b->n_edges = n_edges;
     b->args_host = new BatchArgs<R>();
+    b->args_em_host = new BatchArgs<R>();
     return batch_build_graph<R>(b);
 }
 
@@ -1453,13 +1489,15 @@ extern "C" void rtmc_batch_destroy(rtmc_batch *b)
     if (b->graph) cudaGraphDestroy(b->graph);
     b->params.release();
     b->items.release();
+    b->items_em.release();
     b->tabs.release();
     b->edges.release();
     b->hists.release();
     b->ctl.release();
-    if (b->args_host) {
-        if (b->prec == RTMC_FP64) delete static_cast<BatchArgs<double> *>(b->args_host);
-        else delete static_cast<BatchArgs<float> *>(b->args_host);
+    for (void *h : {b->args_host, b->args_em_host}) {
+        if (!h) continue;
+        if (b->prec == RTMC_FP64) delete static_cast<BatchArgs<double> *>(h);
+        else delete static_cast<BatchArgs<float> *>(h);
     }
     delete b;
 }

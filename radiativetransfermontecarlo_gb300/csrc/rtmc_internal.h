@@ -171,6 +171,9 @@ int launch_bin_slices(const BinParams &b, int grid_x, size_t smem, void *stream)
 int launch_transport_batch_f32(const BatchArgs<float> &a, int grid, int block, size_t smem, void *stream);
 int launch_transport_batch_f64(const BatchArgs<double> &a, int grid, int block, size_t smem, void *stream);
 int transport_batch_setup(int precision, int obs, int block, size_t smem, int *blocks_per_sm);
+int launch_transport_batch_em_f32(const BatchArgs<float> &a, int grid, int block, size_t smem, void *stream);
+int launch_transport_batch_em_f64(const BatchArgs<double> &a, int grid, int block, size_t smem, void *stream);
+int transport_batch_em_setup(int precision, int obs, int block, size_t smem, int *blocks_per_sm);
 int bin_slices_set_smem(size_t smem);
 // device address of the static scratch of rtmc_forward_noalloc (noalloc.cu); device current
 int static_scratch(int device, unsigned char **ptr, size_t *bytes);

@@ -1247,6 +1247,52 @@ __global__ void __launch_bounds__(512, 1) rt_transport_batch(const BatchArgs<R> 
     if (bad) atomicExch(a.status, 1);
 }
 
+// Batched transport of the event-heavy instances: the same work-item loop, one particle
+// per thread (event-major), observations as 64-bit atomics into the instance's histogram
+// (no shared-memory copy, so three blocks fit on an SM instead of one).
+template <typename R, int OBS>
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2) rt_transport_batch_em(const BatchArgs<R> a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ DevParams<R> sp;
+    __shared__ int s_item;
+    R *sedges = reinterpret_cast<R *>(smem_raw);
+    const int T = blockDim.x;
+    for (int k = threadIdx.x; k < a.n_edges; k += T) sedges[k] = a.edges[k];
+    const int lane = threadIdx.x & 31;
+    Counters cnt = {0u, 0u, 0u, 0u, 0u, 0u};
+    bool bad = false;
+    int cur = -1;
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_item = atomicAdd(a.counter, 1);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= a.n_items) break;
+        const BatchItem bi = a.items[it];
+        if (bi.inst != cur) {
+            const uint32_t *src = reinterpret_cast<const uint32_t *>(a.params + bi.inst);
+            uint32_t *dst = reinterpret_cast<uint32_t *>(&sp);
+            for (int k = threadIdx.x; k < (int)(sizeof(DevParams<R>) / 4); k += T) dst[k] = src[k];
+            __syncthreads();
+            if (threadIdx.x == 0) sp.hist = a.hists + (int64_t)bi.inst * a.hist_len;
+            cur = bi.inst;
+            __syncthreads();
+        }
+        const int64_t end = bi.first + bi.count;
+        for (int64_t i = bi.first + threadIdx.x; i < end; i += T)
+            run_particle<R, SINK_GLOBAL, OBS>(sp, sedges, nullptr, i, cnt, bad);
+    }
+    const unsigned full = 0xffffffffu;
+    unsigned v[6] = {cnt.scat, cnt.bnd, cnt.kill, cnt.absorb, cnt.obs, cnt.conv};
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        const unsigned t = __reduce_add_sync(full, v[c]);
+        if (lane == 0 && t) atomicAdd(a.stats + c, (unsigned long long)t);
+    }
+    if (bad) atomicExch(a.status, 1);
+}
+
 // Fold the dense index array into the histogram, one time slice at a time: blockIdx.y
 // is the slice (so the L2 holds the slice being written), blockIdx.x a contiguous chunk
 // of the slice's entries.  While particles crowd a few bins (early times) many entries
@@ -1600,6 +1646,13 @@ int launch_bin_slices(const BinParams &b, int grid_x, size_t smem, void *stream)
     return (int)cudaGetLastError();
 }
 
+template <typename R> void *pick_batch_em(int obs)
+{
+    return obs == OBS_CART ? (void *)rt_transport_batch_em<R, OBS_CART>
+                           : (obs == OBS_RADIAL ? (void *)rt_transport_batch_em<R, OBS_RADIAL>
+                                                : (void *)rt_transport_batch_em<R, OBS_GENERAL>);
+}
+
 template <typename R> void *pick_batch(int obs)
 {
     return obs == OBS_CART ? (void *)rt_transport_batch<R, OBS_CART>
@@ -1620,6 +1673,30 @@ int launch_transport_batch_f32(const BatchArgs<float> &a, int grid, int block, s
 int launch_transport_batch_f64(const BatchArgs<double> &a, int grid, int block, size_t smem, void *stream)
 {
     return launch_batch(a, grid, block, smem, stream);
+}
+
+template <typename R> static int launch_batch_em(const BatchArgs<R> &a, int grid, int block, size_t smem, void *stream)
+{
+    void *args[] = {(void *)&a};
+    return (int)cudaLaunchKernel(pick_batch_em<R>(a.obs_kind), dim3(grid), dim3(block), args, smem, (cudaStream_t)stream);
+}
+
+int launch_transport_batch_em_f32(const BatchArgs<float> &a, int grid, int block, size_t smem, void *stream)
+{
+    return launch_batch_em(a, grid, block, smem, stream);
+}
+
+int launch_transport_batch_em_f64(const BatchArgs<double> &a, int grid, int block, size_t smem, void *stream)
+{
+    return launch_batch_em(a, grid, block, smem, stream);
+}
+
+int transport_batch_em_setup(int precision, int obs, int block, size_t smem, int *blocks_per_sm)
+{
+    void *fn = precision == RTMC_FP64 ? pick_batch_em<double>(obs) : pick_batch_em<float>(obs);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, block, smem);
+    return (int)e;
 }
 
 int transport_batch_setup(int precision, int obs, int block, size_t smem, int *blocks_per_sm)
