@@ -144,9 +144,22 @@ template <typename R> int upload_tables(rtmc_context *ctx, const rtmc_tables *t,
         total += table_bytes<R>(t->cdf[i].size());
     }
     if (ctx->tabs.grow(total)) return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for tables failed");
-    std::vector<unsigned char> host(total, 0);
     unsigned char *base = static_cast<unsigned char *>(ctx->tabs.p);
-    for (int i = 0; i < t->n_tables; ++i) stage_table<R>(t->cdf[i], t->theta[i], host.data() + off[i], base + off[i], dt, i);
+    std::lock_guard<std::mutex> lock(t->image_mu);
+    std::vector<unsigned char> &host = t->image[sizeof(R) == 4 ? 0 : 1];
+    const bool have = host.size() == total;
+    if (!have) host.assign(total, 0);
+    for (int i = 0; i < t->n_tables; ++i) {
+        if (!have) {
+            stage_table<R>(t->cdf[i], t->theta[i], host.data() + off[i], base + off[i], dt, i);
+        } else {
+            const size_t n = t->cdf[i].size();
+            dt->knot[i] = reinterpret_cast<const Knot<R> *>(base + off[i]);
+            dt->guide[i] = reinterpret_cast<const int32_t *>(base + off[i] + align_up(n * sizeof(Knot<R>), 256));
+            dt->n[i] = (int32_t)n;
+            dt->gbits[i] = guide_bits(n);
+        }
+    }
     for (int i = t->n_tables; i < 4; ++i) {
         dt->knot[i] = nullptr;
         dt->guide[i] = nullptr;
@@ -351,6 +364,8 @@ void fill_params(rtmc_context *ctx, const rtmc_problem *P, const DevTables<R> &t
     (void)ctx;
 }
 
+constexpr int kCopyGroups = 5; // slice groups of the last fold, each copied as soon as it is final
+
 int ensure_pipeline(rtmc_context *ctx)
 {
     cudaError_t e = cudaSuccess;
@@ -504,6 +519,8 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         bp.mode_stride = P->mode_stride;
         bp.hist_shift = P->hist_shift;
         bp.hist = static_cast<unsigned long long *>(ctx->hist.p);
+        bp.j_first = 1;
+        bp.j_count = P->n_obs;
         const size_t slice_bytes = (size_t)P->time_stride * nm * sizeof(uint32_t);
         const int group = (int)std::min<size_t>((size_t)P->n_obs, (size_t)(200 << 10) / std::max<size_t>(slice_bytes, 1));
         if (group >= 8) {
@@ -568,6 +585,7 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
             cudaStreamSynchronize(ctx->fold_stream);
         }
     }
+    bool copied = false; // the histogram reached host_out during the last fold
     for (int64_t base = 0; !n_pipe && base < P->n_particles && !le; base += chunk) {
         DevParams<R> q = p;
         q.pid0 = P->pid0 + base;
@@ -578,13 +596,43 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         else le = launch_transport_f64(q, (int)grid, block, smem, ctx->stream);
         CK(cudaEventRecord(ctx->ev_k1, ctx->stream), "event");
         ++launches;
+        const bool last = base + chunk >= P->n_particles;
         if (!le && sink == kSinkIndex) {
             BinParams b = bp;
             b.n = q.n_particles;
             if (b.group) b.part_per_block = (b.n + fold_grid - 1) / fold_grid;
-            le = launch_bin_slices(b, fold_grid, fold_smem, ctx->stream);
-            CK(cudaEventRecord(ctx->ev_k2, ctx->stream), "event");
-            ++launches;
+            if (last && host_out && !b.group && P->n_obs >= 2 * kCopyGroups && ensure_pipeline(ctx) == 0) {
+                // the last fold in slice groups: each group's slices are final, so their
+                // copy to the host runs on the second stream while the next group folds
+                const int64_t ts = P->time_stride;
+                for (int g = 0; g < kCopyGroups && !le; ++g) {
+                    const int ja = 1 + (int)((int64_t)P->n_obs * g / kCopyGroups);
+                    const int jb = 1 + (int)((int64_t)P->n_obs * (g + 1) / kCopyGroups); // exclusive
+                    b.j_first = ja;
+                    b.j_count = jb - ja;
+                    le = launch_bin_slices(b, fold_grid, fold_smem, ctx->stream);
+                    if (le) break;
+                    ++launches;
+                    CK(cudaEventRecord(ctx->ev_a1[g], ctx->stream), "event");
+                    CK(cudaStreamWaitEvent(ctx->fold_stream, ctx->ev_a1[g], 0), "copy wait");
+                    const int64_t s0 = g == 0 ? 0 : (int64_t)ja * ts; // slice 0 (t = 0) goes with the first group
+                    const int64_t s1 = (int64_t)jb * ts;
+                    for (int m = 0; m < nm; ++m) {
+                        const int64_t o = m * P->mode_stride;
+                        CK(cudaMemcpyAsync(host_out + o + s0, static_cast<int64_t *>(ctx->hist.p) + o + s0,
+                                           (size_t)(s1 - s0) * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->fold_stream),
+                           "histogram copy");
+                    }
+                }
+                CK(cudaEventRecord(ctx->ev_b1[0], ctx->fold_stream), "event");
+                CK(cudaEventRecord(ctx->ev_k2, ctx->stream), "event");
+                CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_b1[0], 0), "copy join");
+                copied = true;
+            } else {
+                le = launch_bin_slices(b, fold_grid, fold_smem, ctx->stream);
+                CK(cudaEventRecord(ctx->ev_k2, ctx->stream), "event");
+                ++launches;
+            }
         }
         CK(cudaEventSynchronize(sink == kSinkIndex ? ctx->ev_k2 : ctx->ev_k1), "transport");
         float a = 0, b = 0;
@@ -599,7 +647,8 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
     int64_t dstats[32];
     CK(cudaMemcpyAsync(dstats, ctx->stats.p, 256, cudaMemcpyDeviceToHost, ctx->stream), "counters");
     if (host_out) {
-        CK(cudaMemcpyAsync(host_out, ctx->hist.p, hist_bytes, cudaMemcpyDeviceToHost, ctx->stream), "histogram copy");
+        if (!copied)
+            CK(cudaMemcpyAsync(host_out, ctx->hist.p, hist_bytes, cudaMemcpyDeviceToHost, ctx->stream), "histogram copy");
         d2h += (double)hist_bytes;
     }
     if (p.trace) {

@@ -5,6 +5,7 @@
 #include "../../include/rtmc.h"
 
 #include <atomic>
+#include <mutex>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -15,6 +16,10 @@ struct rtmc_tables {
     std::vector<double> theta[4];
     rtmc_tables_info info{};
     uint64_t gen = 0; // identity of the knot set, used to cache device uploads
+    // host images of the device layout per precision (0 FP32, 1 FP64), built on the first
+    // upload and reused: an upload is then one host-to-device copy
+    mutable std::mutex image_mu;
+    mutable std::vector<unsigned char> image[2];
 };
 
 namespace rtmc {
@@ -116,6 +121,7 @@ struct BinParams {
     int64_t time_stride, mode_stride, part_per_block;
     int32_t hist_shift;
     unsigned long long *hist;
+    int32_t j_first, j_count; // rt_bin_slices: slices j_first .. j_first + j_count - 1 (1-based)
 };
 
 // One work item of a batched run: particles [first, first + count) of instance inst.

@@ -1329,7 +1329,7 @@ __global__ void __launch_bounds__(kFoldThreads) rt_bin_slices(const BinParams b)
     __shared__ int keys[kHashSlots];
     __shared__ unsigned cnts[kHashSlots];
     __shared__ int used, valid, dense;
-    const int j = blockIdx.y + 1;
+    const int j = b.j_first + blockIdx.y;
     const int32_t *row = b.idx + (int64_t)(j - 1) * b.rows; // rows is a multiple of 32: 16-byte aligned
     unsigned long long *slice = b.hist + (int64_t)j * b.time_stride;
     const unsigned long long inc = 1ull << b.hist_shift;
@@ -1640,7 +1640,8 @@ int launch_bin_slices(const BinParams &b, int grid_x, size_t smem, void *stream)
         dim3 g(grid_x, (b.n_obs + b.group - 1) / b.group);
         rt_bin_slices_smem<<<g, 512, smem, (cudaStream_t)stream>>>(b);
     } else {
-        dim3 g(grid_x, b.n_obs);
+        if (b.j_first < 1 || b.j_count < 1 || b.j_first + b.j_count - 1 > b.n_obs) return (int)cudaErrorInvalidValue;
+        dim3 g(grid_x, b.j_count);
         rt_bin_slices<<<g, kFoldThreads, 0, (cudaStream_t)stream>>>(b);
     }
     return (int)cudaGetLastError();
