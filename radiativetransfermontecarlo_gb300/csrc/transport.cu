@@ -1452,6 +1452,7 @@ __global__ void __launch_bounds__(kAdjointThreads, sizeof(R) == 4 ? 3 : 2) rt_ad
     for (int k = threadIdx.x; k < p.n_edges; k += blockDim.x) sedges[k] = p.edges[k];
     __syncthreads();
     const R *wts = static_cast<const R *>(a.adjoint);
+    const R *dls = sizeof(R) == 4 ? reinterpret_cast<const R *>(a.dlogsigma_f) : reinterpret_cast<const R *>(a.dlogsigma);
     const int np = a.n_params;
     double g[RTMC_MAX_PARAMS];
 #pragma unroll
@@ -1464,9 +1465,12 @@ __global__ void __launch_bounds__(kAdjointThreads, sizeof(R) == 4 ? 3 : 2) rt_ad
         const uint64_t pid = (uint64_t)(p.pid0 + i);
         Part<R> s;
         init_particle(p, pid, s);
-        R A[RTMC_MAX_PARAMS]; // this particle's score, scattering part
+        // this particle's score (scattering part) and sum of A * segment weights, in the
+        // transport's precision; FP64 once per particle
+        R A[RTMC_MAX_PARAMS], G[RTMC_MAX_PARAMS];
 #pragma unroll
-        for (int q = 0; q < RTMC_MAX_PARAMS; ++q) A[q] = (R)0;
+        for (int q = 0; q < RTMC_MAX_PARAMS; ++q) { A[q] = (R)0; G[q] = (R)0; }
+        R SAJ = (R)0;
         int j = 1;
         for (;;) {
             const int e = next_event(s);
@@ -1485,10 +1489,10 @@ __global__ void __launch_bounds__(kAdjointThreads, sizeof(R) == 4 ? 3 : 2) rt_ad
                 saj += w * (R)j;
                 cnt.obs++;
             }
-            const double sad = (double)sa, sajd = (double)saj;
 #pragma unroll
             for (int q = 0; q < RTMC_MAX_PARAMS; ++q)
-                if (q < np) g[q] = fma((double)A[q], sad, fma(a.b_obs[q], sajd, g[q]));
+                if (q < np) G[q] += A[q] * sa;
+            SAJ += saj;
             if (j > p.n_obs || e > p.s_end) break;
             const int kind = process_event(p, pid, s, cnt);
             if ((int)s.k > p.max_events) { bad = true; break; }
@@ -1498,16 +1502,20 @@ __global__ void __launch_bounds__(kAdjointThreads, sizeof(R) == 4 ? 3 : 2) rt_ad
                 f *= tmax;
                 int k = (int)f;
                 k = k > a.n_theta - 2 ? a.n_theta - 2 : k;
-                const double w = (double)(f - (R)k);
+                const R w = f - (R)k;
 #pragma unroll
                 for (int q = 0; q < RTMC_MAX_PARAMS; ++q) {
                     if (q < np) {
-                        const double *t = a.dlogsigma + (size_t)q * a.n_theta + k;
-                        A[q] += (R)(fma(w, __ldg(t + 1) - __ldg(t), __ldg(t)) + a.a_inc[q]);
+                        const R *t = dls + (size_t)q * a.n_theta + k;
+                        const R t0 = __ldg(t), t1 = __ldg(t + 1);
+                        A[q] += t0 + w * (t1 - t0) + (sizeof(R) == 4 ? (R)a.a_inc_f[q] : (R)a.a_inc[q]);
                     }
                 }
             }
         }
+#pragma unroll
+        for (int q = 0; q < RTMC_MAX_PARAMS; ++q)
+            if (q < np) g[q] += (double)G[q] + a.b_obs[q] * (double)SAJ;
     }
     // block reduction in a fixed order: warp shuffles, then warp 0 over the warps
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
