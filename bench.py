@@ -7,7 +7,8 @@ int64 fixed-point histogram (2^-40).  One step = one whole simulation of that wo
 (histogram clear + particle init + transport + binning) with the tables resident.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-  python bench.py --workload c3|c4|c5   (half-space / batched sweep / gradient; one extra JSON line)
+  python bench.py --workload c1|c3|c4|c5   (3D acoustic FP64 / half-space / batched sweep / gradient;
+                                            one extra JSON line each)
 
 Prints one JSON line.  `value` is device time (CUDA events on the library's stream);
 `e2e` times rtmc_forward through the C ABI with host buffers (tables uploaded and the
@@ -379,6 +380,53 @@ def run_c4(args):
     return line
 
 
+def run_c1(args):
+    """3D acoustic isotropic unbounded, 1e6 particles, spherical 120 r x 251 t, FP64 as the
+    reference runs it (and FP32); the CPU port runs the whole workload."""
+    from oracle import oracle as O
+    from radiativetransfermontecarlo_gb300 import build_problem, get_context, normalise
+    from radiativetransfermontecarlo_gb300 import workloads as W
+    n = args.particles if args.particles != 10_000_000 else 1_000_000
+    ctx = get_context(0)
+    out = {}
+    for prec in ("fp64", "fp32"):
+        geo, src, mat, obs, opts = W.c1_acoustic3d(n=n, precision=prec)
+        prob, grid, N = build_problem(geo, src, mat, obs, dict(opts, exact_count=True))
+        P, keep = prob.to_ctypes()
+        for _ in range(args.warmup):
+            ctx.forward_device(P, prob.tables)
+        ms, ev = [], 0
+        with ClockSampler(0) as clk:
+            for _ in range(args.steps):
+                ctx.flush_l2()
+                st = ctx.forward_device(P, prob.tables)
+                ms.append(st["total_ms"])
+                ev += st["scatter_events"]
+        h, st1 = ctx.forward(P, prob.tables)
+        out[prec] = {"value": ev / (sum(ms) / 1000.0), "ms": float(np.mean(ms)), "clocks": clk.summary(),
+                     "energy": normalise(h, grid, N)[1], "obs": st1["observations"], "sink": st1["sink"],
+                     "prob": prob}
+    e64, e32 = out["fp64"]["energy"], out["fp32"]["energy"]
+    line = {"metric": METRIC, "value": out["fp64"]["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": out["fp64"]["ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "3D acoustic isotropic unbounded, exp lc=0.1 cv=0.05/0.05 f=10 v=1, point source "
+                                   "lambda=0.05, 1e6 particles, spherical 120 r x 251 t", "particles": n},
+            "gpu_launches": args.steps, "clocks": out["fp64"]["clocks"], "sink": out["fp64"]["sink"],
+            "fp32": {"value": out["fp32"]["value"], "ms_per_step": out["fp32"]["ms"]},
+            "energy_conserved_fp64": bool(np.all(e64[1:, 0] == 1.0)), "energy_conserved_fp32": bool(np.all(e32[1:, 0] == 1.0))}
+    if not args.no_cpu:
+        prob = out["fp64"]["prob"]
+        nth = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        _, st, _ = O.run(prob, O.table_knots(prob.tables), scheme="substep", u24=False, nthreads=nth)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": st["scatter_events"] / dt, "unit": UNIT, "cores": nth, "kind": "port",
+                                "sample": f"the whole workload ({n} particles, 250 sub-steps each), reference sub-step "
+                                          f"order, {dt:.1f} s"}
+    return line
+
+
 def run_c3(args):
     """2D elastic P-SV half-space, free surface with Zoeppritz reflection, Q = 200, 1e8
     particles, cylindrical 200 r x 401 t; FP32 vs FP64 (1e7 particles, the same ids)."""
@@ -518,8 +566,9 @@ def main():
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"],
-                    help="c2: the headline line (default); c3: 2D half-space; c4: batched sweep; c5: gradient")
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
+                    help="c2: the headline line (default); c1: 3D acoustic FP64; c3: 2D half-space; "
+                         "c4: batched sweep; c5: gradient")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
@@ -527,7 +576,7 @@ def main():
     __graft_entry__.build()
     if args.workload != "c2":
         if rank == 0:
-            line = {"c3": run_c3, "c4": run_c4, "c5": run_c5}[args.workload](args)
+            line = {"c1": run_c1, "c3": run_c3, "c4": run_c4, "c5": run_c5}[args.workload](args)
             print(json.dumps(line), flush=True)
         return
     if args.impl == "reference":
