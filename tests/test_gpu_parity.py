@@ -383,3 +383,34 @@ def test_schedules_give_identical_results(name, precision):
     assert np.array_equal(s0, s1)
     for k in ("scatter_events", "boundary_hits", "kills", "absorbed", "observations", "conversions"):
         assert st0[k] == st1[k], k
+
+
+def test_2d_isotropic_scattering_matches_paasschens_fp32():
+    """Known answer at 1e7 particles on the GPU (FP32): radial energy of 2D isotropic
+    acoustic scattering against Paasschens' exact solution inside the ballistic front."""
+    import sys
+    from tests.test_oracle import _paasschens_2d_diffuse
+    geo = {"dimension": 2, "frame": "cylindrical"}
+    mat = MaterialClass()
+    mat.acoustics, mat.v, mat.sigma = True, 1.0, [1 / math.pi]
+    n = 10_000_000
+    obs = {"x": colon(0, 0.1, 4), "time": colon(0, 0.5, 3)}
+    prob, grid, N = build_problem(geo, {"numberParticles": n, "lambda": 1e-4}, mat, obs,
+                                  {"exact_count": True, "precision": "fp32", "seed": 31})
+    P, keep = prob.to_ctypes()
+    h, st = get_context(0).forward(P, prob.tables)
+    assert st["device_status"] == 0
+    h = h.reshape(grid.shape, order="F")[:, 0, :, 0].astype(float) / N
+    edges, zs = grid.edges[0], []
+    for it, t in enumerate(grid.t):
+        if t < 1.0:
+            continue
+        for k in range(edges.size - 1):
+            if edges[k + 1] > t - 0.1:
+                break
+            rr = np.linspace(edges[k], edges[k + 1], 201)
+            f = 2 * math.pi * rr * _paasschens_2d_diffuse(rr, t, 0.5, 1.0)
+            want = float(np.sum((f[1:] + f[:-1]) * np.diff(rr)) / 2)
+            zs.append((h[k, it] - want) / math.sqrt(want * (1 - want) / N))
+    zs = np.array(zs)
+    assert zs.size > 40 and abs(zs.mean()) < 0.5 and np.sqrt(np.mean(zs ** 2)) < 1.5, (zs.mean(), np.sqrt(np.mean(zs ** 2)))

@@ -373,3 +373,51 @@ def test_plane_source_event_scheme_equals_substep_scheme():
     obs = {"x": colon(-1, 0.1, 3), "time": colon(0, 0.1, 2.0)}
     prob, grid, N, he, hs, se, ss = _both(geo, src, mat, obs, {}, 20000)
     assert _chi2_per_dof(he, hs) < 1.3
+
+
+def _paasschens_2d_diffuse(r, t, mft, v):
+    """Diffuse part of Paasschens' exact 2D solution for isotropic scattering from an
+    isotropic point source (analyticalPaasschens.m:64-68, the ballistic delta left out):
+    E = (S/v)^2 / (2 pi a) (1 - (b/a)^2)^(-1/2) exp(-a + sqrt(a^2 - b^2)) for b < a,
+    a = t / mft, b = r / (v mft), normalised so that the integral of 2 pi r E dr is the
+    scattered fraction 1 - exp(-a)."""
+    S = 1.0 / mft
+    a, b = t * S, r * S / v
+    out = np.zeros_like(r)
+    m = b < a
+    out[m] = (S / v) ** 2 / (2 * math.pi * a) / np.sqrt(1 - (b[m] / a) ** 2) * np.exp(-a + np.sqrt(a * a - b[m] ** 2))
+    return out
+
+
+def test_2d_isotropic_scattering_matches_paasschens():
+    """Known answer: the radial energy of 2D isotropic acoustic scattering against
+    Paasschens' exact solution (Phys. Rev. E 56, 1135 (1997)), annulus by annulus inside
+    the ballistic front, within Monte Carlo error plus 2 % (the sub-step scheme's O(h))."""
+    geo = {"dimension": 2, "frame": "cylindrical"}
+    mat = MaterialClass()
+    mat.acoustics, mat.v, mat.sigma = True, 1.0, [1 / math.pi]  # Sigma = 2 pi sigma = 2: mft 0.5
+    n = 200_000
+    src = {"numberParticles": n, "lambda": 1e-4}
+    obs = {"x": colon(0, 0.1, 4), "time": colon(0, 0.5, 3)}
+    prob, grid, N = build_problem(geo, src, mat, obs, {"exact_count": True, "precision": "fp64"})
+    assert math.isclose(prob.mft[0], 0.5, rel_tol=1e-9)
+    h, st, _ = O.run(prob, O.table_knots(prob.tables), scheme="event")
+    h = h.reshape(grid.shape, order="F")[:, 0, :, 0].astype(float) / N
+    edges = grid.edges[0]
+    checked, zs = 0, []
+    for it, t in enumerate(grid.t):
+        if t < 1.0:
+            continue
+        for k in range(edges.size - 1):
+            r0, r1 = edges[k], edges[k + 1]
+            if r1 > t - 0.1:  # stay clear of the ballistic front at r = v t
+                break
+            rr = np.linspace(r0, r1, 201)
+            f = 2 * math.pi * rr * _paasschens_2d_diffuse(rr, t, 0.5, 1.0)
+            want = float(np.sum((f[1:] + f[:-1]) * np.diff(rr)) / 2)
+            sig = math.sqrt(want * (1 - want) / N)
+            assert abs(h[k, it] - want) <= 4 * sig + 0.02 * want, (t, r0, h[k, it], want)
+            zs.append((h[k, it] - want) / sig)
+            checked += 1
+    zs = np.array(zs)
+    assert checked > 40 and abs(zs.mean()) < 0.3 and np.sqrt(np.mean(zs ** 2)) < 1.3
