@@ -380,7 +380,11 @@ def test_schedules_give_identical_results(name, precision):
     (h0, s0, st0), (h1, s1, st1) = out
     assert st0["device_status"] == 0 and st1["device_status"] == 0 and st0["sink"] == st1["sink"]
     assert np.array_equal(h0, h1)
-    assert np.array_equal(s0, s1)
+    # the same events: counts identical; the event code is inlined into two kernels, so
+    # the compiler may contract multiply-adds differently (last-bit differences)
+    assert np.array_equal(s0[:, 9:], s1[:, 9:])
+    tol = 1e-12 if precision == "fp64" else 1e-5
+    assert np.all(np.abs(s0[:, :9] - s1[:, :9]) <= tol * (1 + np.abs(s1[:, :9])))
     for k in ("scatter_events", "boundary_hits", "kills", "absorbed", "observations", "conversions"):
         assert st0[k] == st1[k], k
 
