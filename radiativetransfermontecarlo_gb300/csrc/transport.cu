@@ -781,10 +781,6 @@ __device__ __forceinline__ int obs_offset(const DevParams<R> &p, const R *sedges
     }
 }
 
-// Bit 30 of a ring entry's start sub-step (starts stay below 2^30) tags the particle
-// generation when a lane runs ahead into its next particle (run_stream).
-constexpr int kGenBit = 1 << 30;
-
 // Per-lane ring of segments in shared memory, field-major so that lane t of every
 // slot sits in bank t % 32.
 template <typename R> struct Ring {
@@ -792,13 +788,12 @@ template <typename R> struct Ring {
     int *s0, *mode;
     R *th; // adjoint only
     int cap, stride;
-    template <bool TH = false>
-    __device__ __forceinline__ void put(int slot, const Part<R> &s, R t = (R)-1, int tag = 0) const
+    template <bool TH = false> __device__ __forceinline__ void put(int slot, const Part<R> &s, R t = (R)-1) const
     {
         const int k = slot * stride + threadIdx.x;
         x0[k] = s.x[0]; x1[k] = s.x[1]; x2[k] = s.x[2];
         d0[k] = s.d[0]; d1[k] = s.d[1]; d2[k] = s.d[2];
-        s0[k] = s.s0 | tag; mode[k] = s.mode;
+        s0[k] = s.s0; mode[k] = s.mode;
         if (TH) th[k] = t;
     }
     template <bool TH = false> __device__ __forceinline__ void get(int slot, Seg<R> &g) const
@@ -806,14 +801,8 @@ template <typename R> struct Ring {
         const int k = slot * stride + threadIdx.x;
         g.x[0] = x0[k]; g.x[1] = x1[k]; g.x[2] = x2[k];
         g.d[0] = d0[k]; g.d[1] = d1[k]; g.d[2] = d2[k];
-        g.s0 = s0[k] & (kGenBit - 1); g.mode = mode[k];
+        g.s0 = s0[k]; g.mode = mode[k];
         if (TH) g.th = th[k];
-    }
-    // start of the segment in slot if it belongs to generation gen (0 or kGenBit), else never
-    __device__ __forceinline__ int start_gen(int slot, int gen) const
-    {
-        const int v = s0[slot * stride + threadIdx.x];
-        return (v & kGenBit) == gen ? v & (kGenBit - 1) : 0x7fffffff;
     }
     __device__ __forceinline__ int start(int slot) const { return s0[slot * stride + threadIdx.x]; }
 };
@@ -1061,228 +1050,6 @@ __device__ __forceinline__ void run_batch(const DevParams<R> &p, const R *sedges
     }
 }
 
-// A warp's stream of batches base0, base0 + stride, ... (32 particles each, clipped at
-// n_end): run_batch's two cursors, except that a lane whose particle has no events left
-// starts its particle of the next batch in phase 1 and pushes that particle's segments
-// into the ring behind the current ones (tagged with the other generation).  Phase 1 then
-// keeps most lanes busy instead of waiting for the warp's busiest particle; phase 2 and
-// every bin are unchanged.  Forward sinks only (SMEM, GLOBAL, INDEX).
-template <typename R, int SINK, int OBS>
-__device__ __forceinline__ void run_stream(const DevParams<R> &p, const R *sedges, unsigned *shist, const Ring<R> &ring,
-                                           int64_t base, int64_t stride, int64_t n_end, Counters &cnt, bool &bad)
-{
-    constexpr bool SMEM = SINK == SINK_SMEM;
-    constexpr int NEVER = 0x7fffffff;
-    const unsigned full = 0xffffffffu;
-    const int lane = threadIdx.x & 31;
-    const unsigned long long inc = 1ull << p.hist_shift;
-    const int s_end = p.s_end;
-    const int C = ring.cap;
-    int head = 0, count = 0;
-    int gen = 0;                     // generation tag of the current batch (0 or kGenBit)
-    Part<R> s;                       // event cursor
-    int s_slot;                      // 0: s is the current particle, 1: the next one, -1: none
-    int64_t s_i = 0;                 // particle index of s
-    unsigned s_scat0 = 0, s_bnd0 = 0; // counters when s's particle started (final-state trace)
-    int lim_cur = NEVER, lim_next = NEVER; // observation limit of a particle whose events are over
-    bool next_started = false;
-    Seg<R> cur;
-
-    auto dummy = [&]() {
-        s.alive = 0; s.s_death = 0; s.s0 = 0; s.sS = s.sK = s.sB = s_end + 1; s.k = 0; s.mode = 0;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) { s.x[c] = (R)0; s.d[c] = (R)0; s.q[c] = (R)0; }
-    };
-    auto start_particle = [&](int64_t i) {
-        init_particle(p, (uint64_t)(p.pid0 + i), s);
-        s_i = i;
-        s_scat0 = cnt.scat;
-        s_bnd0 = cnt.bnd;
-    };
-    auto trace = [&]() {
-        if (!p.trace) return;
-        double *f = p.trace + 16 * s_i;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) { f[c] = s.x[c]; f[3 + c] = s.d[c]; f[6 + c] = s.q[c]; }
-        f[9] = s.mode; f[10] = s.alive; f[11] = cnt.scat - s_scat0; f[12] = cnt.bnd - s_bnd0;
-        f[13] = s.s0; f[14] = s.s_death; f[15] = s.k;
-    };
-
-    // first batch
-    int64_t i = base + lane;
-    bool have = i < n_end;
-    if (have) { start_particle(i); s_slot = 0; } else { dummy(); s_slot = -1; lim_cur = 0; }
-    seg_from(s, cur);
-    seg_prepare<R, OBS>(p, sedges, cur);
-    for (;;) {
-        const int64_t i_next = i + stride;
-        const bool next_have = i_next < n_end;
-        int32_t *optr = (SINK == SINK_INDEX && have) ? p.obs_idx + i : nullptr;
-        int jn = 1; // warp-uniform
-        while (jn <= p.n_obs) {
-            // ---- phase 1: refill the rings; lanes whose particle is over run ahead
-            const int so_next = jn * p.n_sub;
-            for (;;) {
-                while (count > 0 && ring.start_gen(head, gen) <= so_next) {
-                    ring.get(head, cur);
-                    seg_prepare<R, OBS>(p, sedges, cur);
-                    head = (head + 1) % C;
-                    --count;
-                }
-                if (s_slot >= 0 && (!s.alive || next_event(s) > s_end)) { // s's particle is over
-                    (s_slot == 0 ? lim_cur : lim_next) = s.alive ? NEVER : s.s_death;
-                    trace();
-                    s_slot = -1;
-                }
-                if (s_slot < 0 && !next_started && next_have && count < C) {
-                    start_particle(i_next);
-                    s_slot = 1;
-                    next_started = true;
-                    ring.put((head + count) % C, s, (R)-1, gen ^ kGenBit); // its first segment
-                    ++count;
-                }
-                const bool need = s_slot >= 0 && s.alive && count < C && next_event(s) <= s_end;
-                if (!__any_sync(full, need)) break;
-                if (need) {
-                    process_event(p, (uint64_t)(p.pid0 + s_i), s, cnt);
-                    if ((int)s.k > p.max_events) { s.alive = 0; s.s_death = s.s0; bad = true; }
-                    if (s.alive) {
-                        if (s_slot == 0 && count == 0 && s.s0 <= so_next) {
-                            seg_from(s, cur);
-                            seg_prepare<R, OBS>(p, sedges, cur);
-                        } else {
-                            ring.put((head + count) % C, s, (R)-1, s_slot == 0 ? gen : gen ^ kGenBit);
-                            ++count;
-                        }
-                    }
-                }
-            }
-            // ---- window: observations every live lane has covered
-            int cur_lim;
-            bool pending = false;
-            if (s_slot == 0) {
-                cur_lim = s.alive ? NEVER : s.s_death;
-                pending = s.alive && next_event(s) <= s_end;
-            } else {
-                cur_lim = lim_cur;
-            }
-            unsigned avail = 0x7fffffffu;
-            if (cur_lim == NEVER) {
-                const int limit = pending ? next_event(s) : s_end + 1;
-                int last = (limit - 1) / p.n_sub;
-                last = last < p.n_obs ? last : p.n_obs;
-                avail = (unsigned)(last - jn + 1);
-            }
-            unsigned nw = __reduce_min_sync(full, avail);
-            if (nw > (unsigned)(p.n_obs - jn + 1)) {
-                if (SINK == SINK_INDEX) {
-                    nw = (unsigned)(p.n_obs - jn + 1); // no live lane left: write the rest
-                } else {
-                    int rem = 0;
-                    if (have && cur_lim > jn * p.n_sub) rem = min(p.n_obs, (cur_lim - 1) / p.n_sub) - jn + 1;
-                    nw = __reduce_max_sync(full, (unsigned)(rem > 0 ? rem : 0));
-                    if (nw == 0) break;
-                }
-            }
-            // ---- phase 2: nw observations per lane, two at a time
-            const int obs_limit = cur_lim;
-            int next_start = count > 0 ? ring.start_gen(head, gen) : NEVER;
-            int so = jn * p.n_sub;
-            auto advance = [&](int at) {
-                do {
-                    ring.get(head, cur);
-                    head = (head + 1) % C;
-                    --count;
-                } while (count > 0 && ring.start_gen(head, gen) <= at);
-                seg_prepare<R, OBS>(p, sedges, cur);
-                next_start = count > 0 ? ring.start_gen(head, gen) : NEVER;
-            };
-            auto emit = [&](int v, int mode, int j) {
-                if (SINK == SINK_INDEX) {
-                    if (have) {
-                        *optr = v < 0 ? -1 : (v | (mode << 30));
-                        optr += p.obs_rows;
-                    }
-                    if (v >= 0) cnt.obs++;
-                } else if (v >= 0) {
-                    const int64_t idx = (int64_t)j * p.time_stride + (mode ? p.mode_stride : 0) + v;
-                    if (idx < p.hist_len) {
-                        cnt.obs++;
-                        if (SMEM) atomicAdd(shist + idx, 1u);
-                        else atomicAdd(p.hist + idx, inc);
-                    } else {
-                        bad = true;
-                    }
-                }
-            };
-            unsigned w = 0;
-            for (; w + 1 < nw; w += 2, jn += 2, so += 2 * p.n_sub) {
-                const int so1 = so + p.n_sub;
-                int v0 = -1, v1 = -1, m0 = cur.mode, m1 = cur.mode;
-                if (so < obs_limit) {
-                    if (so >= next_start) advance(so);
-                    m0 = m1 = cur.mode;
-                    v0 = obs_offset<R, OBS>(p, sedges, cur, so);
-                    if (so1 < obs_limit) {
-                        if (so1 >= next_start) {
-                            advance(so1);
-                            m1 = cur.mode;
-                        }
-                        v1 = obs_offset<R, OBS>(p, sedges, cur, so1);
-                    }
-                }
-                emit(v0, m0, jn);
-                emit(v1, m1, jn + 1);
-            }
-            for (; w < nw; ++w, ++jn, so += p.n_sub) {
-                int v = -1;
-                if (so < obs_limit) {
-                    if (so >= next_start) advance(so);
-                    v = obs_offset<R, OBS>(p, sedges, cur, so);
-                }
-                emit(v, cur.mode, jn);
-            }
-        }
-        // ---- the batch is over
-        if (s_slot == 0) { // its events past the last instant never run
-            lim_cur = s.alive ? NEVER : s.s_death;
-            trace();
-            s_slot = -1;
-        }
-        base += stride;
-        if (base >= n_end) break; // warp-uniform
-        gen ^= kGenBit;
-        // segments of the finished batch that no instant reached (a particle dying before
-        // the next instant) are dropped
-        while (count > 0 && (ring.start_gen(head, gen) == 0x7fffffff)) {
-            head = (head + 1) % C;
-            --count;
-        }
-        i = i_next;
-        have = next_have;
-        if (next_started) { // its first segment heads the ring
-            ring.get(head, cur);
-            head = (head + 1) % C;
-            --count;
-            seg_prepare<R, OBS>(p, sedges, cur);
-            if (s_slot == 1) s_slot = 0; else lim_cur = lim_next;
-        } else if (have) {
-            start_particle(i);
-            s_slot = 0;
-            seg_from(s, cur);
-            seg_prepare<R, OBS>(p, sedges, cur);
-        } else {
-            dummy();
-            s_slot = -1;
-            lim_cur = 0;
-            seg_from(s, cur);
-            seg_prepare<R, OBS>(p, sedges, cur);
-        }
-        next_started = false;
-        lim_next = NEVER;
-    }
-}
-
 // Event-major schedule for event-heavy problems: one particle per thread, each event
 // followed by the observations of the segment it ends.  A warp then runs as many
 // iterations as its busiest lane has events (tens to hundreds, close to the mean), where
@@ -1380,8 +1147,8 @@ __global__ void __launch_bounds__(Bounds<R, SINK>::threads, Bounds<R, SINK>::min
         for (int64_t i = (int64_t)blockIdx.x * T + threadIdx.x; i < p.n_particles; i += (int64_t)gridDim.x * T)
             run_particle<R, SINK, OBS>(p, sedges, shist, i, cnt, bad);
     } else {
-        const int64_t base = (((int64_t)blockIdx.x * T + threadIdx.x) >> 5) << 5;
-        if (base < p.n_particles) run_stream<R, SINK, OBS>(p, sedges, shist, ring, base, warps * 32, p.n_particles, cnt, bad);
+        for (int64_t base = (((int64_t)blockIdx.x * T + threadIdx.x) >> 5) << 5; base < p.n_particles; base += warps * 32)
+            run_batch<R, SINK, OBS>(p, sedges, shist, ring, base, p.n_particles, cnt, bad);
     }
 
     // counters: warp reduction, one global atomic per warp
