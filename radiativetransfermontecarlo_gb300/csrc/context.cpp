@@ -62,7 +62,6 @@ struct rtmc_context {
     int opt_event_major = -1; // -1 automatic, 0 two-cursor batches, 1 one particle per thread
     static constexpr int kPipe = 32;
     cudaStream_t fold_stream = nullptr;
-    cudaStream_t copy_stream[3] = {};   // more host copies in flight beside fold_stream
     cudaEvent_t ev_a0[kPipe] = {}, ev_a1[kPipe] = {}, ev_b0[kPipe] = {}, ev_b1[kPipe] = {};
 };
 
@@ -365,15 +364,12 @@ void fill_params(rtmc_context *ctx, const rtmc_problem *P, const DevTables<R> &t
     (void)ctx;
 }
 
-constexpr int kCopyGroups = 5;  // slice groups of the last fold, each copied as soon as it is final
-constexpr int kCopyStreams = 2; // streams the group copies rotate over (fold_stream first)
+constexpr int kCopyGroups = 5; // slice groups of the last fold, each copied as soon as it is final
 
 int ensure_pipeline(rtmc_context *ctx)
 {
     cudaError_t e = cudaSuccess;
     if (!ctx->fold_stream) e = cudaStreamCreateWithFlags(&ctx->fold_stream, cudaStreamNonBlocking);
-    for (int k = 0; k < 3 && e == cudaSuccess; ++k)
-        if (!ctx->copy_stream[k]) e = cudaStreamCreateWithFlags(&ctx->copy_stream[k], cudaStreamNonBlocking);
     for (int i = 0; i < rtmc_context::kPipe && e == cudaSuccess; ++i) {
         if (!ctx->ev_a0[i]) e = cudaEventCreate(&ctx->ev_a0[i]);
         if (e == cudaSuccess && !ctx->ev_a1[i]) e = cudaEventCreate(&ctx->ev_a1[i]);
@@ -618,23 +614,19 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
                     if (le) break;
                     ++launches;
                     CK(cudaEventRecord(ctx->ev_a1[g], ctx->stream), "event");
-                    cudaStream_t cs = g % kCopyStreams == 0 ? ctx->fold_stream : ctx->copy_stream[g % kCopyStreams - 1];
-                    CK(cudaStreamWaitEvent(cs, ctx->ev_a1[g], 0), "copy wait");
+                    CK(cudaStreamWaitEvent(ctx->fold_stream, ctx->ev_a1[g], 0), "copy wait");
                     const int64_t s0 = g == 0 ? 0 : (int64_t)ja * ts; // slice 0 (t = 0) goes with the first group
                     const int64_t s1 = (int64_t)jb * ts;
                     for (int m = 0; m < nm; ++m) {
                         const int64_t o = m * P->mode_stride;
                         CK(cudaMemcpyAsync(host_out + o + s0, static_cast<int64_t *>(ctx->hist.p) + o + s0,
-                                           (size_t)(s1 - s0) * sizeof(int64_t), cudaMemcpyDeviceToHost, cs),
+                                           (size_t)(s1 - s0) * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->fold_stream),
                            "histogram copy");
                     }
                 }
+                CK(cudaEventRecord(ctx->ev_b1[0], ctx->fold_stream), "event");
                 CK(cudaEventRecord(ctx->ev_k2, ctx->stream), "event");
-                for (int k = 0; k < kCopyStreams && k < kCopyGroups; ++k) {
-                    cudaStream_t cs = k == 0 ? ctx->fold_stream : ctx->copy_stream[k - 1];
-                    CK(cudaEventRecord(ctx->ev_b1[k], cs), "event");
-                    CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_b1[k], 0), "copy join");
-                }
+                CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_b1[0], 0), "copy join");
                 copied = true;
             } else {
                 le = launch_bin_slices(b, fold_grid, fold_smem, ctx->stream);
@@ -1120,11 +1112,6 @@ extern "C" void rtmc_destroy(rtmc_context *ctx)
         if (ctx->ev_b1[i]) cudaEventDestroy(ctx->ev_b1[i]);
     }
     if (ctx->fold_stream) cudaStreamDestroy(ctx->fold_stream);
-    for (int k = 0; k < 3; ++k)
-        if (ctx->copy_stream[k]) {
-            cudaStreamSynchronize(ctx->copy_stream[k]);
-            cudaStreamDestroy(ctx->copy_stream[k]);
-        }
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
