@@ -1,10 +1,10 @@
 """GPU transport vs the CPU oracle, through the C ABI (rtmc_forward_trace / rtmc_forward).
 
 Same Philox stream on both sides ("event" oracle): FP64 trajectories must match to
-1e-9 relative (both sides run the same event sequence; libm vs CUDA math differ in the
+1e-12 relative (both sides run the same event sequence; libm vs CUDA math differ in the
 last bits) and bins exactly away from edge ties; FP32 trajectories match the oracle fed
-the same 24-bit uniforms to 1e-3 relative for >= 99% of particles (the rest leave the
-shared path when a float rounding flips an integer sub-step count).  Independent streams
+the same 24-bit uniforms to 1e-5 relative for >= 98% of particles and to 1e-3 for >= 99%
+(the rest leave the shared path when a float rounding flips an integer sub-step count).  Independent streams
 ("substep" oracle, the reference's own sub-step order): histograms agree within 3 sigma
 of the Monte Carlo error.
 """
@@ -56,7 +56,7 @@ def test_fp64_trajectories_and_bins_match_oracle(name):
     n = 20000 if name != "c3_halfspace2d" else 4000
     prob, grid, N, hist, states, stats, ref_hist, ref_states, ref_stats = _run_both(geo, src, mat, obs, opts, n, "fp64")
     assert stats["device_status"] == 0
-    ok = _path_match(states, ref_states, 1e-9)
+    ok = _path_match(states, ref_states, 1e-12)  # measured: at most 7e-15
     assert ok.mean() == 1.0, f"{(~ok).sum()} particles left the oracle's trajectory"
     assert stats["scatter_events"] == ref_stats["scatter_events"]
     assert stats["boundary_hits"] == ref_stats["boundary_hits"]
@@ -74,6 +74,8 @@ def test_fp32_trajectories_match_oracle_with_same_uniforms(name):
     assert stats["device_status"] == 0
     ok = _path_match(states, ref_states, 1e-3)
     assert ok.mean() >= 0.99, ok.mean()
+    # measured: 99.9 % (C1), 99.8 % (C2), 98.6 % (C3) of the particles within 1e-5
+    assert _path_match(states, ref_states, 1e-5).mean() >= 0.98
     rel = abs(stats["scatter_events"] - ref_stats["scatter_events"]) / max(1, ref_stats["scatter_events"])
     assert rel < 0.01
 
