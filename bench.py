@@ -283,6 +283,7 @@ def run_our_arm(args, rank, world, dist):
                                "kernels": kernels},
                   "gpu_launches": args.steps * launches_per_step, "clocks": clocks,
                   "events_per_step": events / args.steps, "observations_per_step": obs_per_step,
+                  "observations_per_s": obs_per_step * args.steps / total_s,
                   "transport_ms": kmean, "fold_ms": fmean, "sink": int(st["sink"])}
     # FP64 leg (same seed: the same trajectories up to rounding), then the accuracy check
     if rank == 0 and not args.no_fp64:
