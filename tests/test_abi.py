@@ -5,6 +5,7 @@ import re
 from pathlib import Path
 
 import numpy as np
+import pytest
 
 from radiativetransfermontecarlo_gb300 import _lib
 
@@ -63,3 +64,55 @@ def test_tables_from_knots_roundtrip_and_eval():
     # griddedInterpolant: linear inside, linear extrapolation outside
     u = np.array([-0.1, 0.0, 0.125, 0.75, 1.0, 1.2])
     assert np.allclose(T.eval(0, u), [-0.4, 0.0, 0.5, 2.25, 3.0, 3.6])
+
+
+def _has_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(_has_gpu(), reason="passes a placeholder device pointer: host-only check")
+def test_problem_validation_needs_no_gpu():
+    """rtmc_forward_noalloc validates the problem before any CUDA call: boundary kinds,
+    source shapes, radial profiles and the sub-step budget are refused with a message.
+    (Every problem here is invalid, so the placeholder histogram pointer is never used.)"""
+
+    from radiativetransfermontecarlo_gb300 import build_problem
+    from radiativetransfermontecarlo_gb300 import workloads as W
+    lib = _lib.load()
+    geo, src, mat, obs, opts = W.c1_acoustic3d()
+    prob, grid, N = build_problem(geo, dict(src, numberParticles=100), mat, obs, dict(opts, exact_count=True))
+
+    def refused(mutate, msg):
+        P, keep = prob.to_ctypes()
+        extra = mutate(P)
+        rc = lib.rtmc_forward_noalloc(C.byref(P), prob.tables.handle, C.c_void_p(256), None, None)
+        err = lib.rtmc_last_error(None)
+        del extra
+        assert rc == 1 and msg.encode() in err, (rc, err)  # RTMC_ERR_ARG
+
+    def bnd(P, d, v):
+        P.n_bnd, P.bnd_dir[0], P.bnd_val[0] = 1, d, v
+    refused(lambda P: bnd(P, 5, 1.0), "boundary dir")
+    refused(lambda P: bnd(P, 4, 0.0), "cylinder radius")
+    refused(lambda P: setattr(P, "src_type", 2), "source type")
+
+    def plane(P, d, normal):
+        P.src_type, P.d = 1, d
+        for i in range(3):
+            P.src_normal[i], P.src_u[i], P.src_v[i] = normal[i], (1.0, 0, 0)[i], (0, 1.0, 0)[i]
+    refused(lambda P: plane(P, 2, (0, 0, 1.0)), "3D only")
+    refused(lambda P: plane(P, 3, (0, 0, 2.0)), "unit vectors")
+
+    def radial(P, c, r):
+        c, r = np.ascontiguousarray(c, float), np.ascontiguousarray(r, float)
+        P.src_radial_n, P.src_radial_cdf, P.src_radial_r = c.size, _lib.dptr(c), _lib.dptr(r)
+        return c, r
+    refused(lambda P: radial(P, [0.0], [0.0]), "2 to 65536 knots")
+    refused(lambda P: radial(P, [0.0, 0.5, 0.5, 1.0], [0, 1, 2, 3]), "strictly increasing")
+    refused(lambda P: setattr(P, "n_sub", 1 << 23), "2^30")
+    refused(lambda P: setattr(P, "h", -1.0), "sub-step h")
+    refused(lambda P: setattr(P, "mft", (C.c_double * 2)(-1.0, -1.0)), "mean free times")
