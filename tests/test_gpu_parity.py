@@ -421,3 +421,23 @@ def test_2d_isotropic_scattering_matches_paasschens_fp32():
             zs.append((h[k, it] - want) / math.sqrt(want * (1 - want) / N))
     zs = np.array(zs)
     assert zs.size > 40 and abs(zs.mean()) < 0.5 and np.sqrt(np.mean(zs ** 2)) < 1.5, (zs.mean(), np.sqrt(np.mean(zs ** 2)))
+
+
+@pytest.mark.parametrize("index_mb", [0, 16])
+def test_index_path_with_overlapped_copy_matches_oracle(index_mb):
+    """Large slices (C2's 4-axis grid): the last fold runs in slice groups whose host copies
+    overlap it, alone (one particle chunk) or after earlier chunks (a 16 MB index budget)."""
+    geo, src, mat, obs, opts = W.c2_elastic3d(t_end=1.0)
+    ctx = get_context(0)
+    ctx.set_launch(0, 0, index_mb)
+    try:
+        prob, grid, N, hist, states, stats, ref_hist, ref_states, ref_stats = _run_both(
+            geo, src, mat, obs, opts, 20000, "fp64")
+    finally:
+        ctx.set_launch(0, 0, 0)
+    assert stats["device_status"] == 0 and stats["sink"] == 2
+    if index_mb:
+        assert stats["launches"] >= 4
+    assert _path_match(states, ref_states, 1e-12).mean() == 1.0
+    assert stats["observations"] == ref_stats["observations"]
+    assert _l1_diff(hist, ref_hist) >> prob.hist_shift <= max(4, 1e-6 * stats["observations"])
