@@ -1547,7 +1547,7 @@ __global__ void __launch_bounds__(kAdjointThreads, sizeof(R) == 4 ? 3 : 2) rt_ad
 // parameters): events run together in phase 1 and carry their scattering angle through
 // the ring; phase 2 accumulates adjoint weights per observation in lockstep.
 template <typename R, int OBS>
-__global__ void __launch_bounds__(kAdjointThreads, sizeof(R) == 4 ? 2 : 1) rt_adjoint_ring(const DevParams<R> p, const AdjointArgs a)
+__global__ void __launch_bounds__(kAdjointThreads, sizeof(R) == 4 ? 3 : 1) rt_adjoint_ring(const DevParams<R> p, const AdjointArgs a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ double red[kAdjointThreads / 32][kAdjRingParams];
