@@ -208,6 +208,14 @@ int rtmc_abi_sizes(int64_t out[4]);
 int rtmc_forward(rtmc_context *ctx, const rtmc_problem *problem, const rtmc_tables *tables,
                  int64_t *hist_out, rtmc_stats *stats);
 
+/* rtmc_forward with the histogram in the reference's own type: hist_out is a HOST buffer
+ * of problem->hist_len uint32, each bin's count (value >> hist_shift) saturated at
+ * 4294967295 as MATLAB's uint32 additions saturate (initializeObservation.m:133,
+ * observeTime.m:12, radiativeTransfer.m:88).  The narrowing runs on the device, so half
+ * the bytes of rtmc_forward cross to the host. */
+int rtmc_forward_u32(rtmc_context *ctx, const rtmc_problem *problem, const rtmc_tables *tables,
+                     uint32_t *hist_out, rtmc_stats *stats);
+
 /* Same, with the histogram left in device memory owned by ctx (no host copy);
  * rtmc_copy_histogram reads it back later. */
 int rtmc_forward_device(rtmc_context *ctx, const rtmc_problem *problem, const rtmc_tables *tables,

@@ -98,6 +98,7 @@ SIGNATURES = {
     "rtmc_abi_version": (C.c_int32, []),
     "rtmc_abi_sizes": (C.c_int, [C.POINTER(C.c_int64)]),
     "rtmc_forward": (C.c_int, [_P, C.POINTER(RtmcProblem), _P, C.POINTER(C.c_int64), C.POINTER(RtmcStats)]),
+    "rtmc_forward_u32": (C.c_int, [_P, C.POINTER(RtmcProblem), _P, C.POINTER(C.c_uint32), C.POINTER(RtmcStats)]),
     "rtmc_forward_trace": (C.c_int, [_P, C.POINTER(RtmcProblem), _P, C.POINTER(C.c_int64), C.POINTER(C.c_double),
                                      C.POINTER(RtmcStats)]),
     "rtmc_forward_device": (C.c_int, [_P, C.POINTER(RtmcProblem), _P, C.POINTER(RtmcStats)]),
@@ -247,6 +248,17 @@ class Context:
         st = RtmcStats()
         check(self.lib.rtmc_forward(self.handle, C.byref(problem), tables.handle,
                                     out.ctypes.data_as(C.POINTER(C.c_int64)), C.byref(st)), self.handle)
+        return out, st.as_dict()
+
+    def forward_u32(self, problem: RtmcProblem, tables: Tables, out: np.ndarray | None = None):
+        """rtmc_forward_u32: (uint32 counts on the host, saturating like the reference's E;
+        stats dict)."""
+        if out is None:
+            out = np.empty(problem.hist_len, dtype=np.uint32)
+        assert out.dtype == np.uint32 and out.size >= problem.hist_len and out.flags.c_contiguous
+        st = RtmcStats()
+        check(self.lib.rtmc_forward_u32(self.handle, C.byref(problem), tables.handle,
+                                        out.ctypes.data_as(C.POINTER(C.c_uint32)), C.byref(st)), self.handle)
         return out, st.as_dict()
 
     def forward_trace(self, problem: RtmcProblem, tables: Tables):

@@ -47,6 +47,7 @@ struct rtmc_context {
     cudaEvent_t ev_start = nullptr, ev_k0 = nullptr, ev_k1 = nullptr, ev_k2 = nullptr, ev_end = nullptr;
     std::string err;
     DevBuf hist, tabs, aux, stats, flush, trace, idx, adj, partial;
+    DevBuf narrow; // uint32 copy of the histogram (rtmc_forward_u32)
     uint64_t tabs_gen = 0;
     int tabs_prec = -1;
     DevTables<float> tf{};
@@ -379,9 +380,10 @@ int ensure_pipeline(rtmc_context *ctx)
     return (int)e;
 }
 
+// host_out receives the int64 histogram, or host_u32 the uint32 counts (at most one)
 template <typename R>
 int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t *host_out, rtmc_stats *st,
-        double *trace_out)
+        double *trace_out, uint32_t *host_u32)
 {
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
     CK(cudaEventRecord(ctx->ev_start, ctx->stream), "event");
@@ -418,6 +420,13 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
     CK(cudaMemsetAsync(ctx->hist.p, 0, hist_bytes, ctx->stream), "histogram clear");
     CK(cudaMemsetAsync(ctx->stats.p, 0, 256, ctx->stream), "counter clear");
     ctx->hist_len = P->hist_len;
+    uint32_t *narrow = nullptr;
+    if (host_u32) {
+        if (ctx->narrow.grow((size_t)P->hist_len * sizeof(uint32_t)))
+            return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for the uint32 histogram failed");
+        narrow = static_cast<uint32_t *>(ctx->narrow.p);
+    }
+    const int narrow_grid = 8 * ctx->num_sms;
     p.hist = static_cast<unsigned long long *>(ctx->hist.p);
     p.stats = static_cast<unsigned long long *>(ctx->stats.p);
     p.status = reinterpret_cast<int32_t *>(static_cast<unsigned char *>(ctx->stats.p) + 128);
@@ -601,7 +610,7 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
             BinParams b = bp;
             b.n = q.n_particles;
             if (b.group) b.part_per_block = (b.n + fold_grid - 1) / fold_grid;
-            if (last && host_out && !b.group && P->n_obs >= 2 * kCopyGroups && ensure_pipeline(ctx) == 0) {
+            if (last && (host_out || host_u32) && !b.group && P->n_obs >= 2 * kCopyGroups && ensure_pipeline(ctx) == 0) {
                 // the last fold in slice groups: each group's slices are final, so their
                 // copy to the host runs on the second stream while the next group folds
                 const int64_t ts = P->time_stride;
@@ -613,15 +622,27 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
                     le = launch_bin_slices(b, fold_grid, fold_smem, ctx->stream);
                     if (le) break;
                     ++launches;
-                    CK(cudaEventRecord(ctx->ev_a1[g], ctx->stream), "event");
-                    CK(cudaStreamWaitEvent(ctx->fold_stream, ctx->ev_a1[g], 0), "copy wait");
                     const int64_t s0 = g == 0 ? 0 : (int64_t)ja * ts; // slice 0 (t = 0) goes with the first group
                     const int64_t s1 = (int64_t)jb * ts;
+                    for (int m = 0; m < nm && narrow && !le; ++m) {
+                        const int64_t o = m * P->mode_stride + s0;
+                        le = launch_narrow_u32(p.hist + o, narrow + o, s1 - s0, P->hist_shift, narrow_grid, ctx->stream);
+                        ++launches;
+                    }
+                    if (le) break;
+                    CK(cudaEventRecord(ctx->ev_a1[g], ctx->stream), "event");
+                    CK(cudaStreamWaitEvent(ctx->fold_stream, ctx->ev_a1[g], 0), "copy wait");
                     for (int m = 0; m < nm; ++m) {
-                        const int64_t o = m * P->mode_stride;
-                        CK(cudaMemcpyAsync(host_out + o + s0, static_cast<int64_t *>(ctx->hist.p) + o + s0,
-                                           (size_t)(s1 - s0) * sizeof(int64_t), cudaMemcpyDeviceToHost, ctx->fold_stream),
-                           "histogram copy");
+                        const int64_t o = m * P->mode_stride + s0;
+                        if (narrow)
+                            CK(cudaMemcpyAsync(host_u32 + o, narrow + o, (size_t)(s1 - s0) * sizeof(uint32_t),
+                                               cudaMemcpyDeviceToHost, ctx->fold_stream),
+                               "histogram copy");
+                        else
+                            CK(cudaMemcpyAsync(host_out + o, static_cast<int64_t *>(ctx->hist.p) + o,
+                                               (size_t)(s1 - s0) * sizeof(int64_t), cudaMemcpyDeviceToHost,
+                                               ctx->fold_stream),
+                               "histogram copy");
                     }
                 }
                 CK(cudaEventRecord(ctx->ev_b1[0], ctx->fold_stream), "event");
@@ -650,6 +671,15 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         if (!copied)
             CK(cudaMemcpyAsync(host_out, ctx->hist.p, hist_bytes, cudaMemcpyDeviceToHost, ctx->stream), "histogram copy");
         d2h += (double)hist_bytes;
+    } else if (host_u32) {
+        const size_t u32_bytes = (size_t)P->hist_len * sizeof(uint32_t);
+        if (!copied) {
+            le = launch_narrow_u32(p.hist, narrow, P->hist_len, P->hist_shift, narrow_grid, ctx->stream);
+            if (le) return cuda_fail(ctx, (cudaError_t)le, "histogram narrowing");
+            ++launches;
+            CK(cudaMemcpyAsync(host_u32, narrow, u32_bytes, cudaMemcpyDeviceToHost, ctx->stream), "histogram copy");
+        }
+        d2h += (double)u32_bytes;
     }
     if (p.trace) {
         CK(cudaMemcpyAsync(trace_out, p.trace, trace_bytes, cudaMemcpyDeviceToHost, ctx->stream), "trace copy");
@@ -684,13 +714,13 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
 }
 
 int forward(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t *host_out, rtmc_stats *st,
-            double *trace_out = nullptr)
+            double *trace_out = nullptr, uint32_t *host_u32 = nullptr)
 {
     if (!ctx || !P) return fail(ctx ? &ctx->err : nullptr, RTMC_ERR_ARG, "rtmc_forward: NULL argument");
     int s = check_problem(ctx, P, t);
     if (s) return s;
-    return P->precision == RTMC_FP64 ? run<double>(ctx, P, t, host_out, st, trace_out)
-                                     : run<float>(ctx, P, t, host_out, st, trace_out);
+    return P->precision == RTMC_FP64 ? run<double>(ctx, P, t, host_out, st, trace_out, host_u32)
+                                     : run<float>(ctx, P, t, host_out, st, trace_out, host_u32);
 }
 
 // ---- rtmc_gradient: score-function adjoint replay ----------------------------------
@@ -1092,7 +1122,9 @@ extern "C" void rtmc_destroy(rtmc_context *ctx)
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    if (ctx->fold_stream) cudaStreamSynchronize(ctx->fold_stream);
     ctx->hist.release();
+    ctx->narrow.release();
     ctx->tabs.release();
     ctx->aux.release();
     ctx->stats.release();
@@ -1106,7 +1138,6 @@ extern "C" void rtmc_destroy(rtmc_context *ctx)
     if (ctx->ev_k1) cudaEventDestroy(ctx->ev_k1);
     if (ctx->ev_k2) cudaEventDestroy(ctx->ev_k2);
     if (ctx->ev_end) cudaEventDestroy(ctx->ev_end);
-    if (ctx->fold_stream) cudaStreamSynchronize(ctx->fold_stream);
     for (int i = 0; i < rtmc_context::kPipe; ++i) {
         if (ctx->ev_a0[i]) cudaEventDestroy(ctx->ev_a0[i]);
         if (ctx->ev_a1[i]) cudaEventDestroy(ctx->ev_a1[i]);
@@ -1129,6 +1160,13 @@ extern "C" int rtmc_forward(rtmc_context *ctx, const rtmc_problem *P, const rtmc
 {
     if (!hist_out) return fail(ctx ? &ctx->err : nullptr, RTMC_ERR_ARG, "rtmc_forward: hist_out is NULL");
     return forward(ctx, P, t, hist_out, st);
+}
+
+extern "C" int rtmc_forward_u32(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, uint32_t *hist_out,
+                                rtmc_stats *st)
+{
+    if (!hist_out) return fail(ctx ? &ctx->err : nullptr, RTMC_ERR_ARG, "rtmc_forward_u32: hist_out is NULL");
+    return forward(ctx, P, t, nullptr, st, nullptr, hist_out);
 }
 
 extern "C" int rtmc_forward_device(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, rtmc_stats *st)

@@ -174,6 +174,8 @@ constexpr int kAdjointThreads = 256;
 int transport_set_smem(int precision, int sink, int obs, size_t smem);
 int transport_max_threads(int precision, int sink, int obs);
 int launch_bin_slices(const BinParams &b, int grid_x, size_t smem, void *stream);
+// n histogram bins as uint32 counts (value >> shift, saturating), at most max_grid blocks
+int launch_narrow_u32(const unsigned long long *src, uint32_t *dst, int64_t n, int shift, int max_grid, void *stream);
 int launch_transport_batch_f32(const BatchArgs<float> &a, int grid, int block, size_t smem, void *stream);
 int launch_transport_batch_f64(const BatchArgs<double> &a, int grid, int block, size_t smem, void *stream);
 int transport_batch_setup(int precision, int obs, int block, size_t smem, int *blocks_per_sm);

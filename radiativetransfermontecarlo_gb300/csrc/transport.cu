@@ -1431,6 +1431,32 @@ __global__ void __launch_bounds__(512) rt_bin_slices_smem(const BinParams b)
     }
 }
 
+// The reference's histogram type: counts (value >> shift) of n bins as uint32, saturating
+// at 2^32 - 1 as MATLAB's uint32 additions do (initializeObservation.m:133,
+// radiativeTransfer.m:88).  HBM-bound: 8 B read and 4 B written per bin; each thread keeps
+// four independent loads in flight.
+constexpr int kNarrowThreads = 256, kNarrowUnroll = 4;
+__global__ void __launch_bounds__(kNarrowThreads) rt_narrow_u32(const unsigned long long *__restrict__ src,
+                                                                 uint32_t *__restrict__ dst, int64_t n, int shift)
+{
+    const int64_t stride = (int64_t)gridDim.x * kNarrowThreads;
+    for (int64_t k0 = (int64_t)blockIdx.x * kNarrowThreads * kNarrowUnroll + threadIdx.x; k0 < n;
+         k0 += stride * kNarrowUnroll) {
+        unsigned long long v[kNarrowUnroll];
+#pragma unroll
+        for (int u = 0; u < kNarrowUnroll; ++u) {
+            const int64_t k = k0 + (int64_t)u * kNarrowThreads;
+            v[u] = k < n ? __ldcs(src + k) : 0ull;
+        }
+#pragma unroll
+        for (int u = 0; u < kNarrowUnroll; ++u) {
+            const int64_t k = k0 + (int64_t)u * kNarrowThreads;
+            const unsigned long long c = v[u] >> shift;
+            if (k < n) __stcs(dst + k, c > 0xffffffffull ? 0xffffffffu : (uint32_t)c);
+        }
+    }
+}
+
 template <typename R, int SINK, int OBS> void *kernel_ptr() { return (void *)rt_transport<R, SINK, OBS>; }
 
 template <typename R, int SINK> void *pick_obs(int obs)
@@ -1654,6 +1680,17 @@ int launch_bin_slices(const BinParams &b, int grid_x, size_t smem, void *stream)
         dim3 g(grid_x, b.j_count);
         rt_bin_slices<<<g, kFoldThreads, 0, (cudaStream_t)stream>>>(b);
     }
+    return (int)cudaGetLastError();
+}
+
+int launch_narrow_u32(const unsigned long long *src, uint32_t *dst, int64_t n, int shift, int max_grid, void *stream)
+{
+    if (n <= 0) return 0;
+    if (shift < 0 || shift > 62 || max_grid < 1) return (int)cudaErrorInvalidValue;
+    const int64_t per = (int64_t)kNarrowThreads * kNarrowUnroll;
+    const int64_t need = (n + per - 1) / per;
+    const int grid = (int)(need < max_grid ? need : max_grid);
+    rt_narrow_u32<<<grid, kNarrowThreads, 0, (cudaStream_t)stream>>>(src, dst, n, shift);
     return (int)cudaGetLastError();
 }
 

@@ -353,10 +353,12 @@ def get_context(device: int = 0) -> _lib.Context:
     return ctx
 
 
-def run_transport(prob: TransportProblem, device: int = 0, out: np.ndarray | None = None):
-    """One rtmc_forward call: int64 histogram (host) and the kernel statistics."""
+def run_transport(prob: TransportProblem, device: int = 0, out: np.ndarray | None = None, counts_u32: bool = False):
+    """One rtmc_forward call: int64 histogram (host) and the kernel statistics; with
+    counts_u32, rtmc_forward_u32's uint32 counts (the reference's E, half the bytes)."""
     P, keep = prob.to_ctypes()
-    hist, stats = get_context(device).forward(P, prob.tables, out)
+    ctx = get_context(device)
+    hist, stats = (ctx.forward_u32 if counts_u32 else ctx.forward)(P, prob.tables, out)
     del keep
     return hist, stats
 
@@ -368,14 +370,17 @@ def radiativeTransfer(geometry: dict, source: dict, material: MaterialClass, obs
     options (not in the reference): precision 'fp32' | 'fp64', seed, device, exact_count
     (skip the rounding of numberParticles up to a multiple of 1e5), histogram 'reference'
     (two binned axes) | 'extended' (up to four), hist_shift (int64 fixed-point shift),
-    return_counts (add the raw int64 histogram as obs['E']).
+    return_counts (add the raw int64 histogram as obs['E']; otherwise the histogram comes
+    back as uint32 counts, the reference's type).
     """
     opt = dict(DEFAULT_OPTIONS)
     opt.update(options or {})
     prob, grid, N = build_problem(geometry, source, material, observation, opt)
-    hist, stats = run_transport(prob, int(opt["device"]))
+    # uint32 counts as in the reference's E, unless the int64 fixed-point histogram is asked for
+    u32 = not opt["return_counts"]
+    hist, stats = run_transport(prob, int(opt["device"]), counts_u32=u32)
     obs = dict(grid.obs)
-    obs["energyDensity"], obs["energy"] = normalise(hist, grid, N, prob.hist_shift)
+    obs["energyDensity"], obs["energy"] = normalise(hist, grid, N, 0 if u32 else prob.hist_shift)
     obs["stats"] = stats
     if opt["return_counts"]:
         obs["E"] = hist.reshape(grid.shape, order="F")

@@ -52,6 +52,7 @@ def test_host_functions_report_errors():
     assert b"strictly increasing" in lib.rtmc_last_error(None)
     # forward with a NULL problem is an argument error, not a crash
     assert lib.rtmc_forward(None, None, None, None, None) == 1
+    assert lib.rtmc_forward_u32(None, None, None, None, None) == 1
     assert lib.rtmc_forward_noalloc(None, None, None, None, None) == 1
 
 

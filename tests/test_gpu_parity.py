@@ -14,7 +14,7 @@ import numpy as np
 import pytest
 
 from oracle import oracle as O
-from radiativetransfermontecarlo_gb300 import MaterialClass, build_problem, colon, get_context, normalise
+from radiativetransfermontecarlo_gb300 import MaterialClass, build_problem, colon, get_context, normalise, radiativeTransfer
 from radiativetransfermontecarlo_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -441,3 +441,49 @@ def test_index_path_with_overlapped_copy_matches_oracle(index_mb):
     assert _path_match(states, ref_states, 1e-12).mean() == 1.0
     assert stats["observations"] == ref_stats["observations"]
     assert _l1_diff(hist, ref_hist) >> prob.hist_shift <= max(4, 1e-6 * stats["observations"])
+
+
+@pytest.mark.parametrize("case", ["c2_overlapped_copy", "c2_pipelined", "c1_smem", "c3_global"])
+def test_uint32_histogram_is_the_int64_count(case):
+    """rtmc_forward_u32 delivers the reference's uint32 E: the int64 histogram's counts
+    (value >> hist_shift), narrowed on the device, whichever sink and copy path ran."""
+    ctx = get_context(0)
+    if case.startswith("c2"):
+        geo, src, mat, obs, opts = W.c2_elastic3d(t_end=1.0)
+        n = 20000
+    elif case == "c1_smem":
+        geo, src, mat, obs, opts = W.c1_acoustic3d()
+        n = 50000
+    else:
+        geo, src, mat, obs, opts = W.c3_halfspace2d(t_end=2.0)
+        n = 4000
+    prob, grid, N = build_problem(geo, dict(src, numberParticles=n), mat, obs, dict(opts, exact_count=True))
+    P, keep = prob.to_ctypes()
+    if case == "c2_pipelined":
+        ctx.set_pipeline(3, 2)
+    try:
+        h64, st64 = ctx.forward(P, prob.tables)
+        h32, st32 = ctx.forward_u32(P, prob.tables)
+    finally:
+        ctx.set_pipeline(0, 0)
+    assert st32["device_status"] == 0 and st32["sink"] == st64["sink"]
+    assert st32["observations"] == st64["observations"] > 0
+    want = np.minimum(h64.view(np.uint64) >> np.uint64(prob.hist_shift), np.uint64(0xFFFFFFFF)).astype(np.uint32)
+    assert np.array_equal(h32, want)
+    assert st32["d2h_bytes"] < st64["d2h_bytes"]
+
+
+def test_radiativeTransfer_drop_in():
+    """The reference's call, obs = radiativeTransfer(geometry, source, material, observation):
+    the obs struct of initializeObservation plus energyDensity [N1, N2, Nt, modes] and energy
+    [Nt, modes]; energy(2:end) == 1 at Q = Inf; the uint32 path it takes gives the same
+    fields as the int64 histogram (return_counts)."""
+    geo, src, mat, obs, opts = W.c1_acoustic3d(n=100_000)
+    a = radiativeTransfer(geo, src, mat, obs, dict(opts, precision="fp32"))
+    b = radiativeTransfer(geo, src, mat, obs, dict(opts, precision="fp32", return_counts=True))
+    assert a["energyDensity"].shape == (120, 1, 251, 1) and a["energy"].shape == (251, 1)
+    assert np.allclose(a["t"], colon(0, 0.02, 5))
+    assert np.all(a["energy"][1:, 0] == 1.0) and a["energy"][0, 0] == 0.0
+    assert np.array_equal(a["energyDensity"], b["energyDensity"]) and np.array_equal(a["energy"], b["energy"])
+    assert b["E"].dtype == np.int64 and int(b["E"].sum()) == 250 * 100_000
+    assert a["stats"]["d2h_bytes"] < b["stats"]["d2h_bytes"]
