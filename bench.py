@@ -310,6 +310,17 @@ def run_our_arm(args, rank, world, dist):
                              api="rtmc_forward_u32 (uint32 counts, the reference's E type)")
         result["e2e_int64"] = dict(e2e_leg(ctx.forward, buf.array(np.int64, prob.hist_len)),
                                    api="rtmc_forward (int64 fixed point, 2^-40)")
+        # the host link alone: one plain device-to-host copy of the histogram, as a yardstick
+        # for the end-to-end figures (each is transport + the first fold group + its bytes
+        # at this rate when the link bounds it)
+        out = buf.array(np.int64, prob.hist_len)
+        ctx.copy_histogram(out)
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            ctx.copy_histogram(out)
+            ts.append(time.perf_counter() - t0)
+        result["host_link_d2h_gbs"] = prob.hist_len * 8 / min(ts) / 1e9
     # FP64 leg (same seed: the same trajectories up to rounding), then the accuracy check
     if rank == 0 and not args.no_fp64:
         geo, src, mat, obs, opts = W.c2_elastic3d(n=n, precision="fp64", t_end=args.t_end)

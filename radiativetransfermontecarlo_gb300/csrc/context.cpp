@@ -147,9 +147,14 @@ template <typename R> int upload_tables(rtmc_context *ctx, const rtmc_tables *t,
     if (ctx->tabs.grow(total)) return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for tables failed");
     unsigned char *base = static_cast<unsigned char *>(ctx->tabs.p);
     std::lock_guard<std::mutex> lock(t->image_mu);
-    std::vector<unsigned char> &host = t->image[sizeof(R) == 4 ? 0 : 1];
+    const int k = sizeof(R) == 4 ? 0 : 1;
+    std::vector<unsigned char> &host = t->image[k];
     const bool have = host.size() == total;
-    if (!have) host.assign(total, 0);
+    if (!have) {
+        if (t->image_pinned[k]) cudaHostUnregister(host.data());
+        t->image_pinned[k] = false;
+        host.assign(total, 0);
+    }
     for (int i = 0; i < t->n_tables; ++i) {
         if (!have) {
             stage_table<R>(t->cdf[i], t->theta[i], host.data() + off[i], base + off[i], dt, i);
@@ -164,6 +169,12 @@ template <typename R> int upload_tables(rtmc_context *ctx, const rtmc_tables *t,
     for (int i = t->n_tables; i < 4; ++i) {
         dt->knot[i] = nullptr;
         dt->guide[i] = nullptr;
+    }
+    // page-lock the image once, so that every later upload is one copy at the link's rate
+    // (a pageable copy is staged through a bounce buffer); unpinned it still works
+    if (!t->image_pinned[k]) {
+        t->image_pinned[k] = cudaHostRegister(host.data(), total, cudaHostRegisterPortable) == cudaSuccess;
+        if (!t->image_pinned[k]) cudaGetLastError();
     }
     CK(cudaMemcpyAsync(ctx->tabs.p, host.data(), total, cudaMemcpyHostToDevice, ctx->stream), "table upload");
     CK(cudaStreamSynchronize(ctx->stream), "table upload");

@@ -20,6 +20,7 @@ struct rtmc_tables {
     // upload and reused: an upload is then one host-to-device copy
     mutable std::mutex image_mu;
     mutable std::vector<unsigned char> image[2];
+    mutable bool image_pinned[2] = {false, false}; // page-locked (cudaHostRegister) for async uploads
 };
 
 namespace rtmc {

@@ -12,6 +12,8 @@
 // refraction angles turn complex beyond the critical angles).
 #include "rtmc_internal.h"
 
+#include <cuda_runtime_api.h>
+
 #include <algorithm>
 #include <cmath>
 #include <complex>
@@ -488,7 +490,13 @@ extern "C" int rtmc_tables_eval(const rtmc_tables *t, int32_t i, int64_t n, cons
     return RTMC_OK;
 }
 
-extern "C" void rtmc_tables_free(rtmc_tables *t) { delete t; }
+extern "C" void rtmc_tables_free(rtmc_tables *t)
+{
+    if (!t) return;
+    for (int k = 0; k < 2; ++k)
+        if (t->image_pinned[k]) cudaHostUnregister(t->image[k].data());
+    delete t;
+}
 
 // ---------------------------------------------------------------------------------
 // Zoeppritz, solid over fluid (ZoeppritzFluid.m:47-222)
