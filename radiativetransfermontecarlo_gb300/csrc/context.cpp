@@ -378,6 +378,16 @@ void fill_params(rtmc_context *ctx, const rtmc_problem *P, const DevTables<R> &t
 
 constexpr int kCopyGroups = 5; // slice groups of the last fold, each copied as soon as it is final
 
+// First slice (1-based) of copy group g in [0, kCopyGroups]; g = kCopyGroups gives n_obs + 1.
+// The first group is small (1/25 of the slices), so the first copy starts soon after the
+// transport; the fold outruns the host link, so later copies follow back to back.
+int copy_group_start(int n_obs, int g)
+{
+    if (g <= 0) return 1;
+    const int first = std::max(1, n_obs / 25);
+    return 1 + first + (int)((int64_t)(n_obs - first) * (g - 1) / (kCopyGroups - 1));
+}
+
 int ensure_pipeline(rtmc_context *ctx)
 {
     cudaError_t e = cudaSuccess;
@@ -626,8 +636,8 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
                 // copy to the host runs on the second stream while the next group folds
                 const int64_t ts = P->time_stride;
                 for (int g = 0; g < kCopyGroups && !le; ++g) {
-                    const int ja = 1 + (int)((int64_t)P->n_obs * g / kCopyGroups);
-                    const int jb = 1 + (int)((int64_t)P->n_obs * (g + 1) / kCopyGroups); // exclusive
+                    const int ja = copy_group_start(P->n_obs, g);
+                    const int jb = copy_group_start(P->n_obs, g + 1); // exclusive
                     b.j_first = ja;
                     b.j_count = jb - ja;
                     le = launch_bin_slices(b, fold_grid, fold_smem, ctx->stream);
