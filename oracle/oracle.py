@@ -91,13 +91,19 @@ def philox(ctr, key):
 
 
 def run(prob, knots, scheme: str = "event", u24: bool | None = None, nthreads: int | None = None,
-        n_particles: int | None = None, pid0: int | None = None, want_state: bool = False):
+        n_particles: int | None = None, pid0: int | None = None, want_state: bool = False,
+        hist: np.ndarray | None = None):
     """Run the oracle on a TransportProblem-like object with the given table knots
     [(cdf, theta), ...].  scheme 'substep' (reference order) or 'event' (snap, GPU stream).
+    hist, if given, is an int64 array of hist_len that the run adds into (timing runs
+    reuse one, so allocation and first-touch page faults stay out of the particles' time).
     Returns (int64 histogram, stats dict, final states [N,16] or None)."""
     lib = load()
     P, keep = _problem(prob, knots, scheme, u24, nthreads, n_particles, pid0)
-    hist = np.zeros(prob.hist_len, dtype=np.int64)
+    if hist is None:
+        hist = np.zeros(prob.hist_len, dtype=np.int64)
+    elif hist.dtype != np.int64 or hist.size != prob.hist_len or not hist.flags.c_contiguous:
+        raise ValueError("hist must be a contiguous int64 array of hist_len")
     stats = np.zeros(8, dtype=np.int64)
     fs = np.zeros((P.n_particles, 16)) if want_state else None
     rc = lib.oracle_run(C.byref(P), hist.ctypes.data_as(C.POINTER(C.c_int64)),
