@@ -423,6 +423,28 @@ def test_2d_isotropic_scattering_matches_paasschens_fp32():
     assert zs.size > 40 and abs(zs.mean()) < 0.5 and np.sqrt(np.mean(zs ** 2)) < 1.5, (zs.mean(), np.sqrt(np.mean(zs ** 2)))
 
 
+def test_3d_isotropic_scattering_matches_paasschens_fp32():
+    """Known answer at 1e7 particles on the GPU (FP32, large time steps): radial energy of
+    3D isotropic acoustic scattering against Paasschens' approximate solution, with the
+    approximation's own few-per-cent error as the bar (mean within 3 %, each shell within
+    6 % plus 4 Monte Carlo sigmas)."""
+    from tests.test_oracle import paasschens_3d_deviation
+    geo = {"dimension": 3, "frame": "spherical"}
+    mat = MaterialClass()
+    mat.acoustics, mat.v, mat.sigma = True, 1.0, [1 / (2 * math.pi)]
+    mat.timeSteps = 1
+    obs = {"x": colon(0, 0.1, 4), "time": colon(0, 0.5, 3)}
+    prob, grid, N = build_problem(geo, {"numberParticles": 10_000_000, "lambda": 1e-4}, mat, obs,
+                                  {"exact_count": True, "precision": "fp32", "seed": 33})
+    P, keep = prob.to_ctypes()
+    h, st = get_context(0).forward(P, prob.tables)
+    assert st["device_status"] == 0
+    h = h.reshape(grid.shape, order="F")[:, 0, :, 0].astype(float) / N
+    rel, sig = paasschens_3d_deviation(h, grid, N)
+    assert rel.size > 50 and abs(rel.mean()) < 0.03, rel.mean()
+    assert np.all(np.abs(rel) <= 0.06 + 4 * sig), rel
+
+
 @pytest.mark.parametrize("index_mb", [0, 1])
 def test_index_path_with_overlapped_copy_matches_oracle(index_mb):
     """Large slices (C2's 4-axis grid): the last fold runs in slice groups whose host copies
@@ -487,3 +509,30 @@ def test_radiativeTransfer_drop_in():
     assert np.array_equal(a["energyDensity"], b["energyDensity"]) and np.array_equal(a["energy"], b["energy"])
     assert b["E"].dtype == np.int64 and int(b["E"].sum()) == 250 * 100_000
     assert a["stats"]["d2h_bytes"] < b["stats"]["d2h_bytes"]
+
+
+@pytest.mark.parametrize("case", ["c1_smem", "c2_index", "c3_global"])
+def test_zero_and_one_particle(case):
+    """Edge sizes: no particles leaves an all-zero histogram and launches no transport; a
+    single particle (one live lane of one warp) follows the oracle's path and bins."""
+    if case == "c1_smem":
+        geo, src, mat, obs, opts = W.c1_acoustic3d()
+    elif case == "c2_index":
+        geo, src, mat, obs, opts = W.c2_elastic3d(t_end=1.0)
+    else:
+        geo, src, mat, obs, opts = W.c3_halfspace2d(t_end=2.0)
+    prob, grid, N = build_problem(geo, dict(src, numberParticles=0), mat, obs,
+                                  dict(opts, precision="fp64", exact_count=True))
+    assert prob.n_particles == 0
+    P, keep = prob.to_ctypes()
+    for call in (get_context(0).forward, get_context(0).forward_u32):
+        hist, stats = call(P, prob.tables)
+        assert stats["device_status"] == 0 and stats["observations"] == 0 and stats["scatter_events"] == 0
+        assert not hist.any()
+    for pid0 in (0, 12345):
+        prob1, grid1, N1, hist1, states1, stats1, ref_hist1, ref_states1, ref_stats1 = _run_both(
+            geo, src, mat, obs, dict(opts, pid0=pid0), 1, "fp64")
+        assert prob1.n_particles == 1 and stats1["device_status"] == 0
+        assert _path_match(states1, ref_states1, 1e-12).all()
+        assert stats1["observations"] == ref_stats1["observations"]
+        assert np.array_equal(hist1, ref_hist1)

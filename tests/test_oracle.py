@@ -421,3 +421,77 @@ def test_2d_isotropic_scattering_matches_paasschens():
             checked += 1
     zs = np.array(zs)
     assert checked > 40 and abs(zs.mean()) < 0.3 and np.sqrt(np.mean(zs ** 2)) < 1.3
+
+
+def _paasschens_3d_diffuse(r, t, mft, v):
+    """Diffuse part of Paasschens' approximate 3D solution for isotropic scattering from an
+    isotropic point source (analyticalPaasschens.m:69-73, the ballistic delta left out):
+    E = (S/v)^3 (1 - (b/a)^2)^(1/8) exp(-a) G(a (1 - (b/a)^2)^(3/4)) / (4 pi a / 3)^(3/2)
+    for b < a, with G(x) = exp(x) sqrt(1 + 2.026 / x), a = t / mft, b = r / (v mft).  The
+    interpolation is accurate to a few per cent (Phys. Rev. E 56, 1135 (1997))."""
+    S = 1.0 / mft
+    a, b = t * S, r * S / v
+    out = np.zeros_like(r)
+    m = b < a
+    q = 1 - (b[m] / a) ** 2
+    x = a * q ** 0.75
+    out[m] = (S / v) ** 3 * q ** 0.125 * np.exp(-a) * np.exp(x) * np.sqrt(1 + 2.026 / x) / (4 * math.pi / 3 * a) ** 1.5
+    return out
+
+
+def paasschens_3d_deviation(h, grid, N):
+    """Relative deviations and their Monte Carlo sigmas of the per-shell energy fractions
+    h[k, it] (shells clear of the origin and of the ballistic front, t >= 1) from the 3D
+    approximation with mft 0.5 and v 1."""
+    edges, rel, sig = grid.edges[0], [], []
+    for it, t in enumerate(grid.t):
+        if t < 1.0:
+            continue
+        for k in range(edges.size - 1):
+            r0, r1 = edges[k], edges[k + 1]
+            if r0 < 0.3 or r1 > t - 0.3:
+                continue
+            rr = np.linspace(r0, r1, 201)
+            f = 4 * math.pi * rr ** 2 * _paasschens_3d_diffuse(rr, t, 0.5, 1.0)
+            want = float(np.sum((f[1:] + f[:-1]) * np.diff(rr)) / 2)
+            rel.append((h[k, it] - want) / want)
+            sig.append(math.sqrt(want * (1 - want) / N) / want)
+    return np.array(rel), np.array(sig)
+
+
+def test_3d_isotropic_scattering_matches_paasschens():
+    """Known answer: the radial energy of 3D isotropic acoustic scattering against
+    Paasschens' approximate solution.  The approximation itself is off by a few per cent
+    (at 1e6 particles both time schemes sit 1.6 % below it on average, 3.8 % at most), so
+    the bar is a mean within 3 % and each shell within 6 % plus 4 Monte Carlo sigmas."""
+    geo = {"dimension": 3, "frame": "spherical"}
+    mat = MaterialClass()
+    mat.acoustics, mat.v, mat.sigma = True, 1.0, [1 / (2 * math.pi)]  # Sigma = 4 pi sigma = 2: mft 0.5
+    n = 200_000
+    obs = {"x": colon(0, 0.1, 4), "time": colon(0, 0.5, 3)}
+    prob, grid, N = build_problem(geo, {"numberParticles": n, "lambda": 1e-4}, mat, obs,
+                                  {"exact_count": True, "precision": "fp64"})
+    assert math.isclose(prob.mft[0], 0.5, rel_tol=1e-9)
+    h, st, _ = O.run(prob, O.table_knots(prob.tables), scheme="event")
+    h = h.reshape(grid.shape, order="F")[:, 0, :, 0].astype(float) / N
+    rel, sig = paasschens_3d_deviation(h, grid, N)
+    assert rel.size > 50 and abs(rel.mean()) < 0.03
+    assert np.all(np.abs(rel) <= 0.06 + 4 * sig), rel
+
+
+def test_zero_particles_and_a_supplied_histogram():
+    """No particles: an all-zero histogram and zero counters in both schemes; a supplied
+    histogram is added into (the timing runs reuse one) and must match hist_len."""
+    geo, src, mat, obs, opts = W.c1_acoustic3d()
+    prob, grid, N = build_problem(geo, dict(src, numberParticles=0), mat, obs,
+                                  dict(opts, exact_count=True, precision="fp64"))
+    kn = O.table_knots(prob.tables)
+    for scheme in ("event", "substep"):
+        h, st, _ = O.run(prob, kn, scheme=scheme)
+        assert not h.any() and st["scatter_events"] == 0 and st["observations"] == 0
+    h1, st1, _ = O.run(prob, kn, scheme="substep", n_particles=500)
+    acc = h1.copy()
+    O.run(prob, kn, scheme="substep", n_particles=500, hist=acc)
+    assert np.array_equal(acc, 2 * h1) and st1["observations"] == int(h1.sum()) > 0
+    with pytest.raises(ValueError, match="hist_len"):
+        O.run(prob, kn, scheme="substep", n_particles=10, hist=np.zeros(5, dtype=np.int64))
