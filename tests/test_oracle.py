@@ -1,6 +1,8 @@
 """The CPU oracle: the event (snap) scheme against the reference's sub-step order, and
 the known answers that pin both (energy conservation, Q-kill survival, equipartition,
-the elastic boundary energy partition of Examples/BoundaryReflectionEnergyTests.m)."""
+the elastic boundary energy partition of Examples/BoundaryReflectionEnergyTests.m,
+Paasschens' 2D and 3D solutions and the diffusion limit of
++Comparison/analyticalPaasschens.m)."""
 import math
 
 import numpy as np
@@ -477,6 +479,41 @@ def test_3d_isotropic_scattering_matches_paasschens():
     rel, sig = paasschens_3d_deviation(h, grid, N)
     assert rel.size > 50 and abs(rel.mean()) < 0.03
     assert np.all(np.abs(rel) <= 0.06 + 4 * sig), rel
+
+
+def test_3d_diffusion_limit():
+    """Known answer: at times long against the mean free time the energy approaches the
+    diffusion solution E_diff = (S/v)^3 / (4 pi a / 3)^(3/2) exp(-3 b^2 / (4 a))
+    (analyticalPaasschens.m:78-80, diffusivity v^2 mft / 3).  Over the shells within
+    v t / 4 of the source the excess over E_diff falls from about 6 % at 10 mean free times
+    to about 2 % at 40."""
+    geo = {"dimension": 3, "frame": "spherical"}
+    mat = MaterialClass()
+    mat.acoustics, mat.v, mat.sigma = True, 1.0, [1 / (2 * math.pi)]  # mft 0.5
+    mat.timeSteps = 1
+    n = 400_000
+    obs = {"x": colon(0, 0.25, 8), "time": colon(0, 2.5, 20)}
+    prob, grid, N = build_problem(geo, {"numberParticles": n, "lambda": 1e-4}, mat, obs,
+                                  {"exact_count": True, "precision": "fp64", "seed": 5})
+    h, st, _ = O.run(prob, O.table_knots(prob.tables), scheme="event")
+    h = h.reshape(grid.shape, order="F")[:, 0, :, 0].astype(float) / N
+    edges = grid.edges[0]
+
+    def excess(t):
+        it = int(np.argmin(np.abs(grid.t - t)))
+        S, devs = 2.0, []
+        for k in range(1, edges.size - 1):
+            r0, r1 = edges[k], edges[k + 1]
+            if r1 > 0.25 * t:
+                break
+            rr = np.linspace(r0, r1, 201)
+            a, b = t * S, rr * S
+            f = 4 * math.pi * rr ** 2 * S ** 3 / (4 * math.pi / 3 * a) ** 1.5 * np.exp(-0.75 * b ** 2 / a)
+            want = float(np.sum((f[1:] + f[:-1]) * np.diff(rr)) / 2)
+            devs.append((h[k, it] - want) / want)
+        return float(np.mean(devs))
+    e5, e20 = excess(5.0), excess(20.0)
+    assert 0.03 < e5 < 0.10 and -0.01 < e20 < 0.04 and e20 < 0.5 * e5, (e5, e20)
 
 
 def test_zero_particles_and_a_supplied_histogram():
