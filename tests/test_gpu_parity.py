@@ -423,6 +423,32 @@ def test_2d_isotropic_scattering_matches_paasschens_fp32():
     assert zs.size > 40 and abs(zs.mean()) < 0.5 and np.sqrt(np.mean(zs ** 2)) < 1.5, (zs.mean(), np.sqrt(np.mean(zs ** 2)))
 
 
+def test_mode_conversion_kinetics_fp32():
+    """Known answer on the GPU (FP32, 2e6 particles): the P fraction of an elastic P source
+    relaxes as P_eq + (1 - P_eq) exp(-(S_ps + S_sp) t) (see the oracle's test)."""
+    geo = {"dimension": 3}
+    mat = MaterialClass.preset(3)
+    d, K = 3, mat.vp / mat.vs
+    spp = sps = 0.2 * mat.vp
+    ssp = sps / ((d - 1) * K ** d)
+    mat.sigma = [[spp / (4 * math.pi), sps / (4 * math.pi)], [ssp / (4 * math.pi), (spp + sps - ssp) / (4 * math.pi)]]
+    n = 2_000_000
+    obs = {"x": colon(0, 1, 100), "time": colon(0, 0.1, 6)}
+    prob, grid, N = build_problem(geo, {"lambda": 0.002, "polarization": "P", "numberParticles": n}, mat, obs,
+                                  {"exact_count": True, "precision": "fp32", "seed": 7})
+    P, keep = prob.to_ctypes()
+    h, st = get_context(0).forward(P, prob.tables)
+    assert st["device_status"] == 0
+    e = h.reshape(grid.shape, order="F").sum(axis=(0, 1)).astype(float)
+    assert np.all(e[1:].sum(axis=1) == N)
+    t = np.asarray(grid.t)[1:]
+    frac = e[1:, 0] / N
+    p_eq = ssp / (sps + ssp)
+    want = p_eq + (1 - p_eq) * np.exp(-(sps + ssp) * t)
+    sig = np.sqrt(want * (1 - want) / N)
+    assert np.all(np.abs(frac - want) <= 4 * sig + 0.005), np.max(np.abs(frac - want))
+
+
 def test_3d_isotropic_scattering_matches_paasschens_fp32():
     """Known answer at 1e7 particles on the GPU (FP32, large time steps): radial energy of
     3D isotropic acoustic scattering against Paasschens' approximate solution, with the

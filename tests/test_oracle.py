@@ -85,6 +85,34 @@ def test_equipartition_elastic_3d():
     assert abs(ratio - want) / want < 0.05
 
 
+def test_mode_conversion_kinetics_elastic_3d():
+    """Known answer for P/S conversion by isotropic scattering: with every particle inside
+    the grid the P fraction obeys dP/dt = -S_ps P + S_sp (1 - P), so from a P source
+    P(t) = P_eq + (1 - P_eq) exp(-(S_ps + S_sp) t) with P_eq = S_sp / (S_ps + S_sp) (the
+    long-time limit is the equipartition ratio above), at every observation time."""
+    geo = {"dimension": 3}
+    mat = MaterialClass.preset(3)
+    d, K = 3, mat.vp / mat.vs
+    spp = sps = 0.2 * mat.vp
+    ssp = sps / ((d - 1) * K ** d)
+    sss = spp + sps - ssp
+    mat.sigma = [[spp / (4 * math.pi), sps / (4 * math.pi)], [ssp / (4 * math.pi), sss / (4 * math.pi)]]
+    n = 40_000
+    obs = {"x": colon(0, 1, 100), "time": colon(0, 0.1, 6)}
+    prob, grid, N = build_problem(geo, {"lambda": 0.002, "polarization": "P", "numberParticles": n}, mat, obs,
+                                  {"exact_count": True, "precision": "fp64"})
+    S_ps, S_sp = sps, ssp  # 4 pi sigma of the isotropic cross-sections
+    h, st, _ = O.run(prob, O.table_knots(prob.tables), scheme="event")
+    e = h.reshape(grid.shape, order="F").sum(axis=(0, 1)).astype(float)
+    t = np.asarray(grid.t)[1:]
+    frac = e[1:, 0] / (e[1:, 0] + e[1:, 1])
+    assert np.all(e[1:].sum(axis=1) == N)  # every particle observed once per instant
+    p_eq = S_sp / (S_ps + S_sp)
+    want = p_eq + (1 - p_eq) * np.exp(-(S_ps + S_sp) * t)
+    sig = np.sqrt(want * (1 - want) / N)
+    assert np.all(np.abs(frac - want) <= 4 * sig + 0.005), np.max(np.abs(frac - want) / (sig + 1e-12))
+
+
 @pytest.mark.parametrize("mode,angle", [("P", 15), ("P", 30), ("P", 45), ("P", 60), ("SV", 10), ("SV", 20),
                                         ("SV", 30), ("SV", 45), ("SH", 15), ("SH", 60)])
 def test_boundary_energy_partition(mode, angle):
