@@ -378,6 +378,11 @@ void fill_params(rtmc_context *ctx, const rtmc_problem *P, const DevTables<R> &t
 
 constexpr int kCopyGroups = 5; // slice groups of the last fold, each copied as soon as it is final
 
+// Row stride of the index array for a chunk of particles: a multiple of 32 entries, so
+// every row starts on a 128-byte boundary (the fold reads rows as 16-byte vectors, up to
+// the vector holding the chunk's last particle) and a warp's 32 lanes write whole lines.
+inline int64_t index_row_stride(int64_t particles) { return (particles + 31) / 32 * 32; }
+
 // First slice (1-based) of copy group g in [0, kCopyGroups]; g = kCopyGroups gives n_obs + 1.
 // The first group is small (1/25 of the slices), so the first copy starts soon after the
 // transport; the fold outruns the host link, so later copies follow back to back.
@@ -510,8 +515,10 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         }
         if (!n_pipe) {
             chunk = std::min<int64_t>(P->n_particles, rows);
-            if (chunk > 0 && ctx->idx.grow((size_t)chunk * P->n_obs * sizeof(int32_t)) == 0) sink = kSinkIndex;
-            else chunk = P->n_particles;
+            if (chunk > 0 && ctx->idx.grow((size_t)index_row_stride(chunk) * P->n_obs * sizeof(int32_t)) == 0)
+                sink = kSinkIndex;
+            else
+                chunk = P->n_particles;
         }
     }
     {
@@ -539,9 +546,10 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
     BinParams bp{};
     size_t fold_smem = 0;
     int fold_grid = 1;
+    const int64_t idx_rows = index_row_stride(chunk); // == chunk when pipelined
     if (sink == kSinkIndex) {
         bp.idx = static_cast<const int32_t *>(ctx->idx.p);
-        bp.rows = chunk;
+        bp.rows = idx_rows;
         bp.n_obs = P->n_obs;
         bp.n_modes = nm;
         bp.slice_bins = (int32_t)P->time_stride;
@@ -568,12 +576,12 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
             fold_grid = (int)std::max<int64_t>(1, std::min<int64_t>((chunk + 16383) / 16384, ctx->num_sms));
         }
         p.obs_idx = static_cast<int32_t *>(ctx->idx.p);
-        p.obs_rows = chunk;
+        p.obs_rows = idx_rows;
     }
     int le = 0, launches = 0;
     double kms = 0, fms = 0;
     if (n_pipe) {
-        const size_t slot_elems = (size_t)chunk * P->n_obs;
+        const size_t slot_elems = (size_t)idx_rows * P->n_obs;
         int32_t *idx0 = static_cast<int32_t *>(ctx->idx.p);
         int c = 0;
         for (int64_t base = 0; base < P->n_particles && !le; base += chunk, ++c) {
@@ -581,7 +589,7 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
             q.pid0 = P->pid0 + base;
             q.n_particles = std::min<int64_t>(chunk, P->n_particles - base);
             q.obs_idx = idx0 + (c & 1) * slot_elems;
-            q.obs_rows = chunk;
+            q.obs_rows = idx_rows;
             if (p.trace) q.trace = p.trace + 16 * base;
             if (c >= 2) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_b1[c - 2], 0), "pipeline wait");
             CK(cudaEventRecord(ctx->ev_a0[c], ctx->stream), "event");
@@ -592,7 +600,7 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
             CK(cudaStreamWaitEvent(ctx->fold_stream, ctx->ev_a1[c], 0), "pipeline wait");
             BinParams b = bp;
             b.idx = q.obs_idx;
-            b.rows = chunk;
+            b.rows = idx_rows;
             b.n = q.n_particles;
             if (b.group) b.part_per_block = (b.n + fold_grid - 1) / fold_grid;
             CK(cudaEventRecord(ctx->ev_b0[c], ctx->fold_stream), "event");
@@ -1023,7 +1031,7 @@ int forward_noalloc(const rtmc_problem *P, const rtmc_tables *t, int64_t *d_hist
     p.ring_cap = sizeof(R) == 4 ? 8 : 6;
     p.obs_idx = reinterpret_cast<int32_t *>(base + i_off);
     const int64_t chunk = std::min<int64_t>(std::max<int64_t>(P->n_particles, 1), rows);
-    p.obs_rows = chunk;
+    p.obs_rows = index_row_stride(chunk); // <= rows, a multiple of 32
     int block = 256;
     const int mt = transport_max_threads(prec, kSinkIndex, p.obs_kind);
     if (mt > 0 && block > mt) block = mt - mt % 32;
@@ -1036,7 +1044,7 @@ int forward_noalloc(const rtmc_problem *P, const rtmc_tables *t, int64_t *d_hist
     const int64_t grid = std::max<int64_t>(1, std::min<int64_t>((int64_t)sms * bps, (chunk + block - 1) / block));
     BinParams bp{};
     bp.idx = p.obs_idx;
-    bp.rows = chunk;
+    bp.rows = p.obs_rows;
     bp.n_obs = P->n_obs;
     bp.n_modes = P->acoustics ? 1 : 2;
     bp.slice_bins = (int32_t)P->time_stride;
