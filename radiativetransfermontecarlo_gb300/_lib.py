@@ -155,8 +155,14 @@ def check(status: int, ctx=None):
         raise RtmcError(f"librtmc error {status}: {msg.decode() if msg else ''}")
 
 
+def _need(ok: bool, what: str):
+    """Argument check that survives python -O: the library writes through these buffers."""
+    if not ok:
+        raise ValueError(what)
+
+
 def dptr(a: np.ndarray):
-    assert a.dtype == np.float64 and a.flags.c_contiguous
+    _need(a.dtype == np.float64 and a.flags.c_contiguous, "expected a contiguous float64 array")
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
 
@@ -179,6 +185,8 @@ class Tables:
         n = len(knots)
         cs = [np.ascontiguousarray(c, dtype=np.float64) for c, _ in knots]
         ts = [np.ascontiguousarray(t, dtype=np.float64) for _, t in knots]
+        _need(all(c.ndim == 1 and c.shape == t.shape for c, t in zip(cs, ts)),
+              "each table needs as many theta values as CDF knots")
         nk = (C.c_int64 * n)(*[len(c) for c in cs])
         cp = (C.POINTER(C.c_double) * n)(*[dptr(c) for c in cs])
         tp = (C.POINTER(C.c_double) * n)(*[dptr(t) for t in ts])
@@ -244,7 +252,8 @@ class Context:
         """Run the transport; returns (int64 histogram on the host, stats dict)."""
         if out is None:
             out = np.empty(problem.hist_len, dtype=np.int64)
-        assert out.dtype == np.int64 and out.size >= problem.hist_len and out.flags.c_contiguous
+        _need(out.dtype == np.int64 and out.size >= problem.hist_len and out.flags.c_contiguous,
+              "out must be a contiguous int64 array of at least hist_len elements")
         st = RtmcStats()
         check(self.lib.rtmc_forward(self.handle, C.byref(problem), tables.handle,
                                     out.ctypes.data_as(C.POINTER(C.c_int64)), C.byref(st)), self.handle)
@@ -255,7 +264,8 @@ class Context:
         stats dict)."""
         if out is None:
             out = np.empty(problem.hist_len, dtype=np.uint32)
-        assert out.dtype == np.uint32 and out.size >= problem.hist_len and out.flags.c_contiguous
+        _need(out.dtype == np.uint32 and out.size >= problem.hist_len and out.flags.c_contiguous,
+              "out must be a contiguous uint32 array of at least hist_len elements")
         st = RtmcStats()
         check(self.lib.rtmc_forward_u32(self.handle, C.byref(problem), tables.handle,
                                         out.ctypes.data_as(C.POINTER(C.c_uint32)), C.byref(st)), self.handle)
@@ -277,7 +287,8 @@ class Context:
         Returns (grad [n_params], stats)."""
         dls = np.ascontiguousarray(dlogsigma, dtype=np.float64)
         adj = np.ascontiguousarray(adjoint, dtype=np.float64).ravel()
-        assert dls.ndim == 2 and adj.size == problem.hist_len
+        _need(dls.ndim == 2 and adj.size == problem.hist_len,
+              "dlogsigma must be [n_params, n_theta] and adjoint hold hist_len weights")
         sc = RtmcScore()
         sc.n_params, sc.n_theta = dls.shape
         sc.dlogsigma = dptr(dls)
@@ -295,6 +306,7 @@ class Context:
         return st.as_dict()
 
     def copy_histogram(self, out: np.ndarray):
+        _need(out.dtype == np.int64 and out.flags.c_contiguous, "out must be a contiguous int64 array")
         check(self.lib.rtmc_copy_histogram(self.handle, out.ctypes.data_as(C.POINTER(C.c_int64)), out.size),
               self.handle)
         return out

@@ -1590,7 +1590,7 @@ extern "C" int rtmc_batch_run(rtmc_batch *b, rtmc_stats *st)
 
 extern "C" int rtmc_batch_histograms(rtmc_batch *b, int32_t first, int32_t count, int64_t *out)
 {
-    if (!b || !out || first < 0 || count < 0 || first + count > b->n)
+    if (!b || !out || first < 0 || count < 0 || (int64_t)first + count > b->n)
         return fail(b ? &b->ctx->err : nullptr, RTMC_ERR_ARG, "rtmc_batch_histograms: bad range");
     rtmc_context *ctx = b->ctx;
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
