@@ -449,6 +449,37 @@ def test_mode_conversion_kinetics_fp32():
     assert np.all(np.abs(frac - want) <= 4 * sig + 0.005), np.max(np.abs(frac - want))
 
 
+def test_3d_elastic_isotropic_matches_sato_fp32():
+    """Known answer on the GPU (FP32, 1e7 particles): total energy density of the P source
+    of Examples/IsotropicElastic3D.m against Sato's semi-analytical solution at r = 4.95
+    and 7.95 from 2.5 s to 10 s (see the oracle's test; here the Monte Carlo noise is about
+    0.4 %): mean ratio within 2.5 %, one-second averages within 4 %, samples within 5 %."""
+    from tests.test_oracle import sato_3d_energy
+    geo = {"dimension": 3}
+    mat = MaterialClass.preset(3)
+    d, K = 3, mat.vp / mat.vs
+    spp = sps = 0.2 * mat.vp
+    ssp = sps / ((d - 1) * K ** d)
+    sss = spp + sps - ssp
+    mat.sigma = [[spp / (4 * math.pi), sps / (4 * math.pi)], [ssp / (4 * math.pi), sss / (4 * math.pi)]]
+    obs = {"x": colon(0, 0.1, 20), "y": [-math.pi, math.pi], "z": [-math.pi / 2, math.pi / 2],
+           "directions": [0, math.pi], "time": colon(0, 0.1, 10)}
+    prob, grid, N = build_problem(geo, {"lambda": 0.002, "polarization": "P", "numberParticles": 10_000_000}, mat,
+                                  obs, {"exact_count": True, "precision": "fp32", "seed": 41})
+    P, keep = prob.to_ctypes()
+    h, st = get_context(0).forward_u32(P, prob.tables)
+    assert st["device_status"] == 0
+    dens, energy = normalise(h, grid, N)
+    r, t = np.asarray(grid.obs["x"]), np.asarray(grid.t)
+    rows, cols = [49, 79], t >= 2.5 - 1e-9
+    want = sato_3d_energy(mat.vp, mat.vs, spp, sps, ssp, sss, r[rows], t[cols])
+    ratio = (dens[rows, 0][:, cols, 0] + dens[rows, 0][:, cols, 1]) / want
+    assert abs(ratio.mean() - 1) < 0.025, ratio.mean()
+    windows = ratio[:, : ratio.shape[1] // 10 * 10].reshape(2, -1, 10).mean(axis=2)
+    assert np.all(np.abs(windows - 1) < 0.04), windows
+    assert np.all(np.abs(ratio - 1) < 0.05), np.abs(ratio - 1).max()
+
+
 def test_3d_isotropic_scattering_matches_paasschens_fp32():
     """Known answer at 1e7 particles on the GPU (FP32, large time steps): radial energy of
     3D isotropic acoustic scattering against Paasschens' approximate solution, with the
