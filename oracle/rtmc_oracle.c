@@ -5,9 +5,10 @@
  * only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it, as the
  * checker.  The reference (cottereau/RadiativeTransferMonteCarlo) is MATLAB and cannot
  * run here; parity against it is therefore pinned by known answers (energy conservation,
- * Zoeppritz energy balance, the boundary energy partition, equipartition, Paasschens)
- * rather than by reference outputs: "parity unpinned" against reference-produced
- * vectors, which do not exist.
+ * Zoeppritz energy balance, the boundary energy partition, equipartition and P/S
+ * conversion kinetics, Paasschens' 2D and 3D solutions and the diffusion limit, Sato's 3D
+ * elastic solution) rather than by reference outputs: "parity unpinned" against
+ * reference-produced vectors, which do not exist.
  *
  * Two restatements of the reference transport are provided:
  *
