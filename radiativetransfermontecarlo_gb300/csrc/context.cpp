@@ -1046,6 +1046,8 @@ int forward_noalloc(const rtmc_problem *P, const rtmc_tables *t, int64_t *d_hist
     bp.idx = p.obs_idx;
     bp.rows = p.obs_rows;
     bp.n_obs = P->n_obs;
+    bp.j_first = 1; // every slice (large slices take rt_bin_slices, which reads the range)
+    bp.j_count = P->n_obs;
     bp.n_modes = P->acoustics ? 1 : 2;
     bp.slice_bins = (int32_t)P->time_stride;
     bp.time_stride = P->time_stride;

@@ -1677,8 +1677,18 @@ int launch_bin_slices(const BinParams &b, int grid_x, size_t smem, void *stream)
         rt_bin_slices_smem<<<g, 512, smem, (cudaStream_t)stream>>>(b);
     } else {
         if (b.j_first < 1 || b.j_count < 1 || b.j_first + b.j_count - 1 > b.n_obs) return (int)cudaErrorInvalidValue;
-        dim3 g(grid_x, b.j_count);
-        rt_bin_slices<<<g, kFoldThreads, 0, (cudaStream_t)stream>>>(b);
+        // one slice per blockIdx.y, at most 65535 of them per launch
+        constexpr int kMaxGridY = 65535;
+        for (int done = 0; done < b.j_count; done += kMaxGridY) {
+            BinParams c = b;
+            c.j_first = b.j_first + done;
+            c.j_count = b.j_count - done < kMaxGridY ? b.j_count - done : kMaxGridY;
+            dim3 g(grid_x, c.j_count);
+            rt_bin_slices<<<g, kFoldThreads, 0, (cudaStream_t)stream>>>(c);
+            const cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) return (int)e;
+        }
+        return 0;
     }
     return (int)cudaGetLastError();
 }

@@ -59,3 +59,20 @@ def test_noalloc_rejects_problems_beyond_the_static_array():
     assert rc == 1  # RTMC_ERR_ARG
     assert b"static scratch" in _lib.load().rtmc_last_error(None)
     assert int(out.abs().sum().item()) == 0  # nothing was written
+
+
+def test_noalloc_large_slices():
+    """C2's 4-axis grid (13.8 MB slices): the fold runs one slice per block row
+    (rt_bin_slices) over the whole slice range; equal to rtmc_forward bin for bin."""
+    torch = pytest.importorskip("torch")
+    geo, src, mat, obs, opts = W.c2_elastic3d(t_end=1.0)
+    prob, grid, N = build_problem(geo, dict(src, numberParticles=1001), mat, obs, dict(opts, exact_count=True))
+    P, keep = prob.to_ctypes()
+    ref, ref_stats = get_context(0).forward(P, prob.tables)
+    out = torch.empty(prob.hist_len, dtype=torch.int64, device="cuda:0")
+    torch.cuda.synchronize()
+    st = _lib.RtmcStats()
+    _lib.check(_lib.load().rtmc_forward_noalloc(C.byref(P), prob.tables.handle, C.c_void_p(out.data_ptr()), None,
+                                                C.byref(st)))
+    assert st.device_status == 0 and st.observations == ref_stats["observations"]
+    assert np.array_equal(out.cpu().numpy(), ref)
