@@ -87,23 +87,26 @@ def test_equipartition_elastic_3d():
     assert abs(ratio - want) / want < 0.05
 
 
-def test_mode_conversion_kinetics_elastic_3d():
+@pytest.mark.parametrize("d", [3, 2])
+def test_mode_conversion_kinetics_elastic(d):
     """Known answer for P/S conversion by isotropic scattering: with every particle inside
     the grid the P fraction obeys dP/dt = -S_ps P + S_sp (1 - P), so from a P source
     P(t) = P_eq + (1 - P_eq) exp(-(S_ps + S_sp) t) with P_eq = S_sp / (S_ps + S_sp) (the
-    long-time limit is the equipartition ratio above), at every observation time."""
-    geo = {"dimension": 3}
+    long-time limit is the equipartition ratio above), at every observation time; 3D and
+    2D (S_sp = S_ps / ((d - 1) K^d), Examples/IsotropicElastic2D.m:25-29)."""
+    geo = {"dimension": d}
     mat = MaterialClass.preset(3)
-    d, K = 3, mat.vp / mat.vs
+    K = mat.vp / mat.vs
     spp = sps = 0.2 * mat.vp
     ssp = sps / ((d - 1) * K ** d)
     sss = spp + sps - ssp
-    mat.sigma = [[spp / (4 * math.pi), sps / (4 * math.pi)], [ssp / (4 * math.pi), sss / (4 * math.pi)]]
+    w = 4 * math.pi if d == 3 else 2 * math.pi  # isotropic: Sigma = (solid angle) x sigma
+    mat.sigma = [[spp / w, sps / w], [ssp / w, sss / w]]
     n = 40_000
     obs = {"x": colon(0, 1, 100), "time": colon(0, 0.1, 6)}
     prob, grid, N = build_problem(geo, {"lambda": 0.002, "polarization": "P", "numberParticles": n}, mat, obs,
                                   {"exact_count": True, "precision": "fp64"})
-    S_ps, S_sp = sps, ssp  # 4 pi sigma of the isotropic cross-sections
+    S_ps, S_sp = sps, ssp  # (solid angle) x sigma of the isotropic cross-sections
     h, st, _ = O.run(prob, O.table_knots(prob.tables), scheme="event")
     e = h.reshape(grid.shape, order="F").sum(axis=(0, 1)).astype(float)
     t = np.asarray(grid.t)[1:]
