@@ -13,7 +13,8 @@ int64 fixed-point histogram (2^-40).  One step = one whole simulation of that wo
 Prints one JSON line.  `value` is device time (CUDA events on the library's stream);
 `e2e` times rtmc_forward through the C ABI with host buffers (tables uploaded and the
 histogram copied to pinned host memory every step).  `--impl reference` times the CPU
-restatement of the reference's own sub-step algorithm on the host cores.
+restatement of the reference's own sub-step algorithm on the host cores, on a problem and
+tables set up by the oracle itself (oracle/reference_problem.py), so it loads no product code.
 """
 from __future__ import annotations
 
@@ -147,14 +148,14 @@ def cpu_sample(prob, knots, target_s: float = 12.0, threads: int | None = None, 
         n = 4000
         while True:  # calibrate the time per particle
             t0 = time.perf_counter()
-            O.run(prob, knots, scheme="substep", u24=False, nthreads=nth, n_particles=n, pid0=0, hist=hist)
+            O.run(prob, knots, scheme="substep", ufloat=False, nthreads=nth, n_particles=n, pid0=0, hist=hist)
             dt = time.perf_counter() - t0
             if dt > 1.0 or n >= 1_000_000:
                 break
             n *= 4
         n2 = int(min(4_000_000, max(n, target_s * n / dt)))
     t0 = time.perf_counter()
-    _, st, _ = O.run(prob, knots, scheme="substep", u24=False, nthreads=nth, n_particles=n2, pid0=10_000_000,
+    _, st, _ = O.run(prob, knots, scheme="substep", ufloat=False, nthreads=nth, n_particles=n2, pid0=10_000_000,
                      hist=hist)
     dt = time.perf_counter() - t0
     N = int(prob.n_particles)
@@ -196,14 +197,11 @@ def rel_l2_density(a: np.ndarray, b: np.ndarray, grid, chunk_bins: int) -> float
 def run_reference_arm(args, rank, world):
     if rank != 0:
         return None
-    from oracle import oracle as O
-    from radiativetransfermontecarlo_gb300 import build_problem
-    from radiativetransfermontecarlo_gb300 import workloads as W
-    geo, src, mat, obs, opts = W.c2_elastic3d(precision="fp64")
-    prob, grid, N = build_problem(geo, src, mat, obs, dict(opts, exact_count=True))
-    knots = O.table_knots(prob.tables)
+    # the oracle's own problem set-up and table builder: this arm loads no product code
+    from oracle import reference_problem
+    prob, knots = reference_problem.c2_problem()
     nth = os.cpu_count() or 1
-    per_step = max(2.0, 120.0 / max(1, args.steps + args.warmup))
+    per_step = args.ref_seconds or max(2.0, 120.0 / max(1, args.steps + args.warmup))
     hist, fixed = cpu_histogram(prob)
     times, full_events, full_seconds, nparts, particles = [], 0.0, 0.0, 0, None
     for i in range(args.warmup + args.steps):
@@ -344,6 +342,12 @@ def run_our_arm(args, rank, world, dist):
                     "ms_per_step_median": 1000 * float(np.median(times))}
         result["e2e"] = dict(e2e_leg(ctx.forward_u32, buf.array(np.uint32, prob.hist_len)),
                              api="rtmc_forward_u32 (uint32 counts, the reference's E type)")
+        # the same call into pageable host memory, which is what a MEX gateway receives from
+        # mxCreateNumericMatrix (the first, untimed call touches its pages)
+        pageable = np.empty(prob.hist_len, dtype=np.uint32)
+        result["e2e_pageable"] = dict(e2e_leg(ctx.forward_u32, pageable),
+                                      api="rtmc_forward_u32 into pageable host memory (a MEX gateway's mxArray)")
+        del pageable
         result["e2e_int64"] = dict(e2e_leg(ctx.forward, buf.array(np.int64, prob.hist_len)),
                                    api="rtmc_forward (int64 fixed point, 2^-40)")
         # the host link alone: one plain device-to-host copy of the histogram, as a yardstick
@@ -431,7 +435,7 @@ def run_c4(args):
             "autotune_ms": {f"{b}x{r}x{c}": t for (b, r, c), t in tune.items()}}
     if not args.no_cpu:
         prob = batch.problems[int(np.argmax(batch.N))]
-        line["cpu_baseline"] = baseline_fields(cpu_sample(prob, O.table_knots(prob.tables)))
+        line["cpu_baseline"] = baseline_fields(cpu_sample(prob, O.table_knots(prob.tables), target_s=args.cpu_seconds))
         line["cpu_baseline"]["sample"] = "the largest instance, " + line["cpu_baseline"]["sample"]
     batch.close()
     return line
@@ -460,10 +464,12 @@ def run_c1(args):
                 ms.append(st["total_ms"])
                 ev += st["scatter_events"]
         h, st1 = ctx.forward(P, prob.tables)
+        dens, energy = normalise(h, grid, N)
         out[prec] = {"value": ev / (sum(ms) / 1000.0), "ms": float(np.mean(ms)), "clocks": clk.summary(),
-                     "energy": normalise(h, grid, N)[1], "obs": st1["observations"], "sink": st1["sink"],
+                     "energy": energy, "density": dens, "obs": st1["observations"], "sink": st1["sink"],
                      "prob": prob}
     e64, e32 = out["fp64"]["energy"], out["fp32"]["energy"]
+    d64, d32 = out["fp64"]["density"], out["fp32"]["density"]
     line = {"metric": METRIC, "value": out["fp64"]["value"], "unit": UNIT, "n_gpus": 1, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": out["fp64"]["ms"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -471,12 +477,14 @@ def run_c1(args):
                                    "lambda=0.05, 1e6 particles, spherical 120 r x 251 t", "particles": n},
             "gpu_launches": args.steps, "clocks": out["fp64"]["clocks"], "sink": out["fp64"]["sink"],
             "fp32": {"value": out["fp32"]["value"], "ms_per_step": out["fp32"]["ms"]},
+            "fp32_over_fp64": out["fp32"]["value"] / out["fp64"]["value"],
+            "rel_l2_energy_density_fp32_vs_fp64": float(np.linalg.norm(d32 - d64) / np.linalg.norm(d64)),
             "energy_conserved_fp64": bool(np.all(e64[1:, 0] == 1.0)), "energy_conserved_fp32": bool(np.all(e32[1:, 0] == 1.0))}
     if not args.no_cpu:
         prob = out["fp64"]["prob"]
         nth = os.cpu_count() or 1
         t0 = time.perf_counter()
-        _, st, _ = O.run(prob, O.table_knots(prob.tables), scheme="substep", u24=False, nthreads=nth)
+        _, st, _ = O.run(prob, O.table_knots(prob.tables), scheme="substep", ufloat=False, nthreads=nth)
         dt = time.perf_counter() - t0
         line["cpu_baseline"] = {"value": st["scatter_events"] / dt, "unit": UNIT, "cores": nth, "kind": "port",
                                 "sample": f"the whole workload ({n} particles, 250 sub-steps each), reference sub-step "
@@ -544,7 +552,7 @@ def run_c3(args):
                                           "per_bin_diff_over_sqrt_count_p99": float(np.quantile(np.abs(z), 0.99)),
                                           "bins": int(m.sum())}}
     if not args.no_cpu:
-        line["cpu_baseline"] = baseline_fields(cpu_sample(prob, O.table_knots(prob.tables), target_s=12.0))
+        line["cpu_baseline"] = baseline_fields(cpu_sample(prob, O.table_knots(prob.tables), target_s=args.cpu_seconds))
     return line
 
 
@@ -604,6 +612,34 @@ def run_c5(args):
     return line
 
 
+def sub_records(args):
+    """Compact records of the other four workloads (C1 3D acoustic FP64 and FP32, C3
+    half-space, C4 batched sweep, C5 gradient), each measured as its own --workload run
+    does with fewer steps and shorter CPU samples."""
+    import copy
+    out = {}
+    keep = ("value", "unit", "ms_per_step", "clocks", "fp32", "fp32_over_fp64", "rel_l2_energy_density_fp32_vs_fp64",
+            "energy_conserved_fp64", "energy_conserved_fp32", "events_per_step", "fp64_vs_fp32_same_1e7_ids",
+            "cpu_baseline", "e2e", "launch_shape", "forward_ms", "adjoint_ms", "rel_error_scaled_vector_1e-3",
+            "rel_error_per_param_1e-3", "scattering_events_per_s", "metric", "config")
+    for name, fn, steps in (("c1", run_c1, 5), ("c3", run_c3, 2), ("c4", run_c4, 3), ("c5", run_c5, 2)):
+        a = copy.copy(args)
+        a.steps, a.warmup, a.cpu_seconds = steps, 2, 4.0
+        a.particles = 10_000_000  # each workload's own default count
+        t0 = time.perf_counter()
+        try:
+            line = fn(a)
+            rec = {k: line[k] for k in keep if k in line}
+            if "cpu_baseline" in rec:
+                rec["cpu_baseline"] = {k: rec["cpu_baseline"][k] for k in ("value", "unit", "cores", "kind")}
+            rec["seconds"] = time.perf_counter() - t0
+            out[name] = rec
+        except Exception as e:  # one failing record must not take the headline line with it
+            out[name] = {"error": f"{type(e).__name__}: {e}"}
+        log(f"sub-record {name}: {time.perf_counter() - t0:.1f} s")
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -618,26 +654,34 @@ def main():
     ap.add_argument("--chunks", type=int, default=0, help="transport/fold pipeline chunks (0: automatic, 1: off)")
     ap.add_argument("--schedule", type=int, default=-1, help="-1 automatic, 0 lockstep warp batches, 1 particle per thread")
     ap.add_argument("--k1-bps", type=int, default=0, help="transport blocks per SM while pipelined (0: automatic)")
+    ap.add_argument("--ref-seconds", type=float, default=0.0,
+                    help="reference arm: seconds of CPU work per step (0: about 120 s over all steps)")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-accuracy", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="seconds of each CPU-baseline sample")
+    ap.add_argument("--no-sub", action="store_true",
+                    help="skip the compact C1/C3/C4/C5 records that the default C2 line carries")
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],
                     help="c2: the headline line (default); c1: 3D acoustic FP64; c3: 2D half-space; "
                          "c4: batched sweep; c5: gradient")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.impl == "reference" and args.workload == "c2":
+        # the reference arm runs the oracle alone: build it, and nothing of the product
+        from oracle import oracle as O
+        O.build()
+        line = run_reference_arm(args, rank, world)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return
     import __graft_entry__
     __graft_entry__.build()
     if args.workload != "c2":
         if rank == 0:
             line = {"c1": run_c1, "c3": run_c3, "c4": run_c4, "c5": run_c5}[args.workload](args)
-            print(json.dumps(line), flush=True)
-        return
-    if args.impl == "reference":
-        line = run_reference_arm(args, rank, world)
-        if line is not None:
             print(json.dumps(line), flush=True)
         return
     dist = None
@@ -648,6 +692,8 @@ def main():
         td.init_process_group("nccl")
         dist = td
     line = run_our_arm(args, rank, world, dist)
+    if rank == 0 and not args.no_sub and world == 1:
+        line["workloads"] = sub_records(args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist is not None:

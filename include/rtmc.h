@@ -133,8 +133,13 @@ typedef struct {
     int32_t n_sub;        /* sub-steps per observation interval (propagateParticleSmallDt.m:4-7) */
     int32_t n_obs;        /* observation instants = Nt - 1 (t = 0 is never filled) */
     int32_t n_bnd;        /* plane boundaries, <= RTMC_MAX_BND */
-    int32_t hist_shift;   /* a unit count adds 1 << hist_shift (int64 fixed point) */
-    int32_t reserved[2];
+    int32_t hist_shift;   /* a unit count adds 1 << hist_shift (64-bit fixed point); a bin of one
+                             time slice holds at most n_particles counts, so n_particles must
+                             stay below 2^(64 - hist_shift) (checked) */
+    int32_t max_events;   /* per-particle event cap, a watchdog with no counterpart in the
+                             reference: a particle reaching it stops and the call returns
+                             RTMC_ERR_DEVICE (device_status bit 0); 0 = 4 n_sub n_obs + 64 */
+    int32_t reserved;
     int64_t n_particles;
     int64_t pid0;         /* global id of the first particle (replica sharding) */
     uint64_t seed;
@@ -284,6 +289,13 @@ int rtmc_batch_set_launch(rtmc_batch *batch, int32_t block, int32_t ring_cap, in
 
 /* One replay of the graph; histograms stay on the device.  stats sums all instances. */
 int rtmc_batch_run(rtmc_batch *batch, rtmc_stats *stats);
+
+/* Which kernel runs each instance: event_major[i] = 1 for the event-major kernel
+ * (rt_transport_batch_em: one particle per thread, 64-bit atomics into the instance's
+ * histogram; event-heavy instances), 0 for the lockstep kernel with a shared-memory
+ * histogram (rt_transport_batch).  event_major holds one int32 per instance.  A launch of
+ * the batch runs one kernel per non-empty group (rtmc_stats.launches). */
+int rtmc_batch_schedule(const rtmc_batch *batch, int32_t *event_major);
 
 /* Copies the int64 histograms of instances [first, first + count) into out (host),
  * instance-major, hist_len each. */

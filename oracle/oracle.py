@@ -34,7 +34,7 @@ def build(force: bool = False) -> Path:
 
 class OracleProblem(C.Structure):
     _fields_ = [("d", C.c_int32), ("frame", C.c_int32), ("acoustics", C.c_int32), ("scheme", C.c_int32),
-                ("u24", C.c_int32), ("src_dir", C.c_int32), ("polarization", C.c_int32), ("n_sub", C.c_int32),
+                ("ufloat", C.c_int32), ("src_dir", C.c_int32), ("polarization", C.c_int32), ("n_sub", C.c_int32),
                 ("n_obs", C.c_int32), ("n_bnd", C.c_int32), ("hist_shift", C.c_int32), ("nthreads", C.c_int32),
                 ("n_particles", C.c_int64), ("pid0", C.c_int64), ("seed", C.c_uint64),
                 ("src_pos", C.c_double * 3), ("src_lambda", C.c_double), ("v", C.c_double * 2),
@@ -48,7 +48,8 @@ class OracleProblem(C.Structure):
                 ("tab_theta", C.POINTER(C.c_double) * 4), ("src_type", C.c_int32), ("src_aperture", C.c_int32),
                 ("src_radial_n", C.c_int64), ("src_radial_cdf", C.POINTER(C.c_double)),
                 ("src_radial_r", C.POINTER(C.c_double)), ("src_normal", C.c_double * 3), ("src_u", C.c_double * 3),
-                ("src_v", C.c_double * 3), ("src_extent", C.c_double * 2)]
+                ("src_v", C.c_double * 3), ("src_extent", C.c_double * 2),
+                ("cross_margin", C.POINTER(C.c_double))]
 
 
 _lib = None
@@ -90,16 +91,23 @@ def philox(ctr, key):
     return list(o)
 
 
-def run(prob, knots, scheme: str = "event", u24: bool | None = None, nthreads: int | None = None,
+def run(prob, knots, scheme: str = "event", ufloat: bool | None = None, nthreads: int | None = None,
         n_particles: int | None = None, pid0: int | None = None, want_state: bool = False,
-        hist: np.ndarray | None = None):
+        hist: np.ndarray | None = None, margins: np.ndarray | None = None):
     """Run the oracle on a TransportProblem-like object with the given table knots
     [(cdf, theta), ...].  scheme 'substep' (reference order) or 'event' (snap, GPU stream).
     hist, if given, is an int64 array of hist_len that the run adds into (timing runs
     reuse one, so allocation and first-touch page faults stay out of the particles' time).
+    margins, if given, is a float64 array of n_particles that the event scheme fills with
+    each particle's smallest plane-crossing margin (distance of the deciding sub-step
+    position from the plane; inf without crossings).
     Returns (int64 histogram, stats dict, final states [N,16] or None)."""
     lib = load()
-    P, keep = _problem(prob, knots, scheme, u24, nthreads, n_particles, pid0)
+    P, keep = _problem(prob, knots, scheme, ufloat, nthreads, n_particles, pid0)
+    if margins is not None:
+        if margins.dtype != np.float64 or margins.size != P.n_particles or not margins.flags.c_contiguous:
+            raise ValueError("margins must be a contiguous float64 array of n_particles")
+        P.cross_margin = _dp(margins)
     if hist is None:
         hist = np.zeros(prob.hist_len, dtype=np.int64)
     elif hist.dtype != np.int64 or hist.size != prob.hist_len or not hist.flags.c_contiguous:
@@ -113,11 +121,11 @@ def run(prob, knots, scheme: str = "event", u24: bool | None = None, nthreads: i
     return hist, dict(zip(ST_NAMES, map(int, stats[:6]))), fs
 
 
-def gradient(prob, knots, dlogsigma, dlogSigma, adjoint, u24: bool | None = None, nthreads: int | None = None):
+def gradient(prob, knots, dlogsigma, dlogSigma, adjoint, ufloat: bool | None = None, nthreads: int | None = None):
     """Score-function gradient by the event scheme (the restatement of rtmc_gradient):
     returns (grad [n_params], stats).  prob must be acoustic with qrate = 0."""
     lib = load()
-    P, keep = _problem(prob, knots, "event", u24, nthreads, None, None)
+    P, keep = _problem(prob, knots, "event", ufloat, nthreads, None, None)
     dls = np.ascontiguousarray(dlogsigma, dtype=np.float64)
     adj = np.ascontiguousarray(adjoint, dtype=np.float64).ravel()
     hS = prob.h / prob.mft[0] if math.isfinite(prob.mft[0]) else 0.0
@@ -134,12 +142,12 @@ def gradient(prob, knots, dlogsigma, dlogSigma, adjoint, u24: bool | None = None
     return grad, dict(zip(ST_NAMES, map(int, stats[:6])))
 
 
-def _problem(prob, knots, scheme, u24, nthreads, n_particles, pid0):
+def _problem(prob, knots, scheme, ufloat, nthreads, n_particles, pid0):
     lib = load()
     P = OracleProblem()
     P.d, P.frame, P.acoustics = prob.d, prob.frame, int(prob.acoustics)
     P.scheme = 0 if scheme == "substep" else 1
-    P.u24 = int(prob.precision == 0) if u24 is None else int(u24)
+    P.ufloat = int(prob.precision == 0) if ufloat is None else int(ufloat)
     P.src_dir, P.polarization, P.n_sub, P.n_obs = prob.src_dir, prob.polarization, prob.n_sub, prob.n_obs
     P.n_bnd, P.hist_shift = len(prob.bnd), prob.hist_shift
     P.nthreads = nthreads or max(1, lib.oracle_max_threads())

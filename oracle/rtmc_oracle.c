@@ -31,7 +31,8 @@
  * Random numbers: Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11), counter =
  * (pid_lo, pid_hi, step, block), key = (seed_lo, seed_hi ^ stream).  A 32-bit output x
  * maps to u = (x + 0.5) * 2^-32 ("u32" mode) or, to reproduce the FP32 GPU path's
- * uniforms, u = ((x >> 8) + 0.5) * 2^-24 ("u24" mode).
+ * uniforms, u = ((x >> 9) + 0.5) * 2^-23 ("ufloat" mode: 24 significant bits, so the
+ * value is exact in float and the FP32 kernels see the same number).
  */
 #include <math.h>
 #include <stdint.h>
@@ -52,7 +53,7 @@ typedef struct {
     int32_t frame;        /* 0 cartesian, 1 cylindrical, 2 spherical */
     int32_t acoustics;    /* 1 acoustic, 0 elastic */
     int32_t scheme;       /* 0 substep, 1 event */
-    int32_t u24;          /* 1: 24-bit uniforms (FP32 GPU stream) */
+    int32_t ufloat;       /* 1: 23-bit uniforms exact in float (FP32 GPU stream) */
     int32_t src_dir;      /* 0 uniform, 1 outgoing, 2 upper */
     int32_t polarization; /* 0 P, 1 S */
     int32_t n_sub;        /* sub-steps per observation interval */
@@ -96,6 +97,11 @@ typedef struct {
     const double *src_radial_r;
     double src_normal[3], src_u[3], src_v[3];
     double src_extent[2];
+    /* optional [n_particles] output of the event scheme: the smallest distance, over the
+     * plane-crossing decisions that fix the particle's next event, between the sub-step
+     * position that decides the crossing and the plane (length units).  A float
+     * trajectory whose position error exceeds it may cross one sub-step earlier or later. */
+    double *cross_margin;
 } oracle_problem;
 
 enum { ST_SCATTER = 0, ST_BOUNDARY, ST_KILL, ST_ABSORB, ST_OBS, ST_CONVERT, ST_N };
@@ -130,7 +136,7 @@ void oracle_philox4x32_10(const uint32_t *ctr, const uint32_t *key, uint32_t *ou
 typedef struct {
     uint32_t key[2];
     uint64_t pid;
-    int u24;
+    int ufloat;
 } rng_t;
 
 static inline void rng_block(const rng_t *g, uint32_t step, uint32_t block, double u[4])
@@ -139,8 +145,8 @@ static inline void rng_block(const rng_t *g, uint32_t step, uint32_t block, doub
     uint32_t o[4];
     philox4x32_10(ctr, g->key, o);
     for (int i = 0; i < 4; ++i) {
-        if (g->u24)
-            u[i] = ((double)(o[i] >> 8) + 0.5) * (1.0 / 16777216.0);
+        if (g->ufloat)
+            u[i] = ((double)(o[i] >> 9) + 0.5) * (1.0 / 8388608.0);
         else
             u[i] = ((double)o[i] + 0.5) * (1.0 / 4294967296.0);
     }
@@ -595,7 +601,7 @@ static void run_substep(const oracle_problem *P, int64_t pid, int64_t *hist, int
     g.key[0] = (uint32_t)P->seed;
     g.key[1] = (uint32_t)(P->seed >> 32) ^ 0x5u; /* stream 5: sub-step scheme */
     g.pid = (uint64_t)pid;
-    g.u24 = P->u24;
+    g.ufloat = P->ufloat;
     particle_t pt;
     double ub1[4];
     init_particle(P, &g, &pt, ub1);
@@ -719,7 +725,7 @@ static void run_event(const oracle_problem *P, int64_t pid, int64_t *hist, int u
     g.key[0] = (uint32_t)P->seed;
     g.key[1] = (uint32_t)(P->seed >> 32);
     g.pid = (uint64_t)pid;
-    g.u24 = P->u24;
+    g.ufloat = P->ufloat;
     particle_t pt;
     double ub1[4], ub2[4];
     init_particle(P, &g, &pt, ub1);
@@ -735,6 +741,10 @@ static void run_event(const oracle_problem *P, int64_t pid, int64_t *hist, int u
     int next_obs = 1; /* observation j at sub-step j*n_sub */
     uint32_t k = 0;   /* event counter (step index of the Philox counter) */
     int64_t nscat = 0, nbnd = 0;
+    double *margin = P->cross_margin ? P->cross_margin + (pid - P->pid0) : NULL;
+    int64_t cand[OR_MAX_BND];
+    double cmar[OR_MAX_BND];
+    if (margin) *margin = INFINITY;
     for (;;) {
         int m = pt.mode;
         double step = P->v[m] * P->h;
@@ -749,11 +759,23 @@ static void run_event(const oracle_problem *P, int64_t pid, int64_t *hist, int u
             int kk = P->bnd_dir[b] - 1;
             int64_t j = plane_cross_steps(pt.x[kk] - P->bnd_val[b], step * pt.d[kk], cap);
             if (j < cap && s0 + j < sB) sB = s0 + j;
+            if (margin && j < cap) {
+                /* |a| - (j - 1) |b|: how far the position after j - 1 sub-steps is from the plane */
+                double bb = fabs(step * pt.d[kk]), rem = fabs(pt.x[kk] - P->bnd_val[b]) - (double)(j - 1) * bb;
+                double mg = rem < bb - rem ? rem : bb - rem;
+                cand[b] = s0 + j;
+                cmar[b] = mg;
+            } else {
+                cand[b] = cap + 1;
+            }
         }
         int64_t e = sK;
         int kind = 2; /* 2 kill, 1 boundary, 0 scatter; ties resolve kill > boundary > scatter */
         if (sB < e) { e = sB; kind = 1; }
         if (sS < e) { e = sS; kind = 0; }
+        if (margin)
+            for (int b = 0; b < P->n_bnd; ++b) /* a crossing one sub-step off would change the event */
+                if (P->bnd_dir[b] != 4 && cand[b] <= e + 1 && cand[b] <= s_end && cmar[b] < *margin) *margin = cmar[b];
         if (e > s_end) { e = cap; kind = -1; }
         /* observations strictly before the event */
         while (next_obs <= P->n_obs && (int64_t)next_obs * P->n_sub < e) {

@@ -41,7 +41,7 @@ class RtmcTablesInfo(C.Structure):
 class RtmcProblem(C.Structure):
     _fields_ = [("d", C.c_int32), ("frame", C.c_int32), ("acoustics", C.c_int32), ("precision", C.c_int32),
                 ("src_dir", C.c_int32), ("polarization", C.c_int32), ("n_sub", C.c_int32), ("n_obs", C.c_int32),
-                ("n_bnd", C.c_int32), ("hist_shift", C.c_int32), ("reserved", C.c_int32 * 2),
+                ("n_bnd", C.c_int32), ("hist_shift", C.c_int32), ("max_events", C.c_int32), ("reserved", C.c_int32),
                 ("n_particles", C.c_int64), ("pid0", C.c_int64), ("seed", C.c_uint64),
                 ("src_pos", C.c_double * 3), ("src_lambda", C.c_double), ("v", C.c_double * 2),
                 ("mft", C.c_double * 2), ("p2p", C.c_double), ("s2s", C.c_double), ("qrate", C.c_double * 2),
@@ -115,6 +115,7 @@ SIGNATURES = {
     "rtmc_batch_set_launch": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int64]),
     "rtmc_batch_run": (C.c_int, [_P, C.POINTER(RtmcStats)]),
     "rtmc_batch_histograms": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_int64)]),
+    "rtmc_batch_schedule": (C.c_int, [_P, C.POINTER(C.c_int32)]),
     "rtmc_batch_destroy": (None, [_P]),
     "rtmc_last_timing": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
 }

@@ -57,6 +57,13 @@ class Batch:
         _lib.check(self.ctx.lib.rtmc_batch_run(self.handle, C.byref(st)), self.ctx.handle)
         return st.as_dict()
 
+    def schedule(self) -> np.ndarray:
+        """1 for the instances the event-major kernel runs, 0 for the lockstep kernel's."""
+        out = np.zeros(len(self.problems), dtype=np.int32)
+        _lib.check(self.ctx.lib.rtmc_batch_schedule(self.handle, out.ctypes.data_as(C.POINTER(C.c_int32))),
+                   self.ctx.handle)
+        return out
+
     def histograms(self, first: int = 0, count: int | None = None) -> np.ndarray:
         count = len(self.problems) - first if count is None else count
         out = np.empty((count, self.hist_len), dtype=np.int64)

@@ -1,7 +1,9 @@
 """Build recipe of librtmc.so (in-tree, sm_103a only).
 
-Three translation units compiled in parallel: transport.cu with nvcc for sm_103a, the
-host table builder and the context/C-ABI with g++; linked by nvcc into
+Translation units compiled in parallel: the transport kernel family (kernels.cu over
+transport.cuh, compiled once per precision and kernel group: transport, batched,
+adjoint), the slice fold (fold.cu) and the static scratch (noalloc.cu) with nvcc for
+sm_103a, the host table builder and the context/C-ABI with g++; linked by nvcc into
 radiativetransfermontecarlo_gb300/librtmc.so with the CUDA runtime linked statically.
 """
 from __future__ import annotations
@@ -30,7 +32,7 @@ def _cuda_home() -> Path:
 
 
 def _sources():
-    return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp")) + sorted(CSRC.glob("*.h")) + [PKG.parent / "include" / "rtmc.h"]
+    return sorted(CSRC.glob("*.cu")) + sorted(CSRC.glob("*.cpp")) + sorted(CSRC.glob("*.h")) + sorted(CSRC.glob("*.cuh")) + [PKG.parent / "include" / "rtmc.h"]
 
 
 def up_to_date() -> bool:
@@ -49,10 +51,20 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     inc = [f"-I{cuda / 'include'}", f"-I{PKG.parent / 'include'}"]
     jobs = []
     objs = []
+    units = []
     for cu in sorted(CSRC.glob("*.cu")):
-        o = BUILD / (cu.stem + ".o")
-        extra = os.environ.get("RTMC_NVCC_EXTRA", "").split()  # e.g. -DRTMC_TRANSPORT_MIN_BLOCKS=3
-        cmd = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", *extra, *inc, "-c", str(cu), "-o", str(o)]
+        if cu.name == "kernels.cu":
+            for real, suf in (("float", "f32"), ("double", "f64")):
+                for part in (1, 2, 3):
+                    units.append((cu, f"kernels_{suf}_{part}", [f"-DRTMC_REAL={real}", f"-DRTMC_SUFFIX={suf}",
+                                                                 f"-DRTMC_PART={part}"]))
+        else:
+            units.append((cu, cu.stem, []))
+    extra = os.environ.get("RTMC_NVCC_EXTRA", "").split()  # e.g. -DRTMC_TRANSPORT_MIN_BLOCKS=3
+    for cu, stem, defs in units:
+        o = BUILD / (stem + ".o")
+        cmd = [nvcc, ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", *defs, *extra, *inc, "-c", str(cu),
+               "-o", str(o)]
         if ptxas_info:
             cmd.insert(2, "-Xptxas=-v")
         jobs.append(cmd)

@@ -11,6 +11,7 @@
 #include <algorithm>
 #include <numeric>
 #include <cmath>
+#include <limits>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -53,6 +54,7 @@ struct rtmc_context {
     DevTables<float> tf{};
     DevTables<double> td{};
     int64_t hist_len = 0;
+    bool hist_may_exceed_int64 = false; // the last histogram may hold bins >= 2^63
     double last_kernel_ms = 0;
     int last_launches = 0;
     int cache_tables = 1;
@@ -193,6 +195,12 @@ int check_problem(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t
         return fail(e, RTMC_ERR_ARG, "n_sub * n_obs must stay below 2^30 sub-steps");
     if (P->n_particles < 0 || P->pid0 < 0) return fail(e, RTMC_ERR_ARG, "particle count and first id must be >= 0");
     if (P->hist_shift < 0 || P->hist_shift > 62) return fail(e, RTMC_ERR_ARG, "hist_shift must be in [0, 62]");
+    // one bin of one time slice receives at most one count per particle: its unsigned
+    // 64-bit fixed-point sum cannot wrap while n_particles < 2^(64 - hist_shift)
+    if (P->hist_shift >= 2 && P->n_particles >= ((int64_t)1 << (64 - P->hist_shift)))
+        return fail(e, RTMC_ERR_ARG,
+                    "n_particles << hist_shift could wrap a 64-bit histogram bin: keep n_particles below 2^(64 - hist_shift)");
+    if (P->max_events < 0) return fail(e, RTMC_ERR_ARG, "max_events must be >= 0 (0: automatic)");
     if (P->n_bnd < 0 || P->n_bnd > RTMC_MAX_BND) return fail(e, RTMC_ERR_ARG, "at most 4 boundaries");
     for (int b = 0; b < P->n_bnd; ++b) {
         if (P->bnd_dir[b] < 1 || P->bnd_dir[b] > 4)
@@ -269,6 +277,27 @@ int check_problem(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t
     return RTMC_OK;
 }
 
+// True when [lo, hi] holds every value coordinate `axis` of the frame can take (an
+// integrated axis whose check always passes): +-Inf, the azimuth atan2 in [-pi, pi], sin of
+// the 3D elevation in [-1, 1], and the direction variable (observeTime.m:21-24): dir_z in
+// [-1, 1] in 3D, acos(dir_z) in [0, pi] in 2D.
+bool range_covers_axis(int frame, int d, int axis, double lo, double hi)
+{
+    if (lo == -INFINITY && hi == INFINITY) return true;
+    if (axis == 1 && frame != RTMC_FRAME_CARTESIAN) return lo <= -M_PI && hi >= M_PI;
+    if (axis == 2 && frame == RTMC_FRAME_SPHERICAL && d == 3) return lo <= -1.0 && hi >= 1.0;
+    if (axis == 3) return d == 3 ? (lo <= -1.0 && hi >= 1.0) : (lo <= 0.0 && hi >= M_PI);
+    return false;
+}
+
+// largest R <= x: for every R-valued u, u > round_down(x) exactly when u > x
+template <typename R> R round_down(double x)
+{
+    R r = (R)x;
+    if ((double)r > x) r = std::nextafter(r, -std::numeric_limits<R>::infinity());
+    return r;
+}
+
 template <typename R, typename Vec>
 void fill_params(rtmc_context *ctx, const rtmc_problem *P, const DevTables<R> &tab, DevParams<R> *p, int *n_edges_out,
                  Vec *edges, Vec *zoe)
@@ -279,7 +308,7 @@ void fill_params(rtmc_context *ctx, const rtmc_problem *P, const DevTables<R> &t
     p->n_sub = P->n_sub; p->n_obs = P->n_obs; p->n_bnd = P->n_bnd;
     p->hist_shift = P->hist_shift;
     p->s_end = P->n_sub * P->n_obs;
-    p->max_events = 4 * p->s_end + 64;
+    p->max_events = P->max_events > 0 ? P->max_events : 4 * p->s_end + 64;
     p->n_particles = P->n_particles; p->pid0 = P->pid0;
     p->key0 = (uint32_t)P->seed; p->key1 = (uint32_t)(P->seed >> 32);
     for (int i = 0; i < 3; ++i) p->src_pos[i] = (R)P->src_pos[i];
@@ -289,11 +318,13 @@ void fill_params(rtmc_context *ctx, const rtmc_problem *P, const DevTables<R> &t
         p->step[m] = (R)(P->v[mm] * P->h);
         const double mft = P->mft[mm];
         p->scat_on[m] = std::isfinite(mft) ? 1 : 0;
-        p->inv_lam[m] = p->scat_on[m] ? (R)(1.0 / (P->h / mft)) : (R)0;
+        p->inv_lam64[m] = p->scat_on[m] ? 1.0 / (P->h / mft) : 0.0;
+        p->inv_lam[m] = (R)p->inv_lam64[m];
         p->kill_on[m] = P->qrate[mm] > 0 ? 1 : 0;
-        p->inv_q[m] = p->kill_on[m] ? (R)(1.0 / P->qrate[mm]) : (R)0;
+        p->inv_q64[m] = p->kill_on[m] ? 1.0 / P->qrate[mm] : 0.0;
+        p->inv_q[m] = (R)p->inv_q64[m];
     }
-    p->p2p = (R)P->p2p; p->s2s = (R)P->s2s;
+    p->p2p = round_down<R>(P->p2p); p->s2s = round_down<R>(P->s2s);
     if (!P->acoustics) {
         p->vs_over_vp = (R)(P->v[1] / P->v[0]);
         p->vp_over_vs = (R)(P->v[0] / P->v[1]);
@@ -301,10 +332,19 @@ void fill_params(rtmc_context *ctx, const rtmc_problem *P, const DevTables<R> &t
     p->cos_half_pi = (R)std::cos(M_PI / 2);
     edges->clear();
     bool finite_uniform[4] = {true, true, true, true};
+    int am[4]; // effective axis modes: checks that every coordinate passes are dropped
     for (int a = 0; a < 4; ++a) {
-        p->ax_mode[a] = P->axis_mode[a];
+        am[a] = P->axis_mode[a];
+        const int ne = P->axis_nedges[a];
+        const bool one_bin = am[a] == RTMC_AXIS_BINNED && ne == 2;
+        if ((am[a] == RTMC_AXIS_RANGE || one_bin) && range_covers_axis(P->frame, P->d, a, P->axis_edges[a][0],
+                                                                         P->axis_edges[a][ne - 1]))
+            am[a] = RTMC_AXIS_IGNORED;
+    }
+    for (int a = 0; a < 4; ++a) {
+        p->ax_mode[a] = am[a];
         p->ax_nbe[a] = 1;
-        if (P->axis_mode[a] == RTMC_AXIS_IGNORED) continue;
+        if (am[a] == RTMC_AXIS_IGNORED) continue;
         const int ne = P->axis_nedges[a];
         const double *E = P->axis_edges[a];
         p->ax_n[a] = ne;
@@ -320,18 +360,18 @@ void fill_params(rtmc_context *ctx, const rtmc_problem *P, const DevTables<R> &t
             if (std::fabs((E[k] - E[k - 1]) - w) > 1e-6 * std::fabs(w)) uni = false;
         p->ax_uniform[a] = uni ? 1 : 0;
         p->ax_inv_w[a] = (R)(1.0 / w);
-        if (P->axis_mode[a] == RTMC_AXIS_BINNED) p->ax_nbe[a] = ne - 1;
+        if (am[a] == RTMC_AXIS_BINNED) p->ax_nbe[a] = ne - 1;
         else p->ax_stride32[a] = 0;
         finite_uniform[a] = uni && std::isfinite(E[0]) && std::isfinite(E[ne - 1]);
     }
-    // observation path (see obs_offset in transport.cu)
+    // observation path (see obs_offset in transport.cuh)
     p->obs_kind = 0;
     if (P->frame == RTMC_FRAME_CARTESIAN) {
         bool ok = true;
-        for (int a = 0; a < 3; ++a) ok = ok && (P->axis_mode[a] == RTMC_AXIS_IGNORED || finite_uniform[a]);
+        for (int a = 0; a < 3; ++a) ok = ok && (am[a] == RTMC_AXIS_IGNORED || finite_uniform[a]);
         if (ok) p->obs_kind = 1;
-    } else if (P->axis_mode[1] == RTMC_AXIS_IGNORED && P->axis_mode[2] == RTMC_AXIS_IGNORED &&
-               P->axis_mode[0] != RTMC_AXIS_IGNORED && finite_uniform[0]) {
+    } else if (am[1] == RTMC_AXIS_IGNORED && am[2] == RTMC_AXIS_IGNORED && am[0] != RTMC_AXIS_IGNORED &&
+               finite_uniform[0]) {
         p->obs_kind = 2;
         p->radial_3d = (P->frame == RTMC_FRAME_SPHERICAL && P->d == 3) ? 1 : 0;
         p->ax_a0 = (R)(-P->axis_edges[0][0] * (double)(P->axis_nedges[0] - 1) /
@@ -694,6 +734,12 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         }
     }
     if (le) return cuda_fail(ctx, (cudaError_t)le, "transport launch");
+    ctx->hist_may_exceed_int64 = may_exceed_int64(P);
+    if (host_out && ctx->hist_may_exceed_int64) {
+        le = launch_check_int64(p.hist, P->hist_len, p.status, narrow_grid, ctx->stream);
+        if (le) return cuda_fail(ctx, (cudaError_t)le, "histogram range check");
+        ++launches;
+    }
     int64_t dstats[32];
     CK(cudaMemcpyAsync(dstats, ctx->stats.p, 256, cudaMemcpyDeviceToHost, ctx->stream), "counters");
     if (host_out) {
@@ -738,6 +784,10 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         st->h2d_bytes = h2d;
         st->d2h_bytes = d2h + 256;
     }
+    if (status & 2)
+        return fail(&ctx->err, RTMC_ERR_DEVICE,
+                    "a histogram bin reached 2^63 and does not fit int64 at this hist_shift: use rtmc_forward_u32 "
+                    "or a smaller hist_shift");
     if (status) return fail(&ctx->err, RTMC_ERR_DEVICE, "a transport guard tripped (event cap or histogram index)");
     return RTMC_OK;
 }
@@ -1229,8 +1279,19 @@ extern "C" int rtmc_copy_histogram(rtmc_context *ctx, int64_t *hist_out, int64_t
     if (!ctx || !hist_out) return fail(ctx ? &ctx->err : nullptr, RTMC_ERR_ARG, "rtmc_copy_histogram: NULL argument");
     if (n < 0 || n > ctx->hist_len) return fail(&ctx->err, RTMC_ERR_ARG, "rtmc_copy_histogram: n exceeds the histogram");
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    int32_t flag = 0;
+    int32_t *status = reinterpret_cast<int32_t *>(static_cast<unsigned char *>(ctx->stats.p) + 128);
+    if (ctx->hist_may_exceed_int64) {
+        CK(cudaMemsetAsync(status, 0, sizeof(int32_t), ctx->stream), "status clear");
+        const int le = launch_check_int64(static_cast<const unsigned long long *>(ctx->hist.p), n, status,
+                                          8 * ctx->num_sms, ctx->stream);
+        if (le) return cuda_fail(ctx, (cudaError_t)le, "histogram range check");
+        CK(cudaMemcpyAsync(&flag, status, sizeof flag, cudaMemcpyDeviceToHost, ctx->stream), "status");
+    }
     CK(cudaMemcpyAsync(hist_out, ctx->hist.p, (size_t)n * 8, cudaMemcpyDeviceToHost, ctx->stream), "histogram copy");
     CK(cudaStreamSynchronize(ctx->stream), "histogram copy");
+    if (flag & 2)
+        return fail(&ctx->err, RTMC_ERR_DEVICE, "a histogram bin reached 2^63 and does not fit int64 at this hist_shift");
     return RTMC_OK;
 }
 
@@ -1569,7 +1630,8 @@ extern "C" int rtmc_batch_run(rtmc_batch *b, rtmc_stats *st)
     float ms = 0;
     cudaEventElapsedTime(&ms, ctx->ev_k0, ctx->ev_k1);
     ctx->last_kernel_ms = ms;
-    ctx->last_launches = 1;
+    const int kernels = (b->n_items ? 1 : 0) + (b->n_items_em ? 1 : 0); // kernel nodes of the graph
+    ctx->last_launches = kernels;
     const int32_t status = (int32_t)(d[16] & 0xffffffff);
     if (st) {
         std::memset(st, 0, sizeof *st);
@@ -1580,13 +1642,20 @@ extern "C" int rtmc_batch_run(rtmc_batch *b, rtmc_stats *st)
         st->observations = d[4];
         st->conversions = d[5];
         st->device_status = status;
-        st->launches = 1;
+        st->launches = kernels;
         st->sink = kSinkSmem;
         st->kernel_ms = ms;
         st->total_ms = ms;
         st->d2h_bytes = 192;
     }
     if (status) return fail(&ctx->err, RTMC_ERR_DEVICE, "a transport guard tripped in a batched run");
+    return RTMC_OK;
+}
+
+extern "C" int rtmc_batch_schedule(const rtmc_batch *b, int32_t *event_major)
+{
+    if (!b || !event_major) return fail(nullptr, RTMC_ERR_ARG, "rtmc_batch_schedule: NULL argument");
+    for (int i = 0; i < b->n; ++i) event_major[i] = b->event_major[i];
     return RTMC_OK;
 }
 

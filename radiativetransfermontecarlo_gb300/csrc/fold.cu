@@ -1,0 +1,303 @@
+// Slice fold and narrowing kernels of librtmc (sm_103a), and the precision dispatch of
+// the transport's attribute helpers.
+#include "rtmc_internal.h"
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+namespace rtmc {
+namespace {
+
+// Fold the dense index array into the histogram, one time slice at a time: blockIdx.y
+// is the slice (so the L2 holds the slice being written), blockIdx.x a contiguous chunk
+// of the slice's entries.  While particles crowd a few bins (early times) many entries
+// of a chunk share a bin, and 64-bit reductions on the same L2 lines serialise; entries
+// therefore go into a shared-memory hash table (bin -> count) of the block, which sends
+// one atomic per distinct bin to the L2 at the end.  A probe window decides: unless its
+// entries crowd into few bins (at most a quarter of the table, each hit twice on
+// average) the rest of the chunk goes straight to the L2; a crowded chunk keeps using
+// the table until it is three quarters full.
+constexpr int kFoldThreads = 512;
+constexpr int kHashSlots = 4096;
+
+__device__ __forceinline__ bool hash_insert(int *keys, unsigned *cnts, int *used, int v)
+{
+    unsigned h = ((unsigned)v * 2654435761u) >> (32 - 12); // 12 = log2(kHashSlots)
+#pragma unroll 1
+    for (int probe = 0; probe < 8; ++probe) {
+        int k = *((volatile int *)keys + h);
+        if (k == -1) {
+            k = atomicCAS(keys + h, -1, v);
+            if (k == -1) atomicAdd(used, 1);
+        }
+        if (k == -1 || k == v) {
+            atomicAdd(cnts + h, 1u);
+            return true;
+        }
+        h = (h + 1) & (kHashSlots - 1);
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(kFoldThreads) rt_bin_slices(const BinParams b)
+{
+    __shared__ int keys[kHashSlots];
+    __shared__ unsigned cnts[kHashSlots];
+    __shared__ int used, valid, dense;
+    const int j = b.j_first + blockIdx.y;
+    const int32_t *row = b.idx + (int64_t)(j - 1) * b.rows; // rows is a multiple of 32: 16-byte aligned
+    unsigned long long *slice = b.hist + (int64_t)j * b.time_stride;
+    const unsigned long long inc = 1ull << b.hist_shift;
+    for (int k = threadIdx.x; k < kHashSlots; k += blockDim.x) { keys[k] = -1; cnts[k] = 0u; }
+    if (threadIdx.x == 0) { used = 0; valid = 0; }
+    // this block's chunk of the slice, in 16-byte vectors
+    const int64_t n4 = (b.n + 3) >> 2;
+    const int64_t per = (n4 + gridDim.x - 1) / gridDim.x;
+    const int64_t q0 = (int64_t)blockIdx.x * per, q1 = min(n4, q0 + per);
+    const int4 *row4 = reinterpret_cast<const int4 *>(row);
+    __syncthreads();
+    // probe window: one vector per thread through the table
+    int64_t q = q0 + threadIdx.x;
+    if (q < q1) {
+        const int4 a = __ldcs(row4 + q);
+        const int va[4] = {a.x, a.y, a.z, a.w};
+        int nv = 0;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int v = va[u];
+            if (v < 0 || q * 4 + u >= b.n) continue;
+            ++nv;
+            if (!hash_insert(keys, cnts, &used, v))
+                atomicAdd(slice + ((v >> 30) ? b.mode_stride : 0) + (v & 0x3fffffff), inc);
+        }
+        if (nv) atomicAdd(&valid, nv);
+    }
+    __syncthreads();
+    // crowded: the window's entries fell in at most a quarter of the table, with every
+    // bin hit twice on average
+    if (threadIdx.x == 0) dense = valid >= 64 && used * 4 <= kHashSlots && used * 2 <= valid;
+    __syncthreads();
+    if (dense) {
+        for (q += blockDim.x; q < q1; q += blockDim.x) {
+            const int4 a = __ldcs(row4 + q);
+            const int va[4] = {a.x, a.y, a.z, a.w};
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int v = va[u];
+                if (v < 0 || q * 4 + u >= b.n) continue;
+                // a table three-quarters full takes no new bins
+                if (*((volatile int *)&used) >= 3 * kHashSlots / 4 || !hash_insert(keys, cnts, &used, v))
+                    atomicAdd(slice + ((v >> 30) ? b.mode_stride : 0) + (v & 0x3fffffff), inc);
+            }
+        }
+    } else {
+        // two 16-byte loads in flight per thread before their atomics
+        for (q += blockDim.x; q < q1; q += 2 * blockDim.x) {
+            const int64_t q2 = q + blockDim.x;
+            const int4 a = __ldcs(row4 + q);
+            const int4 c = q2 < q1 ? __ldcs(row4 + q2) : make_int4(-1, -1, -1, -1);
+            const int va[8] = {a.x, a.y, a.z, a.w, c.x, c.y, c.z, c.w};
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int v = va[u];
+                const int64_t e = (u < 4 ? q : q2) * 4 + (u & 3);
+                if (v >= 0 && e < b.n) atomicAdd(slice + ((v >> 30) ? b.mode_stride : 0) + (v & 0x3fffffff), inc);
+            }
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < kHashSlots; k += blockDim.x) {
+        const int v = keys[k];
+        if (v >= 0) atomicAdd(slice + ((v >> 30) ? b.mode_stride : 0) + (v & 0x3fffffff), (unsigned long long)cnts[k] << b.hist_shift);
+    }
+}
+
+// Same fold with a group of slices privatised in shared memory (u32 counts), flushed
+// with one 64-bit atomic per touched bin: blockIdx.y is the slice group, blockIdx.x a
+// contiguous particle range.
+__global__ void __launch_bounds__(512) rt_bin_slices_smem(const BinParams b)
+{
+    extern __shared__ __align__(16) unsigned sh[];
+    const int j0 = 1 + blockIdx.y * b.group;
+    const int j1 = min(b.n_obs, j0 + b.group - 1);
+    const int per = b.slice_bins * b.n_modes; // bins of one slice, all modes
+    const int nb = (j1 - j0 + 1) * per;
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) sh[k] = 0u;
+    __syncthreads();
+    const int64_t p0 = (int64_t)blockIdx.x * b.part_per_block;
+    const int64_t p1 = min(b.n, p0 + b.part_per_block);
+    for (int j = j0; j <= j1; ++j) {
+        const int32_t *row = b.idx + (int64_t)(j - 1) * b.rows;
+        unsigned *sj = sh + (j - j0) * per;
+        for (int64_t k = p0 + threadIdx.x; k < p1; k += blockDim.x) {
+            const int v = __ldcs(row + k);
+            if (v >= 0) atomicAdd(sj + ((v >> 30) ? b.slice_bins : 0) + (v & 0x3fffffff), 1u);
+        }
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < nb; k += blockDim.x) {
+        const unsigned c = sh[k];
+        if (!c) continue;
+        const int jj = j0 + k / per, r = k % per;
+        const int m = r / b.slice_bins, o = r % b.slice_bins;
+        atomicAdd(b.hist + (int64_t)jj * b.time_stride + (m ? b.mode_stride : 0) + o, (unsigned long long)c << b.hist_shift);
+    }
+}
+
+// The reference's histogram type: counts (value >> shift) of n bins as uint32, saturating
+// at 2^32 - 1 as MATLAB's uint32 additions do (initializeObservation.m:133,
+// radiativeTransfer.m:88).  HBM-bound: 8 B read and 4 B written per bin; each thread keeps
+// four independent loads in flight.
+constexpr int kNarrowThreads = 256, kNarrowUnroll = 4;
+__global__ void __launch_bounds__(kNarrowThreads) rt_narrow_u32(const unsigned long long *__restrict__ src,
+                                                                 uint32_t *__restrict__ dst, int64_t n, int shift)
+{
+    const int64_t stride = (int64_t)gridDim.x * kNarrowThreads;
+    for (int64_t k0 = (int64_t)blockIdx.x * kNarrowThreads * kNarrowUnroll + threadIdx.x; k0 < n;
+         k0 += stride * kNarrowUnroll) {
+        unsigned long long v[kNarrowUnroll];
+#pragma unroll
+        for (int u = 0; u < kNarrowUnroll; ++u) {
+            const int64_t k = k0 + (int64_t)u * kNarrowThreads;
+            v[u] = k < n ? __ldcs(src + k) : 0ull;
+        }
+#pragma unroll
+        for (int u = 0; u < kNarrowUnroll; ++u) {
+            const int64_t k = k0 + (int64_t)u * kNarrowThreads;
+            const unsigned long long c = v[u] >> shift;
+            if (k < n) __stcs(dst + k, c > 0xffffffffull ? 0xffffffffu : (uint32_t)c);
+        }
+    }
+}
+
+// Sets bit 1 of *status when a bin of the unsigned 64-bit fixed-point histogram holds 2^63
+// or more, i.e. does not fit the int64 that rtmc_forward returns.  Reads every bin once
+// (16-byte streaming loads), one flag per warp.
+constexpr int kCheckThreads = 256;
+__global__ void __launch_bounds__(kCheckThreads) rt_check_int64(const unsigned long long *__restrict__ h, int64_t n,
+                                                                int32_t *status)
+{
+    unsigned long long acc = 0;
+    const int64_t n2 = n >> 1;
+    const ulonglong2 *h2 = reinterpret_cast<const ulonglong2 *>(h);
+    for (int64_t k = (int64_t)blockIdx.x * kCheckThreads + threadIdx.x; k < n2; k += (int64_t)gridDim.x * kCheckThreads) {
+        const ulonglong2 v = __ldcs(h2 + k);
+        acc |= v.x | v.y;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0 && (n & 1)) acc |= h[n - 1];
+    if (__any_sync(0xffffffffu, (acc >> 63) != 0ull) && (threadIdx.x & 31) == 0) atomicOr(status, 2);
+}
+
+} // namespace
+
+int launch_check_int64(const unsigned long long *hist, int64_t n, int32_t *status, int max_grid, void *stream)
+{
+    if (n <= 0) return 0;
+    const int64_t need = ((n >> 1) + kCheckThreads - 1) / kCheckThreads;
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>(need, max_grid));
+    rt_check_int64<<<grid, kCheckThreads, 0, (cudaStream_t)stream>>>(hist, n, status);
+    return (int)cudaGetLastError();
+}
+
+int launch_bin_slices(const BinParams &b, int grid_x, size_t smem, void *stream)
+{
+    if (b.group > 0) {
+        dim3 g(grid_x, (b.n_obs + b.group - 1) / b.group);
+        rt_bin_slices_smem<<<g, 512, smem, (cudaStream_t)stream>>>(b);
+    } else {
+        if (b.j_first < 1 || b.j_count < 1 || b.j_first + b.j_count - 1 > b.n_obs) return (int)cudaErrorInvalidValue;
+        // one slice per blockIdx.y, at most 65535 of them per launch
+        constexpr int kMaxGridY = 65535;
+        for (int done = 0; done < b.j_count; done += kMaxGridY) {
+            BinParams c = b;
+            c.j_first = b.j_first + done;
+            c.j_count = b.j_count - done < kMaxGridY ? b.j_count - done : kMaxGridY;
+            dim3 g(grid_x, c.j_count);
+            rt_bin_slices<<<g, kFoldThreads, 0, (cudaStream_t)stream>>>(c);
+            const cudaError_t e = cudaGetLastError();
+            if (e != cudaSuccess) return (int)e;
+        }
+        return 0;
+    }
+    return (int)cudaGetLastError();
+}
+
+int launch_narrow_u32(const unsigned long long *src, uint32_t *dst, int64_t n, int shift, int max_grid, void *stream)
+{
+    if (n <= 0) return 0;
+    if (shift < 0 || shift > 62 || max_grid < 1) return (int)cudaErrorInvalidValue;
+    const int64_t per = (int64_t)kNarrowThreads * kNarrowUnroll;
+    const int64_t need = (n + per - 1) / per;
+    const int grid = (int)(need < max_grid ? need : max_grid);
+    rt_narrow_u32<<<grid, kNarrowThreads, 0, (cudaStream_t)stream>>>(src, dst, n, shift);
+    return (int)cudaGetLastError();
+}
+
+int bin_slices_set_smem(size_t smem)
+{
+    return (int)cudaFuncSetAttribute((const void *)rt_bin_slices_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+int transport_set_smem(int precision, int sink, int obs, size_t smem)
+{
+    return kernel_set_smem(precision, 0, sink, obs, smem);
+}
+
+int transport_max_threads(int precision, int sink, int obs)
+{
+    cudaFuncAttributes a;
+    if (cudaFuncGetAttributes(&a, kernel_of(precision, 0, sink, obs)) != cudaSuccess) return 0;
+    return a.maxThreadsPerBlock;
+}
+
+int transport_occupancy(int precision, int sink, int obs, int block, size_t smem, int *blocks_per_sm)
+{
+    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, kernel_of(precision, 0, sink, obs), block, smem);
+}
+
+static int set_and_occupancy(int precision, int kind, int obs, int block, size_t smem, int *blocks_per_sm)
+{
+    void *fn = kernel_of(precision, kind, 0, obs);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, block, smem);
+    return (int)e;
+}
+
+int transport_batch_setup(int precision, int obs, int block, size_t smem, int *blocks_per_sm)
+{
+    return set_and_occupancy(precision, 1, obs, block, smem, blocks_per_sm);
+}
+
+int transport_batch_em_setup(int precision, int obs, int block, size_t smem, int *blocks_per_sm)
+{
+    return set_and_occupancy(precision, 2, obs, block, smem, blocks_per_sm);
+}
+
+int adjoint_occupancy(int precision, int obs, int block, size_t smem, int *blocks_per_sm)
+{
+    return set_and_occupancy(precision, 3, obs, block, smem, blocks_per_sm);
+}
+
+int adjoint_ring_occupancy(int precision, int obs, int block, size_t smem, int *blocks_per_sm)
+{
+    return set_and_occupancy(precision, 4, obs, block, smem, blocks_per_sm);
+}
+
+int kernel_set_smem(int precision, int kind, int sink, int obs, size_t smem)
+{
+    return (int)cudaFuncSetAttribute(kernel_of(precision, kind, sink, obs), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+}
+
+void *kernel_of(int precision, int kind, int sink, int obs)
+{
+    const bool d = precision == RTMC_FP64;
+    switch (kind) {
+    case 0: return d ? kernel_of_transport_f64(sink, obs) : kernel_of_transport_f32(sink, obs);
+    case 1: case 2: return d ? kernel_of_batch_f64(kind == 2, obs) : kernel_of_batch_f32(kind == 2, obs);
+    default: return d ? kernel_of_adjoint_f64(kind == 4, obs) : kernel_of_adjoint_f32(kind == 4, obs);
+    }
+}
+
+} // namespace rtmc

@@ -1,0 +1,55 @@
+// Instantiation unit of the transport kernel family (transport.cuh).  The build compiles
+// this file six times, once per precision RTMC_REAL (float, double) and part RTMC_PART
+// (1 the transport kernels, 2 the batched kernels, 3 the adjoint kernels), so the
+// variants compile in parallel; RTMC_SUFFIX names the precision (f32, f64).
+#include "transport.cuh"
+
+#if !defined(RTMC_REAL) || !defined(RTMC_PART) || !defined(RTMC_SUFFIX)
+#error "compile with -DRTMC_REAL=float|double -DRTMC_SUFFIX=f32|f64 -DRTMC_PART=1|2|3"
+#endif
+
+#define RTMC_CAT2(a, b) a##_##b
+#define RTMC_CAT(a, b) RTMC_CAT2(a, b)
+#define RTMC_NAME(n) RTMC_CAT(n, RTMC_SUFFIX)
+
+namespace rtmc {
+
+#if RTMC_PART == 1
+int RTMC_NAME(launch_transport)(const DevParams<RTMC_REAL> &p, int grid, int block, size_t smem, void *stream)
+{
+    return launch_transport_t<RTMC_REAL>(p, grid, block, smem, stream);
+}
+
+void *RTMC_NAME(kernel_of_transport)(int sink, int obs) { return pick_t<RTMC_REAL>(sink, obs); }
+#elif RTMC_PART == 2
+int RTMC_NAME(launch_transport_batch)(const BatchArgs<RTMC_REAL> &a, int grid, int block, size_t smem, void *stream)
+{
+    return launch_batch_t<RTMC_REAL>(a, grid, block, smem, stream, false);
+}
+
+int RTMC_NAME(launch_transport_batch_em)(const BatchArgs<RTMC_REAL> &a, int grid, int block, size_t smem, void *stream)
+{
+    return launch_batch_t<RTMC_REAL>(a, grid, block, smem, stream, true);
+}
+
+void *RTMC_NAME(kernel_of_batch)(int em, int obs) { return em ? pick_batch_em<RTMC_REAL>(obs) : pick_batch<RTMC_REAL>(obs); }
+#elif RTMC_PART == 3
+int RTMC_NAME(launch_adjoint)(const DevParams<RTMC_REAL> &p, const AdjointArgs &a, int grid, int block, size_t smem,
+                              void *stream)
+{
+    return launch_adjoint_t<RTMC_REAL>(p, a, grid, block, smem, stream, false);
+}
+
+int RTMC_NAME(launch_adjoint_ring)(const DevParams<RTMC_REAL> &p, const AdjointArgs &a, int grid, int block, size_t smem,
+                                   void *stream)
+{
+    return launch_adjoint_t<RTMC_REAL>(p, a, grid, block, smem, stream, true);
+}
+
+void *RTMC_NAME(kernel_of_adjoint)(int ring, int obs)
+{
+    return ring ? pick_adjoint_ring<RTMC_REAL>(obs) : pick_adjoint<RTMC_REAL>(obs);
+}
+#endif
+
+} // namespace rtmc

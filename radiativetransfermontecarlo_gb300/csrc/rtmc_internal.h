@@ -1,5 +1,5 @@
 // Internal declarations shared by the host (tables.cpp, context.cpp) and device
-// (transport.cu) translation units of librtmc.
+// (kernels.cu, fold.cu, noalloc.cu) translation units of librtmc.
 #pragma once
 
 #include "../../include/rtmc.h"
@@ -85,8 +85,9 @@ template <typename R> struct DevParams {
     R step[2];      // v * h per mode
     R inv_lam[2];   // mft / h (reciprocal of the per-sub-step scattering rate)
     R inv_q[2];     // Q / (omega h)
+    double inv_lam64[2], inv_q64[2]; // the same in FP64 (settles FP32 counts near an integer)
     int32_t scat_on[2], kill_on[2];
-    R p2p, s2s;
+    R p2p, s2s;     // FP32: rounded down, so u > p2p in float equals u > p2p in FP64 for float u
     R vs_over_vp, vp_over_vs;
     R cos_half_pi;  // cos(pi/2) in working precision: the 2D source's z direction
     // observation axes (0 X, 1 Y, 2 Z, 3 PSI)
@@ -160,7 +161,18 @@ struct AdjointArgs {
     double *partial;          // [gridDim.x][n_params] block sums
 };
 
-// Launch wrappers (transport.cu).  Return a cudaError_t value.
+// Launch wrappers (kernels.cu, fold.cu).  Return a cudaError_t value.
+// kernel_of(precision, kind, sink, obs): the kernel function of a transport (kind 0, with
+// its sink and observation path), batch (1), event-major batch (2), adjoint (3) or ring
+// adjoint (4) variant; kernel_set_smem sets its dynamic shared-memory limit.
+void *kernel_of_transport_f32(int sink, int obs);
+void *kernel_of_transport_f64(int sink, int obs);
+void *kernel_of_batch_f32(int em, int obs);
+void *kernel_of_batch_f64(int em, int obs);
+void *kernel_of_adjoint_f32(int ring, int obs);
+void *kernel_of_adjoint_f64(int ring, int obs);
+void *kernel_of(int precision, int kind, int sink, int obs);
+int kernel_set_smem(int precision, int kind, int sink, int obs, size_t smem);
 int launch_transport_f32(const DevParams<float> &p, int grid, int block, size_t smem, void *stream);
 int launch_transport_f64(const DevParams<double> &p, int grid, int block, size_t smem, void *stream);
 int transport_occupancy(int precision, int sink, int obs, int block, size_t smem, int *blocks_per_sm);
@@ -177,6 +189,13 @@ int transport_max_threads(int precision, int sink, int obs);
 int launch_bin_slices(const BinParams &b, int grid_x, size_t smem, void *stream);
 // n histogram bins as uint32 counts (value >> shift, saturating), at most max_grid blocks
 int launch_narrow_u32(const unsigned long long *src, uint32_t *dst, int64_t n, int shift, int max_grid, void *stream);
+// sets bit 1 of *status when a bin of the n-bin histogram is >= 2^63 (out of int64 range)
+int launch_check_int64(const unsigned long long *hist, int64_t n, int32_t *status, int max_grid, void *stream);
+// a histogram of this problem may hold bins of 2^63 or more (n_particles << hist_shift >= 2^63)
+inline bool may_exceed_int64(const rtmc_problem *P)
+{
+    return P->hist_shift >= 1 && P->n_particles >= ((int64_t)1 << (63 - P->hist_shift));
+}
 int launch_transport_batch_f32(const BatchArgs<float> &a, int grid, int block, size_t smem, void *stream);
 int launch_transport_batch_f64(const BatchArgs<double> &a, int grid, int block, size_t smem, void *stream);
 int transport_batch_setup(int precision, int obs, int block, size_t smem, int *blocks_per_sm);

@@ -1,4 +1,4 @@
-// Transport kernels of librtmc (sm_103a).
+// Transport kernels of librtmc (sm_103a), as templates over the working precision R.
 //
 // One particle per thread, state in registers for the particle's whole life.  The
 // kernel restates, event by event, the small-dt process of propagateParticleSmallDt.m
@@ -21,6 +21,10 @@
 // whole histogram fits (flushed once with 64-bit global atomics), else direct 64-bit
 // global atomics.  Random numbers: Philox4x32-10 keyed by (seed), counter
 // (particle id, event index, block).
+//
+// kernels.cu instantiates this header once per precision and kernel group, so the
+// variants build in parallel.
+#pragma once
 #include "rtmc_internal.h"
 
 #include <cuda_runtime.h>
@@ -55,8 +59,10 @@ __device__ __forceinline__ float m_max(float a, float b) { return fmaxf(a, b); }
 __device__ __forceinline__ double m_max(double a, double b) { return fmax(a, b); }
 __device__ __forceinline__ double m_cospi(double x) { return cospi(x); }
 
-// 32-bit Philox output -> uniform in (0,1): 24 bits for FP32, 32 bits for FP64
-__device__ __forceinline__ float to_uniform(uint32_t x, float) { return ((float)(x >> 8) + 0.5f) * 5.9604644775390625e-08f; }
+// 32-bit Philox output -> uniform in (0,1): 23 bits for FP32, 32 bits for FP64.  The
+// FP32 value (k + 1/2) 2^-23, k < 2^23, has 24 significant bits, so it is exact in float
+// and equal to the double the oracle computes from the same output.
+__device__ __forceinline__ float to_uniform(uint32_t x, float) { return ((float)(x >> 9) + 0.5f) * 1.1920928955078125e-07f; }
 __device__ __forceinline__ double to_uniform(uint32_t x, double) { return ((double)x + 0.5) * 2.3283064365386962890625e-10; }
 
 // ----------------------------------------------------------------------------------
@@ -88,13 +94,42 @@ __device__ __forceinline__ U4<R> draw(const DevParams<R> &p, uint64_t pid, uint3
     return U4<R>{to_uniform(o.x, R()), to_uniform(o.y, R()), to_uniform(o.z, R()), to_uniform(o.w, R())};
 }
 
-// sub-steps to the first success of Bernoulli(1 - exp(-rate)) trials; cap = never
-template <typename R> __device__ __forceinline__ int geom_steps(R u, R inv_rate, int on, int cap)
+template <typename T> __device__ __forceinline__ T by_mode(const T v[2], int m) { return m ? v[1] : v[0]; }
+
+// sub-steps to the first success of Bernoulli(1 - exp(-rate)) trials, ceil(-log(u) /
+// rate) clamped to [1, cap]; cap = never.  inv64 is 1 / rate in FP64.
+__device__ __forceinline__ int geom_steps(double u, double inv_rate, double, int on, int cap)
 {
     if (!on) return cap;
-    R k = m_ceil(-m_log(u) * inv_rate);
-    if (!(k < (R)cap)) return cap;
-    return k < (R)1 ? 1 : (int)k;
+    const double k = ceil(-log(u) * inv_rate);
+    if (!(k < (double)cap)) return cap;
+    return k < 1.0 ? 1 : (int)k;
+}
+
+// FP32: the float product -logf(u) * inv_rate carries a few ulps of rounding (logf, the
+// product, the rounded reciprocal), so when it lies within 8 ulps of an integer its ceil
+// may differ from the FP64 one; those rare draws (about 1e-5 of them at C3's rates) are
+// settled in FP64 from the same exact uniform, so every sub-step count equals the FP64
+// count.  Beyond 2^23 the float has no fraction left and the FP64 branch decides too.
+__device__ __forceinline__ int geom_steps(float u, float inv_rate, double inv64, int on, int cap)
+{
+    if (!on) return cap;
+    const float y = -logf(u) * inv_rate;
+    if (y > (float)cap * 1.0001f + 1.f) return cap;
+    if (fabsf(y - rintf(y)) <= 4.8e-7f * y) return geom_steps((double)u, inv64, inv64, 1, cap);
+    const float k = ceilf(y);
+    if (!(k < (float)cap)) return cap;
+    return k < 1.f ? 1 : (int)k;
+}
+
+// sub-steps to the next scattering / Q-kill of a particle in mode m
+template <typename R> __device__ __forceinline__ int scat_steps(const DevParams<R> &p, R u, int m, int cap)
+{
+    return geom_steps(u, by_mode(p.inv_lam, m), by_mode(p.inv_lam64, m), by_mode(p.scat_on, m), cap);
+}
+template <typename R> __device__ __forceinline__ int kill_steps(const DevParams<R> &p, R u, int m, int cap)
+{
+    return geom_steps(u, by_mode(p.inv_q, m), by_mode(p.inv_q64, m), by_mode(p.kill_on, m), cap);
 }
 
 // ----------------------------------------------------------------------------------
@@ -156,7 +191,6 @@ template <typename R> __device__ __forceinline__ void put3(R a[3], int k, R v)
     a[2] = k == 2 ? v : a[2];
 }
 
-template <typename T> __device__ __forceinline__ T by_mode(const T v[2], int m) { return m ? v[1] : v[0]; }
 
 __device__ __forceinline__ float m_rnorm(float x) { return rsqrtf(x); }
 __device__ __forceinline__ double m_rnorm(double x) { return 1.0 / sqrt(x); }
@@ -312,11 +346,11 @@ template <typename R> __device__ void init_particle(const DevParams<R> &p, uint6
     s.s0 = 0;
     s.s_death = -1;
     const int cap = p.s_end + 1;
-    s.sS = geom_steps(b.d, by_mode(p.inv_lam, s.mode), by_mode(p.scat_on, s.mode), cap);
+    s.sS = scat_steps(p, b.d, s.mode, cap);
     s.sK = cap;
     if (by_mode(p.kill_on, s.mode)) {
         const U4<R> c = draw(p, pid, 0u, 2u);  // Q-kill
-        s.sK = geom_steps(c.a, by_mode(p.inv_q, s.mode), 1, cap);
+        s.sK = kill_steps(p, c.a, s.mode, cap);
     }
     next_boundary(p, s);
 }
@@ -608,9 +642,9 @@ __device__ int process_event(const DevParams<R> &p, uint64_t pid, Part<R> &s, Co
         s.s0 = e;
         if (changed) {
             const U4<R> r0 = draw(p, pid, s.k, 0u);
-            const int js = geom_steps(r0.a, by_mode(p.inv_lam, s.mode), by_mode(p.scat_on, s.mode), cap);
+            const int js = scat_steps(p, r0.a, s.mode, cap);
             s.sS = js >= cap ? cap : e - 1 + js;
-            const int jk = geom_steps(r0.b, by_mode(p.inv_q, s.mode), by_mode(p.kill_on, s.mode), cap);
+            const int jk = kill_steps(p, r0.b, s.mode, cap);
             s.sK = jk >= cap ? cap : e + jk;
         }
     } else {
@@ -620,11 +654,11 @@ __device__ int process_event(const DevParams<R> &p, uint64_t pid, Part<R> &s, Co
         scatter(p, s, r0.b, r0.c, r0.d);
         cnt.scat++;
         s.s0 = e;
-        const int js = geom_steps(r0.a, by_mode(p.inv_lam, s.mode), by_mode(p.scat_on, s.mode), cap);
+        const int js = scat_steps(p, r0.a, s.mode, cap);
         s.sS = js >= cap ? cap : e + js;
         if (s.mode != m0 && by_mode(p.kill_on, s.mode)) {
             const U4<R> r1 = draw(p, pid, s.k, 1u);
-            const int jk = geom_steps(r1.a, by_mode(p.inv_q, s.mode), 1, cap);
+            const int jk = kill_steps(p, r1.a, s.mode, cap);
             s.sK = jk >= cap ? cap : e + jk;
         } else if (s.mode != m0) {
             s.sK = cap;
@@ -1295,168 +1329,6 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2) rt_transport_batc
     if (bad) atomicExch(a.status, 1);
 }
 
-// Fold the dense index array into the histogram, one time slice at a time: blockIdx.y
-// is the slice (so the L2 holds the slice being written), blockIdx.x a contiguous chunk
-// of the slice's entries.  While particles crowd a few bins (early times) many entries
-// of a chunk share a bin, and 64-bit reductions on the same L2 lines serialise; entries
-// therefore go into a shared-memory hash table (bin -> count) of the block, which sends
-// one atomic per distinct bin to the L2 at the end.  A probe window decides: unless its
-// entries crowd into few bins (at most a quarter of the table, each hit twice on
-// average) the rest of the chunk goes straight to the L2; a crowded chunk keeps using
-// the table until it is three quarters full.
-constexpr int kFoldThreads = 512;
-constexpr int kHashSlots = 4096;
-
-__device__ __forceinline__ bool hash_insert(int *keys, unsigned *cnts, int *used, int v)
-{
-    unsigned h = ((unsigned)v * 2654435761u) >> (32 - 12); // 12 = log2(kHashSlots)
-#pragma unroll 1
-    for (int probe = 0; probe < 8; ++probe) {
-        int k = *((volatile int *)keys + h);
-        if (k == -1) {
-            k = atomicCAS(keys + h, -1, v);
-            if (k == -1) atomicAdd(used, 1);
-        }
-        if (k == -1 || k == v) {
-            atomicAdd(cnts + h, 1u);
-            return true;
-        }
-        h = (h + 1) & (kHashSlots - 1);
-    }
-    return false;
-}
-
-__global__ void __launch_bounds__(kFoldThreads) rt_bin_slices(const BinParams b)
-{
-    __shared__ int keys[kHashSlots];
-    __shared__ unsigned cnts[kHashSlots];
-    __shared__ int used, valid, dense;
-    const int j = b.j_first + blockIdx.y;
-    const int32_t *row = b.idx + (int64_t)(j - 1) * b.rows; // rows is a multiple of 32: 16-byte aligned
-    unsigned long long *slice = b.hist + (int64_t)j * b.time_stride;
-    const unsigned long long inc = 1ull << b.hist_shift;
-    for (int k = threadIdx.x; k < kHashSlots; k += blockDim.x) { keys[k] = -1; cnts[k] = 0u; }
-    if (threadIdx.x == 0) { used = 0; valid = 0; }
-    // this block's chunk of the slice, in 16-byte vectors
-    const int64_t n4 = (b.n + 3) >> 2;
-    const int64_t per = (n4 + gridDim.x - 1) / gridDim.x;
-    const int64_t q0 = (int64_t)blockIdx.x * per, q1 = min(n4, q0 + per);
-    const int4 *row4 = reinterpret_cast<const int4 *>(row);
-    __syncthreads();
-    // probe window: one vector per thread through the table
-    int64_t q = q0 + threadIdx.x;
-    if (q < q1) {
-        const int4 a = __ldcs(row4 + q);
-        const int va[4] = {a.x, a.y, a.z, a.w};
-        int nv = 0;
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const int v = va[u];
-            if (v < 0 || q * 4 + u >= b.n) continue;
-            ++nv;
-            if (!hash_insert(keys, cnts, &used, v))
-                atomicAdd(slice + ((v >> 30) ? b.mode_stride : 0) + (v & 0x3fffffff), inc);
-        }
-        if (nv) atomicAdd(&valid, nv);
-    }
-    __syncthreads();
-    // crowded: the window's entries fell in at most a quarter of the table, with every
-    // bin hit twice on average
-    if (threadIdx.x == 0) dense = valid >= 64 && used * 4 <= kHashSlots && used * 2 <= valid;
-    __syncthreads();
-    if (dense) {
-        for (q += blockDim.x; q < q1; q += blockDim.x) {
-            const int4 a = __ldcs(row4 + q);
-            const int va[4] = {a.x, a.y, a.z, a.w};
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const int v = va[u];
-                if (v < 0 || q * 4 + u >= b.n) continue;
-                // a table three-quarters full takes no new bins
-                if (*((volatile int *)&used) >= 3 * kHashSlots / 4 || !hash_insert(keys, cnts, &used, v))
-                    atomicAdd(slice + ((v >> 30) ? b.mode_stride : 0) + (v & 0x3fffffff), inc);
-            }
-        }
-    } else {
-        // two 16-byte loads in flight per thread before their atomics
-        for (q += blockDim.x; q < q1; q += 2 * blockDim.x) {
-            const int64_t q2 = q + blockDim.x;
-            const int4 a = __ldcs(row4 + q);
-            const int4 c = q2 < q1 ? __ldcs(row4 + q2) : make_int4(-1, -1, -1, -1);
-            const int va[8] = {a.x, a.y, a.z, a.w, c.x, c.y, c.z, c.w};
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-                const int v = va[u];
-                const int64_t e = (u < 4 ? q : q2) * 4 + (u & 3);
-                if (v >= 0 && e < b.n) atomicAdd(slice + ((v >> 30) ? b.mode_stride : 0) + (v & 0x3fffffff), inc);
-            }
-        }
-    }
-    __syncthreads();
-    for (int k = threadIdx.x; k < kHashSlots; k += blockDim.x) {
-        const int v = keys[k];
-        if (v >= 0) atomicAdd(slice + ((v >> 30) ? b.mode_stride : 0) + (v & 0x3fffffff), (unsigned long long)cnts[k] << b.hist_shift);
-    }
-}
-
-// Same fold with a group of slices privatised in shared memory (u32 counts), flushed
-// with one 64-bit atomic per touched bin: blockIdx.y is the slice group, blockIdx.x a
-// contiguous particle range.
-__global__ void __launch_bounds__(512) rt_bin_slices_smem(const BinParams b)
-{
-    extern __shared__ __align__(16) unsigned sh[];
-    const int j0 = 1 + blockIdx.y * b.group;
-    const int j1 = min(b.n_obs, j0 + b.group - 1);
-    const int per = b.slice_bins * b.n_modes; // bins of one slice, all modes
-    const int nb = (j1 - j0 + 1) * per;
-    for (int k = threadIdx.x; k < nb; k += blockDim.x) sh[k] = 0u;
-    __syncthreads();
-    const int64_t p0 = (int64_t)blockIdx.x * b.part_per_block;
-    const int64_t p1 = min(b.n, p0 + b.part_per_block);
-    for (int j = j0; j <= j1; ++j) {
-        const int32_t *row = b.idx + (int64_t)(j - 1) * b.rows;
-        unsigned *sj = sh + (j - j0) * per;
-        for (int64_t k = p0 + threadIdx.x; k < p1; k += blockDim.x) {
-            const int v = __ldcs(row + k);
-            if (v >= 0) atomicAdd(sj + ((v >> 30) ? b.slice_bins : 0) + (v & 0x3fffffff), 1u);
-        }
-    }
-    __syncthreads();
-    for (int k = threadIdx.x; k < nb; k += blockDim.x) {
-        const unsigned c = sh[k];
-        if (!c) continue;
-        const int jj = j0 + k / per, r = k % per;
-        const int m = r / b.slice_bins, o = r % b.slice_bins;
-        atomicAdd(b.hist + (int64_t)jj * b.time_stride + (m ? b.mode_stride : 0) + o, (unsigned long long)c << b.hist_shift);
-    }
-}
-
-// The reference's histogram type: counts (value >> shift) of n bins as uint32, saturating
-// at 2^32 - 1 as MATLAB's uint32 additions do (initializeObservation.m:133,
-// radiativeTransfer.m:88).  HBM-bound: 8 B read and 4 B written per bin; each thread keeps
-// four independent loads in flight.
-constexpr int kNarrowThreads = 256, kNarrowUnroll = 4;
-__global__ void __launch_bounds__(kNarrowThreads) rt_narrow_u32(const unsigned long long *__restrict__ src,
-                                                                 uint32_t *__restrict__ dst, int64_t n, int shift)
-{
-    const int64_t stride = (int64_t)gridDim.x * kNarrowThreads;
-    for (int64_t k0 = (int64_t)blockIdx.x * kNarrowThreads * kNarrowUnroll + threadIdx.x; k0 < n;
-         k0 += stride * kNarrowUnroll) {
-        unsigned long long v[kNarrowUnroll];
-#pragma unroll
-        for (int u = 0; u < kNarrowUnroll; ++u) {
-            const int64_t k = k0 + (int64_t)u * kNarrowThreads;
-            v[u] = k < n ? __ldcs(src + k) : 0ull;
-        }
-#pragma unroll
-        for (int u = 0; u < kNarrowUnroll; ++u) {
-            const int64_t k = k0 + (int64_t)u * kNarrowThreads;
-            const unsigned long long c = v[u] >> shift;
-            if (k < n) __stcs(dst + k, c > 0xffffffffull ? 0xffffffffu : (uint32_t)c);
-        }
-    }
-}
-
 template <typename R, int SINK, int OBS> void *kernel_ptr() { return (void *)rt_transport<R, SINK, OBS>; }
 
 template <typename R, int SINK> void *pick_obs(int obs)
@@ -1648,60 +1520,11 @@ template <typename R> void *pick_t(int sink, int obs)
 
 } // namespace
 
-static void *pick(int precision, int sink, int obs)
+// Launchers, instantiated per precision and kernel group by kernels.cu.
+template <typename R> int launch_transport_t(const DevParams<R> &p, int grid, int block, size_t smem, void *stream)
 {
-    return precision == RTMC_FP64 ? pick_t<double>(sink, obs) : pick_t<float>(sink, obs);
-}
-
-template <typename R> static int launch(const DevParams<R> &p, int grid, int block, size_t smem, void *stream)
-{
-    void *fn = pick(sizeof(R) == 8 ? RTMC_FP64 : RTMC_FP32, p.sink, p.obs_kind);
     void *args[] = {(void *)&p};
-    return (int)cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, (cudaStream_t)stream);
-}
-
-int launch_transport_f32(const DevParams<float> &p, int grid, int block, size_t smem, void *stream)
-{
-    return launch(p, grid, block, smem, stream);
-}
-
-int launch_transport_f64(const DevParams<double> &p, int grid, int block, size_t smem, void *stream)
-{
-    return launch(p, grid, block, smem, stream);
-}
-
-int launch_bin_slices(const BinParams &b, int grid_x, size_t smem, void *stream)
-{
-    if (b.group > 0) {
-        dim3 g(grid_x, (b.n_obs + b.group - 1) / b.group);
-        rt_bin_slices_smem<<<g, 512, smem, (cudaStream_t)stream>>>(b);
-    } else {
-        if (b.j_first < 1 || b.j_count < 1 || b.j_first + b.j_count - 1 > b.n_obs) return (int)cudaErrorInvalidValue;
-        // one slice per blockIdx.y, at most 65535 of them per launch
-        constexpr int kMaxGridY = 65535;
-        for (int done = 0; done < b.j_count; done += kMaxGridY) {
-            BinParams c = b;
-            c.j_first = b.j_first + done;
-            c.j_count = b.j_count - done < kMaxGridY ? b.j_count - done : kMaxGridY;
-            dim3 g(grid_x, c.j_count);
-            rt_bin_slices<<<g, kFoldThreads, 0, (cudaStream_t)stream>>>(c);
-            const cudaError_t e = cudaGetLastError();
-            if (e != cudaSuccess) return (int)e;
-        }
-        return 0;
-    }
-    return (int)cudaGetLastError();
-}
-
-int launch_narrow_u32(const unsigned long long *src, uint32_t *dst, int64_t n, int shift, int max_grid, void *stream)
-{
-    if (n <= 0) return 0;
-    if (shift < 0 || shift > 62 || max_grid < 1) return (int)cudaErrorInvalidValue;
-    const int64_t per = (int64_t)kNarrowThreads * kNarrowUnroll;
-    const int64_t need = (n + per - 1) / per;
-    const int grid = (int)(need < max_grid ? need : max_grid);
-    rt_narrow_u32<<<grid, kNarrowThreads, 0, (cudaStream_t)stream>>>(src, dst, n, shift);
-    return (int)cudaGetLastError();
+    return (int)cudaLaunchKernel(pick_t<R>(p.sink, p.obs_kind), dim3(grid), dim3(block), args, smem, (cudaStream_t)stream);
 }
 
 template <typename R> void *pick_batch_em(int obs)
@@ -1717,124 +1540,19 @@ template <typename R> void *pick_batch(int obs)
                            : (obs == OBS_RADIAL ? (void *)rt_transport_batch<R, OBS_RADIAL> : (void *)rt_transport_batch<R, OBS_GENERAL>);
 }
 
-template <typename R> static int launch_batch(const BatchArgs<R> &a, int grid, int block, size_t smem, void *stream)
+template <typename R> int launch_batch_t(const BatchArgs<R> &a, int grid, int block, size_t smem, void *stream, bool em)
 {
     void *args[] = {(void *)&a};
-    return (int)cudaLaunchKernel(pick_batch<R>(a.obs_kind), dim3(grid), dim3(block), args, smem, (cudaStream_t)stream);
-}
-
-int launch_transport_batch_f32(const BatchArgs<float> &a, int grid, int block, size_t smem, void *stream)
-{
-    return launch_batch(a, grid, block, smem, stream);
-}
-
-int launch_transport_batch_f64(const BatchArgs<double> &a, int grid, int block, size_t smem, void *stream)
-{
-    return launch_batch(a, grid, block, smem, stream);
-}
-
-template <typename R> static int launch_batch_em(const BatchArgs<R> &a, int grid, int block, size_t smem, void *stream)
-{
-    void *args[] = {(void *)&a};
-    return (int)cudaLaunchKernel(pick_batch_em<R>(a.obs_kind), dim3(grid), dim3(block), args, smem, (cudaStream_t)stream);
-}
-
-int launch_transport_batch_em_f32(const BatchArgs<float> &a, int grid, int block, size_t smem, void *stream)
-{
-    return launch_batch_em(a, grid, block, smem, stream);
-}
-
-int launch_transport_batch_em_f64(const BatchArgs<double> &a, int grid, int block, size_t smem, void *stream)
-{
-    return launch_batch_em(a, grid, block, smem, stream);
-}
-
-int transport_batch_em_setup(int precision, int obs, int block, size_t smem, int *blocks_per_sm)
-{
-    void *fn = precision == RTMC_FP64 ? pick_batch_em<double>(obs) : pick_batch_em<float>(obs);
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, block, smem);
-    return (int)e;
-}
-
-int transport_batch_setup(int precision, int obs, int block, size_t smem, int *blocks_per_sm)
-{
-    void *fn = precision == RTMC_FP64 ? pick_batch<double>(obs) : pick_batch<float>(obs);
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, block, smem);
-    return (int)e;
-}
-
-int bin_slices_set_smem(size_t smem)
-{
-    return (int)cudaFuncSetAttribute((const void *)rt_bin_slices_smem, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-}
-
-int transport_set_smem(int precision, int sink, int obs, size_t smem)
-{
-    return (int)cudaFuncSetAttribute(pick(precision, sink, obs), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-}
-
-int transport_max_threads(int precision, int sink, int obs)
-{
-    cudaFuncAttributes a;
-    if (cudaFuncGetAttributes(&a, pick(precision, sink, obs)) != cudaSuccess) return 0;
-    return a.maxThreadsPerBlock;
+    void *fn = em ? pick_batch_em<R>(a.obs_kind) : pick_batch<R>(a.obs_kind);
+    return (int)cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, (cudaStream_t)stream);
 }
 
 template <typename R>
-static int launch_adj(const DevParams<R> &p, const AdjointArgs &a, int grid, int block, size_t smem, void *stream)
+int launch_adjoint_t(const DevParams<R> &p, const AdjointArgs &a, int grid, int block, size_t smem, void *stream, bool ring)
 {
     void *args[] = {(void *)&p, (void *)&a};
-    return (int)cudaLaunchKernel(pick_adjoint<R>(p.obs_kind), dim3(grid), dim3(block), args, smem, (cudaStream_t)stream);
-}
-
-int launch_adjoint_f32(const DevParams<float> &p, const AdjointArgs &a, int grid, int block, size_t smem, void *stream)
-{
-    return launch_adj(p, a, grid, block, smem, stream);
-}
-
-int launch_adjoint_f64(const DevParams<double> &p, const AdjointArgs &a, int grid, int block, size_t smem, void *stream)
-{
-    return launch_adj(p, a, grid, block, smem, stream);
-}
-
-template <typename R>
-static int launch_adj_ring(const DevParams<R> &p, const AdjointArgs &a, int grid, int block, size_t smem, void *stream)
-{
-    void *args[] = {(void *)&p, (void *)&a};
-    return (int)cudaLaunchKernel(pick_adjoint_ring<R>(p.obs_kind), dim3(grid), dim3(block), args, smem, (cudaStream_t)stream);
-}
-
-int launch_adjoint_ring_f32(const DevParams<float> &p, const AdjointArgs &a, int grid, int block, size_t smem, void *stream)
-{
-    return launch_adj_ring(p, a, grid, block, smem, stream);
-}
-
-int launch_adjoint_ring_f64(const DevParams<double> &p, const AdjointArgs &a, int grid, int block, size_t smem, void *stream)
-{
-    return launch_adj_ring(p, a, grid, block, smem, stream);
-}
-
-int adjoint_ring_occupancy(int precision, int obs, int block, size_t smem, int *blocks_per_sm)
-{
-    void *fn = precision == RTMC_FP64 ? pick_adjoint_ring<double>(obs) : pick_adjoint_ring<float>(obs);
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, block, smem);
-    return (int)e;
-}
-
-int adjoint_occupancy(int precision, int obs, int block, size_t smem, int *blocks_per_sm)
-{
-    void *fn = precision == RTMC_FP64 ? pick_adjoint<double>(obs) : pick_adjoint<float>(obs);
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, block, smem);
-    return (int)e;
-}
-
-int transport_occupancy(int precision, int sink, int obs, int block, size_t smem, int *blocks_per_sm)
-{
-    return (int)cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, pick(precision, sink, obs), block, smem);
+    void *fn = ring ? pick_adjoint_ring<R>(p.obs_kind) : pick_adjoint<R>(p.obs_kind);
+    return (int)cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, (cudaStream_t)stream);
 }
 
 } // namespace rtmc

@@ -66,13 +66,14 @@ class TransportProblem:
     src_v: tuple = (0.0, 1.0, 0.0)
     src_extent: tuple = (0.0, 0.0)
     src_radial: tuple | None = None              # (cdf knots, radii) of a radial point source
+    max_events: int = 0                          # per-particle event cap (0: automatic)
 
     def to_ctypes(self):
         """Return (RtmcProblem, keep-alive list of the arrays it points into)."""
         P = _lib.RtmcProblem()
         P.d, P.frame, P.acoustics, P.precision = self.d, self.frame, int(self.acoustics), self.precision
         P.src_dir, P.polarization, P.n_sub, P.n_obs = self.src_dir, self.polarization, self.n_sub, self.n_obs
-        P.n_bnd, P.hist_shift = len(self.bnd), self.hist_shift
+        P.n_bnd, P.hist_shift, P.max_events = len(self.bnd), self.hist_shift, self.max_events
         P.n_particles, P.pid0, P.seed = self.n_particles, self.pid0, self.seed
         for i in range(3):
             P.src_pos[i] = self.src_pos[i]

@@ -15,11 +15,11 @@ from radiativetransfermontecarlo_gb300 import workloads as W
 
 class _OracleContext:
     def forward(self, prob, tables, out=None):
-        h, st, _ = O.run(prob, O.table_knots(tables), scheme="event", u24=False)
+        h, st, _ = O.run(prob, O.table_knots(tables), scheme="event", ufloat=False)
         return h, st
 
     def gradient(self, prob, tables, dls, dlS, adjoint):
-        return O.gradient(prob, O.table_knots(tables), dls, dlS, adjoint, u24=False)
+        return O.gradient(prob, O.table_knots(tables), dls, dlS, adjoint, ufloat=False)
 
 
 @pytest.fixture
@@ -57,7 +57,7 @@ def test_gradient_host_pipeline(oracle_backend):
     r = np.where(keep, 2 * (E - T) / np.where(keep, T, 1.0) - unit / np.where(keep, T, 1.0), 0.0)
     scat = ["lc", "cv_kappa", "cv_rho", "mfp"]
     dls, dlS = A.score_tables(mat, 3, scat)
-    g, _ = O.gradient(prob, O.table_knots(prob.tables), dls, dlS, (r * unit).ravel(order="F"), u24=False)
+    g, _ = O.gradient(prob, O.table_knots(prob.tables), dls, dlS, (r * unit).ravel(order="F"), ufloat=False)
     for q, p in enumerate(scat):
         assert math.isclose(res["grad"][p], g[q], rel_tol=1e-9, abs_tol=1e-12)
     # Q: exact, equal to central differences of the weight-mode misfit

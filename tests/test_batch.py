@@ -62,3 +62,32 @@ def test_batch_autotune_keeps_results():
     b.run()
     assert np.array_equal(b.histograms(), H)
     b.close()
+
+
+def test_batch_instances_match_oracle_fp64():
+    """C4 instances in one FP64 batched launch against the oracle's event scheme on the same
+    Philox stream: lockstep instances (1, 8, 9) and event-heavy ones (0, 13, 36: 120-350
+    scatterings per particle, Q = 500, 100 and Inf) that the event-major kernel runs.
+    Counts, scatterings and kills are equal; bins equal up to edge ties."""
+    from oracle import oracle as O
+    picks = [0, 1, 8, 9, 13, 36]
+    inst = []
+    for i in picks:
+        geo, src, mat, obs, opts = W.c4_instance(i)
+        src = dict(src, numberParticles=1500)
+        inst.append((geo, src, mat, obs, dict(opts, exact_count=True, seed=200 + i, precision="fp64")))
+    b = Batch(inst)
+    sched = b.schedule()
+    assert list(sched) == [1, 0, 0, 0, 1, 1], sched  # event-heavy instances on rt_transport_batch_em
+    st = b.run()
+    assert st["device_status"] == 0 and st["launches"] == 2  # both kernels of the graph ran
+    H = b.histograms()
+    tot = {"scatter_events": 0, "kills": 0}
+    for k, prob in enumerate(b.problems):
+        ref, rs, _ = O.run(prob, O.table_knots(prob.tables), scheme="event")
+        diff = int(np.abs(H[k] - ref).sum() >> prob.hist_shift)
+        assert diff <= max(4, 1e-6 * rs["observations"]), (picks[k], diff)
+        for key in tot:
+            tot[key] += rs[key]
+    assert st["scatter_events"] == tot["scatter_events"] and st["kills"] == tot["kills"]
+    b.close()

@@ -1,6 +1,7 @@
 """Golden fixtures (tests/golden/oracle_event.npz, made by tests/golden/make_golden.py):
 the oracle must keep reproducing them exactly, and the GPU must reproduce them through
-the C ABI (FP64: trajectories to 1e-9, bins up to edge ties; FP32: 99 % of trajectories)."""
+the C ABI (FP64: trajectories to 1e-9, bins up to edge ties; FP32: 99 % of trajectories
+to 1e-5)."""
 import platform
 from pathlib import Path
 
@@ -47,11 +48,8 @@ def test_gpu_reproduces_golden(name, precision):
     ref[GOLDEN[key + "_idx"]] = GOLDEN[key + "_val"]
     g = GOLDEN[key + "_states"]
     s = states[:N_STATES]
-    # FP32 on the 2^20-step grid of the large-time-step scheme: a float rounding of a
-    # sub-step count moves an event by one sub-step, so sub-step indices are not compared
-    cols = [9, 10, 11, 12, 13, 14, 15] if precision == "fp64" else [9, 10, 11, 12, 15]
-    same = np.all(s[:, cols] == g[:, cols], axis=1)
-    tol = 1e-9 if precision == "fp64" else 1e-3
+    same = np.all(s[:, 9:16] == g[:, 9:16], axis=1)
+    tol = 1e-9 if precision == "fp64" else 1e-5
     close = np.all(np.abs(s[:, :9] - g[:, :9]) <= tol * (1 + np.abs(g[:, :9])), axis=1)
     ok = (same & close).mean()
     diff = int(np.abs(hist - ref).sum() >> prob.hist_shift)
@@ -59,5 +57,5 @@ def test_gpu_reproduces_golden(name, precision):
         assert ok == 1.0
         assert diff <= max(4, 1e-6 * stats["observations"])
     else:
-        assert ok >= 0.99
-        assert diff <= 0.02 * stats["observations"]
+        assert ok >= 0.99  # 200 particles: at most two may leave the oracle's path
+        assert diff <= 2e-3 * stats["observations"] + 4

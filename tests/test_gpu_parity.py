@@ -3,8 +3,9 @@
 Same Philox stream on both sides ("event" oracle): FP64 trajectories must match to
 1e-12 relative (both sides run the same event sequence; libm vs CUDA math differ in the
 last bits) and bins exactly away from edge ties; FP32 trajectories match the oracle fed
-the same 24-bit uniforms to 1e-5 relative for >= 98% of particles and to 1e-3 for >= 99%
-(the rest leave the shared path when a float rounding flips an integer sub-step count).  Independent streams
+the same uniforms (23-bit, exact in float) to 1e-5 relative for >= 99.9% of particles:
+every integer decision (sub-step counts settled in FP64 near an integer, mode thresholds
+rounded so float and FP64 compares agree) follows the oracle's.  Independent streams
 ("substep" oracle, the reference's own sub-step order): histograms agree within 3 sigma
 of the Monte Carlo error.
 """
@@ -72,12 +73,13 @@ def test_fp32_trajectories_match_oracle_with_same_uniforms(name):
     n = 20000 if name != "c3_halfspace2d" else 4000
     prob, grid, N, hist, states, stats, ref_hist, ref_states, ref_stats = _run_both(geo, src, mat, obs, opts, n, "fp32")
     assert stats["device_status"] == 0
-    ok = _path_match(states, ref_states, 1e-3)
-    assert ok.mean() >= 0.99, ok.mean()
-    # measured: 99.9 % (C1), 99.8 % (C2), 98.6 % (C3) of the particles within 1e-5
-    assert _path_match(states, ref_states, 1e-5).mean() >= 0.98
+    ok = _path_match(states, ref_states, 1e-5)
+    # measured: 100 % of the particles within 1e-5 on C1, C2 and C3 (and C3 over 10 s)
+    assert ok.mean() >= 0.999, f"{(~ok).sum()} particles left the oracle's trajectory"
     rel = abs(stats["scatter_events"] - ref_stats["scatter_events"]) / max(1, ref_stats["scatter_events"])
-    assert rel < 0.01
+    assert rel < 1e-3
+    for k in ("boundary_hits", "kills"):
+        assert abs(stats[k] - ref_stats[k]) <= 1e-3 * max(1, ref_stats[k]) + 1, k
 
 
 def test_energy_conserved_unbounded_q_inf():
@@ -224,11 +226,9 @@ def test_large_time_steps_scheme_matches_oracle(precision):
         assert _path_match(states, ref_states, 1e-9).mean() == 1.0
         assert _l1_diff(hist, ref_hist) >> prob.hist_shift <= max(4, 1e-6 * stats["observations"])
     else:
-        # at 2^20 sub-steps per interval a float rounding of a sub-step count moves an event
-        # by one sub-step (1e-6 of an interval): compare everything but the sub-step indices
-        same = np.all(states[:, [9, 10, 11, 12, 15]] == ref_states[:, [9, 10, 11, 12, 15]], axis=1)
-        close = np.all(np.abs(states[:, :9] - ref_states[:, :9]) <= 1e-3 * (1 + np.abs(ref_states[:, :9])), axis=1)
-        assert (same & close).mean() >= 0.99
+        # sub-step counts beyond float's integer range (2^20 sub-steps per interval) are
+        # settled in FP64, so every event lands on the oracle's sub-step
+        assert _path_match(states, ref_states, 1e-5).mean() >= 0.999
 
 
 def _feature_cases():
@@ -594,3 +594,50 @@ def test_zero_and_one_particle(case):
         assert _path_match(states1, ref_states1, 1e-12).all()
         assert stats1["observations"] == ref_stats1["observations"]
         assert np.array_equal(hist1, ref_hist1)
+
+
+def _observation_case(d, frame, pair):
+    """An observation that bins exactly the axes `pair` (1 X, 2 Y, 3 Z, 4 PSI) of a frame,
+    as initializeObservation's ibins; the other axes are integrated over one range."""
+    radial = frame != "cartesian"
+    span = colon(0, 0.2, 2.6) if radial else colon(-2, 0.25, 2)
+    binned = {1: ("x", span), 2: ("y", colon(-math.pi, math.pi / 6, math.pi) if radial else colon(-2, 0.25, 2)),
+              3: ("z", colon(-math.pi / 2, math.pi / 12, math.pi / 2) if frame == "spherical" else colon(-2, 0.5, 2)),
+              # 2D: the direction variable is acos(dir_z) = pi/2 for every particle; pi/7 steps
+              # keep that value off the edges
+              4: ("directions", colon(0, math.pi / 8, math.pi) if d == 3 else colon(0, math.pi / 7, math.pi))}
+    obs = {"x": [0.0, 3.0] if radial else [-3.0, 3.0], "time": colon(0, 0.05, 1.5)}
+    for a in pair:
+        k, e = binned[a]
+        obs[k] = e
+    return obs
+
+
+OBS_CASES = [(3, f, p) for f in ("cartesian", "cylindrical", "spherical")
+             for p in ((1, 2), (1, 3), (1, 4), (2, 4), (3, 4), (2, 3))] + \
+            [(2, f, p) for f in ("cartesian", "cylindrical", "spherical") for p in ((1, 2), (1, 4), (2, 4))]
+
+
+@pytest.mark.parametrize("d,frame,pair", OBS_CASES, ids=[f"{d}d-{f}-{p[0]}{p[1]}" for d, f, p in OBS_CASES])
+def test_observation_frames_and_bin_pairs_match_oracle(d, frame, pair):
+    """observeTime.m:45-127 in every frame with each binned pair of initializeObservation
+    (3D: the six pairs; 2D: the three without z), including the direction axis (dir_z in
+    3D, acos(dir_z) in 2D): GPU bins against the oracle, FP64 and FP32."""
+    from radiativetransfermontecarlo_gb300.observation import initialize_observation
+    geo = {"dimension": d, "frame": frame}
+    mat = MaterialClass(geo, 10, True, 1, [0.1, 0.1], 0, "exp", 0.1)
+    src = {"lambda": 0.05, "position": [0.1, -0.05, 0.02][:d]}
+    obs = _observation_case(d, frame, pair)
+    grid = initialize_observation(dict(geo), True, obs, 1000)
+    assert list(grid.ibins) == list(pair)
+    for precision in ("fp64", "fp32"):
+        prob, grid, N, hist, states, stats, ref_hist, ref_states, ref_stats = _run_both(
+            geo, src, mat, obs, {"seed": 31}, 4000, precision)
+        assert stats["device_status"] == 0
+        assert stats["observations"] > 0.5 * ref_stats["observations"] > 0
+        if precision == "fp64":
+            assert _path_match(states, ref_states, 1e-12).mean() == 1.0
+            assert _l1_diff(hist, ref_hist) <= max(4, 1e-6 * stats["observations"])
+        else:
+            assert _path_match(states, ref_states, 1e-5).mean() >= 0.999
+            assert _l1_diff(hist, ref_hist) <= 2e-3 * stats["observations"] + 4
