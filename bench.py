@@ -401,7 +401,10 @@ def run_c4(args):
     t0 = time.perf_counter()
     batch = Batch([W.c4_instance(i) for i in range(256)])
     setup_s = time.perf_counter() - t0
-    shape, tune = autotune(batch, repeats=1)
+    if args.no_tune:
+        shape, tune = (0, 0, 0), {}
+    else:
+        shape, tune = autotune(batch, repeats=1)
     for _ in range(args.warmup):
         batch.run()
     ms, ev = [], 0
@@ -661,6 +664,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="seconds of each CPU-baseline sample")
+    ap.add_argument("--no-tune", action="store_true", help="c4: the default launch shape, no autotuning")
     ap.add_argument("--no-sub", action="store_true",
                     help="skip the compact C1/C3/C4/C5 records that the default C2 line carries")
     ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c3", "c4", "c5"],

@@ -227,6 +227,12 @@ int rtmc_forward_device(rtmc_context *ctx, const rtmc_problem *problem, const rt
                         rtmc_stats *stats);
 int rtmc_copy_histogram(rtmc_context *ctx, int64_t *hist_out, int64_t n);
 
+/* Device address and length (int64 elements) of the histogram rtmc_forward_device left
+ * in ctx, valid until the next call on ctx or rtmc_destroy.  Lets a caller reduce replica
+ * histograms in place on the device (the parfor sum E = E + E_local of
+ * radiativeTransfer.m:88, across GPUs) before one rtmc_copy_histogram. */
+int rtmc_histogram_device(rtmc_context *ctx, void **ptr, int64_t *n);
+
 /* rtmc_forward plus the final state of every particle, for particle-by-particle checks:
  * state_out is a HOST buffer of n_particles x 16 doubles {x[3] at the last event, dir[3],
  * perp[3], mode (0 P, 1 S), alive, scatterings, boundary crossings, sub-step of the last
@@ -327,7 +333,10 @@ void rtmc_batch_destroy(rtmc_batch *batch);
  * legacy default stream); the call returns after the stream has finished its work.
  * All calls share the one array and it keeps the last call's contents (the call clears
  * what must start at zero): calls that overlap on the GPU, from several host threads or
- * streams, race and must be serialised by the caller. */
+ * streams, race and must be serialised by the caller.  On the host the call stages the
+ * tables through a 2 MB file-scope buffer (no heap, no large stack frame) and holds a
+ * library mutex while it runs, so calls from the threads of one process already run one
+ * after another. */
 int rtmc_forward_noalloc(const rtmc_problem *problem, const rtmc_tables *tables, int64_t *hist_device,
                          void *stream, rtmc_stats *stats);
 
@@ -352,9 +361,13 @@ int rtmc_set_pipeline(rtmc_context *ctx, int32_t chunks, int32_t transport_block
 /* Transport schedule: 0 = warps walk 32 particles' observation instants in lockstep
  * (events run ahead into a shared-memory ring; best when observations outnumber events);
  * 1 = one particle per thread, each event followed by its segment's observations (best
- * for event-heavy problems); -1 = automatic (1 when 8 x expected events per particle >=
- * observation instants, and the histogram does not go through the index array).  Both
- * give the same histogram. */
+ * for event-heavy problems); 2 = split: one kernel runs every particle's events (each
+ * thread a stream of particles) and writes its trajectory segments to device memory, a
+ * second bins the observation instants of 32 particles per warp in lockstep (the segments
+ * per particle follow the expected events, or the ring capacity of rtmc_set_launch when
+ * one is set; particles with more are rerun one per thread); -1 = automatic (1 when 8 x
+ * expected events per particle >= observation instants and the histogram does not go
+ * through the index array, else 2).  All give the same histogram. */
 int rtmc_set_schedule(rtmc_context *ctx, int32_t event_major);
 
 /* enable (1, default) or disable (0) reuse of the device copy of a tables handle across

@@ -103,6 +103,7 @@ SIGNATURES = {
                                      C.POINTER(RtmcStats)]),
     "rtmc_forward_device": (C.c_int, [_P, C.POINTER(RtmcProblem), _P, C.POINTER(RtmcStats)]),
     "rtmc_copy_histogram": (C.c_int, [_P, C.POINTER(C.c_int64), C.c_int64]),
+    "rtmc_histogram_device": (C.c_int, [_P, C.POINTER(C.c_void_p), C.POINTER(C.c_int64)]),
     "rtmc_forward_noalloc": (C.c_int, [C.POINTER(RtmcProblem), _P, C.c_void_p, C.c_void_p, C.POINTER(RtmcStats)]),
     "rtmc_host_alloc": (C.c_int, [C.c_int64, C.POINTER(_P)]),
     "rtmc_host_free": (C.c_int, [_P]),
@@ -306,6 +307,12 @@ class Context:
         check(self.lib.rtmc_forward_device(self.handle, C.byref(problem), tables.handle, C.byref(st)), self.handle)
         return st.as_dict()
 
+    def histogram_device(self):
+        """(device address, int64 elements) of the histogram rtmc_forward_device left here."""
+        ptr, n = C.c_void_p(), C.c_int64()
+        check(self.lib.rtmc_histogram_device(self.handle, C.byref(ptr), C.byref(n)), self.handle)
+        return ptr.value, n.value
+
     def copy_histogram(self, out: np.ndarray):
         _need(out.dtype == np.int64 and out.flags.c_contiguous, "out must be a contiguous int64 array")
         check(self.lib.rtmc_copy_histogram(self.handle, out.ctypes.data_as(C.POINTER(C.c_int64)), out.size),
@@ -321,7 +328,8 @@ class Context:
         check(self.lib.rtmc_set_pipeline(self.handle, chunks, transport_blocks_per_sm), self.handle)
 
     def set_schedule(self, event_major: int = -1):
-        """rtmc_set_schedule: -1 automatic, 0 lockstep warp batches, 1 one particle per thread."""
+        """rtmc_set_schedule: -1 automatic, 0 lockstep warp batches, 1 one particle per thread,
+        2 split (events kernel, then observation kernel)."""
         check(self.lib.rtmc_set_schedule(self.handle, event_major), self.handle)
 
     def last_timing(self):

@@ -2,7 +2,7 @@
 
 Translation units compiled in parallel: the transport kernel family (kernels.cu over
 transport.cuh, compiled once per precision and kernel group: transport, batched,
-adjoint), the slice fold (fold.cu) and the static scratch (noalloc.cu) with nvcc for
+adjoint, split schedule), the slice fold (fold.cu) and the static scratch (noalloc.cu) with nvcc for
 sm_103a, the host table builder and the context/C-ABI with g++; linked by nvcc into
 radiativetransfermontecarlo_gb300/librtmc.so with the CUDA runtime linked statically.
 """
@@ -55,7 +55,7 @@ def build(verbose: bool = False, force: bool = False, ptxas_info: bool = False) 
     for cu in sorted(CSRC.glob("*.cu")):
         if cu.name == "kernels.cu":
             for real, suf in (("float", "f32"), ("double", "f64")):
-                for part in (1, 2, 3):
+                for part in (1, 2, 3, 4):
                     units.append((cu, f"kernels_{suf}_{part}", [f"-DRTMC_REAL={real}", f"-DRTMC_SUFFIX={suf}",
                                                                  f"-DRTMC_PART={part}"]))
         else:

@@ -49,6 +49,7 @@ struct rtmc_context {
     std::string err;
     DevBuf hist, tabs, aux, stats, flush, trace, idx, adj, partial;
     DevBuf narrow; // uint32 copy of the histogram (rtmc_forward_u32)
+    DevBuf segs, seg_head, ovf; // split schedule: trajectory segments, per-particle heads, overflow list
     uint64_t tabs_gen = 0;
     int tabs_prec = -1;
     DevTables<float> tf{};
@@ -62,7 +63,7 @@ struct rtmc_context {
     // transport / fold pipeline over particle chunks (index sink): a second stream and
     // per-chunk events, created on first use
     int opt_chunks = 0, opt_k1_bps = 0;
-    int opt_event_major = -1; // -1 automatic, 0 two-cursor batches, 1 one particle per thread
+    int opt_event_major = -1; // -1 automatic, 0 two-cursor batches, 1 one particle per thread, 2 split
     static constexpr int kPipe = 32;
     cudaStream_t fold_stream = nullptr;
     cudaEvent_t ev_a0[kPipe] = {}, ev_a1[kPipe] = {}, ev_b0[kPipe] = {}, ev_b1[kPipe] = {};
@@ -385,7 +386,8 @@ void fill_params(rtmc_context *ctx, const rtmc_problem *P, const DevTables<R> &t
         for (int m = 0; m < (P->acoustics ? 1 : 2); ++m)
             if (std::isfinite(P->mft[m])) rate = std::max(rate, 1.0 / P->mft[m]);
         const double events = rate * P->h * (double)P->n_sub * (double)P->n_obs;
-        p->event_major = (ctx && ctx->opt_event_major >= 0) ? ctx->opt_event_major : (events * 8.0 >= (double)P->n_obs ? 1 : 0);
+        const int o = ctx ? ctx->opt_event_major : -1;
+        p->event_major = o == 1 ? 1 : ((o == 0 || o == 2) ? 0 : (events * 8.0 >= (double)P->n_obs ? 1 : 0));
     }
     *n_edges_out = (int)edges->size();
     p->n_edges = *n_edges_out;
@@ -580,6 +582,68 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
     int64_t grid = (int64_t)ctx->num_sms * bps;
     const int64_t need = (std::max<int64_t>(chunk, 1) + block - 1) / block;
     grid = std::max<int64_t>(1, std::min<int64_t>(grid, need));
+    int le = 0, launches = 0;
+    // split schedule (rt_events, rt_observe): the lockstep problems, unless switched off
+    const bool split = !p.event_major && ctx->opt_event_major != 0;
+    SplitLaunch sl{};
+    if (split) {
+        // segments per particle: 1 + the expected events + 4 standard deviations + 4
+        double rate = 0;
+        for (int m = 0; m < nm; ++m)
+            if (std::isfinite(P->mft[m])) rate = std::max(rate, 1.0 / P->mft[m]);
+        const double mean = rate * P->h * (double)P->n_sub * (double)P->n_obs;
+        int K = (int)std::ceil(1.0 + mean + 4.0 * std::sqrt(mean) + 4.0);
+        K = std::min(64, std::max(8, (K + 3) / 4 * 4));
+        if (ctx->opt_ring) K = ctx->opt_ring; // an explicit ring capacity sets the segments per particle
+        const size_t rec = 8 * sizeof(R);
+        const int64_t rows_max = std::max<int64_t>(chunk, 1);
+        if (ctx->segs.grow((size_t)rows_max * K * rec) || ctx->seg_head.grow((size_t)rows_max * 8) ||
+            ctx->ovf.grow((size_t)rows_max * 4))
+            return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for trajectory segments failed");
+        p.split = 1;
+        p.seg_cap = K;
+        p.segs = ctx->segs.p;
+        p.seg_head = static_cast<int32_t *>(ctx->seg_head.p);
+        p.ovf_list = static_cast<int32_t *>(ctx->ovf.p);
+        p.ovf_count = reinterpret_cast<uint32_t *>(static_cast<unsigned char *>(ctx->stats.p) + 192);
+        sl.smem_events = edge_smem;
+        int be = 0, bo = 0;
+        if (kernel_set_smem(prec, 5, sink, p.obs_kind, sl.smem_events) != 0 ||
+            kernel_set_smem(prec, 7, sink, p.obs_kind, sl.smem_events) != 0 ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&be, kernel_of(prec, 5, sink, p.obs_kind), 256, sl.smem_events) !=
+                cudaSuccess || be < 1)
+            return fail(&ctx->err, RTMC_ERR_CUDA, "event kernel does not fit on the device");
+        sl.block_observe = sink == kSinkSmem ? 512 : 256;
+        sl.smem_observe = edge_smem + (sink == kSinkSmem ? hist_smem : 0);
+        if (kernel_set_smem(prec, 6, sink, p.obs_kind, sl.smem_observe) != 0 ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bo, kernel_of(prec, 6, sink, p.obs_kind), sl.block_observe,
+                                                          sl.smem_observe) != cudaSuccess || bo < 1)
+            return fail(&ctx->err, RTMC_ERR_CUDA, "observation kernel does not fit on the device");
+        if (n_pipe) {
+            be = std::min(be, ctx->opt_k1_bps ? ctx->opt_k1_bps : 2);
+            bo = std::min(bo, ctx->opt_k1_bps ? ctx->opt_k1_bps : 2);
+        }
+        const int64_t cmax = std::max<int64_t>(chunk, 1);
+        sl.grid_events = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->num_sms * be, (cmax + 255) / 256));
+        sl.grid_observe = (int)std::max<int64_t>(
+            1, std::min<int64_t>((int64_t)ctx->num_sms * bo, (cmax + sl.block_observe - 1) / sl.block_observe));
+        sl.grid_list = ctx->num_sms;
+        if (sink == kSinkSmem && P->n_particles / sl.grid_observe >= ((int64_t)1 << 32) - 1)
+            return fail(&ctx->err, RTMC_ERR_ARG, "too many particles per block for 32-bit shared-memory counts");
+    }
+    // one transport launch over q: the fused kernel, or the split schedule's three kernels
+    auto launch_one = [&](const DevParams<R> &q) -> int {
+        if (split) {
+            const cudaError_t e = cudaMemsetAsync(q.ovf_count, 0, sizeof(uint32_t), ctx->stream);
+            if (e != cudaSuccess) return (int)e;
+            launches += 3;
+            if constexpr (sizeof(R) == 4) return launch_split_f32(q, sl, ctx->stream);
+            else return launch_split_f64(q, sl, ctx->stream);
+        }
+        ++launches;
+        if constexpr (sizeof(R) == 4) return launch_transport_f32(q, (int)grid, block, smem, ctx->stream);
+        else return launch_transport_f64(q, (int)grid, block, smem, ctx->stream);
+    };
     if (sink == kSinkSmem && P->n_particles / grid >= ((int64_t)1 << 32) - 1)
         return fail(&ctx->err, RTMC_ERR_ARG, "too many particles per block for 32-bit shared-memory counts");
     // slice fold: privatise groups of slices in shared memory when 8 or more fit
@@ -618,7 +682,6 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         p.obs_idx = static_cast<int32_t *>(ctx->idx.p);
         p.obs_rows = idx_rows;
     }
-    int le = 0, launches = 0;
     double kms = 0, fms = 0;
     if (n_pipe) {
         const size_t slot_elems = (size_t)idx_rows * P->n_obs;
@@ -633,8 +696,7 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
             if (p.trace) q.trace = p.trace + 16 * base;
             if (c >= 2) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_b1[c - 2], 0), "pipeline wait");
             CK(cudaEventRecord(ctx->ev_a0[c], ctx->stream), "event");
-            if constexpr (sizeof(R) == 4) le = launch_transport_f32(q, (int)grid, block, smem, ctx->stream);
-            else le = launch_transport_f64(q, (int)grid, block, smem, ctx->stream);
+            le = launch_one(q);
             if (le) break;
             CK(cudaEventRecord(ctx->ev_a1[c], ctx->stream), "event");
             CK(cudaStreamWaitEvent(ctx->fold_stream, ctx->ev_a1[c], 0), "pipeline wait");
@@ -647,7 +709,7 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
             le = launch_bin_slices(b, fold_grid, fold_smem, ctx->fold_stream);
             if (le) break;
             CK(cudaEventRecord(ctx->ev_b1[c], ctx->fold_stream), "event");
-            launches += 2;
+            ++launches;
         }
         if (!le) {
             CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_b1[c - 1], 0), "pipeline join");
@@ -670,10 +732,8 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         q.n_particles = std::min<int64_t>(chunk, P->n_particles - base);
         if (p.trace) q.trace = p.trace + 16 * base;
         CK(cudaEventRecord(ctx->ev_k0, ctx->stream), "event");
-        if constexpr (sizeof(R) == 4) le = launch_transport_f32(q, (int)grid, block, smem, ctx->stream);
-        else le = launch_transport_f64(q, (int)grid, block, smem, ctx->stream);
+        le = launch_one(q);
         CK(cudaEventRecord(ctx->ev_k1, ctx->stream), "event");
-        ++launches;
         const bool last = base + chunk >= P->n_particles;
         if (!le && sink == kSinkIndex) {
             BinParams b = bp;
@@ -958,29 +1018,67 @@ int gradient_run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t,
 // ---- rtmc_forward_noalloc: everything staged in the static device scratch ----------
 
 // fixed-capacity vector on the stack (fill_params' edge and Zoeppritz lists)
-template <typename R, int N> struct StackVec {
-    R v[N];
-    size_t n = 0;
-    void clear() { n = 0; }
-    void push_back(R x) { if (n < (size_t)N) v[n++] = x; }
-    void resize(size_t k) { n = k < (size_t)N ? k : (size_t)N; }
+// Host staging area of rtmc_forward_noalloc.  It is file-scope, so a call allocates
+// nothing and keeps no large stack frame (callers may run on small worker-thread stacks).
+// Two halves alternate: a half is filled while the other's copy runs, and the stream is
+// synchronised only before a half is refilled, about once per megabyte of tables.  The
+// fixed-size edge and Zoeppritz lists live here too.  g_stage_mu serialises the calls of
+// the threads of one process.
+constexpr size_t kStageHalf = (size_t)1 << 20;
+constexpr size_t kListBytes = (2 * RTMC_ZOE_N + 2 * (size_t)RTMC_MAX_RADIAL) * sizeof(double);
+alignas(256) unsigned char g_stage[2 * kStageHalf];
+alignas(256) unsigned char g_lists[2][kListBytes];
+std::mutex g_stage_mu;
+
+// push_back list over a fixed area (fill_params' edge and Zoeppritz lists); values past
+// the capacity are counted in `over` rather than stored
+template <typename R> struct FixedVec {
+    R *v;
+    size_t cap, n = 0, over = 0;
+    FixedVec(void *area, size_t bytes) : v(static_cast<R *>(area)), cap(bytes / sizeof(R)) {}
+    void clear() { n = over = 0; }
+    void push_back(R x) { if (n < cap) v[n++] = x; else ++over; }
+    void resize(size_t k) { if (k <= cap) n = k; else { n = cap; over += k - cap; } }
     size_t size() const { return n; }
     R &operator[](size_t i) { return v[i]; }
     R *data() { return v; }
 };
 
-// host -> device copy from a stack buffer that is reused right after
-template <typename T> int copy_chunk(unsigned char *dst, const T *src, size_t count, cudaStream_t st)
+struct Stager {
+    cudaStream_t st;
+    int half = 0;
+    bool busy[2] = {false, false};
+    // a half of the staging area that is free to fill
+    int take(unsigned char **out)
+    {
+        if (busy[half]) {
+            const cudaError_t e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) return (int)e;
+            busy[0] = busy[1] = false;
+        }
+        *out = g_stage + (size_t)half * kStageHalf;
+        return 0;
+    }
+    // copy the first `bytes` of the half just filled to dst; the next take() uses the other half
+    int send(unsigned char *dst, size_t bytes)
+    {
+        const cudaError_t e = cudaMemcpyAsync(dst, g_stage + (size_t)half * kStageHalf, bytes, cudaMemcpyHostToDevice, st);
+        busy[half] = true;
+        half ^= 1;
+        return (int)e;
+    }
+};
+
+// host -> device copy of a list that stays untouched until the call has synchronised
+template <typename T> int copy_list(unsigned char *dst, const T *src, size_t count, cudaStream_t st)
 {
-    cudaError_t e = cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    return (int)e;
+    return (int)cudaMemcpyAsync(dst, src, count * sizeof(T), cudaMemcpyHostToDevice, st);
 }
 
-// same layout as upload_tables, written through stack buffers in chunks
+// same layout as upload_tables, written through the staging area in chunks
 template <typename R>
 int stage_tables_static(const rtmc_tables *t, unsigned char *base, size_t cap, size_t *used, DevTables<R> *dt,
-                        cudaStream_t st, std::string *err)
+                        Stager &sg, std::string *err)
 {
     size_t off[4], total = 0;
     for (int i = 0; i < t->n_tables; ++i) {
@@ -990,27 +1088,28 @@ int stage_tables_static(const rtmc_tables *t, unsigned char *base, size_t cap, s
     if (total > cap)
         return fail(err, RTMC_ERR_ARG, "rtmc_forward_noalloc: the tables need " + std::to_string(total) +
                                             " bytes, more than the static scratch of " + std::to_string(cap) + " bytes");
-    constexpr size_t B = 4096; // staging chunk on the stack
-    Knot<R> kbuf[B];
-    int32_t gbuf[B];
+    constexpr size_t KB = kStageHalf / sizeof(Knot<R>), GB = kStageHalf / sizeof(int32_t);
     for (int i = 0; i < t->n_tables; ++i) {
         const std::vector<double> &c = t->cdf[i], &th = t->theta[i];
         const size_t n = c.size();
         const int bits = guide_bits(n);
         unsigned char *kd = base + off[i];
         unsigned char *gd = kd + align_up(n * sizeof(Knot<R>), 256);
+        unsigned char *h = nullptr;
         int e;
-        for (size_t k0 = 0; k0 < n; k0 += B) {
-            const size_t m = std::min(B, n - k0);
-            fill_knots<R>(c, th, k0, m, kbuf);
-            if ((e = copy_chunk(kd + k0 * sizeof(Knot<R>), kbuf, m, st))) return e;
+        for (size_t k0 = 0; k0 < n; k0 += KB) {
+            const size_t m = std::min(KB, n - k0);
+            if ((e = sg.take(&h))) return e;
+            fill_knots<R>(c, th, k0, m, reinterpret_cast<Knot<R> *>(h));
+            if ((e = sg.send(kd + k0 * sizeof(Knot<R>), m * sizeof(Knot<R>)))) return e;
         }
         const int64_t ng = ((int64_t)1 << bits) + 1;
         size_t k = 0;
-        for (int64_t j0 = 0; j0 < ng; j0 += (int64_t)B) {
-            const int64_t m = std::min<int64_t>((int64_t)B, ng - j0);
-            fill_guide(c, bits, j0, m, &k, gbuf);
-            if ((e = copy_chunk(gd + (size_t)j0 * sizeof(int32_t), gbuf, (size_t)m, st))) return e;
+        for (int64_t j0 = 0; j0 < ng; j0 += (int64_t)GB) {
+            const int64_t m = std::min<int64_t>((int64_t)GB, ng - j0);
+            if ((e = sg.take(&h))) return e;
+            fill_guide(c, bits, j0, m, &k, reinterpret_cast<int32_t *>(h));
+            if ((e = sg.send(gd + (size_t)j0 * sizeof(int32_t), (size_t)m * sizeof(int32_t)))) return e;
         }
         dt->knot[i] = reinterpret_cast<const Knot<R> *>(kd);
         dt->guide[i] = reinterpret_cast<const int32_t *>(gd);
@@ -1027,6 +1126,7 @@ int forward_noalloc(const rtmc_problem *P, const rtmc_tables *t, int64_t *d_hist
     rtmc_context slot; // error slot for check_problem; owns no device resources
     int s = check_problem(&slot, P, t);
     if (s) return fail(nullptr, s, slot.err);
+    std::lock_guard<std::mutex> lock(g_stage_mu);
     std::string err;
     int dev = 0, sms = 0, smem_optin = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -1041,16 +1141,15 @@ int forward_noalloc(const rtmc_problem *P, const rtmc_tables *t, int64_t *d_hist
     const int prec = sizeof(R) == 4 ? RTMC_FP32 : RTMC_FP64;
     DevTables<R> dt{};
     size_t used = 0;
-    if ((s = stage_tables_static<R>(t, base, cap, &used, &dt, st, &err)) != 0)
+    Stager sg{st};
+    if ((s = stage_tables_static<R>(t, base, cap, &used, &dt, sg, &err)) != 0)
         return s == RTMC_ERR_ARG ? fail(nullptr, s, err) : fail(nullptr, RTMC_ERR_CUDA, "rtmc_forward_noalloc: table staging");
     DevParams<R> p;
-    StackVec<R, kMaxEdges> edges;
-    StackVec<R, kMaxEdges> zoe; // same type as the edge list: 2 x 181 values and the radial table
+    FixedVec<R> edges(g_lists[0], sizeof g_lists[0]);
+    FixedVec<R> zoe(g_lists[1], sizeof g_lists[1]); // 2 x 181 Zoeppritz values and the radial table
     int n_edges = 0;
-    if (2 * RTMC_ZOE_N + 2 * P->src_radial_n > kMaxEdges)
-        return fail(nullptr, RTMC_ERR_ARG, "rtmc_forward_noalloc: a radial source profile holds at most " +
-                                               std::to_string((kMaxEdges - 2 * RTMC_ZOE_N) / 2) + " knots here");
     fill_params<R>(&slot, P, dt, &p, &n_edges, &edges, &zoe);
+    if (edges.over || zoe.over) return fail(nullptr, RTMC_ERR_ARG, "rtmc_forward_noalloc: edge or source tables too long");
     p.event_major = 0; // index path: each warp writes its 32 rows together
     const size_t e_off = align_up(used, 256);
     const size_t z_off = align_up(e_off + std::max<size_t>(1, edges.size()) * sizeof(R), 256);
@@ -1063,9 +1162,9 @@ int forward_noalloc(const rtmc_problem *P, const rtmc_tables *t, int64_t *d_hist
                                                std::to_string(cap) + " bytes");
     if (P->time_stride >= ((int64_t)1 << 30))
         return fail(nullptr, RTMC_ERR_ARG, "rtmc_forward_noalloc: a time slice must hold fewer than 2^30 bins");
-    if (edges.size() && (s = copy_chunk(base + e_off, edges.data(), edges.size(), st)) != 0)
+    if (edges.size() && (s = copy_list(base + e_off, edges.data(), edges.size(), st)) != 0)
         return fail(nullptr, RTMC_ERR_CUDA, "rtmc_forward_noalloc: edge staging");
-    if ((s = copy_chunk(base + z_off, zoe.data(), zoe.size(), st)) != 0)
+    if ((s = copy_list(base + z_off, zoe.data(), zoe.size(), st)) != 0)
         return fail(nullptr, RTMC_ERR_CUDA, "rtmc_forward_noalloc: Zoeppritz staging");
     e = cudaMemsetAsync(d_hist, 0, (size_t)P->hist_len * sizeof(int64_t), st);
     if (e == cudaSuccess) e = cudaMemsetAsync(base + c_off, 0, 256, st);
@@ -1295,6 +1394,15 @@ extern "C" int rtmc_copy_histogram(rtmc_context *ctx, int64_t *hist_out, int64_t
     return RTMC_OK;
 }
 
+extern "C" int rtmc_histogram_device(rtmc_context *ctx, void **ptr, int64_t *n)
+{
+    if (!ctx || !ptr || !n) return fail(ctx ? &ctx->err : nullptr, RTMC_ERR_ARG, "rtmc_histogram_device: NULL argument");
+    if (!ctx->hist.p || ctx->hist_len <= 0) return fail(&ctx->err, RTMC_ERR_ARG, "rtmc_histogram_device: no histogram yet");
+    *ptr = ctx->hist.p;
+    *n = ctx->hist_len;
+    return RTMC_OK;
+}
+
 extern "C" int rtmc_forward_noalloc(const rtmc_problem *P, const rtmc_tables *t, int64_t *hist_device, void *stream,
                                     rtmc_stats *stats)
 {
@@ -1344,7 +1452,7 @@ extern "C" int rtmc_set_pipeline(rtmc_context *ctx, int32_t chunks, int32_t tran
 extern "C" int rtmc_set_schedule(rtmc_context *ctx, int32_t event_major)
 {
     if (!ctx) return fail(nullptr, RTMC_ERR_ARG, "rtmc_set_schedule: NULL context");
-    if (event_major < -1 || event_major > 1) return fail(&ctx->err, RTMC_ERR_ARG, "event_major must be -1, 0 or 1");
+    if (event_major < -1 || event_major > 2) return fail(&ctx->err, RTMC_ERR_ARG, "schedule must be -1, 0, 1 or 2");
     ctx->opt_event_major = event_major;
     return RTMC_OK;
 }

@@ -128,12 +128,24 @@ __global__ void __launch_bounds__(512) rt_bin_slices_smem(const BinParams b)
     __syncthreads();
     const int64_t p0 = (int64_t)blockIdx.x * b.part_per_block;
     const int64_t p1 = min(b.n, p0 + b.part_per_block);
+    // 16-byte loads over the vectors covering [p0, p1) (rows are 128-byte aligned and
+    // padded to a multiple of 32 entries), two in flight per thread; entries outside the
+    // range are skipped
+    const int64_t q0 = p0 >> 2, q1 = (p1 + 3) >> 2;
     for (int j = j0; j <= j1; ++j) {
-        const int32_t *row = b.idx + (int64_t)(j - 1) * b.rows;
+        const int4 *row4 = reinterpret_cast<const int4 *>(b.idx + (int64_t)(j - 1) * b.rows);
         unsigned *sj = sh + (j - j0) * per;
-        for (int64_t k = p0 + threadIdx.x; k < p1; k += blockDim.x) {
-            const int v = __ldcs(row + k);
-            if (v >= 0) atomicAdd(sj + ((v >> 30) ? b.slice_bins : 0) + (v & 0x3fffffff), 1u);
+        for (int64_t q = q0 + threadIdx.x; q < q1; q += 2 * (int64_t)blockDim.x) {
+            const int64_t q2 = q + blockDim.x;
+            const int4 a = __ldcs(row4 + q);
+            const int4 c = q2 < q1 ? __ldcs(row4 + q2) : make_int4(-1, -1, -1, -1);
+            const int va[8] = {a.x, a.y, a.z, a.w, c.x, c.y, c.z, c.w};
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+                const int v = va[u];
+                const int64_t k = (u < 4 ? q : q2) * 4 + (u & 3);
+                if (v >= 0 && k >= p0 && k < p1) atomicAdd(sj + ((v >> 30) ? b.slice_bins : 0) + (v & 0x3fffffff), 1u);
+            }
         }
     }
     __syncthreads();
@@ -296,7 +308,8 @@ void *kernel_of(int precision, int kind, int sink, int obs)
     switch (kind) {
     case 0: return d ? kernel_of_transport_f64(sink, obs) : kernel_of_transport_f32(sink, obs);
     case 1: case 2: return d ? kernel_of_batch_f64(kind == 2, obs) : kernel_of_batch_f32(kind == 2, obs);
-    default: return d ? kernel_of_adjoint_f64(kind == 4, obs) : kernel_of_adjoint_f32(kind == 4, obs);
+    case 3: case 4: return d ? kernel_of_adjoint_f64(kind == 4, obs) : kernel_of_adjoint_f32(kind == 4, obs);
+    default: return d ? kernel_of_split_f64(kind, sink, obs) : kernel_of_split_f32(kind, sink, obs);
     }
 }
 

@@ -1,11 +1,12 @@
 // Instantiation unit of the transport kernel family (transport.cuh).  The build compiles
-// this file six times, once per precision RTMC_REAL (float, double) and part RTMC_PART
-// (1 the transport kernels, 2 the batched kernels, 3 the adjoint kernels), so the
-// variants compile in parallel; RTMC_SUFFIX names the precision (f32, f64).
+// this file eight times, once per precision RTMC_REAL (float, double) and part RTMC_PART
+// (1 the transport kernels, 2 the batched kernels, 3 the adjoint kernels, 4 the kernels of
+// the split schedule), so the variants compile in parallel; RTMC_SUFFIX names the
+// precision (f32, f64).
 #include "transport.cuh"
 
 #if !defined(RTMC_REAL) || !defined(RTMC_PART) || !defined(RTMC_SUFFIX)
-#error "compile with -DRTMC_REAL=float|double -DRTMC_SUFFIX=f32|f64 -DRTMC_PART=1|2|3"
+#error "compile with -DRTMC_REAL=float|double -DRTMC_SUFFIX=f32|f64 -DRTMC_PART=1|2|3|4"
 #endif
 
 #define RTMC_CAT2(a, b) a##_##b
@@ -21,6 +22,16 @@ int RTMC_NAME(launch_transport)(const DevParams<RTMC_REAL> &p, int grid, int blo
 }
 
 void *RTMC_NAME(kernel_of_transport)(int sink, int obs) { return pick_t<RTMC_REAL>(sink, obs); }
+#elif RTMC_PART == 4
+int RTMC_NAME(launch_split)(const DevParams<RTMC_REAL> &p, const SplitLaunch &l, void *stream)
+{
+    return launch_split_t<RTMC_REAL>(p, l, stream);
+}
+
+void *RTMC_NAME(kernel_of_split)(int kind, int sink, int obs)
+{
+    return kind == 5 ? pick_events<RTMC_REAL>(obs) : (kind == 6 ? pick_observe<RTMC_REAL>(sink, obs) : pick_list<RTMC_REAL>(obs));
+}
 #elif RTMC_PART == 2
 int RTMC_NAME(launch_transport_batch)(const BatchArgs<RTMC_REAL> &a, int grid, int block, size_t smem, void *stream)
 {

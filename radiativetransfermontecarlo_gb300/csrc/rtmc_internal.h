@@ -112,6 +112,15 @@ template <typename R> struct DevParams {
     double *trace;  // optional [n_particles][16] final particle states
     int32_t *obs_idx;  // index sink: [n_obs][obs_rows] in-slice bin | mode << 30, or -1
     int64_t obs_rows;
+    // split schedule (rt_events, then rt_observe): seg_cap trajectory segments per particle
+    // in segs, the segment count and death sub-step of each particle in seg_head (count -1:
+    // more segments than seg_cap; such particles are listed in ovf_list and rerun by
+    // rt_transport_list)
+    void *segs;
+    int32_t *seg_head;  // [n_particles][2]
+    int32_t *ovf_list;
+    uint32_t *ovf_count;
+    int32_t seg_cap, split;
 };
 
 // Parameters of the slice fold (rt_bin_slices*).
@@ -161,10 +170,22 @@ struct AdjointArgs {
     double *partial;          // [gridDim.x][n_params] block sums
 };
 
+// Launch shape of the split schedule (rt_events, rt_observe, rt_transport_list).
+struct SplitLaunch {
+    int grid_events, grid_observe, block_observe, grid_list;
+    size_t smem_events, smem_observe;
+};
+
 // Launch wrappers (kernels.cu, fold.cu).  Return a cudaError_t value.
+int launch_split_f32(const DevParams<float> &p, const SplitLaunch &l, void *stream);
+int launch_split_f64(const DevParams<double> &p, const SplitLaunch &l, void *stream);
+// kind 5: rt_events, 6: rt_observe (sink, obs), 7: rt_transport_list
+void *kernel_of_split_f32(int kind, int sink, int obs);
+void *kernel_of_split_f64(int kind, int sink, int obs);
 // kernel_of(precision, kind, sink, obs): the kernel function of a transport (kind 0, with
-// its sink and observation path), batch (1), event-major batch (2), adjoint (3) or ring
-// adjoint (4) variant; kernel_set_smem sets its dynamic shared-memory limit.
+// its sink and observation path), batch (1), event-major batch (2), adjoint (3), ring
+// adjoint (4), split-schedule events (5), observations (6, with its sink) or overflow
+// rerun (7) variant; kernel_set_smem sets its dynamic shared-memory limit.
 void *kernel_of_transport_f32(int sink, int obs);
 void *kernel_of_transport_f64(int sink, int obs);
 void *kernel_of_batch_f32(int em, int obs);

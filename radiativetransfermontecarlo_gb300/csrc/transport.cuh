@@ -713,6 +713,27 @@ __device__ __forceinline__ double m_fast_sqrt(double x) { return sqrt(x); }
 __device__ __forceinline__ int m_floor_int(float x) { return __float2int_rd(x); }
 __device__ __forceinline__ int m_floor_int(double x) { return __double2int_rd(x); }
 
+// Bin of a coordinate t measured in bin widths: floor(t) for t in [0, 2^23), and a value
+// outside [0, 2^23) (negative, or at least 2^23) for every other t, infinities and NaN
+// included, so one unsigned compare against the bin count rejects all of those.  FP32:
+// adding 2^23 with rounding toward zero leaves floor(t) in the low mantissa bits (one
+// FADD and one integer add on the FMA/ALU pipes instead of a float-to-int conversion).
+__device__ __forceinline__ int bin_floor(float t) { return __float_as_int(__fadd_rz(t, 8388608.0f)) - 0x4B000000; }
+__device__ __forceinline__ int bin_floor(double t)
+{
+    return t >= 0.0 && t < 8388608.0 ? __double2int_rd(t) : -1;
+}
+
+// Multiply-adds and products of the binning written out, so that every kernel that bins
+// (the fused transports, the batch, the split schedule's observation kernel) rounds them
+// the same way and puts an observation on a bin edge into the same bin.
+__device__ __forceinline__ float m_fma(float a, float b, float c) { return __fmaf_rn(a, b, c); }
+__device__ __forceinline__ double m_fma(double a, double b, double c) { return __fma_rn(a, b, c); }
+__device__ __forceinline__ float m_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double m_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float m_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double m_sub(double a, double b) { return __dsub_rn(a, b); }
+
 // observeTime.m:14-144 for the position axes X, Y, Z of one observation in any frame:
 // offset of the bin inside the time slice (direction part excluded), or -1
 template <typename R>
@@ -759,7 +780,9 @@ __device__ __forceinline__ int pos_offset(const DevParams<R> &p, const R *sedges
 enum { OBS_GENERAL = 0, OBS_CART = 1, OBS_RADIAL = 2 };
 
 // A straight piece of trajectory: position x at sub-step s0, direction d, mode, plus the
-// per-segment binning terms of the observation path.
+// per-segment binning terms of the observation path.  On the cartesian and radius-only
+// paths the ring holds the prepared terms (A, B or x, B, and the direction offset), so a
+// segment coming into force in the observation phase needs no arithmetic.
 template <typename R> struct Seg {
     R x[3], d[3];
     R A[3], B[3];
@@ -775,12 +798,12 @@ __device__ __forceinline__ void seg_prepare(const DevParams<R> &p, const R *sedg
     if (OBS == OBS_CART) {
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            g.A[a] = (g.x[a] - p.ax_lo[a]) * p.ax_inv_w[a];
-            g.B[a] = step * g.d[a] * p.ax_inv_w[a];
+            g.A[a] = m_mul(m_sub(g.x[a], p.ax_lo[a]), p.ax_inv_w[a]);
+            g.B[a] = m_mul(m_mul(step, g.d[a]), p.ax_inv_w[a]);
         }
     } else if (OBS == OBS_RADIAL) {
 #pragma unroll
-        for (int a = 0; a < 3; ++a) g.B[a] = step * g.d[a];
+        for (int a = 0; a < 3; ++a) g.B[a] = m_mul(step, g.d[a]);
     }
 }
 
@@ -788,30 +811,31 @@ __device__ __forceinline__ void seg_prepare(const DevParams<R> &p, const R *sedg
 template <typename R, int OBS>
 __device__ __forceinline__ int obs_offset(const DevParams<R> &p, const R *sedges, const Seg<R> &g, int so)
 {
-    if (g.doff < 0) return -1;
     const R dl = (R)(so - g.s0);
     if (OBS == OBS_CART) {
+        // branch-free: the three bins, one combined range test
         int idx = g.doff;
+        bool ok = g.doff >= 0;
 #pragma unroll
         for (int a = 0; a < 3; ++a) {
-            const int b = m_floor_int(g.A[a] + g.B[a] * dl);
-            if ((unsigned)b >= (unsigned)p.ax_nbe[a]) return -1;
+            const int b = bin_floor(m_fma(g.B[a], dl, g.A[a]));
+            ok = ok && (unsigned)b < (unsigned)p.ax_nbe[a];
             idx += b * p.ax_stride32[a];
         }
-        return idx;
+        return ok ? idx : -1;
     } else if (OBS == OBS_RADIAL) {
-        const R x0 = g.x[0] + g.B[0] * dl, x1 = g.x[1] + g.B[1] * dl;
-        R r2 = x0 * x0 + x1 * x1;
+        const R x0 = m_fma(g.B[0], dl, g.x[0]), x1 = m_fma(g.B[1], dl, g.x[1]);
+        R r2 = m_fma(x1, x1, m_mul(x0, x0));
         if (p.radial_3d) {
-            const R x2 = g.x[2] + g.B[2] * dl;
-            r2 += x2 * x2;
+            const R x2 = m_fma(g.B[2], dl, g.x[2]);
+            r2 = m_fma(x2, x2, r2);
         }
-        const int b = m_floor_int(m_fast_sqrt(r2) * p.ax_inv_w[0] + p.ax_a0);
-        if ((unsigned)b >= (unsigned)p.ax_nbe[0]) return -1;
-        return g.doff + b * p.ax_stride32[0];
+        const int b = bin_floor(m_fma(m_fast_sqrt(r2), p.ax_inv_w[0], p.ax_a0));
+        return (g.doff >= 0 && (unsigned)b < (unsigned)p.ax_nbe[0]) ? g.doff + b * p.ax_stride32[0] : -1;
     } else {
-        const R dt = by_mode(p.step, g.mode) * dl;
-        const R xo[3] = {g.x[0] + dt * g.d[0], g.x[1] + dt * g.d[1], g.x[2] + dt * g.d[2]};
+        if (g.doff < 0) return -1;
+        const R dt = m_mul(by_mode(p.step, g.mode), dl);
+        const R xo[3] = {m_fma(dt, g.d[0], g.x[0]), m_fma(dt, g.d[1], g.x[1]), m_fma(dt, g.d[2], g.x[2])};
         const int po = pos_offset(p, sedges, xo);
         return po < 0 ? -1 : po + g.doff;
     }
@@ -840,7 +864,31 @@ template <typename R> struct Ring {
         g.s0 = s0[k]; g.mode = mode[k];
         if (TH) g.th = th[k];
     }
-    __device__ __forceinline__ int start(int slot) const { return s0[slot * stride + threadIdx.x]; }
+    // prepared segments of the cartesian (A, B) and radius-only (x, B) paths: the start
+    // sub-step (below 2^30) carries the mode in bit 30, and the mode slot holds the
+    // direction offset (negative: outside the direction range)
+    template <int OBS, bool TH = false> __device__ __forceinline__ void put_prepared(int slot, const Seg<R> &g, R t) const
+    {
+        const int k = slot * stride + threadIdx.x;
+        const R *u = OBS == OBS_CART ? g.A : g.x;
+        x0[k] = u[0]; x1[k] = u[1]; x2[k] = u[2];
+        d0[k] = g.B[0]; d1[k] = g.B[1]; d2[k] = g.B[2];
+        s0[k] = g.s0 | (g.mode << 30); mode[k] = g.doff;
+        if (TH) th[k] = t;
+    }
+    template <int OBS, bool TH = false> __device__ __forceinline__ void get_prepared(int slot, Seg<R> &g) const
+    {
+        const int k = slot * stride + threadIdx.x;
+        R *u = OBS == OBS_CART ? g.A : g.x;
+        u[0] = x0[k]; u[1] = x1[k]; u[2] = x2[k];
+        g.B[0] = d0[k]; g.B[1] = d1[k]; g.B[2] = d2[k];
+        const int sm = s0[k];
+        g.s0 = sm & 0x3fffffff;
+        g.mode = sm >> 30;
+        g.doff = mode[k];
+        if (TH) g.th = th[k];
+    }
+    __device__ __forceinline__ int start(int slot) const { return s0[slot * stride + threadIdx.x] & 0x3fffffff; }
 };
 
 template <typename R> __device__ __forceinline__ void seg_from(const Part<R> &s, Seg<R> &g)
@@ -960,6 +1008,18 @@ __device__ __forceinline__ void run_batch(const DevParams<R> &p, const R *sedges
     seg_from(s, cur);
     seg_prepare<R, OBS>(p, sedges, cur);
     if (ADJ) adj->start();
+    // the cartesian and radius-only paths keep prepared segments in the ring: their binning
+    // terms are computed in phase 1, where events run converged, not when a lane's segment
+    // comes into force in phase 2
+    constexpr bool PREP = OBS == OBS_CART || OBS == OBS_RADIAL;
+    auto take = [&](int slot) { // cur = the ring's segment in `slot`, ready for binning
+        if constexpr (PREP) {
+            ring.template get_prepared<OBS, ADJ>(slot, cur);
+        } else {
+            ring.template get<ADJ>(slot, cur);
+            seg_prepare<R, OBS>(p, sedges, cur);
+        }
+    };
     int32_t *optr = (SINK == SINK_INDEX && have) ? p.obs_idx + i : nullptr;
     int jn = 1; // warp-uniform
     while (jn <= p.n_obs) {
@@ -969,9 +1029,8 @@ __device__ __forceinline__ void run_batch(const DevParams<R> &p, const R *sedges
             // segments starting at or before the next observation supersede the
             // current one: consume them, so the ring only holds later segments
             while (count > 0 && ring.start(head) <= so_next) {
-                ring.template get<ADJ>(head, cur);
+                take(head);
                 if (ADJ) adj->enter(cur.th);
-                seg_prepare<R, OBS>(p, sedges, cur);
                 head = (head + 1) % C;
                 --count;
             }
@@ -987,7 +1046,14 @@ __device__ __forceinline__ void run_batch(const DevParams<R> &p, const R *sedges
                         if (ADJ) adj->enter(th);
                         seg_prepare<R, OBS>(p, sedges, cur);
                     } else {
-                        ring.template put<ADJ>((head + count) % C, s, th);
+                        if constexpr (PREP) {
+                            Seg<R> g;
+                            seg_from(s, g);
+                            seg_prepare<R, OBS>(p, sedges, g);
+                            ring.template put_prepared<OBS, ADJ>((head + count) % C, g, th);
+                        } else {
+                            ring.template put<ADJ>((head + count) % C, s, th);
+                        }
                         ++count;
                     }
                 }
@@ -1020,12 +1086,11 @@ __device__ __forceinline__ void run_batch(const DevParams<R> &p, const R *sedges
         // make cur the segment in force at sub-step at
         auto advance = [&](int at) {
             do {
-                ring.template get<ADJ>(head, cur);
+                take(head);
                 if (ADJ) adj->enter(cur.th);
                 head = (head + 1) % C;
                 --count;
             } while (count > 0 && ring.start(head) <= at);
-            seg_prepare<R, OBS>(p, sedges, cur);
             next_start = count > 0 ? ring.start(head) : 0x7fffffff;
         };
         auto emit = [&](int v, int mode, int j) {
@@ -1202,6 +1267,290 @@ __global__ void __launch_bounds__(Bounds<R, SINK>::threads, Bounds<R, SINK>::min
             if (c) atomicAdd(p.hist + k, (unsigned long long)c << p.hist_shift);
         }
     }
+}
+
+// ---------------------------------------------------------------------------------
+// Split schedule: the events of every particle first (rt_events), then the observations
+// (rt_observe).  In the two-cursor batch a warp's phase 1 runs an event only for the lanes
+// whose particle has one left, so rounds late in a batch run with a few lanes and the
+// latency of the table lookups is exposed; rt_events gives each thread a stream of
+// particles and starts new ones whenever enough lanes are free, so events run with most
+// lanes active, and writes each particle's trajectory segments (prepared for the
+// observation path) to global memory.  rt_observe then bins every observation instant of
+// 32 particles per warp in lockstep with no event code at all.  Same events, same
+// segments, same bins as rt_transport.
+// ---------------------------------------------------------------------------------
+
+// A prepared segment in global memory: u = A (cartesian), x (radius-only, general);
+// v = B (cartesian, radius-only) or d (general); the start sub-step with the mode in bit
+// 30, and the direction offset.  32 bytes in FP32 (two 16-byte vectors), 64 in FP64.
+__device__ __forceinline__ void rec_store(float *r, const float u[3], const float v[3], int sm, int doff)
+{
+    float4 *q = reinterpret_cast<float4 *>(r);
+    q[0] = make_float4(u[0], u[1], u[2], v[0]);
+    q[1] = make_float4(v[1], v[2], __int_as_float(sm), __int_as_float(doff));
+}
+__device__ __forceinline__ void rec_store(double *r, const double u[3], const double v[3], int sm, int doff)
+{
+    double2 *q = reinterpret_cast<double2 *>(r);
+    q[0] = make_double2(u[0], u[1]);
+    q[1] = make_double2(u[2], v[0]);
+    q[2] = make_double2(v[1], v[2]);
+    q[3] = make_double2(__longlong_as_double((long long)(((unsigned long long)(unsigned)doff << 32) | (unsigned)sm)), 0.0);
+}
+__device__ __forceinline__ void rec_load(const float *r, float u[3], float v[3], int &sm, int &doff)
+{
+    const float4 *q = reinterpret_cast<const float4 *>(r);
+    const float4 a = __ldg(q), b = __ldg(q + 1);
+    u[0] = a.x; u[1] = a.y; u[2] = a.z; v[0] = a.w;
+    v[1] = b.x; v[2] = b.y; sm = __float_as_int(b.z); doff = __float_as_int(b.w);
+}
+__device__ __forceinline__ void rec_load(const double *r, double u[3], double v[3], int &sm, int &doff)
+{
+    const double2 *q = reinterpret_cast<const double2 *>(r);
+    const double2 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2), d = __ldg(q + 3);
+    u[0] = a.x; u[1] = a.y; u[2] = b.x; v[0] = b.y; v[1] = c.x; v[2] = c.y;
+    const unsigned long long w = (unsigned long long)__double_as_longlong(d.x);
+    sm = (int)(unsigned)(w & 0xffffffffull);
+    doff = (int)(unsigned)(w >> 32);
+}
+constexpr int kRecWords = 8; // R values per record
+
+template <typename R, int OBS> __device__ __forceinline__ void rec_put(R *r, const Seg<R> &g)
+{
+    const R *u = OBS == OBS_CART ? g.A : g.x;
+    const R *v = OBS == OBS_GENERAL ? g.d : g.B;
+    rec_store(r, u, v, g.s0 | (g.mode << 30), g.doff);
+}
+template <typename R, int OBS> __device__ __forceinline__ void rec_get(const R *r, Seg<R> &g)
+{
+    R *u = OBS == OBS_CART ? g.A : g.x;
+    R *v = OBS == OBS_GENERAL ? g.d : g.B;
+    int sm;
+    rec_load(r, u, v, sm, g.doff);
+    g.s0 = sm & 0x3fffffff;
+    g.mode = sm >> 30;
+}
+
+// lanes of a warp that start new particles together in rt_events
+constexpr int kEventStartLanes = 8;
+
+template <typename R, int OBS>
+__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) rt_events(const DevParams<R> p)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R *sedges = reinterpret_cast<R *>(smem_raw);
+    for (int k = threadIdx.x; k < p.n_edges; k += blockDim.x) sedges[k] = p.edges[k];
+    __syncthreads();
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int K = p.seg_cap;
+    R *segs = static_cast<R *>(p.segs);
+    Counters cnt = {0u, 0u, 0u, 0u, 0u, 0u}, c0 = cnt;
+    bool bad = false;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    bool have = false;
+    int nseg = 0;
+    Part<R> s;
+    Seg<R> g;
+    for (;;) {
+        const bool idle = !have && i < p.n_particles;
+        const unsigned idle_mask = __ballot_sync(full, idle), busy_mask = __ballot_sync(full, have);
+        if (!(idle_mask | busy_mask)) break;
+        // free lanes start their next particles together, once enough of them are free
+        if (idle && (__popc(idle_mask) >= kEventStartLanes || !busy_mask)) {
+            init_particle(p, (uint64_t)(p.pid0 + i), s);
+            c0 = cnt;
+            seg_from(s, g);
+            seg_prepare<R, OBS>(p, sedges, g);
+            rec_put<R, OBS>(segs + (size_t)i * K * kRecWords, g);
+            nseg = 1;
+            have = true;
+        }
+        if (!have) continue;
+        int done = 0; // 1: the particle's run is over, 2: its segments overflow seg_cap
+        if (next_event(s) > p.s_end) {
+            done = 1;
+        } else {
+            process_event(p, (uint64_t)(p.pid0 + i), s, cnt);
+            if ((int)s.k > p.max_events) { s.alive = 0; s.s_death = s.s0; bad = true; }
+            if (!s.alive) {
+                done = 1;
+            } else if (nseg < K) {
+                seg_from(s, g);
+                seg_prepare<R, OBS>(p, sedges, g);
+                rec_put<R, OBS>(segs + ((size_t)i * K + nseg) * kRecWords, g);
+                ++nseg;
+            } else {
+                done = 2;
+            }
+        }
+        if (done) {
+            int32_t *h = p.seg_head + 2 * i;
+            if (done == 1) {
+                h[0] = nseg;
+                h[1] = s.alive ? 0x7fffffff : s.s_death;
+                if (p.trace) { // final state of the particle, the oracle's layout
+                    double *f = p.trace + 16 * i;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) { f[c] = s.x[c]; f[3 + c] = s.d[c]; f[6 + c] = s.q[c]; }
+                    f[9] = s.mode; f[10] = s.alive; f[11] = cnt.scat - c0.scat; f[12] = cnt.bnd - c0.bnd;
+                    f[13] = s.s0; f[14] = s.s_death; f[15] = s.k;
+                }
+            } else { // rerun whole by rt_transport_list: its events are not counted here
+                h[0] = -1;
+                h[1] = 0;
+                cnt = c0;
+                p.ovf_list[atomicAdd(p.ovf_count, 1u)] = (int32_t)i;
+            }
+            have = false;
+            i += stride;
+        }
+    }
+    unsigned v[6] = {cnt.scat, cnt.bnd, cnt.kill, cnt.absorb, cnt.obs, cnt.conv};
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        const unsigned t = __reduce_add_sync(full, v[c]);
+        if (lane == 0 && t) atomicAdd(p.stats + c, (unsigned long long)t);
+    }
+    if (bad) atomicExch(p.status, 1);
+}
+
+// Observations of the particles rt_events traced: a warp takes 32 consecutive particles
+// and walks the observation instants in lockstep, each lane on its own segment list (the
+// segment after the one in force is loaded ahead, so a segment change waits on nothing).
+template <typename R, int SINK, int OBS>
+__device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *sedges, unsigned *shist, int64_t base,
+                                              Counters &cnt, bool &bad)
+{
+    constexpr bool SMEM = SINK == SINK_SMEM;
+    const int lane = threadIdx.x & 31;
+    const unsigned long long inc = 1ull << p.hist_shift;
+    const int K = p.seg_cap;
+    const int64_t i = base + lane;
+    const bool have = i < p.n_particles;
+    int nseg = 0, limit = 0; // observations at sub-steps below `limit` are binned
+    if (have) {
+        const int2 h = __ldg(reinterpret_cast<const int2 *>(p.seg_head) + i);
+        nseg = h.x;
+        limit = nseg > 0 ? h.y : 0; // an overflowing particle is binned by rt_transport_list
+    }
+    const R *rec = static_cast<const R *>(p.segs) + (size_t)(have ? i : 0) * K * kRecWords;
+    Seg<R> cur, nxt;
+    cur.s0 = 0; cur.mode = 0; cur.doff = -1;
+    int k = 0, next_start = 0x7fffffff;
+    if (nseg > 0) rec_get<R, OBS>(rec, cur);
+    if (nseg > 1) { rec_get<R, OBS>(rec + kRecWords, nxt); next_start = nxt.s0; }
+    int32_t *optr = (SINK == SINK_INDEX && have) ? p.obs_idx + i : nullptr;
+    auto observe = [&](int so) -> int {
+        if (so >= limit) return -1;
+        while (so >= next_start) { // the next segment comes into force; load the one after it
+            cur = nxt;
+            ++k;
+            if (k + 1 < nseg) {
+                rec_get<R, OBS>(rec + (size_t)(k + 1) * kRecWords, nxt);
+                next_start = nxt.s0;
+            } else {
+                next_start = 0x7fffffff;
+            }
+        }
+        return obs_offset<R, OBS>(p, sedges, cur, so);
+    };
+    auto emit = [&](int v, int mode, int j) {
+        if (SINK == SINK_INDEX) {
+            if (have) {
+                *optr = v < 0 ? -1 : (v | (mode << 30));
+                optr += p.obs_rows;
+            }
+            if (v >= 0) cnt.obs++;
+        } else if (v >= 0) {
+            const int64_t idx = (int64_t)j * p.time_stride + (mode ? p.mode_stride : 0) + v;
+            if (idx < p.hist_len) {
+                cnt.obs++;
+                if (SMEM) atomicAdd(shist + idx, 1u);
+                else atomicAdd(p.hist + idx, inc);
+            } else {
+                bad = true;
+            }
+        }
+    };
+    int j = 1;
+    for (; j + 1 <= p.n_obs; j += 2) { // two instants per iteration: independent chains
+        const int v0 = observe(j * p.n_sub);
+        const int m0 = cur.mode;
+        const int v1 = observe((j + 1) * p.n_sub);
+        emit(v0, m0, j);
+        emit(v1, cur.mode, j + 1);
+    }
+    if (j <= p.n_obs) {
+        const int v = observe(j * p.n_sub);
+        emit(v, cur.mode, j);
+    }
+}
+
+template <typename R, int SINK> struct ObserveBounds {
+    static constexpr int threads = SINK == SINK_SMEM ? 512 : 256;
+    static constexpr int min_blocks = SINK == SINK_SMEM ? 1 : (sizeof(R) == 4 ? 4 : 2);
+};
+
+template <typename R, int SINK, int OBS>
+__global__ void __launch_bounds__(ObserveBounds<R, SINK>::threads, ObserveBounds<R, SINK>::min_blocks)
+    rt_observe(const DevParams<R> p)
+{
+    constexpr bool SMEM = SINK == SINK_SMEM;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R *sedges = reinterpret_cast<R *>(smem_raw);
+    const size_t off = (((size_t)p.n_edges * sizeof(R) + 15) / 16) * 16;
+    unsigned *shist = reinterpret_cast<unsigned *>(smem_raw + off);
+    const int T = blockDim.x;
+    for (int k = threadIdx.x; k < p.n_edges; k += T) sedges[k] = p.edges[k];
+    if (SMEM)
+        for (int64_t k = threadIdx.x; k < p.hist_len; k += T) shist[k] = 0u;
+    __syncthreads();
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    Counters cnt = {0u, 0u, 0u, 0u, 0u, 0u};
+    bool bad = false;
+    const int64_t warps = ((int64_t)gridDim.x * T) >> 5;
+    for (int64_t base = (((int64_t)blockIdx.x * T + threadIdx.x) >> 5) << 5; base < p.n_particles; base += warps * 32)
+        observe_batch<R, SINK, OBS>(p, sedges, shist, base, cnt, bad);
+    const unsigned t = __reduce_add_sync(full, cnt.obs);
+    if (lane == 0 && t) atomicAdd(p.stats + 4, (unsigned long long)t);
+    if (bad) atomicExch(p.status, 1);
+    if (SMEM) {
+        __syncthreads();
+        for (int64_t k = threadIdx.x; k < p.hist_len; k += T) {
+            const unsigned c = shist[k];
+            if (c) atomicAdd(p.hist + k, (unsigned long long)c << p.hist_shift);
+        }
+    }
+}
+
+// The particles whose segments overflowed seg_cap in rt_events, rerun whole one per
+// thread (the event-major schedule) with their observations added to the histogram by
+// 64-bit global atomics; their rows of the index array hold -1.  The list length is read
+// on the device, so the launch needs no host synchronisation.
+template <typename R, int OBS>
+__global__ void __launch_bounds__(256) rt_transport_list(const DevParams<R> p)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R *sedges = reinterpret_cast<R *>(smem_raw);
+    for (int k = threadIdx.x; k < p.n_edges; k += blockDim.x) sedges[k] = p.edges[k];
+    __syncthreads();
+    const unsigned n = *reinterpret_cast<volatile const uint32_t *>(p.ovf_count);
+    Counters cnt = {0u, 0u, 0u, 0u, 0u, 0u};
+    bool bad = false;
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+        run_particle<R, SINK_GLOBAL, OBS>(p, sedges, nullptr, p.ovf_list[t], cnt, bad);
+    const unsigned full = 0xffffffffu;
+    unsigned v[6] = {cnt.scat, cnt.bnd, cnt.kill, cnt.absorb, cnt.obs, cnt.conv};
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        const unsigned sum = __reduce_add_sync(full, v[c]);
+        if ((threadIdx.x & 31) == 0 && sum) atomicAdd(p.stats + c, (unsigned long long)sum);
+    }
+    if (bad) atomicExch(p.status, 1);
 }
 
 // Batched transport: many independent problems (instances) sharing one observation
@@ -1545,6 +1894,46 @@ template <typename R> int launch_batch_t(const BatchArgs<R> &a, int grid, int bl
     void *args[] = {(void *)&a};
     void *fn = em ? pick_batch_em<R>(a.obs_kind) : pick_batch<R>(a.obs_kind);
     return (int)cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, (cudaStream_t)stream);
+}
+
+template <typename R> void *pick_events(int obs)
+{
+    return obs == OBS_CART ? (void *)rt_events<R, OBS_CART>
+                           : (obs == OBS_RADIAL ? (void *)rt_events<R, OBS_RADIAL> : (void *)rt_events<R, OBS_GENERAL>);
+}
+
+template <typename R, int SINK> void *pick_observe_obs(int obs)
+{
+    return obs == OBS_CART ? (void *)rt_observe<R, SINK, OBS_CART>
+                           : (obs == OBS_RADIAL ? (void *)rt_observe<R, SINK, OBS_RADIAL> : (void *)rt_observe<R, SINK, OBS_GENERAL>);
+}
+
+template <typename R> void *pick_observe(int sink, int obs)
+{
+    return sink == SINK_SMEM ? pick_observe_obs<R, SINK_SMEM>(obs)
+                             : (sink == SINK_GLOBAL ? pick_observe_obs<R, SINK_GLOBAL>(obs) : pick_observe_obs<R, SINK_INDEX>(obs));
+}
+
+template <typename R> void *pick_list(int obs)
+{
+    return obs == OBS_CART ? (void *)rt_transport_list<R, OBS_CART>
+                           : (obs == OBS_RADIAL ? (void *)rt_transport_list<R, OBS_RADIAL> : (void *)rt_transport_list<R, OBS_GENERAL>);
+}
+
+// the split schedule: rt_events, rt_observe, rt_transport_list, in stream order
+template <typename R>
+int launch_split_t(const DevParams<R> &p, const SplitLaunch &l, void *stream)
+{
+    void *args[] = {(void *)&p};
+    cudaError_t e = cudaLaunchKernel(pick_events<R>(p.obs_kind), dim3(l.grid_events), dim3(256), args, l.smem_events,
+                                     (cudaStream_t)stream);
+    if (e == cudaSuccess)
+        e = cudaLaunchKernel(pick_observe<R>(p.sink, p.obs_kind), dim3(l.grid_observe), dim3(l.block_observe), args,
+                             l.smem_observe, (cudaStream_t)stream);
+    if (e == cudaSuccess)
+        e = cudaLaunchKernel(pick_list<R>(p.obs_kind), dim3(l.grid_list), dim3(256), args, l.smem_events,
+                             (cudaStream_t)stream);
+    return (int)e;
 }
 
 template <typename R>

@@ -358,7 +358,9 @@ def test_gradient_against_central_differences():
 @pytest.mark.parametrize("name", ["c1", "c3", "c2_index", "cylinder_elastic", "plane_circle"])
 @pytest.mark.parametrize("precision", ["fp64", "fp32"])
 def test_schedules_give_identical_results(name, precision):
-    """Lockstep warp batches and one particle per thread run the same events and bins."""
+    """Lockstep warp batches, one particle per thread and the split schedule (events kernel,
+    then observation kernel; with 2 segments per particle nearly every particle overflows
+    and is rerun one per thread) run the same events and bins."""
     if name == "c1":
         geo, src, mat, obs, opts = W.c1_acoustic3d()
     elif name == "c3":
@@ -374,21 +376,25 @@ def test_schedules_give_identical_results(name, precision):
     ctx = get_context(0)
     out = []
     try:
-        for sched in (0, 1):
+        for sched, segs in ((0, 0), (1, 0), (2, 0), (2, 2)):
             ctx.set_schedule(sched)
+            ctx.set_launch(0, segs, 0)
             out.append(ctx.forward_trace(P, prob.tables))
     finally:
         ctx.set_schedule(-1)
-    (h0, s0, st0), (h1, s1, st1) = out
-    assert st0["device_status"] == 0 and st1["device_status"] == 0 and st0["sink"] == st1["sink"]
-    assert np.array_equal(h0, h1)
-    # the same events: counts identical; the event code is inlined into two kernels, so
-    # the compiler may contract multiply-adds differently (last-bit differences)
-    assert np.array_equal(s0[:, 9:], s1[:, 9:])
+        ctx.set_launch(0, 0, 0)
+    h0, s0, st0 = out[0]
     tol = 1e-12 if precision == "fp64" else 1e-5
-    assert np.all(np.abs(s0[:, :9] - s1[:, :9]) <= tol * (1 + np.abs(s1[:, :9])))
-    for k in ("scatter_events", "boundary_hits", "kills", "absorbed", "observations", "conversions"):
-        assert st0[k] == st1[k], k
+    for h1, s1, st1 in out[1:]:
+        assert st0["device_status"] == 0 and st1["device_status"] == 0 and st0["sink"] == st1["sink"]
+        # the same events and bins; the event code is inlined into several kernels, so the
+        # compiler may contract multiply-adds differently (last-bit differences, which can
+        # move an observation sitting on a bin edge)
+        assert np.abs(h0 - h1).sum() >> prob.hist_shift <= max(2, 1e-6 * st0["observations"])
+        assert np.array_equal(s0[:, 9:], s1[:, 9:])
+        assert np.all(np.abs(s0[:, :9] - s1[:, :9]) <= tol * (1 + np.abs(s1[:, :9])))
+        for k in ("scatter_events", "boundary_hits", "kills", "absorbed", "observations", "conversions"):
+            assert st0[k] == st1[k], k
 
 
 def test_2d_isotropic_scattering_matches_paasschens_fp32():
