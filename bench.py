@@ -112,14 +112,29 @@ def measured_peak_hbm():
 
 
 def load_traffic():
-    """DRAM bytes per launch of each kernel (read + write) from the last ncu capture of this
-    workload, summarised in profiles/c2_traffic.json; {} when absent."""
+    """DRAM bytes of each kernel for one full-size launch (read + write), from an ncu capture
+    of a smaller case of this workload scaled to the full one by its units (particle-instants),
+    summarised in profiles/c2_traffic.json; {} when absent."""
     p = ROOT / "profiles" / "c2_traffic.json"
     try:
         d = json.loads(p.read_text())
-        return {k: v["dram_read_bytes"] + v["dram_write_bytes"] for k, v in d["kernels"].items()}
+        return {k: v["dram_bytes_full_launch"] for k, v in d["kernels"].items()}
     except Exception:
         return {}
+
+
+# Algorithmic work per unit (the roofline basis): issue slots of one lane per scattering
+# event and per particle start (Philox block, logarithm, sine/cosine pairs, table lookup,
+# rotation and renormalisation), and per (particle, observation instant) on the cartesian
+# path (three multiply-adds, three floors and range tests, the index, one store); a warp
+# instruction issues 32 lanes.  Peak issue: 4 warp instructions per clock per SM.
+ISSUE_PER_EVENT, ISSUE_PER_START, ISSUE_PER_OBS = 100.0, 120.0, 12.0
+
+
+def issue_peak(clocks, sms: int = 152) -> float:
+    """Warp instructions per second the GPU can issue at the sampled SM clock."""
+    mhz = (clocks or {}).get("sm_mhz") or 2070.0
+    return 4.0 * sms * mhz * 1e6
 
 
 def cpu_histogram(prob):
@@ -255,16 +270,29 @@ def run_our_arm(args, rank, world, dist):
     for _ in range(args.warmup):
         step(P32)
     # timed region: device time of each step from CUDA events on the library stream
-    dev_ms, kern_ms, fold_ms, events, obs_n = [], [], [], 0, 0
+    dev_ms, kern_ms, fold_ms, ev_ms, events, obs_n = [], [], [], [], 0, 0
     barrier()
     with ClockSampler(device) as clk:
         t_wall = time.perf_counter()
         for _ in range(args.steps):
             ctx.flush_l2()
             st = step(P32)
+            if dist is not None:
+                # the replicas' histograms summed in place on the devices (NCCL), timed with
+                # the step: the parfor sum E = E + E_local of the reference
+                import torch
+                from radiativetransfermontecarlo_gb300.replicas import allreduce_device_histogram
+                t0 = torch.cuda.Event(enable_timing=True)
+                t1 = torch.cuda.Event(enable_timing=True)
+                t0.record()
+                allreduce_device_histogram(ctx)
+                t1.record()
+                t1.synchronize()
+                st["total_ms"] += t0.elapsed_time(t1)
             dev_ms.append(st["total_ms"])
             kern_ms.append(st["kernel_ms"])
             fold_ms.append(st["fold_ms"])
+            ev_ms.append(st["events_ms"])
             launches_per_step = ctx.last_timing()[1]
             events += st["scatter_events"]
             obs_n += st["observations"]
@@ -286,18 +314,32 @@ def run_our_arm(args, rank, world, dist):
     result = {}
     if rank == 0:
         peak, peak_kind = measured_peak_hbm()
-        kmean, fmean = float(np.mean(kern_ms)), float(np.mean(fold_ms))
+        kmean, fmean, emean = float(np.mean(kern_ms)), float(np.mean(fold_ms)), float(np.mean(ev_ms))
         entries = N * prob.n_obs  # (particle, observation instant) pairs of one step
         obs_per_step = obs_n / args.steps
-        # algorithmic bytes per launch: K1 writes one 4-byte bin index per (particle, instant);
-        # K2 reads it back and does one int64 read-modify-write (16 B) per counted observation
-        k1_bytes = 4.0 * entries
-        k2_bytes = 4.0 * entries + 16.0 * obs_per_step
+        ev_step = events / args.steps
+        ipk = issue_peak(clocks)
         traffic = load_traffic()
+        # rt_events and rt_observe: bound by instruction issue (the algorithmic issue slots
+        # above); rt_observe also writes the 4-byte bin index of every (particle, instant)
+        ev_inst = (ev_step * ISSUE_PER_EVENT + N * ISSUE_PER_START) / 32.0
+        ob_inst = entries * ISSUE_PER_OBS / 32.0
+        omean = max(kmean - emean, 1e-9)
+        # rt_bin_slices: reads the index array and, slice by slice in the L2, reads and
+        # writes the histogram once (its 64-bit reductions stay in the L2)
+        k2_bytes = 4.0 * entries + 16.0 * prob.hist_len
         kernels = {
-            "rt_transport": {"ms": kmean, "algorithmic_bytes": k1_bytes, "achieved_gbs": k1_bytes / kmean / 1e6,
-                             "traffic": traffic.get("rt_transport")},
-            "rt_bin_slices": {"ms": fmean, "algorithmic_bytes": k2_bytes, "achieved_gbs": k2_bytes / max(fmean, 1e-9) / 1e6,
+            "rt_events": {"ms": emean, "bound": "issue", "algorithmic_warp_inst": ev_inst,
+                          "achieved": ev_inst / max(emean, 1e-9) / 1e6, "peak": ipk / 1e9, "unit": "Ginst/s",
+                          "frac": ev_inst / max(emean, 1e-9) * 1e3 / ipk, "traffic": traffic.get("rt_events")},
+            "rt_observe": {"ms": omean, "bound": "issue", "algorithmic_warp_inst": ob_inst,
+                           "achieved": ob_inst / omean / 1e6, "peak": ipk / 1e9, "unit": "Ginst/s",
+                           "frac": ob_inst / omean * 1e3 / ipk, "index_write_gbs": 4.0 * entries / omean / 1e6,
+                           "traffic": traffic.get("rt_observe")},
+            "rt_bin_slices": {"ms": fmean, "bound": "hbm", "algorithmic_bytes": k2_bytes,
+                              "achieved": k2_bytes / max(fmean, 1e-9) / 1e6, "peak": peak, "unit": "GB/s",
+                              "frac": k2_bytes / max(fmean, 1e-9) / 1e6 / peak,
+                              "l2_reductions_per_s": obs_per_step / max(fmean, 1e-9) * 1e3,
                               "traffic": traffic.get("rt_bin_slices")},
         }
         dom = max(kernels, key=lambda k: kernels[k]["ms"])
@@ -308,11 +350,12 @@ def run_our_arm(args, rank, world, dist):
                   "config": {"workload": WORKLOAD, "particles_per_gpu": n, "histogram_bins": int(prob.hist_len),
                              "l2": "512 MB device write between steps; the 6.9 GB histogram exceeds L2",
                              "wall_s_timed": t_wall},
-                  "roofline": {"bound": "hbm", "achieved": kd["achieved_gbs"], "peak": peak, "unit": "GB/s",
-                               "frac": kd["achieved_gbs"] / peak, "traffic": kd["traffic"], "kernel": dom,
-                               "kernel_ms": kd["ms"], "algorithmic_bytes_per_launch": kd["algorithmic_bytes"],
-                               "basis": "K1: 4 B index written per (particle, instant); K2: 4 B read per (particle, "
-                                        f"instant) + 16 B int64 read-modify-write per counted observation; peak {peak_kind}",
+                  "roofline": {"bound": kd["bound"], "achieved": kd["achieved"], "peak": kd["peak"], "unit": kd["unit"],
+                               "frac": kd["frac"], "traffic": kd["traffic"], "kernel": dom, "kernel_ms": kd["ms"],
+                               "basis": "rt_events: 100 issue slots per event + 120 per particle start; rt_observe: 12 "
+                                        "per (particle, instant); issue peak 4 warp instructions/clk/SM at the sampled "
+                                        "clock; rt_bin_slices: 4 B index read per (particle, instant) + the 8 B "
+                                        f"histogram read and written once; HBM peak {peak_kind}",
                                "kernels": kernels},
                   "gpu_launches": args.steps * launches_per_step, "clocks": clocks,
                   "events_per_step": events / args.steps, "observations_per_step": obs_per_step,

@@ -191,6 +191,7 @@ typedef struct {
     double total_ms;         /* whole call, CUDA events (copies included) */
     double h2d_bytes;
     double d2h_bytes;
+    double events_ms;        /* split schedule: the event kernel's share of kernel_ms */
 } rtmc_stats;
 
 /* context on CUDA device `device` with its own stream */

@@ -45,7 +45,7 @@ struct rtmc_context {
     int num_sms = 0;
     int max_smem_optin = 0;
     cudaStream_t stream = nullptr;
-    cudaEvent_t ev_start = nullptr, ev_k0 = nullptr, ev_k1 = nullptr, ev_k2 = nullptr, ev_end = nullptr;
+    cudaEvent_t ev_start = nullptr, ev_k0 = nullptr, ev_k1 = nullptr, ev_k2 = nullptr, ev_end = nullptr, ev_km = nullptr;
     std::string err;
     DevBuf hist, tabs, aux, stats, flush, trace, idx, adj, partial;
     DevBuf narrow; // uint32 copy of the histogram (rtmc_forward_u32)
@@ -485,7 +485,6 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
     p.src_radial = p.zoe + 2 * RTMC_ZOE_N;
     const size_t hist_bytes = (size_t)P->hist_len * sizeof(int64_t);
     if (ctx->hist.grow(hist_bytes)) return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for the histogram failed");
-    CK(cudaMemsetAsync(ctx->hist.p, 0, hist_bytes, ctx->stream), "histogram clear");
     CK(cudaMemsetAsync(ctx->stats.p, 0, 256, ctx->stream), "counter clear");
     ctx->hist_len = P->hist_len;
     uint32_t *narrow = nullptr;
@@ -628,8 +627,17 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         sl.grid_observe = (int)std::max<int64_t>(
             1, std::min<int64_t>((int64_t)ctx->num_sms * bo, (cmax + sl.block_observe - 1) / sl.block_observe));
         sl.grid_list = ctx->num_sms;
+        sl.mid_event = n_pipe ? nullptr : (void *)ctx->ev_km; // times rt_events apart
         if (sink == kSinkSmem && P->n_particles / sl.grid_observe >= ((int64_t)1 << 32) - 1)
             return fail(&ctx->err, RTMC_ERR_ARG, "too many particles per block for 32-bit shared-memory counts");
+    }
+    // the histogram clear: fused into the first rt_events launch of a split run, else one
+    // memset ahead of the transport
+    if (split) {
+        p.clear = static_cast<unsigned long long *>(ctx->hist.p);
+        p.clear_words = P->hist_len;
+    } else {
+        CK(cudaMemsetAsync(ctx->hist.p, 0, hist_bytes, ctx->stream), "histogram clear");
     }
     // one transport launch over q: the fused kernel, or the split schedule's three kernels
     auto launch_one = [&](const DevParams<R> &q) -> int {
@@ -637,6 +645,8 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
             const cudaError_t e = cudaMemsetAsync(q.ovf_count, 0, sizeof(uint32_t), ctx->stream);
             if (e != cudaSuccess) return (int)e;
             launches += 3;
+            p.clear = nullptr; // the first chunk clears the histogram
+            p.clear_words = 0;
             if constexpr (sizeof(R) == 4) return launch_split_f32(q, sl, ctx->stream);
             else return launch_split_f64(q, sl, ctx->stream);
         }
@@ -682,7 +692,7 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         p.obs_idx = static_cast<int32_t *>(ctx->idx.p);
         p.obs_rows = idx_rows;
     }
-    double kms = 0, fms = 0;
+    double kms = 0, fms = 0, ems = 0;
     if (n_pipe) {
         const size_t slot_elems = (size_t)idx_rows * P->n_obs;
         int32_t *idx0 = static_cast<int32_t *>(ctx->idx.p);
@@ -788,12 +798,18 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         float a = 0, b = 0;
         cudaEventElapsedTime(&a, ctx->ev_k0, ctx->ev_k1);
         kms += a;
+        if (split && !le) {
+            float m = 0;
+            cudaEventElapsedTime(&m, ctx->ev_k0, ctx->ev_km);
+            ems += m;
+        }
         if (sink == kSinkIndex) {
             cudaEventElapsedTime(&b, ctx->ev_k1, ctx->ev_k2);
             fms += b;
         }
     }
     if (le) return cuda_fail(ctx, (cudaError_t)le, "transport launch");
+    if (p.clear) CK(cudaMemsetAsync(ctx->hist.p, 0, hist_bytes, ctx->stream), "histogram clear"); // no launch ran
     ctx->hist_may_exceed_int64 = may_exceed_int64(P);
     if (host_out && ctx->hist_may_exceed_int64) {
         le = launch_check_int64(p.hist, P->hist_len, p.status, narrow_grid, ctx->stream);
@@ -838,6 +854,7 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         st->device_status = status;
         st->kernel_ms = kms;
         st->fold_ms = fms;
+        st->events_ms = ems;
         st->launches = launches;
         st->sink = sink;
         st->total_ms = tms;
@@ -1289,6 +1306,7 @@ extern "C" int rtmc_create(int32_t device, rtmc_context **out)
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_k1);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_k2);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_end);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_km);
     if (e != cudaSuccess) {
         rtmc_destroy(ctx);
         return fail(nullptr, RTMC_ERR_CUDA, std::string("rtmc_create: ") + cudaGetErrorString(e));
@@ -1315,6 +1333,7 @@ extern "C" void rtmc_destroy(rtmc_context *ctx)
     ctx->partial.release();
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
     if (ctx->ev_k0) cudaEventDestroy(ctx->ev_k0);
+    if (ctx->ev_km) cudaEventDestroy(ctx->ev_km);
     if (ctx->ev_k1) cudaEventDestroy(ctx->ev_k1);
     if (ctx->ev_k2) cudaEventDestroy(ctx->ev_k2);
     if (ctx->ev_end) cudaEventDestroy(ctx->ev_end);

@@ -121,6 +121,10 @@ template <typename R> struct DevParams {
     int32_t *ovf_list;
     uint32_t *ovf_count;
     int32_t seg_cap, split;
+    // rt_events zeroes clear_words 64-bit words at `clear` as it goes (the histogram, on
+    // the first chunk of a split run), so no separate memset pass precedes the transport
+    unsigned long long *clear;
+    int64_t clear_words;
 };
 
 // Parameters of the slice fold (rt_bin_slices*).
@@ -174,6 +178,7 @@ struct AdjointArgs {
 struct SplitLaunch {
     int grid_events, grid_observe, block_observe, grid_list;
     size_t smem_events, smem_observe;
+    void *mid_event; // optional cudaEvent_t recorded after rt_events
 };
 
 // Launch wrappers (kernels.cu, fold.cu).  Return a cudaError_t value.

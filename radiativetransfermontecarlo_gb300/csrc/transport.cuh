@@ -807,11 +807,11 @@ __device__ __forceinline__ void seg_prepare(const DevParams<R> &p, const R *sedg
     }
 }
 
-// bin offset inside the time slice of an observation at sub-step so, or -1
+// bin offset inside the time slice of an observation dl sub-steps after the start of
+// segment g, or -1
 template <typename R, int OBS>
-__device__ __forceinline__ int obs_offset(const DevParams<R> &p, const R *sedges, const Seg<R> &g, int so)
+__device__ __forceinline__ int obs_offset_dl(const DevParams<R> &p, const R *sedges, const Seg<R> &g, R dl)
 {
-    const R dl = (R)(so - g.s0);
     if (OBS == OBS_CART) {
         // branch-free: the three bins, one combined range test
         int idx = g.doff;
@@ -839,6 +839,13 @@ __device__ __forceinline__ int obs_offset(const DevParams<R> &p, const R *sedges
         const int po = pos_offset(p, sedges, xo);
         return po < 0 ? -1 : po + g.doff;
     }
+}
+
+// the same at sub-step so
+template <typename R, int OBS>
+__device__ __forceinline__ int obs_offset(const DevParams<R> &p, const R *sedges, const Seg<R> &g, int so)
+{
+    return obs_offset_dl<R, OBS>(p, sedges, g, (R)(so - g.s0));
 }
 
 // Per-lane ring of segments in shared memory, field-major so that lane t of every
@@ -1354,7 +1361,16 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) rt_events(const D
     int nseg = 0;
     Part<R> s;
     Seg<R> g;
+    // the histogram clear, fused: each thread zeroes its share in 16-byte stores, a few per
+    // iteration (the event work is bound by instruction issue, the stores by HBM)
+    const int64_t t0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    int64_t cw = t0;
+    const int64_t cn = p.clear_words >> 1;
+    ulonglong2 *cl = reinterpret_cast<ulonglong2 *>(p.clear);
+    if (t0 == 0 && (p.clear_words & 1)) p.clear[p.clear_words - 1] = 0ull;
     for (;;) {
+#pragma unroll 1
+        for (int u = 0; u < 8 && cw < cn; ++u, cw += stride) cl[cw] = make_ulonglong2(0ull, 0ull);
         const bool idle = !have && i < p.n_particles;
         const unsigned idle_mask = __ballot_sync(full, idle), busy_mask = __ballot_sync(full, have);
         if (!(idle_mask | busy_mask)) break;
@@ -1408,6 +1424,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) rt_events(const D
             i += stride;
         }
     }
+    for (; cw < cn; cw += stride) cl[cw] = make_ulonglong2(0ull, 0ull);
     unsigned v[6] = {cnt.scat, cnt.bnd, cnt.kill, cnt.absorb, cnt.obs, cnt.conv};
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
@@ -1420,11 +1437,15 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) rt_events(const D
 // Observations of the particles rt_events traced: a warp takes 32 consecutive particles
 // and walks the observation instants in lockstep, each lane on its own segment list (the
 // segment after the one in force is loaded ahead, so a segment change waits on nothing).
+// Per instant a lane does one compare for a segment change or its end (rare, and then
+// the offset from the segment start is set afresh), the binning, and one store; the
+// offset is carried as a float counter while it stays an exact integer (below 2^24).
 template <typename R, int SINK, int OBS>
 __device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *sedges, unsigned *shist, int64_t base,
                                               Counters &cnt, bool &bad)
 {
     constexpr bool SMEM = SINK == SINK_SMEM;
+    constexpr bool INDEX = SINK == SINK_INDEX;
     const int lane = threadIdx.x & 31;
     const unsigned long long inc = 1ull << p.hist_shift;
     const int K = p.seg_cap;
@@ -1442,30 +1463,52 @@ __device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *se
     int k = 0, next_start = 0x7fffffff;
     if (nseg > 0) rec_get<R, OBS>(rec, cur);
     if (nseg > 1) { rec_get<R, OBS>(rec + kRecWords, nxt); next_start = nxt.s0; }
-    int32_t *optr = (SINK == SINK_INDEX && have) ? p.obs_idx + i : nullptr;
-    auto observe = [&](int so) -> int {
-        if (so >= limit) return -1;
-        while (so >= next_start) { // the next segment comes into force; load the one after it
-            cur = nxt;
-            ++k;
-            if (k + 1 < nseg) {
-                rec_get<R, OBS>(rec + (size_t)(k + 1) * kRecWords, nxt);
-                next_start = nxt.s0;
-            } else {
-                next_start = 0x7fffffff;
-            }
-        }
-        return obs_offset<R, OBS>(p, sedges, cur, so);
+    // index entries carry the mode in bit 30: fold it into the direction offset once per
+    // segment (the index path keeps a time slice below 2^30 bins)
+    auto fold_mode = [&]() {
+        if (INDEX && cur.doff >= 0) cur.doff |= cur.mode << 30;
     };
-    auto emit = [&](int v, int mode, int j) {
-        if (SINK == SINK_INDEX) {
+    fold_mode();
+    const bool count_dl = sizeof(R) == 8 || p.s_end < (1 << 24);
+    int so = p.n_sub;
+    int bound = min(next_start, limit); // the next sub-step at which the lane's state changes
+    R dl = (R)(so - cur.s0);
+    const R dstep = (R)p.n_sub;
+    int32_t *optr = (INDEX && have) ? p.obs_idx + i : nullptr;
+#pragma unroll 2
+    for (int j = 1; j <= p.n_obs; ++j, so += p.n_sub) {
+        if (so >= bound) {
+            if (so >= limit) { // the particle's end: nothing more is binned
+                cur.doff = -1;
+                bound = 0x7fffffff;
+            } else { // the next segment comes into force; load the one after it
+                do {
+                    cur = nxt;
+                    ++k;
+                    if (k + 1 < nseg) {
+                        rec_get<R, OBS>(rec + (size_t)(k + 1) * kRecWords, nxt);
+                        next_start = nxt.s0;
+                    } else {
+                        next_start = 0x7fffffff;
+                    }
+                } while (so >= next_start);
+                fold_mode();
+                bound = min(next_start, limit);
+            }
+            dl = (R)(so - cur.s0);
+        } else if (!count_dl) {
+            dl = (R)(so - cur.s0);
+        }
+        const int v = obs_offset_dl<R, OBS>(p, sedges, cur, dl);
+        dl += dstep;
+        if (INDEX) {
             if (have) {
-                *optr = v < 0 ? -1 : (v | (mode << 30));
+                *optr = v;
                 optr += p.obs_rows;
             }
-            if (v >= 0) cnt.obs++;
+            cnt.obs += v >= 0 ? 1u : 0u;
         } else if (v >= 0) {
-            const int64_t idx = (int64_t)j * p.time_stride + (mode ? p.mode_stride : 0) + v;
+            const int64_t idx = (int64_t)j * p.time_stride + (cur.mode ? p.mode_stride : 0) + v;
             if (idx < p.hist_len) {
                 cnt.obs++;
                 if (SMEM) atomicAdd(shist + idx, 1u);
@@ -1474,18 +1517,6 @@ __device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *se
                 bad = true;
             }
         }
-    };
-    int j = 1;
-    for (; j + 1 <= p.n_obs; j += 2) { // two instants per iteration: independent chains
-        const int v0 = observe(j * p.n_sub);
-        const int m0 = cur.mode;
-        const int v1 = observe((j + 1) * p.n_sub);
-        emit(v0, m0, j);
-        emit(v1, cur.mode, j + 1);
-    }
-    if (j <= p.n_obs) {
-        const int v = observe(j * p.n_sub);
-        emit(v, cur.mode, j);
     }
 }
 
@@ -1927,6 +1958,7 @@ int launch_split_t(const DevParams<R> &p, const SplitLaunch &l, void *stream)
     void *args[] = {(void *)&p};
     cudaError_t e = cudaLaunchKernel(pick_events<R>(p.obs_kind), dim3(l.grid_events), dim3(256), args, l.smem_events,
                                      (cudaStream_t)stream);
+    if (e == cudaSuccess && l.mid_event) e = cudaEventRecord((cudaEvent_t)l.mid_event, (cudaStream_t)stream);
     if (e == cudaSuccess)
         e = cudaLaunchKernel(pick_observe<R>(p.sink, p.obs_kind), dim3(l.grid_observe), dim3(l.block_observe), args,
                              l.smem_observe, (cudaStream_t)stream);
