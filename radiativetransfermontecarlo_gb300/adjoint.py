@@ -194,7 +194,21 @@ def radiativeTransferGradient(geometry: dict, source: dict, material: MaterialCl
     corr = np.zeros_like(E)
     m = E_target > 0
     corr[m] = unit[m] / E_target[m]
-    adjoint = ((dLdE - corr) * unit).ravel(order="F")
+    adj = (dLdE - corr) * unit
+    centred = False
+    if opt.get("centre_weights", True):
+        # Control variate: the score of a path up to an instant has zero mean, so when every
+        # particle is observed at every instant (the grid holds all of them, as at Q = Inf
+        # in weight mode), subtracting from the weights of instant j their mean over the
+        # particles' bins, sum_b w_b count_b / N, leaves the estimate unbiased and removes
+        # the part of its variance that the common weight of the instant carries.
+        c = counts.reshape(E.shape, order="F").astype(np.float64) / float(1 << prob.hist_shift)
+        per_slice = c.sum(axis=tuple(k for k in range(c.ndim) if k != c.ndim - 2))
+        if np.all(per_slice[1:] == N):
+            wbar = (adj * c).sum(axis=tuple(k for k in range(c.ndim) if k != c.ndim - 2)) / N
+            adj = adj - _slice(wbar, adj)
+            centred = True
+    adjoint = adj.ravel(order="F")
     grad = {}
     scat = [p for p in params if p != "Q"]
     st_a = None
@@ -208,7 +222,7 @@ def radiativeTransferGradient(geometry: dict, source: dict, material: MaterialCl
         tq = (omega * grid.t / Q ** 2) if math.isfinite(Q) else np.zeros(grid.Nt)
         grad["Q"] = float(np.sum(dLdE * E * _slice(tq, E)))
     return {"L": L, "grad": grad, "energyDensity": E, "N": N, "bins": int(kept.sum()), "forward_stats": st_f,
-            "adjoint_stats": st_a}
+            "adjoint_stats": st_a, "centred": centred}
 
 
 def finite_difference(geometry, source, material, observation, E_target, name: str, rel: float = 1e-3,
