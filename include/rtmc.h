@@ -371,6 +371,14 @@ int rtmc_set_pipeline(rtmc_context *ctx, int32_t chunks, int32_t transport_block
  * through the index array, else 2).  All give the same histogram. */
 int rtmc_set_schedule(rtmc_context *ctx, int32_t event_major);
 
+/* Fold of the index path (large histograms): 1 = each observation one 64-bit reduction
+ * into its time slice of the histogram; 2 = time-blocked: FP32 counts with the 4
+ * instants of a bin adjacent, a particle's run of instants in one bin added as one vector
+ * reduction, then converted to the histogram (needs fewer than 2^24 particles, so that
+ * FP32 counts are exact); 0 = automatic (2 when it applies).  Both give the same
+ * histogram. */
+int rtmc_set_fold(rtmc_context *ctx, int32_t mode);
+
 /* enable (1, default) or disable (0) reuse of the device copy of a tables handle across
  * calls; with 0 every call uploads its tables again (end-to-end timing) */
 int rtmc_set_table_cache(rtmc_context *ctx, int32_t enable);

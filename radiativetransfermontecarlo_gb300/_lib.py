@@ -113,6 +113,7 @@ SIGNATURES = {
     "rtmc_set_launch": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32]),
     "rtmc_set_pipeline": (C.c_int, [_P, C.c_int32, C.c_int32]),
     "rtmc_set_schedule": (C.c_int, [_P, C.c_int32]),
+    "rtmc_set_fold": (C.c_int, [_P, C.c_int32]),
     "rtmc_batch_create": (C.c_int, [_P, C.c_int32, C.POINTER(RtmcProblem), C.POINTER(_P), C.POINTER(_P)]),
     "rtmc_batch_set_launch": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int64]),
     "rtmc_batch_run": (C.c_int, [_P, C.POINTER(RtmcStats)]),
@@ -327,6 +328,10 @@ class Context:
         """rtmc_set_pipeline: chunks >= 2 overlaps the fold of a chunk with the next chunk's
         transport; 0 = automatic (off), 1 = off."""
         check(self.lib.rtmc_set_pipeline(self.handle, chunks, transport_blocks_per_sm), self.handle)
+
+    def set_fold(self, mode: int = 0):
+        """rtmc_set_fold: 0 automatic, 1 64-bit slice fold, 2 time-blocked FP32 fold."""
+        check(self.lib.rtmc_set_fold(self.handle, mode), self.handle)
 
     def set_schedule(self, event_major: int = -1):
         """rtmc_set_schedule: -1 automatic, 0 lockstep warp batches, 1 one particle per thread,

@@ -50,6 +50,7 @@ struct rtmc_context {
     DevBuf hist, tabs, aux, stats, flush, trace, idx, adj, partial;
     DevBuf narrow; // uint32 copy of the histogram (rtmc_forward_u32)
     DevBuf segs, seg_head, ovf; // split schedule: trajectory segments, per-particle heads, overflow list
+    DevBuf tbacc;               // time-blocked FP32 fold accumulator
     uint64_t tabs_gen = 0;
     int tabs_prec = -1;
     DevTables<float> tf{};
@@ -64,6 +65,7 @@ struct rtmc_context {
     // per-chunk events, created on first use
     int opt_chunks = 0, opt_k1_bps = 0;
     int opt_event_major = -1; // -1 automatic, 0 two-cursor batches, 1 one particle per thread, 2 split
+    int opt_fold = 0;         // 0 automatic, 1 64-bit slice fold, 2 time-blocked FP32 fold
     static constexpr int kPipe = 32;
     cudaStream_t fold_stream = nullptr;
     cudaEvent_t ev_a0[kPipe] = {}, ev_a1[kPipe] = {}, ev_b0[kPipe] = {}, ev_b1[kPipe] = {};
@@ -428,6 +430,16 @@ inline int64_t index_row_stride(int64_t particles) { return (particles + 31) / 3
 // First slice (1-based) of copy group g in [0, kCopyGroups]; g = kCopyGroups gives n_obs + 1.
 // The first group is small (1/25 of the slices), so the first copy starts soon after the
 // transport; the fold outruns the host link, so later copies follow back to back.
+// First t-block of copy group g of the time-blocked fold (g = kCopyGroups gives ntb), with
+// the same proportions as copy_group_start.
+int tb_group_start(int ntb, int g)
+{
+    if (g <= 0) return 0;
+    if (g >= kCopyGroups) return ntb;
+    const int first = std::max(1, ntb / 25);
+    return first + (int)((int64_t)(ntb - first) * (g - 1) / (kCopyGroups - 1));
+}
+
 int copy_group_start(int n_obs, int g)
 {
     if (g <= 0) return 1;
@@ -631,13 +643,33 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         if (sink == kSinkSmem && P->n_particles / sl.grid_observe >= ((int64_t)1 << 32) - 1)
             return fail(&ctx->err, RTMC_ERR_ARG, "too many particles per block for 32-bit shared-memory counts");
     }
-    // the histogram clear: fused into the first rt_events launch of a split run, else one
-    // memset ahead of the transport
+    // time-blocked FP32 fold (index path, one pass over the chunks, exact counts below 2^24
+    // particles): it writes every bin of the histogram, so only its accumulator needs a clear
+    const bool use_tb = sink == kSinkIndex && !n_pipe && P->n_particles < ((int64_t)1 << 24) && ctx->opt_fold != 1;
+    const int ntb = (P->n_obs + 3) / 4;
+    TbParams tpl{};
+    int tb_grid = 1;
+    if (use_tb) {
+        tpl.S = P->time_stride * nm;
+        const size_t acc_bytes = (size_t)ntb * tpl.S * 4 * sizeof(float);
+        if (ctx->tbacc.grow(acc_bytes)) return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for the fold accumulator failed");
+        tpl.acc = static_cast<float *>(ctx->tbacc.p);
+        tpl.idx = static_cast<const int32_t *>(ctx->idx.p);
+        tpl.rows = index_row_stride(chunk);
+        tpl.n_obs = P->n_obs;
+        tpl.slice_bins = (int32_t)P->time_stride;
+        tb_grid = (int)std::max<int64_t>(1, std::min<int64_t>((chunk + 8191) / 8192, 2 * ctx->num_sms));
+    }
+    // the clear: fused into the first rt_events launch of a split run, else one memset
+    // ahead of the transport
+    unsigned long long *to_clear = use_tb ? static_cast<unsigned long long *>(ctx->tbacc.p)
+                                          : static_cast<unsigned long long *>(ctx->hist.p);
+    const int64_t clear_words = use_tb ? (int64_t)ntb * tpl.S * 2 : P->hist_len;
     if (split) {
-        p.clear = static_cast<unsigned long long *>(ctx->hist.p);
-        p.clear_words = P->hist_len;
+        p.clear = to_clear;
+        p.clear_words = clear_words;
     } else {
-        CK(cudaMemsetAsync(ctx->hist.p, 0, hist_bytes, ctx->stream), "histogram clear");
+        CK(cudaMemsetAsync(to_clear, 0, (size_t)clear_words * 8, ctx->stream), "histogram clear");
     }
     // one transport launch over q: the fused kernel, or the split schedule's three kernels
     auto launch_one = [&](const DevParams<R> &q) -> int {
@@ -745,7 +777,58 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         le = launch_one(q);
         CK(cudaEventRecord(ctx->ev_k1, ctx->stream), "event");
         const bool last = base + chunk >= P->n_particles;
-        if (!le && sink == kSinkIndex) {
+        if (!le && use_tb) {
+            TbParams tp = tpl;
+            tp.n = q.n_particles;
+            tp.part_per_block = ((tp.n + tb_grid - 1) / tb_grid + 3) / 4 * 4;
+            unsigned long long *hist = p.hist;
+            if (last && (host_out || host_u32) && ntb >= 2 * kCopyGroups && ensure_pipeline(ctx) == 0) {
+                // the last fold and its conversion in groups of t-blocks: each group's slices
+                // are final, so their copy to the host runs on the second stream while the
+                // next group folds
+                const int64_t ts = P->time_stride;
+                for (int g = 0; g < kCopyGroups && !le; ++g) {
+                    tp.tb_first = tb_group_start(ntb, g);
+                    tp.tb_count = tb_group_start(ntb, g + 1) - tp.tb_first;
+                    if (tp.tb_count < 1) continue;
+                    le = launch_fold_tb(tp, tb_grid, ctx->stream);
+                    if (!le) le = launch_tb_convert(tp, ts, P->mode_stride, P->hist_shift, hist, narrow, narrow_grid, ctx->stream);
+                    launches += 2;
+                    if (le) break;
+                    const int64_t ja = g == 0 ? 0 : 4 * (int64_t)tp.tb_first + 1; // slice 0 with the first group
+                    const int64_t jb = std::min<int64_t>(4 * (int64_t)(tp.tb_first + tp.tb_count), P->n_obs) + 1;
+                    CK(cudaEventRecord(ctx->ev_a1[g], ctx->stream), "event");
+                    CK(cudaStreamWaitEvent(ctx->fold_stream, ctx->ev_a1[g], 0), "copy wait");
+                    for (int m = 0; m < nm; ++m) {
+                        const int64_t o = m * P->mode_stride + ja * ts;
+                        const size_t cnt = (size_t)((jb - ja) * ts);
+                        if (narrow)
+                            CK(cudaMemcpyAsync(host_u32 + o, narrow + o, cnt * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                               ctx->fold_stream),
+                               "histogram copy");
+                        else
+                            CK(cudaMemcpyAsync(host_out + o, static_cast<int64_t *>(ctx->hist.p) + o, cnt * sizeof(int64_t),
+                                               cudaMemcpyDeviceToHost, ctx->fold_stream),
+                               "histogram copy");
+                    }
+                }
+                CK(cudaEventRecord(ctx->ev_b1[0], ctx->fold_stream), "event");
+                CK(cudaEventRecord(ctx->ev_k2, ctx->stream), "event");
+                CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_b1[0], 0), "copy join");
+                copied = true;
+            } else {
+                tp.tb_first = 0;
+                tp.tb_count = ntb;
+                le = launch_fold_tb(tp, tb_grid, ctx->stream);
+                ++launches;
+                if (!le && last) {
+                    le = launch_tb_convert(tp, P->time_stride, P->mode_stride, P->hist_shift, hist, nullptr, narrow_grid,
+                                           ctx->stream);
+                    ++launches;
+                }
+                CK(cudaEventRecord(ctx->ev_k2, ctx->stream), "event");
+            }
+        } else if (!le && sink == kSinkIndex) {
             BinParams b = bp;
             b.n = q.n_particles;
             if (b.group) b.part_per_block = (b.n + fold_grid - 1) / fold_grid;
@@ -1473,6 +1556,14 @@ extern "C" int rtmc_set_schedule(rtmc_context *ctx, int32_t event_major)
     if (!ctx) return fail(nullptr, RTMC_ERR_ARG, "rtmc_set_schedule: NULL context");
     if (event_major < -1 || event_major > 2) return fail(&ctx->err, RTMC_ERR_ARG, "schedule must be -1, 0, 1 or 2");
     ctx->opt_event_major = event_major;
+    return RTMC_OK;
+}
+
+extern "C" int rtmc_set_fold(rtmc_context *ctx, int32_t mode)
+{
+    if (!ctx) return fail(nullptr, RTMC_ERR_ARG, "rtmc_set_fold: NULL context");
+    if (mode < 0 || mode > 2) return fail(&ctx->err, RTMC_ERR_ARG, "fold mode must be 0, 1 or 2");
+    ctx->opt_fold = mode;
     return RTMC_OK;
 }
 

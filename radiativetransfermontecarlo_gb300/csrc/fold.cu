@@ -202,7 +202,176 @@ __global__ void __launch_bounds__(kCheckThreads) rt_check_int64(const unsigned l
     if (__any_sync(0xffffffffu, (acc >> 63) != 0ull) && (threadIdx.x & 31) == 0) atomicOr(status, 2);
 }
 
+// ---- time-blocked FP32 fold ------------------------------------------------------
+// A particle moves a fraction of a bin per observation instant (0.24 bin widths for the P
+// waves of the 3D elastic workload), so its entries of 4 consecutive instants often share
+// a bin.  Laid out with the 4 instants of a bin adjacent (16 bytes), such a run is one
+// vector reduction (red.global.add.v4.f32) where the 64-bit histogram takes one per
+// instant; the fold's cost is the L2's reduction rate, so fewer reductions is faster.
+// Counts are exact in FP32 below 2^24 per bin and instant.  Crowded chunks (early
+// instants) aggregate in a shared-memory hash first, as rt_bin_slices does.
+constexpr int kTbThreads = 512;
+constexpr int kTbSlots = 2048;
+
+__device__ __forceinline__ void red_v4(float *a, float x, float y, float z, float w)
+{
+    asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(a), "f"(x), "f"(y), "f"(z), "f"(w) : "memory");
+}
+
+__device__ __forceinline__ bool tb_hash_insert(int *keys, unsigned (*cnt)[4], int *used, int key, const int m[4])
+{
+    unsigned h = ((unsigned)key * 2654435761u) >> (32 - 11); // 11 = log2(kTbSlots)
+#pragma unroll 1
+    for (int probe = 0; probe < 8; ++probe) {
+        int k = *((volatile int *)keys + h);
+        if (k == -1) {
+            k = atomicCAS(keys + h, -1, key);
+            if (k == -1) atomicAdd(used, 1);
+        }
+        if (k == -1 || k == key) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r)
+                if (m[r]) atomicAdd(&cnt[h][r], 1u);
+            return true;
+        }
+        h = (h + 1) & (kTbSlots - 1);
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(kTbThreads) rt_fold_tb(const TbParams t)
+{
+    __shared__ int keys[kTbSlots];
+    __shared__ unsigned cnt[kTbSlots][4];
+    __shared__ int used, valid, dense;
+    const int tb = t.tb_first + blockIdx.y;
+    const int j0 = 4 * tb + 1; // first instant of the t-block
+    const int nr = min(4, t.n_obs - j0 + 1);
+    const int4 *row[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r)
+        row[r] = reinterpret_cast<const int4 *>(t.idx + (int64_t)(j0 - 1 + (r < nr ? r : 0)) * t.rows);
+    float *acc = t.acc + (size_t)tb * t.S * 4;
+    for (int k = threadIdx.x; k < kTbSlots; k += blockDim.x) {
+        keys[k] = -1;
+        cnt[k][0] = cnt[k][1] = cnt[k][2] = cnt[k][3] = 0u;
+    }
+    if (threadIdx.x == 0) { used = 0; valid = 0; }
+    const int64_t p0 = (int64_t)blockIdx.x * t.part_per_block; // a multiple of 4
+    const int64_t p1 = min(t.n, p0 + t.part_per_block);
+    const int64_t q0 = p0 >> 2, q1 = (p1 + 3) >> 2;
+    __syncthreads();
+    // the entries of 4 particles x the t-block's instants; each particle's distinct bins
+    // go out as one vector each (to the hash when crowded)
+    auto vector = [&](int64_t q, bool use_hash, int *nvalid) {
+        int e[4][4]; // [instant][particle]
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int4 a = r < nr ? __ldcs(row[r] + q) : make_int4(-1, -1, -1, -1);
+            e[r][0] = a.x; e[r][1] = a.y; e[r][2] = a.z; e[r][3] = a.w;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const int64_t k = q * 4 + u;
+            if (k >= p1) continue;
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                const int v = e[r][u];
+                if (v < 0) continue;
+                bool dup = false;
+#pragma unroll
+                for (int r2 = 0; r2 < r; ++r2) dup = dup || e[r2][u] == v;
+                if (dup) continue; // counted with the first instant of its bin
+                const int m[4] = {e[0][u] == v, e[1][u] == v, e[2][u] == v, e[3][u] == v};
+                const int key = (v & 0x3fffffff) + ((v >> 30) ? t.slice_bins : 0);
+                ++*nvalid;
+                if (use_hash && *((volatile int *)&used) < 3 * kTbSlots / 4 && tb_hash_insert(keys, cnt, &used, key, m))
+                    continue;
+                red_v4(acc + (size_t)key * 4, (float)m[0], (float)m[1], (float)m[2], (float)m[3]);
+            }
+        }
+    };
+    // probe window: one vector per thread through the hash
+    int nv = 0;
+    int64_t q = q0 + threadIdx.x;
+    if (q < q1) vector(q, true, &nv);
+    if (nv) atomicAdd(&valid, nv);
+    __syncthreads();
+    // crowded: the window's runs fell in at most a quarter of the table, each bin hit twice
+    if (threadIdx.x == 0) dense = valid >= 64 && used * 4 <= kTbSlots && used * 2 <= valid;
+    __syncthreads();
+    const bool h = dense;
+    for (q += blockDim.x; q < q1; q += blockDim.x) vector(q, h, &nv);
+    __syncthreads();
+    for (int k = threadIdx.x; k < kTbSlots; k += blockDim.x) {
+        const int key = keys[k];
+        if (key >= 0) red_v4(acc + (size_t)key * 4, (float)cnt[k][0], (float)cnt[k][1], (float)cnt[k][2], (float)cnt[k][3]);
+    }
+}
+
+// acc -> the int64 histogram (and the uint32 counts): blockIdx.y is the t-block, threads
+// run over its bins; each reads 16 bytes and writes the bin at 4 instants (coalesced
+// across the threads of a warp)
+constexpr int kConvThreads = 256;
+__global__ void __launch_bounds__(kConvThreads) rt_tb_convert(const TbParams t, int64_t time_stride, int64_t mode_stride,
+                                                              int shift, unsigned long long *__restrict__ hist,
+                                                              uint32_t *__restrict__ u32)
+{
+    const int tb = t.tb_first + blockIdx.y;
+    const float4 *a4 = reinterpret_cast<const float4 *>(t.acc) + (size_t)tb * t.S;
+    for (int64_t s = (int64_t)blockIdx.x * kConvThreads + threadIdx.x; s < t.S; s += (int64_t)gridDim.x * kConvThreads) {
+        const float4 c = __ldcs(a4 + s);
+        const int64_t off = s >= t.slice_bins ? mode_stride + (s - t.slice_bins) : s;
+        const float cv[4] = {c.x, c.y, c.z, c.w};
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            const int j = 4 * tb + r + 1;
+            if (j > t.n_obs) break;
+            const unsigned long long v = (unsigned long long)cv[r];
+            __stcs(hist + (int64_t)j * time_stride + off, v << shift);
+            if (u32) __stcs(u32 + (int64_t)j * time_stride + off, (uint32_t)v);
+        }
+        if (tb == 0) { // instant 0 is never observed
+            __stcs(hist + off, 0ull);
+            if (u32) __stcs(u32 + off, 0u);
+        }
+    }
+}
+
 } // namespace
+
+int launch_fold_tb(const TbParams &t, int grid_x, void *stream)
+{
+    if (t.tb_count < 1 || (t.part_per_block & 3)) return (int)cudaErrorInvalidValue;
+    constexpr int kMaxGridY = 65535;
+    for (int done = 0; done < t.tb_count; done += kMaxGridY) {
+        TbParams c = t;
+        c.tb_first = t.tb_first + done;
+        c.tb_count = t.tb_count - done < kMaxGridY ? t.tb_count - done : kMaxGridY;
+        rt_fold_tb<<<dim3(grid_x, c.tb_count), kTbThreads, 0, (cudaStream_t)stream>>>(c);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return (int)e;
+    }
+    return 0;
+}
+
+int launch_tb_convert(const TbParams &t, int64_t time_stride, int64_t mode_stride, int shift,
+                      unsigned long long *hist, uint32_t *u32, int max_grid, void *stream)
+{
+    if (t.tb_count < 1) return 0;
+    constexpr int kMaxGridY = 65535;
+    const int gx = (int)std::max<int64_t>(1, std::min<int64_t>(max_grid, (t.S + kConvThreads - 1) / kConvThreads));
+    for (int done = 0; done < t.tb_count; done += kMaxGridY) {
+        TbParams c = t;
+        c.tb_first = t.tb_first + done;
+        c.tb_count = t.tb_count - done < kMaxGridY ? t.tb_count - done : kMaxGridY;
+        rt_tb_convert<<<dim3(gx, c.tb_count), kConvThreads, 0, (cudaStream_t)stream>>>(c, time_stride, mode_stride, shift,
+                                                                                      hist, u32);
+        const cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return (int)e;
+    }
+    return 0;
+}
 
 int launch_check_int64(const unsigned long long *hist, int64_t n, int32_t *status, int max_grid, void *stream)
 {

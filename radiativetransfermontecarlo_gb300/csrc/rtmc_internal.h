@@ -139,6 +139,22 @@ struct BinParams {
     int32_t j_first, j_count; // rt_bin_slices: slices j_first .. j_first + j_count - 1 (1-based)
 };
 
+// Parameters of the time-blocked fold (rt_fold_tb) and its conversion (rt_tb_convert).
+// The accumulator holds FP32 counts in blocks of 4 consecutive observation instants:
+// acc[(tb * S + s) * 4 + r] counts in-slice bin s (s = in-mode bin + mode * slice_bins) at
+// instant j = 4 tb + r + 1.  A bin of one instant receives at most one count per particle,
+// so FP32 counts are exact while the particles number fewer than 2^24.
+struct TbParams {
+    const int32_t *idx;       // index array: instant j in row j - 1
+    int64_t rows;             // row stride
+    int64_t n;                // particles in this chunk
+    int64_t part_per_block;   // multiple of 4
+    int64_t S;                // slice_bins * n_modes
+    int32_t n_obs, slice_bins;
+    int32_t tb_first, tb_count; // t-blocks [tb_first, tb_first + tb_count)
+    float *acc;
+};
+
 // One work item of a batched run: particles [first, first + count) of instance inst.
 struct BatchItem {
     int32_t inst, pad;
@@ -215,6 +231,13 @@ int transport_max_threads(int precision, int sink, int obs);
 int launch_bin_slices(const BinParams &b, int grid_x, size_t smem, void *stream);
 // n histogram bins as uint32 counts (value >> shift, saturating), at most max_grid blocks
 int launch_narrow_u32(const unsigned long long *src, uint32_t *dst, int64_t n, int shift, int max_grid, void *stream);
+// time-blocked fold of one chunk over t-blocks [tb_first, tb_first + tb_count)
+int launch_fold_tb(const TbParams &t, int grid_x, void *stream);
+// acc t-blocks [tb_first, tb_first + tb_count) -> the int64 histogram (count << shift) and,
+// when u32 is non-null, the uint32 counts; slice 0 (t = 0, never observed) is zeroed with
+// t-block 0
+int launch_tb_convert(const TbParams &t, int64_t time_stride, int64_t mode_stride, int shift,
+                      unsigned long long *hist, uint32_t *u32, int max_grid, void *stream);
 // sets bit 1 of *status when a bin of the n-bin histogram is >= 2^63 (out of int64 range)
 int launch_check_int64(const unsigned long long *hist, int64_t n, int32_t *status, int max_grid, void *stream);
 // a histogram of this problem may hold bins of 2^63 or more (n_particles << hist_shift >= 2^63)

@@ -647,3 +647,34 @@ def test_observation_frames_and_bin_pairs_match_oracle(d, frame, pair):
         else:
             assert _path_match(states, ref_states, 1e-5).mean() >= 0.999
             assert _l1_diff(hist, ref_hist) <= 2e-3 * stats["observations"] + 4
+
+
+@pytest.mark.parametrize("index_mb", [0, 1])
+def test_time_blocked_fold_equals_slice_fold(index_mb):
+    """The time-blocked FP32 fold (vector reductions over runs of 4 instants, then the
+    conversion) gives the 64-bit slice fold's histogram bit for bit: int64 and uint32 host
+    outputs (converted and copied in groups of instants), the device histogram, and
+    several particle chunks (1 MB of index scratch)."""
+    geo, src, mat, obs, opts = W.c2_elastic3d(t_end=1.0)
+    prob, grid, N = build_problem(geo, dict(src, numberParticles=20000), mat, obs, dict(opts, exact_count=True))
+    P, keep = prob.to_ctypes()
+    ctx = get_context(0)
+    out = {}
+    try:
+        ctx.set_launch(0, 0, index_mb)
+        for mode in (1, 2):
+            ctx.set_fold(mode)
+            h, st = ctx.forward(P, prob.tables)
+            u, _ = ctx.forward_u32(P, prob.tables)
+            sd = ctx.forward_device(P, prob.tables)
+            hd = ctx.copy_histogram(np.empty(prob.hist_len, dtype=np.int64))
+            out[mode] = (h, u, hd, st, sd)
+    finally:
+        ctx.set_fold(0)
+        ctx.set_launch(0, 0, 0)
+    (h1, u1, d1, s1, sd1), (h2, u2, d2, s2, sd2) = out[1], out[2]
+    assert s1["sink"] == 2 and s1["device_status"] == 0 and s2["device_status"] == 0
+    if index_mb:
+        assert s2["launches"] > s1["launches"] - 2  # several chunks on both paths
+    assert np.array_equal(h1, h2) and np.array_equal(u1, u2) and np.array_equal(d1, d2) and np.array_equal(h1, d1)
+    assert s1["observations"] == s2["observations"] == int(h1.sum() >> prob.hist_shift)
