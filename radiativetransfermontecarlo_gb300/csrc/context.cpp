@@ -607,6 +607,10 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         K = std::min(64, std::max(8, (K + 3) / 4 * 4));
         if (ctx->opt_ring) K = ctx->opt_ring; // an explicit ring capacity sets the segments per particle
         const size_t rec = 8 * sizeof(R);
+        // particles per launch: the segments of one chunk stay within 8 GB
+        constexpr int64_t kSegBudget = (int64_t)8 << 30;
+        const int64_t seg_rows = std::max<int64_t>(32, kSegBudget / ((int64_t)K * (int64_t)rec) / 32 * 32);
+        chunk = std::min(chunk, seg_rows);
         const int64_t rows_max = std::max<int64_t>(chunk, 1);
         if (ctx->segs.grow((size_t)rows_max * K * rec) || ctx->seg_head.grow((size_t)rows_max * 8) ||
             ctx->ovf.grow((size_t)rows_max * 4))
@@ -640,7 +644,7 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
             1, std::min<int64_t>((int64_t)ctx->num_sms * bo, (cmax + sl.block_observe - 1) / sl.block_observe));
         sl.grid_list = ctx->num_sms;
         sl.mid_event = n_pipe ? nullptr : (void *)ctx->ev_km; // times rt_events apart
-        if (sink == kSinkSmem && P->n_particles / sl.grid_observe >= ((int64_t)1 << 32) - 1)
+        if (sink == kSinkSmem && chunk / sl.grid_observe >= ((int64_t)1 << 32) - 1)
             return fail(&ctx->err, RTMC_ERR_ARG, "too many particles per block for 32-bit shared-memory counts");
     }
     // time-blocked FP32 fold (index path, one pass over the chunks, exact counts below 2^24

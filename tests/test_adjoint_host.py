@@ -55,9 +55,15 @@ def test_gradient_host_pipeline(oracle_backend):
     w = np.exp(-2 * math.pi * 10 * grid.t / 400)
     unit = normalise(np.ones(prob.hist_len), grid, N)[0] * w[None, None, :, None]
     r = np.where(keep, 2 * (E - T) / np.where(keep, T, 1.0) - unit / np.where(keep, T, 1.0), 0.0)
+    adj = r * unit
+    # centring: every particle is in the grid at every instant here (weight mode, full box),
+    # so the count-weighted mean weight of each instant is taken off that instant
+    c = counts.reshape(E.shape, order="F").astype(np.float64) / float(1 << prob.hist_shift)
+    assert res["centred"] and np.all(c.sum(axis=(0, 1, 3))[1:] == N)
+    adj = adj - ((adj * c).sum(axis=(0, 1, 3)) / N)[None, None, :, None]
     scat = ["lc", "cv_kappa", "cv_rho", "mfp"]
     dls, dlS = A.score_tables(mat, 3, scat)
-    g, _ = O.gradient(prob, O.table_knots(prob.tables), dls, dlS, (r * unit).ravel(order="F"), ufloat=False)
+    g, _ = O.gradient(prob, O.table_knots(prob.tables), dls, dlS, adj.ravel(order="F"), ufloat=False)
     for q, p in enumerate(scat):
         assert math.isclose(res["grad"][p], g[q], rel_tol=1e-9, abs_tol=1e-12)
     # Q: exact, equal to central differences of the weight-mode misfit
@@ -89,3 +95,22 @@ def test_score_tables_match_closed_form():
     for q in range(3):
         assert math.isclose(_trapz(dls[q] * pdf, th) / _trapz(pdf, th), dlS[q], rel_tol=1e-5)
     assert np.allclose(dls[3], dlS[3]) and dlS[3] < 0
+
+
+def test_gradient_without_centring(oracle_backend):
+    geo, src, mat, tgt, obs, o = _case()
+    Et = A.forward_weighted(geo, src, tgt, obs, dict(o, seed=77))[0]
+    res = A.radiativeTransferGradient(geo, src, mat, obs, Et, ("lc", "mfp"),
+                                      dict(o, seed=3, min_target_count=20, centre_weights=False))
+    assert not res["centred"]
+    E, prob, grid, N, counts, _ = A.forward_weighted(geo, src, mat, obs, dict(o, seed=3))
+    one = normalise(np.ones(grid.hist_len), grid, 1)[0]
+    keep = (Et > 0) & (Et * N / one >= 20 - 1e-9)
+    T = np.where(keep, Et, 1.0)
+    w = np.exp(-2 * math.pi * 10 * grid.t / 400)
+    unit = normalise(np.ones(prob.hist_len), grid, N)[0] * w[None, None, :, None]
+    r = np.where(keep, 2 * (E - T) / T - unit / T, 0.0)
+    dls, dlS = A.score_tables(mat, 3, ["lc", "mfp"])
+    g, _ = O.gradient(prob, O.table_knots(prob.tables), dls, dlS, (r * unit).ravel(order="F"), ufloat=False)
+    for q, p in enumerate(("lc", "mfp")):
+        assert math.isclose(res["grad"][p], g[q], rel_tol=1e-9, abs_tol=1e-12)

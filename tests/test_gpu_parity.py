@@ -334,9 +334,12 @@ def test_gradient_replay_matches_oracle(precision):
 
 def test_gradient_against_central_differences():
     """Score-function gradient vs central differences with common random numbers (same
-    seed, 1e-2 relative steps) for lc, cv_kappa, cv_rho, Q and the mean free path, FP32
-    transport, 1e7 particles, bins holding >= 1000 target particles: the gradient in
-    relative coordinates (p dL/dp) within 2%, each well-determined component within 2%."""
+    seed, 1e-3 relative steps, as specified) for lc, cv_kappa, cv_rho, Q and the mean free
+    path, FP32 transport, 1e7 particles, bins holding >= 1000 target particles: the
+    gradient in relative coordinates (p dL/dp) within 2%, and cv_kappa, cv_rho, Q and the
+    mean free path each within 2%.  The lc component (|p dL/dp| = 0.17 against 3.7 for
+    cv_kappa) carries a Monte Carlo spread of about 15% per seed in both estimates at 1e7
+    particles; its 2% check runs at 8e9 particles (next test)."""
     from radiativetransfermontecarlo_gb300 import adjoint as A
     n = 10_000_000
     geo, src, mat, obs, opts, Et = _gradient_case(n, full_grid=True)
@@ -346,13 +349,29 @@ def test_gradient_against_central_differences():
     res = A.radiativeTransferGradient(geo, src, mat, obs, Et, params, o)
     assert res["adjoint_stats"]["device_status"] == 0 and res["bins"] > 1000
     scale = {"lc": 0.1, "cv_kappa": 0.05, "cv_rho": 0.05, "Q": 400.0, "mfp": mat.meanFreePath}
-    fd = {p: A.finite_difference(geo, src, mat, obs, Et, p, 1e-2 if p != "Q" else 1e-3, o) for p in params}
+    fd = {p: A.finite_difference(geo, src, mat, obs, Et, p, 1e-3, o) for p in params}
     g = np.array([res["grad"][p] * scale[p] for p in params])
     f = np.array([fd[p] * scale[p] for p in params])
     assert np.linalg.norm(g - f) <= 0.02 * np.linalg.norm(f), (g, f)
     assert abs(res["grad"]["Q"] - fd["Q"]) <= 1e-5 * abs(fd["Q"])
     for p in ("cv_kappa", "cv_rho", "mfp"):
         assert abs(res["grad"][p] - fd[p]) <= 0.02 * abs(fd[p]), (p, res["grad"][p], fd[p])
+
+
+def test_gradient_lc_within_2_percent_at_8e9_particles():
+    """The lc component against central differences (1e-3 relative step, common random
+    numbers) at 8e9 particles, where the Monte Carlo spread of the difference of the two
+    estimates (0.033 in p dL/dp at 1e7 particles, measured over seeds) falls to 0.7% of
+    the component: within 2%.  The transport runs in chunks of its segment budget."""
+    from radiativetransfermontecarlo_gb300 import adjoint as A
+    geo, src, mat, obs, opts, Et = _gradient_case(10_000_000, full_grid=True)
+    n = 8_000_000_000
+    src = dict(src, numberParticles=n)
+    o = dict(opts, exact_count=True, precision="fp32", seed=5)
+    res = A.radiativeTransferGradient(geo, src, mat, obs, Et, ("lc",), dict(o, target_particles=10_000_000))
+    assert res["adjoint_stats"]["device_status"] == 0
+    fd = A.finite_difference(geo, src, mat, obs, Et, "lc", 1e-3, dict(o, target_particles=10_000_000))
+    assert abs(res["grad"]["lc"] - fd) <= 0.02 * abs(fd), (res["grad"]["lc"], fd)
 
 
 @pytest.mark.parametrize("name", ["c1", "c3", "c2_index", "cylinder_elastic", "plane_circle"])
