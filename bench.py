@@ -442,7 +442,7 @@ def run_c4(args):
     from radiativetransfermontecarlo_gb300 import workloads as W
     from radiativetransfermontecarlo_gb300.batch import Batch, autotune
     t0 = time.perf_counter()
-    batch = Batch([W.c4_instance(i) for i in range(256)])
+    batch = Batch([W.c4_instance(i) for i in range(args.instances)])
     setup_s = time.perf_counter() - t0
     if args.no_tune:
         shape, tune = (0, 0, 0), {}
@@ -470,8 +470,8 @@ def run_c4(args):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": float(np.mean(ms)), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "256-instance 3D acoustic sweep: lc log-U[0.02,1], cv U[0.01,0.2], f log-U[1,20], "
-                                   "Q in {Inf,100,500}, N log-U[1e4,1e7]; spherical 120 x 251 grid",
+            "config": {"workload": f"{args.instances}-instance 3D acoustic sweep: lc log-U[0.02,1], cv U[0.01,0.2], "
+                                   "f log-U[1,20], Q in {Inf,100,500}, N log-U[1e4,1e7]; spherical 120 x 251 grid",
                        "particles_total": n_total, "launch_shape": list(shape), "table_setup_s": setup_s,
                        "l2": "512 MB device write between steps"},
             "gpu_launches": args.steps, "clocks": clk.summary(),
@@ -712,6 +712,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="seconds of each CPU-baseline sample")
     ap.add_argument("--no-tune", action="store_true", help="c4: the default launch shape, no autotuning")
+    ap.add_argument("--instances", type=int, default=256, help="c4: instances of the sweep (the first n of its draw)")
     ap.add_argument("--no-fd", action="store_true", help="c5: skip the finite-difference check (timing only)")
     ap.add_argument("--no-sub", action="store_true",
                     help="skip the compact C1/C3/C4/C5 records that the default C2 line carries")

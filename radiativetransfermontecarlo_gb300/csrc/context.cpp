@@ -628,7 +628,13 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&be, kernel_of(prec, 5, sink, p.obs_kind), 256, sl.smem_events) !=
                 cudaSuccess || be < 1)
             return fail(&ctx->err, RTMC_ERR_CUDA, "event kernel does not fit on the device");
-        sl.block_observe = sink == kSinkSmem ? 512 : 256;
+        {
+            // the kernel's launch bound is its block size
+            cudaFuncAttributes fa{};
+            if (cudaFuncGetAttributes(&fa, kernel_of(prec, 6, sink, p.obs_kind)) != cudaSuccess || fa.maxThreadsPerBlock < 32)
+                return fail(&ctx->err, RTMC_ERR_CUDA, "observation kernel attributes");
+            sl.block_observe = fa.maxThreadsPerBlock - fa.maxThreadsPerBlock % 32;
+        }
         sl.smem_observe = edge_smem + (sink == kSinkSmem ? hist_smem : 0);
         if (kernel_set_smem(prec, 6, sink, p.obs_kind, sl.smem_observe) != 0 ||
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bo, kernel_of(prec, 6, sink, p.obs_kind), sl.block_observe,

@@ -30,7 +30,7 @@ int RTMC_NAME(launch_split)(const DevParams<RTMC_REAL> &p, const SplitLaunch &l,
 
 void *RTMC_NAME(kernel_of_split)(int kind, int sink, int obs)
 {
-    return kind == 5 ? pick_events<RTMC_REAL>(obs) : (kind == 6 ? pick_observe<RTMC_REAL>(sink, obs) : pick_list<RTMC_REAL>(obs));
+    return kind == 5 ? pick_events<RTMC_REAL>(obs) : (kind == 6 ? pick_observe<RTMC_REAL>(sink, obs) : pick_list<RTMC_REAL>(sink, obs));
 }
 #elif RTMC_PART == 2
 int RTMC_NAME(launch_transport_batch)(const BatchArgs<RTMC_REAL> &a, int grid, int block, size_t smem, void *stream)

@@ -1329,6 +1329,12 @@ template <typename R, int OBS> __device__ __forceinline__ void rec_put(R *r, con
     const R *v = OBS == OBS_GENERAL ? g.d : g.B;
     rec_store(r, u, v, g.s0 | (g.mode << 30), g.doff);
 }
+// the start sub-step alone (the word that holds it with the mode: 6 in FP32, the low
+// half of double 6 in FP64)
+template <typename R> __device__ __forceinline__ int rec_start(const R *r)
+{
+    return __ldg(reinterpret_cast<const int *>(r) + (sizeof(R) == 4 ? 6 : 12)) & 0x3fffffff;
+}
 template <typename R, int OBS> __device__ __forceinline__ void rec_get(const R *r, Seg<R> &g)
 {
     R *u = OBS == OBS_CART ? g.A : g.x;
@@ -1436,7 +1442,8 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) rt_events(const D
 
 // Observations of the particles rt_events traced: a warp takes 32 consecutive particles
 // and walks the observation instants in lockstep, each lane on its own segment list (the
-// segment after the one in force is loaded ahead, so a segment change waits on nothing).
+// segment after the one in force, and the start of the one after that, are loaded ahead,
+// so a segment change waits on no load).
 // Per instant a lane does one compare for a segment change or its end (rare, and then
 // the offset from the segment start is set afresh), the binning, and one store; the
 // offset is carried as a float counter while it stays an exact integer (below 2^24).
@@ -1460,9 +1467,12 @@ __device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *se
     const R *rec = static_cast<const R *>(p.segs) + (size_t)(have ? i : 0) * K * kRecWords;
     Seg<R> cur, nxt;
     cur.s0 = 0; cur.mode = 0; cur.doff = -1;
-    int k = 0, next_start = 0x7fffffff;
+    // segment k is in force, k + 1 is held in nxt and the start of k + 2 in after: a
+    // segment change uses only loads issued at the change before it
+    int k = 0, next_start = 0x7fffffff, after = 0x7fffffff;
     if (nseg > 0) rec_get<R, OBS>(rec, cur);
     if (nseg > 1) { rec_get<R, OBS>(rec + kRecWords, nxt); next_start = nxt.s0; }
+    if (nseg > 2) after = rec_start(rec + 2 * kRecWords);
     // index entries carry the mode in bit 30: fold it into the direction offset once per
     // segment (the index path keeps a time slice below 2^30 bins)
     auto fold_mode = [&]() {
@@ -1485,12 +1495,9 @@ __device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *se
                 do {
                     cur = nxt;
                     ++k;
-                    if (k + 1 < nseg) {
-                        rec_get<R, OBS>(rec + (size_t)(k + 1) * kRecWords, nxt);
-                        next_start = nxt.s0;
-                    } else {
-                        next_start = 0x7fffffff;
-                    }
+                    next_start = after; // the start of segment k + 1
+                    if (k + 1 < nseg) rec_get<R, OBS>(rec + (size_t)(k + 1) * kRecWords, nxt);
+                    after = k + 2 < nseg ? rec_start(rec + (size_t)(k + 2) * kRecWords) : 0x7fffffff;
                 } while (so >= next_start);
                 fold_mode();
                 bound = min(next_start, limit);
@@ -1520,8 +1527,10 @@ __device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *se
     }
 }
 
+// the shared-memory sink holds one block per SM (the histogram fills the shared memory):
+// FP32 takes 1024 threads so that 32 warps hide the latencies
 template <typename R, int SINK> struct ObserveBounds {
-    static constexpr int threads = SINK == SINK_SMEM ? 512 : 256;
+    static constexpr int threads = SINK == SINK_SMEM ? (sizeof(R) == 4 ? 1024 : 512) : 256;
     static constexpr int min_blocks = SINK == SINK_SMEM ? 1 : (sizeof(R) == 4 ? 4 : 2);
 };
 
@@ -1559,10 +1568,12 @@ __global__ void __launch_bounds__(ObserveBounds<R, SINK>::threads, ObserveBounds
 }
 
 // The particles whose segments overflowed seg_cap in rt_events, rerun whole one per
-// thread (the event-major schedule) with their observations added to the histogram by
-// 64-bit global atomics; their rows of the index array hold -1.  The list length is read
-// on the device, so the launch needs no host synchronisation.
-template <typename R, int OBS>
+// thread (the event-major schedule).  On the index path the rerun writes the particle's
+// rows of the index array (rt_observe left them at -1), so the fold that follows sees
+// every particle alike; otherwise its observations go to the histogram by 64-bit global
+// atomics.  The list length is read on the device, so the launch needs no host
+// synchronisation.
+template <typename R, int SINK, int OBS>
 __global__ void __launch_bounds__(256) rt_transport_list(const DevParams<R> p)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1573,7 +1584,7 @@ __global__ void __launch_bounds__(256) rt_transport_list(const DevParams<R> p)
     Counters cnt = {0u, 0u, 0u, 0u, 0u, 0u};
     bool bad = false;
     for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
-        run_particle<R, SINK_GLOBAL, OBS>(p, sedges, nullptr, p.ovf_list[t], cnt, bad);
+        run_particle<R, SINK, OBS>(p, sedges, nullptr, p.ovf_list[t], cnt, bad);
     const unsigned full = 0xffffffffu;
     unsigned v[6] = {cnt.scat, cnt.bnd, cnt.kill, cnt.absorb, cnt.obs, cnt.conv};
 #pragma unroll
@@ -1945,10 +1956,17 @@ template <typename R> void *pick_observe(int sink, int obs)
                              : (sink == SINK_GLOBAL ? pick_observe_obs<R, SINK_GLOBAL>(obs) : pick_observe_obs<R, SINK_INDEX>(obs));
 }
 
-template <typename R> void *pick_list(int obs)
+template <typename R, int SINK> void *pick_list_obs(int obs)
 {
-    return obs == OBS_CART ? (void *)rt_transport_list<R, OBS_CART>
-                           : (obs == OBS_RADIAL ? (void *)rt_transport_list<R, OBS_RADIAL> : (void *)rt_transport_list<R, OBS_GENERAL>);
+    return obs == OBS_CART ? (void *)rt_transport_list<R, SINK, OBS_CART>
+                           : (obs == OBS_RADIAL ? (void *)rt_transport_list<R, SINK, OBS_RADIAL>
+                                                : (void *)rt_transport_list<R, SINK, OBS_GENERAL>);
+}
+
+// the rerun of overflowing particles: index rows on the index path, else global atomics
+template <typename R> void *pick_list(int sink, int obs)
+{
+    return sink == SINK_INDEX ? pick_list_obs<R, SINK_INDEX>(obs) : pick_list_obs<R, SINK_GLOBAL>(obs);
 }
 
 // the split schedule: rt_events, rt_observe, rt_transport_list, in stream order
@@ -1963,7 +1981,7 @@ int launch_split_t(const DevParams<R> &p, const SplitLaunch &l, void *stream)
         e = cudaLaunchKernel(pick_observe<R>(p.sink, p.obs_kind), dim3(l.grid_observe), dim3(l.block_observe), args,
                              l.smem_observe, (cudaStream_t)stream);
     if (e == cudaSuccess)
-        e = cudaLaunchKernel(pick_list<R>(p.obs_kind), dim3(l.grid_list), dim3(256), args, l.smem_events,
+        e = cudaLaunchKernel(pick_list<R>(p.sink, p.obs_kind), dim3(l.grid_list), dim3(256), args, l.smem_events,
                              (cudaStream_t)stream);
     return (int)e;
 }
