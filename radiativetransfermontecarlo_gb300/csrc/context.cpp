@@ -65,7 +65,7 @@ struct rtmc_context {
     // per-chunk events, created on first use
     int opt_chunks = 0, opt_k1_bps = 0;
     int opt_event_major = -1; // -1 automatic, 0 two-cursor batches, 1 one particle per thread, 2 split
-    int opt_fold = 0;         // 0 automatic, 1 64-bit slice fold, 2 time-blocked FP32 fold
+    int opt_fold = 0;         // 0 automatic, 1 64-bit slice fold, 2 time-blocked FP32 fold, 3 the same without rolling
     static constexpr int kPipe = 32;
     cudaStream_t fold_stream = nullptr;
     cudaEvent_t ev_a0[kPipe] = {}, ev_a1[kPipe] = {}, ev_b0[kPipe] = {}, ev_b1[kPipe] = {};
@@ -367,6 +367,15 @@ void fill_params(rtmc_context *ctx, const rtmc_problem *P, const DevTables<R> &t
         else p->ax_stride32[a] = 0;
         finite_uniform[a] = uni && std::isfinite(E[0]) && std::isfinite(E[ne - 1]);
     }
+    {
+        uint32_t bias = 0;
+        for (int a = 0; a < 4; ++a) {
+            const float nb = (float)p->ax_nbe[a];
+            std::memcpy(&p->ax_nbits[a], &nb, sizeof(nb));
+            if (a < 3) bias += 0x4B000000u * (uint32_t)p->ax_stride32[a];
+        }
+        std::memcpy(&p->cart_bias, &bias, sizeof(bias));
+    }
     // observation path (see obs_offset in transport.cuh)
     p->obs_kind = 0;
     if (P->frame == RTMC_FRAME_CARTESIAN) {
@@ -657,11 +666,21 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
     // particles): it writes every bin of the histogram, so only its accumulator needs a clear
     const bool use_tb = sink == kSinkIndex && !n_pipe && P->n_particles < ((int64_t)1 << 24) && ctx->opt_fold != 1;
     const int ntb = (P->n_obs + 3) / 4;
+    int roll = 0; // t-blocks per turn of a rolling accumulator (0: the full accumulator)
+    bool narrowed = false; // the conversion also wrote the uint32 counts
     TbParams tpl{};
     int tb_grid = 1;
     if (use_tb) {
         tpl.S = P->time_stride * nm;
-        const size_t acc_bytes = (size_t)ntb * tpl.S * 4 * sizeof(float);
+        // one particle chunk: the accumulator rolls over the t-blocks, as many at a time as
+        // fit in kRollBytes (at least one), so that it stays in the L2 between its
+        // reductions and its conversion; several chunks keep every t-block until the last
+        constexpr int64_t kRollBytes = (int64_t)64 << 20;
+        if (chunk >= P->n_particles && ctx->opt_fold != 3) {
+            roll = (int)std::max<int64_t>(1, std::min<int64_t>(ntb, kRollBytes / (tpl.S * 16)));
+            if (roll >= ntb) roll = 0;
+        }
+        const size_t acc_bytes = (size_t)(roll ? roll : ntb) * tpl.S * 4 * sizeof(float);
         if (ctx->tbacc.grow(acc_bytes)) return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for the fold accumulator failed");
         tpl.acc = static_cast<float *>(ctx->tbacc.p);
         tpl.idx = static_cast<const int32_t *>(ctx->idx.p);
@@ -674,7 +693,7 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
     // ahead of the transport
     unsigned long long *to_clear = use_tb ? static_cast<unsigned long long *>(ctx->tbacc.p)
                                           : static_cast<unsigned long long *>(ctx->hist.p);
-    const int64_t clear_words = use_tb ? (int64_t)ntb * tpl.S * 2 : P->hist_len;
+    const int64_t clear_words = use_tb ? (int64_t)(roll ? roll : ntb) * tpl.S * 2 : P->hist_len;
     if (split) {
         p.clear = to_clear;
         p.clear_words = clear_words;
@@ -792,50 +811,56 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
             tp.n = q.n_particles;
             tp.part_per_block = ((tp.n + tb_grid - 1) / tb_grid + 3) / 4 * 4;
             unsigned long long *hist = p.hist;
-            if (last && (host_out || host_u32) && ntb >= 2 * kCopyGroups && ensure_pipeline(ctx) == 0) {
-                // the last fold and its conversion in groups of t-blocks: each group's slices
-                // are final, so their copy to the host runs on the second stream while the
-                // next group folds
-                const int64_t ts = P->time_stride;
-                for (int g = 0; g < kCopyGroups && !le; ++g) {
-                    tp.tb_first = tb_group_start(ntb, g);
-                    tp.tb_count = tb_group_start(ntb, g + 1) - tp.tb_first;
-                    if (tp.tb_count < 1) continue;
+            // the last fold in groups of t-blocks when the histogram goes to the host: each
+            // group's slices are final, so their copy runs on the second stream while the
+            // next group folds
+            const bool groups = last && (host_out || host_u32) && ntb >= 2 * kCopyGroups && ensure_pipeline(ctx) == 0;
+            const int ng = groups ? kCopyGroups : 1;
+            const int64_t ts = P->time_stride;
+            for (int g = 0; g < ng && !le; ++g) {
+                const int ga = groups ? tb_group_start(ntb, g) : 0, gb = groups ? tb_group_start(ntb, g + 1) : ntb;
+                if (gb <= ga) continue;
+                // a rolling accumulator takes `roll` t-blocks at a time and is zeroed again by
+                // their conversion; the full one takes the group at once
+                const int step = roll ? roll : gb - ga;
+                for (int t0 = ga; t0 < gb && !le; t0 += step) {
+                    tp.tb_first = t0;
+                    tp.tb_count = std::min(step, gb - t0);
+                    tp.acc_tb0 = roll ? t0 : 0;
+                    tp.rezero = roll ? 1 : 0;
                     le = launch_fold_tb(tp, tb_grid, ctx->stream);
-                    if (!le) le = launch_tb_convert(tp, ts, P->mode_stride, P->hist_shift, hist, narrow, narrow_grid, ctx->stream);
-                    launches += 2;
-                    if (le) break;
-                    const int64_t ja = g == 0 ? 0 : 4 * (int64_t)tp.tb_first + 1; // slice 0 with the first group
-                    const int64_t jb = std::min<int64_t>(4 * (int64_t)(tp.tb_first + tp.tb_count), P->n_obs) + 1;
-                    CK(cudaEventRecord(ctx->ev_a1[g], ctx->stream), "event");
-                    CK(cudaStreamWaitEvent(ctx->fold_stream, ctx->ev_a1[g], 0), "copy wait");
-                    for (int m = 0; m < nm; ++m) {
-                        const int64_t o = m * P->mode_stride + ja * ts;
-                        const size_t cnt = (size_t)((jb - ja) * ts);
-                        if (narrow)
-                            CK(cudaMemcpyAsync(host_u32 + o, narrow + o, cnt * sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                                               ctx->fold_stream),
-                               "histogram copy");
-                        else
-                            CK(cudaMemcpyAsync(host_out + o, static_cast<int64_t *>(ctx->hist.p) + o, cnt * sizeof(int64_t),
-                                               cudaMemcpyDeviceToHost, ctx->fold_stream),
-                               "histogram copy");
+                    ++launches;
+                    if (!le && last) {
+                        le = launch_tb_convert(tp, ts, P->mode_stride, P->hist_shift, hist, host_u32 ? narrow : nullptr,
+                                               narrow_grid, ctx->stream);
+                        ++launches;
+                        narrowed = host_u32 != nullptr;
                     }
                 }
+                if (le || !groups) break;
+                const int64_t ja = g == 0 ? 0 : 4 * (int64_t)ga + 1; // slice 0 with the first group
+                const int64_t jb = std::min<int64_t>(4 * (int64_t)gb, P->n_obs) + 1;
+                CK(cudaEventRecord(ctx->ev_a1[g], ctx->stream), "event");
+                CK(cudaStreamWaitEvent(ctx->fold_stream, ctx->ev_a1[g], 0), "copy wait");
+                for (int m = 0; m < nm; ++m) {
+                    const int64_t o = m * P->mode_stride + ja * ts;
+                    const size_t cnt = (size_t)((jb - ja) * ts);
+                    if (host_u32)
+                        CK(cudaMemcpyAsync(host_u32 + o, narrow + o, cnt * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                           ctx->fold_stream),
+                           "histogram copy");
+                    else
+                        CK(cudaMemcpyAsync(host_out + o, static_cast<int64_t *>(ctx->hist.p) + o, cnt * sizeof(int64_t),
+                                           cudaMemcpyDeviceToHost, ctx->fold_stream),
+                           "histogram copy");
+                }
+            }
+            if (groups && !le) {
                 CK(cudaEventRecord(ctx->ev_b1[0], ctx->fold_stream), "event");
                 CK(cudaEventRecord(ctx->ev_k2, ctx->stream), "event");
                 CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_b1[0], 0), "copy join");
                 copied = true;
             } else {
-                tp.tb_first = 0;
-                tp.tb_count = ntb;
-                le = launch_fold_tb(tp, tb_grid, ctx->stream);
-                ++launches;
-                if (!le && last) {
-                    le = launch_tb_convert(tp, P->time_stride, P->mode_stride, P->hist_shift, hist, nullptr, narrow_grid,
-                                           ctx->stream);
-                    ++launches;
-                }
                 CK(cudaEventRecord(ctx->ev_k2, ctx->stream), "event");
             }
         } else if (!le && sink == kSinkIndex) {
@@ -918,9 +943,11 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
     } else if (host_u32) {
         const size_t u32_bytes = (size_t)P->hist_len * sizeof(uint32_t);
         if (!copied) {
-            le = launch_narrow_u32(p.hist, narrow, P->hist_len, P->hist_shift, narrow_grid, ctx->stream);
-            if (le) return cuda_fail(ctx, (cudaError_t)le, "histogram narrowing");
-            ++launches;
+            if (!narrowed) {
+                le = launch_narrow_u32(p.hist, narrow, P->hist_len, P->hist_shift, narrow_grid, ctx->stream);
+                if (le) return cuda_fail(ctx, (cudaError_t)le, "histogram narrowing");
+                ++launches;
+            }
             CK(cudaMemcpyAsync(host_u32, narrow, u32_bytes, cudaMemcpyDeviceToHost, ctx->stream), "histogram copy");
         }
         d2h += (double)u32_bytes;
@@ -1572,7 +1599,7 @@ extern "C" int rtmc_set_schedule(rtmc_context *ctx, int32_t event_major)
 extern "C" int rtmc_set_fold(rtmc_context *ctx, int32_t mode)
 {
     if (!ctx) return fail(nullptr, RTMC_ERR_ARG, "rtmc_set_fold: NULL context");
-    if (mode < 0 || mode > 2) return fail(&ctx->err, RTMC_ERR_ARG, "fold mode must be 0, 1 or 2");
+    if (mode < 0 || mode > 3) return fail(&ctx->err, RTMC_ERR_ARG, "fold mode must be 0, 1, 2 or 3");
     ctx->opt_fold = mode;
     return RTMC_OK;
 }

@@ -251,7 +251,7 @@ __global__ void __launch_bounds__(kTbThreads) rt_fold_tb(const TbParams t)
 #pragma unroll
     for (int r = 0; r < 4; ++r)
         row[r] = reinterpret_cast<const int4 *>(t.idx + (int64_t)(j0 - 1 + (r < nr ? r : 0)) * t.rows);
-    float *acc = t.acc + (size_t)tb * t.S * 4;
+    float *acc = t.acc + (size_t)(tb - t.acc_tb0) * t.S * 4;
     for (int k = threadIdx.x; k < kTbSlots; k += blockDim.x) {
         keys[k] = -1;
         cnt[k][0] = cnt[k][1] = cnt[k][2] = cnt[k][3] = 0u;
@@ -318,9 +318,15 @@ __global__ void __launch_bounds__(kConvThreads) rt_tb_convert(const TbParams t, 
                                                               uint32_t *__restrict__ u32)
 {
     const int tb = t.tb_first + blockIdx.y;
-    const float4 *a4 = reinterpret_cast<const float4 *>(t.acc) + (size_t)tb * t.S;
+    float4 *a4 = reinterpret_cast<float4 *>(t.acc) + (size_t)(tb - t.acc_tb0) * t.S;
     for (int64_t s = (int64_t)blockIdx.x * kConvThreads + threadIdx.x; s < t.S; s += (int64_t)gridDim.x * kConvThreads) {
-        const float4 c = __ldcs(a4 + s);
+        float4 c;
+        if (t.rezero) { // a rolling accumulator: its lines stay in the L2 for the next turn
+            c = __ldcg(a4 + s);
+            a4[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+        } else {
+            c = __ldcs(a4 + s);
+        }
         const int64_t off = s >= t.slice_bins ? mode_stride + (s - t.slice_bins) : s;
         const float cv[4] = {c.x, c.y, c.z, c.w};
 #pragma unroll

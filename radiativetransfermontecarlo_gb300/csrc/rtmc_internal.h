@@ -95,6 +95,11 @@ template <typename R> struct DevParams {
     R ax_lo[4], ax_hi[4], ax_inv_w[4];
     int64_t ax_stride[4];
     int32_t ax_stride32[4];  // in-slice strides (a time slice holds < 2^31 bins)
+    // FP32 cartesian observation kernel: the float bit patterns of the bin counts
+    // (unsigned compares against a coordinate's bits), and 0x4B000000 times the sum of the
+    // three in-slice strides, mod 2^32 (taken off the direction offset once per segment)
+    int32_t ax_nbits[4];
+    int32_t cart_bias;
     int64_t time_stride, mode_stride, hist_len;
     int32_t n_edges;
     int32_t bnd_dir[RTMC_MAX_BND], bnd_absorb[RTMC_MAX_BND];
@@ -152,7 +157,9 @@ struct TbParams {
     int64_t S;                // slice_bins * n_modes
     int32_t n_obs, slice_bins;
     int32_t tb_first, tb_count; // t-blocks [tb_first, tb_first + tb_count)
-    float *acc;
+    float *acc;               // [t-block - acc_tb0][S][4] FP32 counts
+    int32_t acc_tb0;          // the t-block at the start of acc (0, or a rolling accumulator's turn)
+    int32_t rezero;           // the conversion writes zeros back (a rolling accumulator)
 };
 
 // One work item of a batched run: particles [first, first + count) of instance inst.

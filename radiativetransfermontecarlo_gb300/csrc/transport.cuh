@@ -731,6 +731,8 @@ __device__ __forceinline__ float m_fma(float a, float b, float c) { return __fma
 __device__ __forceinline__ double m_fma(double a, double b, double c) { return __fma_rn(a, b, c); }
 __device__ __forceinline__ float m_mul(float a, float b) { return __fmul_rn(a, b); }
 __device__ __forceinline__ double m_mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ float m_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double m_add(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ float m_sub(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ double m_sub(double a, double b) { return __dsub_rn(a, b); }
 
@@ -840,6 +842,26 @@ __device__ __forceinline__ int obs_offset_dl(const DevParams<R> &p, const R *sed
         return po < 0 ? -1 : po + g.doff;
     }
 }
+
+// The FP32 cartesian path of the observation kernel, the same bins as obs_offset_dl with
+// one integer add per axis fewer: t's bit pattern, compared unsigned with that of the bin
+// count, is below it exactly for 0 <= t < count (negative t, NaN and infinities have
+// larger patterns; t is never -0 because the segment's offsets are normalised), and the
+// bin's pattern after adding 2^23 toward zero is 0x4B000000 + floor(t), whose bias the
+// segment's `base` already carries.  A segment whose direction lies outside the grid has A[0] = inf.
+__device__ __forceinline__ int obs_offset_cart32(const DevParams<float> &p, const Seg<float> &g, float dl, int base)
+{
+    bool ok = true;
+    unsigned idx = (unsigned)base;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float t = m_fma(g.B[a], dl, g.A[a]);
+        ok = ok && (unsigned)__float_as_int(t) < (unsigned)p.ax_nbits[a];
+        idx += (unsigned)__float_as_int(__fadd_rz(t, 8388608.0f)) * (unsigned)p.ax_stride32[a];
+    }
+    return ok ? (int)idx : -1;
+}
+__device__ __forceinline__ int obs_offset_cart32(const DevParams<double> &, const Seg<double> &, double, int) { return -1; }
 
 // the same at sub-step so
 template <typename R, int OBS>
@@ -1467,6 +1489,7 @@ __device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *se
     const R *rec = static_cast<const R *>(p.segs) + (size_t)(have ? i : 0) * K * kRecWords;
     Seg<R> cur, nxt;
     cur.s0 = 0; cur.mode = 0; cur.doff = -1;
+    cur.A[0] = cur.A[1] = cur.A[2] = cur.B[0] = cur.B[1] = cur.B[2] = (R)0;
     // segment k is in force, k + 1 is held in nxt and the start of k + 2 in after: a
     // segment change uses only loads issued at the change before it
     int k = 0, next_start = 0x7fffffff, after = 0x7fffffff;
@@ -1475,8 +1498,20 @@ __device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *se
     if (nseg > 2) after = rec_start(rec + 2 * kRecWords);
     // index entries carry the mode in bit 30: fold it into the direction offset once per
     // segment (the index path keeps a time slice below 2^30 bins)
+    // FP32 cartesian: per segment, a direction outside the grid becomes an infinite first
+    // coordinate (every observation of the segment then fails the range test), the
+    // coordinates' offsets lose a negative zero, and the 2^23 bias of the three bin
+    // patterns comes off the direction offset (see obs_offset_cart32)
+    constexpr bool C32 = sizeof(R) == 4 && OBS == OBS_CART;
+    int cbase = 0;
     auto fold_mode = [&]() {
         if (INDEX && cur.doff >= 0) cur.doff |= cur.mode << 30;
+        if (C32) {
+#pragma unroll
+            for (int a = 0; a < 3; ++a) cur.A[a] = m_add(cur.A[a], (R)0);
+            if (cur.doff < 0) cur.A[0] = (R)INFINITY;
+            cbase = (int)((unsigned)cur.doff - (unsigned)p.cart_bias);
+        }
     };
     fold_mode();
     const bool count_dl = sizeof(R) == 8 || p.s_end < (1 << 24);
@@ -1490,6 +1525,7 @@ __device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *se
         if (so >= bound) {
             if (so >= limit) { // the particle's end: nothing more is binned
                 cur.doff = -1;
+                if (C32) cur.A[0] = (R)INFINITY;
                 bound = 0x7fffffff;
             } else { // the next segment comes into force; load the one after it
                 do {
@@ -1506,7 +1542,9 @@ __device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *se
         } else if (!count_dl) {
             dl = (R)(so - cur.s0);
         }
-        const int v = obs_offset_dl<R, OBS>(p, sedges, cur, dl);
+        int v;
+        if constexpr (C32) v = obs_offset_cart32(p, cur, dl, cbase);
+        else v = obs_offset_dl<R, OBS>(p, sedges, cur, dl);
         dl += dstep;
         if (INDEX) {
             if (have) {

@@ -668,20 +668,24 @@ def test_observation_frames_and_bin_pairs_match_oracle(d, frame, pair):
             assert _l1_diff(hist, ref_hist) <= 2e-3 * stats["observations"] + 4
 
 
-@pytest.mark.parametrize("index_mb", [0, 1])
-def test_time_blocked_fold_equals_slice_fold(index_mb):
+@pytest.mark.parametrize("index_mb,width", [(0, None), (1, None), (0, 0.25)])
+def test_time_blocked_fold_equals_slice_fold(index_mb, width):
     """The time-blocked FP32 fold (vector reductions over runs of 4 instants, then the
     conversion) gives the 64-bit slice fold's histogram bit for bit: int64 and uint32 host
-    outputs (converted and copied in groups of instants), the device histogram, and
-    several particle chunks (1 MB of index scratch)."""
+    outputs (converted and copied in groups of instants), the device histogram, several
+    particle chunks (1 MB of index scratch), and the rolling accumulator (one chunk: one
+    t-block per turn on the 60^3 grid, three on a 40^3 grid, whose 13 t-blocks leave a
+    last turn of one) against the full one (mode 3)."""
     geo, src, mat, obs, opts = W.c2_elastic3d(t_end=1.0)
+    if width:
+        obs = dict(obs, x=colon(-5, width, 5), y=colon(-5, width, 5), z=colon(-5, width, 5))
     prob, grid, N = build_problem(geo, dict(src, numberParticles=20000), mat, obs, dict(opts, exact_count=True))
     P, keep = prob.to_ctypes()
     ctx = get_context(0)
     out = {}
     try:
         ctx.set_launch(0, 0, index_mb)
-        for mode in (1, 2):
+        for mode in (1, 2, 3):
             ctx.set_fold(mode)
             h, st = ctx.forward(P, prob.tables)
             u, _ = ctx.forward_u32(P, prob.tables)
@@ -691,9 +695,12 @@ def test_time_blocked_fold_equals_slice_fold(index_mb):
     finally:
         ctx.set_fold(0)
         ctx.set_launch(0, 0, 0)
-    (h1, u1, d1, s1, sd1), (h2, u2, d2, s2, sd2) = out[1], out[2]
-    assert s1["sink"] == 2 and s1["device_status"] == 0 and s2["device_status"] == 0
+    (h1, u1, d1, s1, sd1), (h2, u2, d2, s2, sd2), (h3, u3, d3, s3, sd3) = out[1], out[2], out[3]
+    assert s1["sink"] == 2 and s1["device_status"] == 0 and s2["device_status"] == 0 and s3["device_status"] == 0
     if index_mb:
         assert s2["launches"] > s1["launches"] - 2  # several chunks on both paths
+    else:
+        assert sd2["launches"] > sd3["launches"]  # the rolling accumulator takes turns
     assert np.array_equal(h1, h2) and np.array_equal(u1, u2) and np.array_equal(d1, d2) and np.array_equal(h1, d1)
-    assert s1["observations"] == s2["observations"] == int(h1.sum() >> prob.hist_shift)
+    assert np.array_equal(h1, h3) and np.array_equal(u1, u3) and np.array_equal(d1, d3)
+    assert s1["observations"] == s2["observations"] == s3["observations"] == int(h1.sum() >> prob.hist_shift)
