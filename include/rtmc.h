@@ -375,11 +375,10 @@ int rtmc_set_schedule(rtmc_context *ctx, int32_t event_major);
  * into its time slice of the histogram; 2 = time-blocked: FP32 counts with the 4
  * instants of a bin adjacent, a particle's run of instants in one bin added as one vector
  * reduction, then converted to the histogram (needs fewer than 2^24 particles, so that
- * FP32 counts are exact).  When one particle chunk covers the call, the FP32 accumulator
- * rolls over the time blocks, 64 MB of them at a time, each turn converted (and zeroed)
- * right after its reductions while it sits in the L2; 3 = the same with an accumulator
- * for every time block; 0 = automatic (2 when it applies).  All give the same
- * histogram. */
+ * FP32 counts are exact); 3 = time-blocked with a rolling accumulator when one particle
+ * chunk covers the call: 64 MB of time blocks at a time, each turn converted (and zeroed)
+ * right after its reductions (slower than 2 on the large grids measured; kept for
+ * comparison); 0 = automatic (2 when it applies).  All give the same histogram. */
 int rtmc_set_fold(rtmc_context *ctx, int32_t mode);
 
 /* enable (1, default) or disable (0) reuse of the device copy of a tables handle across

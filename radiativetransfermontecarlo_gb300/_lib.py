@@ -330,8 +330,8 @@ class Context:
         check(self.lib.rtmc_set_pipeline(self.handle, chunks, transport_blocks_per_sm), self.handle)
 
     def set_fold(self, mode: int = 0):
-        """rtmc_set_fold: 0 automatic, 1 64-bit slice fold, 2 time-blocked FP32 fold (rolling
-        accumulator when one chunk covers the call), 3 time-blocked with the full accumulator."""
+        """rtmc_set_fold: 0 automatic, 1 64-bit slice fold, 2 time-blocked FP32 fold, 3 the same
+        with a rolling accumulator when one chunk covers the call."""
         check(self.lib.rtmc_set_fold(self.handle, mode), self.handle)
 
     def set_schedule(self, event_major: int = -1):

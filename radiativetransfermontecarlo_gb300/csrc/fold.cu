@@ -211,6 +211,7 @@ __global__ void __launch_bounds__(kCheckThreads) rt_check_int64(const unsigned l
 // Counts are exact in FP32 below 2^24 per bin and instant.  Crowded chunks (early
 // instants) aggregate in a shared-memory hash first, as rt_bin_slices does.
 constexpr int kTbThreads = 512;
+constexpr int kTbAhead = 1; // index vectors a thread loads before folding them
 constexpr int kTbSlots = 2048;
 
 __device__ __forceinline__ void red_v4(float *a, float x, float y, float z, float w)
@@ -261,47 +262,62 @@ __global__ void __launch_bounds__(kTbThreads) rt_fold_tb(const TbParams t)
     const int64_t p1 = min(t.n, p0 + t.part_per_block);
     const int64_t q0 = p0 >> 2, q1 = (p1 + 3) >> 2;
     __syncthreads();
-    // the entries of 4 particles x the t-block's instants; each particle's distinct bins
-    // go out as one vector each (to the hash when crowded)
-    auto vector = [&](int64_t q, bool use_hash, int *nvalid) {
+    // the entries of 4 particles x the t-block's instants: each run of consecutive instants
+    // a particle spends in one bin goes out as one vector (to the hash when crowded)
+    auto load = [&](int64_t q, int4 (&x)[4]) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) x[r] = r < nr && q < q1 ? __ldcs(row[r] + q) : make_int4(-1, -1, -1, -1);
+    };
+    auto vector = [&](const int4 (&x)[4], int64_t q, bool use_hash, int *nvalid) {
         int e[4][4]; // [instant][particle]
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
-            const int4 a = r < nr ? __ldcs(row[r] + q) : make_int4(-1, -1, -1, -1);
-            e[r][0] = a.x; e[r][1] = a.y; e[r][2] = a.z; e[r][3] = a.w;
+            e[r][0] = x[r].x; e[r][1] = x[r].y; e[r][2] = x[r].z; e[r][3] = x[r].w;
         }
+        auto emit = [&](int v, int m0, int m1, int m2, int m3) {
+            const int key = (v & 0x3fffffff) + ((v >> 30) ? t.slice_bins : 0);
+            ++*nvalid;
+            const int m[4] = {m0, m1, m2, m3};
+            if (use_hash && *((volatile int *)&used) < 3 * kTbSlots / 4 && tb_hash_insert(keys, cnt, &used, key, m))
+                return;
+            red_v4(acc + (size_t)key * 4, (float)m0, (float)m1, (float)m2, (float)m3);
+        };
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
-            const int64_t k = q * 4 + u;
-            if (k >= p1) continue;
-#pragma unroll
-            for (int r = 0; r < 4; ++r) {
-                const int v = e[r][u];
-                if (v < 0) continue;
-                bool dup = false;
-#pragma unroll
-                for (int r2 = 0; r2 < r; ++r2) dup = dup || e[r2][u] == v;
-                if (dup) continue; // counted with the first instant of its bin
-                const int m[4] = {e[0][u] == v, e[1][u] == v, e[2][u] == v, e[3][u] == v};
-                const int key = (v & 0x3fffffff) + ((v >> 30) ? t.slice_bins : 0);
-                ++*nvalid;
-                if (use_hash && *((volatile int *)&used) < 3 * kTbSlots / 4 && tb_hash_insert(keys, cnt, &used, key, m))
-                    continue;
-                red_v4(acc + (size_t)key * 4, (float)m[0], (float)m[1], (float)m[2], (float)m[3]);
-            }
+            if (q * 4 + u >= p1) continue;
+            const int a = e[0][u], b = e[1][u], c = e[2][u], d = e[3][u];
+            const int e01 = a == b, e12 = b == c, e23 = c == d;
+            // a run starts at every instant whose bin differs from the one before; -1
+            // (not observed) is never emitted
+            if (a >= 0) emit(a, 1, e01, e01 & e12, e01 & e12 & e23);
+            if (b >= 0 && !e01) emit(b, 0, 1, e12, e12 & e23);
+            if (c >= 0 && !e12) emit(c, 0, 0, 1, e23);
+            if (d >= 0 && !e23) emit(d, 0, 0, 0, 1);
         }
     };
     // probe window: one vector per thread through the hash
     int nv = 0;
     int64_t q = q0 + threadIdx.x;
-    if (q < q1) vector(q, true, &nv);
+    int4 x[kTbAhead][4];
+    if (q < q1) {
+        load(q, x[0]);
+        vector(x[0], q, true, &nv);
+    }
     if (nv) atomicAdd(&valid, nv);
     __syncthreads();
     // crowded: the window's runs fell in at most a quarter of the table, each bin hit twice
     if (threadIdx.x == 0) dense = valid >= 64 && used * 4 <= kTbSlots && used * 2 <= valid;
     __syncthreads();
     const bool h = dense;
-    for (q += blockDim.x; q < q1; q += blockDim.x) vector(q, h, &nv);
+    // kTbAhead vectors per thread loaded together, then folded
+    const int64_t T = blockDim.x;
+    for (q += T; q < q1; q += kTbAhead * T) {
+#pragma unroll
+        for (int w = 0; w < kTbAhead; ++w) load(q + w * T, x[w]);
+#pragma unroll
+        for (int w = 0; w < kTbAhead; ++w)
+            if (q + w * T < q1) vector(x[w], q + w * T, h, &nv);
+    }
     __syncthreads();
     for (int k = threadIdx.x; k < kTbSlots; k += blockDim.x) {
         const int key = keys[k];

@@ -673,9 +673,9 @@ def test_time_blocked_fold_equals_slice_fold(index_mb, width):
     """The time-blocked FP32 fold (vector reductions over runs of 4 instants, then the
     conversion) gives the 64-bit slice fold's histogram bit for bit: int64 and uint32 host
     outputs (converted and copied in groups of instants), the device histogram, several
-    particle chunks (1 MB of index scratch), and the rolling accumulator (one chunk: one
-    t-block per turn on the 60^3 grid, three on a 40^3 grid, whose 13 t-blocks leave a
-    last turn of one) against the full one (mode 3)."""
+    particle chunks (1 MB of index scratch), and the rolling accumulator (mode 3; one
+    chunk: one t-block per turn on the 60^3 grid, three on a 40^3 grid, whose 13 t-blocks
+    leave a last turn of one) against the full one (mode 2)."""
     geo, src, mat, obs, opts = W.c2_elastic3d(t_end=1.0)
     if width:
         obs = dict(obs, x=colon(-5, width, 5), y=colon(-5, width, 5), z=colon(-5, width, 5))
@@ -700,7 +700,7 @@ def test_time_blocked_fold_equals_slice_fold(index_mb, width):
     if index_mb:
         assert s2["launches"] > s1["launches"] - 2  # several chunks on both paths
     else:
-        assert sd2["launches"] > sd3["launches"]  # the rolling accumulator takes turns
+        assert sd3["launches"] > sd2["launches"]  # the rolling accumulator takes turns
     assert np.array_equal(h1, h2) and np.array_equal(u1, u2) and np.array_equal(d1, d2) and np.array_equal(h1, d1)
     assert np.array_equal(h1, h3) and np.array_equal(u1, u3) and np.array_equal(d1, d3)
     assert s1["observations"] == s2["observations"] == s3["observations"] == int(h1.sum() >> prob.hist_shift)
