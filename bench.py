@@ -112,9 +112,9 @@ def measured_peak_hbm():
 
 
 def load_traffic():
-    """DRAM bytes of each kernel for one full-size launch (read + write), from an ncu capture
-    of a smaller case of this workload scaled to the full one by its units (particle-instants),
-    summarised in profiles/c2_traffic.json; {} when absent."""
+    """DRAM bytes (read + write) of each kernel in one full-size launch of this workload, from
+    a one-pass ncu capture (dram__bytes_read.sum, dram__bytes_write.sum), summarised in
+    profiles/c2_traffic.json; {} when absent."""
     p = ROOT / "profiles" / "c2_traffic.json"
     try:
         d = json.loads(p.read_text())
@@ -270,7 +270,7 @@ def run_our_arm(args, rank, world, dist):
     for _ in range(args.warmup):
         step(P32)
     # timed region: device time of each step from CUDA events on the library stream
-    dev_ms, kern_ms, fold_ms, ev_ms, events, obs_n = [], [], [], [], 0, 0
+    dev_ms, kern_ms, fold_ms, ev_ms, cv_ms, events, obs_n = [], [], [], [], [], 0, 0
     barrier()
     with ClockSampler(device) as clk:
         t_wall = time.perf_counter()
@@ -293,6 +293,7 @@ def run_our_arm(args, rank, world, dist):
             kern_ms.append(st["kernel_ms"])
             fold_ms.append(st["fold_ms"])
             ev_ms.append(st["events_ms"])
+            cv_ms.append(st["convert_ms"])
             launches_per_step = ctx.last_timing()[1]
             events += st["scatter_events"]
             obs_n += st["observations"]
@@ -315,6 +316,7 @@ def run_our_arm(args, rank, world, dist):
     if rank == 0:
         peak, peak_kind = measured_peak_hbm()
         kmean, fmean, emean = float(np.mean(kern_ms)), float(np.mean(fold_ms)), float(np.mean(ev_ms))
+        cmean = float(np.mean(cv_ms))
         entries = N * prob.n_obs  # (particle, observation instant) pairs of one step
         obs_per_step = obs_n / args.steps
         ev_step = events / args.steps
@@ -325,9 +327,6 @@ def run_our_arm(args, rank, world, dist):
         ev_inst = (ev_step * ISSUE_PER_EVENT + N * ISSUE_PER_START) / 32.0
         ob_inst = entries * ISSUE_PER_OBS / 32.0
         omean = max(kmean - emean, 1e-9)
-        # rt_bin_slices: reads the index array and, slice by slice in the L2, reads and
-        # writes the histogram once (its 64-bit reductions stay in the L2)
-        k2_bytes = 4.0 * entries + 16.0 * prob.hist_len
         kernels = {
             "rt_events": {"ms": emean, "bound": "issue", "algorithmic_warp_inst": ev_inst,
                           "achieved": ev_inst / max(emean, 1e-9) / 1e6, "peak": ipk / 1e9, "unit": "Ginst/s",
@@ -336,12 +335,30 @@ def run_our_arm(args, rank, world, dist):
                            "achieved": ob_inst / omean / 1e6, "peak": ipk / 1e9, "unit": "Ginst/s",
                            "frac": ob_inst / omean * 1e3 / ipk, "index_write_gbs": 4.0 * entries / omean / 1e6,
                            "traffic": traffic.get("rt_observe")},
-            "rt_bin_slices": {"ms": fmean, "bound": "hbm", "algorithmic_bytes": k2_bytes,
-                              "achieved": k2_bytes / max(fmean, 1e-9) / 1e6, "peak": peak, "unit": "GB/s",
-                              "frac": k2_bytes / max(fmean, 1e-9) / 1e6 / peak,
-                              "l2_reductions_per_s": obs_per_step / max(fmean, 1e-9) * 1e3,
-                              "traffic": traffic.get("rt_bin_slices")},
         }
+        if cmean > 0:
+            # time-blocked fold: rt_fold_tb reads the index array once (its FP32 vector
+            # reductions land in the L2); rt_tb_convert reads the FP32 accumulator (4 B per
+            # bin and instant) and writes the 8-byte histogram
+            tmean = max(fmean - cmean, 1e-9)
+            fb, cb = 4.0 * entries, 12.0 * prob.hist_len
+            kernels["rt_fold_tb"] = {"ms": tmean, "bound": "hbm", "algorithmic_bytes": fb,
+                                     "achieved": fb / tmean / 1e6, "peak": peak, "unit": "GB/s",
+                                     "frac": fb / tmean / 1e6 / peak,
+                                     "observations_per_s": obs_per_step / tmean * 1e3,
+                                     "traffic": traffic.get("rt_fold_tb")}
+            kernels["rt_tb_convert"] = {"ms": cmean, "bound": "hbm", "algorithmic_bytes": cb,
+                                        "achieved": cb / cmean / 1e6, "peak": peak, "unit": "GB/s",
+                                        "frac": cb / cmean / 1e6 / peak, "traffic": traffic.get("rt_tb_convert")}
+        else:
+            # 64-bit slice fold: reads the index array and, slice by slice in the L2, reads
+            # and writes the histogram once (its 64-bit reductions stay in the L2)
+            k2_bytes = 4.0 * entries + 16.0 * prob.hist_len
+            kernels["rt_bin_slices"] = {"ms": fmean, "bound": "hbm", "algorithmic_bytes": k2_bytes,
+                                        "achieved": k2_bytes / max(fmean, 1e-9) / 1e6, "peak": peak, "unit": "GB/s",
+                                        "frac": k2_bytes / max(fmean, 1e-9) / 1e6 / peak,
+                                        "l2_reductions_per_s": obs_per_step / max(fmean, 1e-9) * 1e3,
+                                        "traffic": traffic.get("rt_bin_slices")}
         dom = max(kernels, key=lambda k: kernels[k]["ms"])
         kd = kernels[dom]
         result = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -354,13 +371,16 @@ def run_our_arm(args, rank, world, dist):
                                "frac": kd["frac"], "traffic": kd["traffic"], "kernel": dom, "kernel_ms": kd["ms"],
                                "basis": "rt_events: 100 issue slots per event + 120 per particle start; rt_observe: 12 "
                                         "per (particle, instant); issue peak 4 warp instructions/clk/SM at the sampled "
-                                        "clock; rt_bin_slices: 4 B index read per (particle, instant) + the 8 B "
-                                        f"histogram read and written once; HBM peak {peak_kind}",
+                                        "clock; rt_fold_tb: the 4 B index entry of every (particle, instant) read once; "
+                                        "rt_tb_convert: 4 B of FP32 count read and the 8 B bin written per (bin, instant); "
+                                        "rt_bin_slices (slice fold): the index read + the 8 B histogram read and written "
+                                        f"once; HBM peak {peak_kind}; traffic: DRAM bytes of one full-size launch "
+                                        "(ncu, one pass)",
                                "kernels": kernels},
                   "gpu_launches": args.steps * launches_per_step, "clocks": clocks,
                   "events_per_step": events / args.steps, "observations_per_step": obs_per_step,
                   "observations_per_s": obs_per_step * args.steps / total_s,
-                  "transport_ms": kmean, "fold_ms": fmean, "sink": int(st["sink"])}
+                  "transport_ms": kmean, "fold_ms": fmean, "convert_ms": cmean, "sink": int(st["sink"])}
     # end to end through the C ABI with host buffers
     # (first, while the host holds no other histogram-sized buffer; the accuracy check below
     # reuses its pinned buffer)
@@ -657,8 +677,10 @@ def run_c5(args):
             "finite_differences_1e-3": fd, "finite_differences_1e-2": fd2,
             "rel_error_scaled_vector_1e-3": float(np.linalg.norm(g - f) / np.linalg.norm(f)),
             "rel_error_scaled_vector_1e-2": float(np.linalg.norm(g - f2) / np.linalg.norm(f2)),
+            "rel_error_per_param_1e-3": {p: abs(res["grad"][p] - fd[p]) / abs(fd[p]) for p in params},
             "rel_error_per_param_1e-2": {p: abs(res["grad"][p] - (fd2.get(p, fd[p]))) / abs(fd2.get(p, fd[p]))
-                                         for p in params}}
+                                         for p in params},
+            "weights_centred": bool(res.get("centred"))}
     return line
 
 

@@ -192,6 +192,7 @@ typedef struct {
     double h2d_bytes;
     double d2h_bytes;
     double events_ms;        /* split schedule: the event kernel's share of kernel_ms */
+    double convert_ms;       /* time-blocked fold without host copies: the conversion's share of fold_ms */
 } rtmc_stats;
 
 /* context on CUDA device `device` with its own stream */

@@ -62,7 +62,7 @@ class RtmcStats(C.Structure):
                 ("device_status", C.c_int64), ("launches", C.c_int32), ("sink", C.c_int32),
                 ("kernel_ms", C.c_double), ("fold_ms", C.c_double),
                 ("total_ms", C.c_double), ("h2d_bytes", C.c_double), ("d2h_bytes", C.c_double),
-                ("events_ms", C.c_double)]
+                ("events_ms", C.c_double), ("convert_ms", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_ if k != "reserved"}

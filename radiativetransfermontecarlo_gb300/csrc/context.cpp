@@ -46,6 +46,7 @@ struct rtmc_context {
     int max_smem_optin = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_start = nullptr, ev_k0 = nullptr, ev_k1 = nullptr, ev_k2 = nullptr, ev_end = nullptr, ev_km = nullptr;
+    cudaEvent_t ev_kc = nullptr; // before the time-blocked conversion
     std::string err;
     DevBuf hist, tabs, aux, stats, flush, trace, idx, adj, partial;
     DevBuf narrow; // uint32 copy of the histogram (rtmc_forward_u32)
@@ -667,6 +668,7 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
     const bool use_tb = sink == kSinkIndex && !n_pipe && P->n_particles < ((int64_t)1 << 24) && ctx->opt_fold != 1;
     const int ntb = (P->n_obs + 3) / 4;
     int roll = 0; // t-blocks per turn of a rolling accumulator (0: the full accumulator)
+    bool timed_convert = false; // ev_kc marks the start of the conversion
     bool narrowed = false; // the conversion also wrote the uint32 counts
     TbParams tpl{};
     int tb_grid = 1;
@@ -756,7 +758,7 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         p.obs_idx = static_cast<int32_t *>(ctx->idx.p);
         p.obs_rows = idx_rows;
     }
-    double kms = 0, fms = 0, ems = 0;
+    double kms = 0, fms = 0, ems = 0, cms = 0;
     if (n_pipe) {
         const size_t slot_elems = (size_t)idx_rows * P->n_obs;
         int32_t *idx0 = static_cast<int32_t *>(ctx->idx.p);
@@ -820,6 +822,8 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
             const bool groups = last && (host_out || host_u32) && ntb >= 2 * kCopyGroups && ensure_pipeline(ctx) == 0;
             const int ng = groups ? kCopyGroups : 1;
             const int64_t ts = P->time_stride;
+            // one fold launch and one conversion: the conversion is timed apart
+            timed_convert = last && !groups && !roll && ntb <= 65535;
             for (int g = 0; g < ng && !le; ++g) {
                 const int ga = groups ? tb_group_start(ntb, g) : 0, gb = groups ? tb_group_start(ntb, g + 1) : ntb;
                 if (gb <= ga) continue;
@@ -834,6 +838,7 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
                     le = launch_fold_tb(tp, tb_grid, ctx->stream);
                     ++launches;
                     if (!le && last) {
+                        if (timed_convert) CK(cudaEventRecord(ctx->ev_kc, ctx->stream), "event");
                         le = launch_tb_convert(tp, ts, P->mode_stride, P->hist_shift, hist, host_u32 ? narrow : nullptr,
                                                narrow_grid, ctx->stream);
                         ++launches;
@@ -927,6 +932,12 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         if (sink == kSinkIndex) {
             cudaEventElapsedTime(&b, ctx->ev_k1, ctx->ev_k2);
             fms += b;
+            if (timed_convert) {
+                float c = 0;
+                cudaEventElapsedTime(&c, ctx->ev_kc, ctx->ev_k2);
+                cms += c;
+                timed_convert = false;
+            }
         }
     }
     if (le) return cuda_fail(ctx, (cudaError_t)le, "transport launch");
@@ -978,6 +989,7 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         st->kernel_ms = kms;
         st->fold_ms = fms;
         st->events_ms = ems;
+        st->convert_ms = cms;
         st->launches = launches;
         st->sink = sink;
         st->total_ms = tms;
@@ -1430,6 +1442,7 @@ extern "C" int rtmc_create(int32_t device, rtmc_context **out)
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_k2);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_end);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_km);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_kc);
     if (e != cudaSuccess) {
         rtmc_destroy(ctx);
         return fail(nullptr, RTMC_ERR_CUDA, std::string("rtmc_create: ") + cudaGetErrorString(e));
@@ -1457,6 +1470,7 @@ extern "C" void rtmc_destroy(rtmc_context *ctx)
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
     if (ctx->ev_k0) cudaEventDestroy(ctx->ev_k0);
     if (ctx->ev_km) cudaEventDestroy(ctx->ev_km);
+    if (ctx->ev_kc) cudaEventDestroy(ctx->ev_kc);
     if (ctx->ev_k1) cudaEventDestroy(ctx->ev_k1);
     if (ctx->ev_k2) cudaEventDestroy(ctx->ev_k2);
     if (ctx->ev_end) cudaEventDestroy(ctx->ev_end);
