@@ -257,6 +257,8 @@ def run_our_arm(args, rank, world, dist):
         ctx.set_pipeline(args.chunks, args.k1_bps)
     if args.schedule >= 0:
         ctx.set_schedule(args.schedule)
+    if args.fold:
+        ctx.set_fold(args.fold)
     P32, keep32 = prob.to_ctypes()
 
     def barrier():
@@ -726,6 +728,8 @@ def main():
     ap.add_argument("--chunks", type=int, default=0, help="transport/fold pipeline chunks (0: automatic, 1: off)")
     ap.add_argument("--schedule", type=int, default=-1, help="-1 automatic, 0 lockstep warp batches, 1 particle per thread")
     ap.add_argument("--k1-bps", type=int, default=0, help="transport blocks per SM while pipelined (0: automatic)")
+    ap.add_argument("--fold", type=int, default=0,
+                    help="fold of the index path: 0 automatic, 1 64-bit slice fold, 2 time-blocked, 3 rolling")
     ap.add_argument("--ref-seconds", type=float, default=0.0,
                     help="reference arm: seconds of CPU work per step (0: about 120 s over all steps)")
     ap.add_argument("--no-fp64", action="store_true")
