@@ -50,7 +50,7 @@ struct rtmc_context {
     std::string err;
     DevBuf hist, tabs, aux, stats, flush, trace, idx, adj, partial;
     DevBuf narrow; // uint32 copy of the histogram (rtmc_forward_u32)
-    DevBuf segs, seg_head, ovf; // split schedule: trajectory segments, per-particle heads, overflow list
+    DevBuf segs, ovf; // split schedule: trajectory segment records, overflow list
     DevBuf tbacc;               // time-blocked FP32 fold accumulator
     uint64_t tabs_gen = 0;
     int tabs_prec = -1;
@@ -616,19 +616,18 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         int K = (int)std::ceil(1.0 + mean + 4.0 * std::sqrt(mean) + 4.0);
         K = std::min(64, std::max(8, (K + 3) / 4 * 4));
         if (ctx->opt_ring) K = ctx->opt_ring; // an explicit ring capacity sets the segments per particle
+        K = std::max(1, K) + 2;               // and two end records (rec_put_end)
         const size_t rec = 8 * sizeof(R);
         // particles per launch: the segments of one chunk stay within 8 GB
         constexpr int64_t kSegBudget = (int64_t)8 << 30;
         const int64_t seg_rows = std::max<int64_t>(32, kSegBudget / ((int64_t)K * (int64_t)rec) / 32 * 32);
         chunk = std::min(chunk, seg_rows);
         const int64_t rows_max = std::max<int64_t>(chunk, 1);
-        if (ctx->segs.grow((size_t)rows_max * K * rec) || ctx->seg_head.grow((size_t)rows_max * 8) ||
-            ctx->ovf.grow((size_t)rows_max * 4))
+        if (ctx->segs.grow((size_t)rows_max * K * rec) || ctx->ovf.grow((size_t)rows_max * 4))
             return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for trajectory segments failed");
         p.split = 1;
         p.seg_cap = K;
         p.segs = ctx->segs.p;
-        p.seg_head = static_cast<int32_t *>(ctx->seg_head.p);
         p.ovf_list = static_cast<int32_t *>(ctx->ovf.p);
         p.ovf_count = reinterpret_cast<uint32_t *>(static_cast<unsigned char *>(ctx->stats.p) + 192);
         sl.smem_events = edge_smem;
@@ -1467,6 +1466,9 @@ extern "C" void rtmc_destroy(rtmc_context *ctx)
     ctx->idx.release();
     ctx->adj.release();
     ctx->partial.release();
+    ctx->segs.release();
+    ctx->ovf.release();
+    ctx->tbacc.release();
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
     if (ctx->ev_k0) cudaEventDestroy(ctx->ev_k0);
     if (ctx->ev_km) cudaEventDestroy(ctx->ev_km);

@@ -117,12 +117,10 @@ template <typename R> struct DevParams {
     double *trace;  // optional [n_particles][16] final particle states
     int32_t *obs_idx;  // index sink: [n_obs][obs_rows] in-slice bin | mode << 30, or -1
     int64_t obs_rows;
-    // split schedule (rt_events, then rt_observe): seg_cap trajectory segments per particle
-    // in segs, the segment count and death sub-step of each particle in seg_head (count -1:
-    // more segments than seg_cap; such particles are listed in ovf_list and rerun by
-    // rt_transport_list)
+    // split schedule (rt_events, then rt_observe): seg_cap records per particle in segs, its
+    // trajectory segments followed by end records (a particle with more than seg_cap - 2
+    // segments gets end records only, is listed in ovf_list and rerun by rt_transport_list)
     void *segs;
-    int32_t *seg_head;  // [n_particles][2]
     int32_t *ovf_list;
     uint32_t *ovf_count;
     int32_t seg_cap, split;

@@ -1361,6 +1361,33 @@ template <typename R, int OBS> __device__ __forceinline__ void rec_get(const R *
     g.mode = sm >> 30;
 }
 
+// A segment as rt_observe wants it: on the index path the mode sits in bit 30 of the
+// direction offset; on the FP32 cartesian path the offsets lose a negative zero, a
+// direction outside the grid becomes an infinite first offset, and the direction offset
+// carries the 2^23 bias of the three bin patterns (see obs_offset_cart32).
+template <typename R, int OBS> __device__ __forceinline__ void rec_put_seg(const DevParams<R> &p, R *r, Seg<R> g)
+{
+    if (p.sink == SINK_INDEX && g.doff >= 0) g.doff |= g.mode << 30;
+    if (sizeof(R) == 4 && OBS == OBS_CART) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) g.A[a] = m_add(g.A[a], (R)0);
+        if (g.doff < 0) g.A[0] = (R)INFINITY;
+        g.doff = (int)((unsigned)g.doff - (unsigned)p.cart_bias);
+    }
+    rec_put<R, OBS>(r, g);
+}
+
+// The records after a particle's last segment: an end record at its death sub-step (it
+// bins nothing: direction offset -1, infinite first offset), then a record that never
+// comes into force (start 2^30 - 1, beyond every observation sub-step).  A particle that
+// lives to the end gets the second only.
+constexpr int kNeverStart = 0x3fffffff;
+template <typename R> __device__ __forceinline__ void rec_put_end(R *r, int s0)
+{
+    const R u[3] = {(R)INFINITY, (R)0, (R)0}, v[3] = {(R)0, (R)0, (R)0};
+    rec_store(r, u, v, s0, -1);
+}
+
 // lanes of a warp that start new particles together in rt_events
 constexpr int kEventStartLanes = 8;
 
@@ -1402,12 +1429,12 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) rt_events(const D
             c0 = cnt;
             seg_from(s, g);
             seg_prepare<R, OBS>(p, sedges, g);
-            rec_put<R, OBS>(segs + (size_t)i * K * kRecWords, g);
+            rec_put_seg<R, OBS>(p, segs + (size_t)i * K * kRecWords, g);
             nseg = 1;
             have = true;
         }
         if (!have) continue;
-        int done = 0; // 1: the particle's run is over, 2: its segments overflow seg_cap
+        int done = 0; // 1: the particle's run is over, 2: its segments overflow seg_cap - 2
         if (next_event(s) > p.s_end) {
             done = 1;
         } else {
@@ -1415,20 +1442,20 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) rt_events(const D
             if ((int)s.k > p.max_events) { s.alive = 0; s.s_death = s.s0; bad = true; }
             if (!s.alive) {
                 done = 1;
-            } else if (nseg < K) {
+            } else if (nseg < K - 2) { // two records stay free for the end records
                 seg_from(s, g);
                 seg_prepare<R, OBS>(p, sedges, g);
-                rec_put<R, OBS>(segs + ((size_t)i * K + nseg) * kRecWords, g);
+                rec_put_seg<R, OBS>(p, segs + ((size_t)i * K + nseg) * kRecWords, g);
                 ++nseg;
             } else {
                 done = 2;
             }
         }
         if (done) {
-            int32_t *h = p.seg_head + 2 * i;
+            R *r = segs + (size_t)i * K * kRecWords;
             if (done == 1) {
-                h[0] = nseg;
-                h[1] = s.alive ? 0x7fffffff : s.s_death;
+                if (!s.alive) rec_put_end(r + (size_t)nseg++ * kRecWords, s.s_death);
+                rec_put_end(r + (size_t)nseg * kRecWords, kNeverStart);
                 if (p.trace) { // final state of the particle, the oracle's layout
                     double *f = p.trace + 16 * i;
 #pragma unroll
@@ -1437,8 +1464,8 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) rt_events(const D
                     f[13] = s.s0; f[14] = s.s_death; f[15] = s.k;
                 }
             } else { // rerun whole by rt_transport_list: its events are not counted here
-                h[0] = -1;
-                h[1] = 0;
+                rec_put_end(r, 0); // nothing binned from sub-step 0
+                rec_put_end(r + kRecWords, kNeverStart);
                 cnt = c0;
                 p.ovf_list[atomicAdd(p.ovf_count, 1u)] = (int32_t)i;
             }
@@ -1472,73 +1499,43 @@ __device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *se
     constexpr bool INDEX = SINK == SINK_INDEX;
     const int lane = threadIdx.x & 31;
     const unsigned long long inc = 1ull << p.hist_shift;
-    const int K = p.seg_cap;
     const int64_t i = base + lane;
     const bool have = i < p.n_particles;
-    int nseg = 0, limit = 0; // observations at sub-steps below `limit` are binned
-    if (have) {
-        const int2 h = __ldg(reinterpret_cast<const int2 *>(p.seg_head) + i);
-        nseg = h.x;
-        limit = nseg > 0 ? h.y : 0; // an overflowing particle is binned by rt_transport_list
-    }
-    const R *rec = static_cast<const R *>(p.segs) + (size_t)(have ? i : 0) * K * kRecWords;
-    Seg<R> cur, nxt;
-    cur.s0 = 0; cur.mode = 0; cur.doff = -1;
-    cur.A[0] = cur.A[1] = cur.A[2] = cur.B[0] = cur.B[1] = cur.B[2] = (R)0;
-    int k = 0, next_start = 0x7fffffff;
-    if (nseg > 0) rec_get<R, OBS>(rec, cur);
-    if (nseg > 1) { rec_get<R, OBS>(rec + kRecWords, nxt); next_start = nxt.s0; }
-    // index entries carry the mode in bit 30: fold it into the direction offset once per
-    // segment (the index path keeps a time slice below 2^30 bins)
-    // FP32 cartesian: per segment, a direction outside the grid becomes an infinite first
-    // coordinate (every observation of the segment then fails the range test), the
-    // coordinates' offsets lose a negative zero, and the 2^23 bias of the three bin
-    // patterns comes off the direction offset (see obs_offset_cart32)
+    // record k (in cur) is in force and record k + 1 waits in nxt; every particle's list
+    // ends in records that bin nothing and never end (rec_put_end), so a change of segment
+    // needs no count or limit checks
+    const R *rec = static_cast<const R *>(p.segs) + (size_t)(have ? i : 0) * p.seg_cap * kRecWords;
     constexpr bool C32 = sizeof(R) == 4 && OBS == OBS_CART;
-    int cbase = 0;
-    auto fold_mode = [&]() {
-        if (INDEX && cur.doff >= 0) cur.doff |= cur.mode << 30;
-        if (C32) {
-#pragma unroll
-            for (int a = 0; a < 3; ++a) cur.A[a] = m_add(cur.A[a], (R)0);
-            if (cur.doff < 0) cur.A[0] = (R)INFINITY;
-            cbase = (int)((unsigned)cur.doff - (unsigned)p.cart_bias);
-        }
-    };
-    fold_mode();
+    Seg<R> cur, nxt;
+    int k = 1, next_start = kNeverStart;
+    if (have) {
+        rec_get<R, OBS>(rec, cur);
+        rec_get<R, OBS>(rec + kRecWords, nxt);
+        next_start = nxt.s0;
+    } else {
+        cur.s0 = 0; cur.mode = 0; cur.doff = -1;
+        cur.A[0] = (R)INFINITY; cur.A[1] = cur.A[2] = cur.B[0] = cur.B[1] = cur.B[2] = (R)0;
+    }
     const bool count_dl = sizeof(R) == 8 || p.s_end < (1 << 24);
     int so = p.n_sub;
-    int bound = min(next_start, limit); // the next sub-step at which the lane's state changes
     R dl = (R)(so - cur.s0);
     const R dstep = (R)p.n_sub;
     int32_t *optr = (INDEX && have) ? p.obs_idx + i : nullptr;
 #pragma unroll 2
     for (int j = 1; j <= p.n_obs; ++j, so += p.n_sub) {
-        if (so >= bound) {
-            if (so >= limit) { // the particle's end: nothing more is binned
-                cur.doff = -1;
-                if (C32) cur.A[0] = (R)INFINITY;
-                bound = 0x7fffffff;
-            } else { // the next segment comes into force; load the one after it
-                do {
-                    cur = nxt;
-                    ++k;
-                    if (k + 1 < nseg) {
-                        rec_get<R, OBS>(rec + (size_t)(k + 1) * kRecWords, nxt);
-                        next_start = nxt.s0;
-                    } else {
-                        next_start = 0x7fffffff;
-                    }
-                } while (so >= next_start);
-                fold_mode();
-                bound = min(next_start, limit);
-            }
+        if (so >= next_start) { // the next segment comes into force; load the one after it
+            do {
+                cur = nxt;
+                ++k;
+                rec_get<R, OBS>(rec + (size_t)k * kRecWords, nxt);
+                next_start = nxt.s0;
+            } while (so >= next_start);
             dl = (R)(so - cur.s0);
         } else if (!count_dl) {
             dl = (R)(so - cur.s0);
         }
         int v;
-        if constexpr (C32) v = obs_offset_cart32(p, cur, dl, cbase);
+        if constexpr (C32) v = obs_offset_cart32(p, cur, dl, cur.doff);
         else v = obs_offset_dl<R, OBS>(p, sedges, cur, dl);
         dl += dstep;
         if (INDEX) {
