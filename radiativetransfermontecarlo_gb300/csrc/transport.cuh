@@ -30,6 +30,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 namespace rtmc {
 namespace {
 
@@ -1516,45 +1518,57 @@ __device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *se
         cur.s0 = 0; cur.mode = 0; cur.doff = -1;
         cur.A[0] = (R)INFINITY; cur.A[1] = cur.A[2] = cur.B[0] = cur.B[1] = cur.B[2] = (R)0;
     }
+    // the offset from the segment start is carried as a float counter while it stays an
+    // exact integer (below 2^24), else converted afresh each instant
     const bool count_dl = sizeof(R) == 8 || p.s_end < (1 << 24);
-    int so = p.n_sub;
-    R dl = (R)(so - cur.s0);
-    const R dstep = (R)p.n_sub;
-    int32_t *optr = (INDEX && have) ? p.obs_idx + i : nullptr;
-#pragma unroll 2
-    for (int j = 1; j <= p.n_obs; ++j, so += p.n_sub) {
-        if (so >= next_start) { // the next segment comes into force; load the one after it
-            do {
-                cur = nxt;
-                ++k;
-                rec_get<R, OBS>(rec + (size_t)k * kRecWords, nxt);
-                next_start = nxt.s0;
-            } while (so >= next_start);
-            dl = (R)(so - cur.s0);
-        } else if (!count_dl) {
-            dl = (R)(so - cur.s0);
-        }
-        int v;
-        if constexpr (C32) v = obs_offset_cart32(p, cur, dl, cur.doff);
-        else v = obs_offset_dl<R, OBS>(p, sedges, cur, dl);
-        dl += dstep;
-        if (INDEX) {
-            if (have) {
+    auto walk = [&](auto count_tag) {
+        constexpr bool CDL = decltype(count_tag)::value;
+        const int s_last = p.n_obs * p.n_sub;
+        const R dstep = (R)p.n_sub;
+        int so = p.n_sub;
+        R dl = (R)(so - cur.s0);
+        // every lane of a warp owns a column of the index array (rows are padded to 32
+        // particles), so lanes past the last particle store their -1 there unconditionally
+        int32_t *optr = INDEX ? p.obs_idx + i : nullptr;
+        int64_t toff = p.time_stride; // slice offset of instant j (shared and global sinks)
+#pragma unroll 1
+        for (; so <= s_last; so += p.n_sub) {
+            if (so >= next_start) { // the next segment comes into force; load the one after it
+                do {
+                    cur = nxt;
+                    ++k;
+                    rec_get<R, OBS>(rec + (size_t)k * kRecWords, nxt);
+                    next_start = nxt.s0;
+                } while (so >= next_start);
+                dl = (R)(so - cur.s0);
+            } else if (!CDL) {
+                dl = (R)(so - cur.s0);
+            }
+            int v;
+            if constexpr (C32) v = obs_offset_cart32(p, cur, dl, cur.doff);
+            else v = obs_offset_dl<R, OBS>(p, sedges, cur, dl);
+            if (CDL) dl += dstep;
+            if (INDEX) {
                 *optr = v;
                 optr += p.obs_rows;
-            }
-            cnt.obs += v >= 0 ? 1u : 0u;
-        } else if (v >= 0) {
-            const int64_t idx = (int64_t)j * p.time_stride + (cur.mode ? p.mode_stride : 0) + v;
-            if (idx < p.hist_len) {
-                cnt.obs++;
-                if (SMEM) atomicAdd(shist + idx, 1u);
-                else atomicAdd(p.hist + idx, inc);
+                cnt.obs += v >= 0 ? 1u : 0u;
             } else {
-                bad = true;
+                if (v >= 0) {
+                    const int64_t idx = toff + (cur.mode ? p.mode_stride : 0) + v;
+                    if (idx < p.hist_len) {
+                        cnt.obs++;
+                        if (SMEM) atomicAdd(shist + idx, 1u);
+                        else atomicAdd(p.hist + idx, inc);
+                    } else {
+                        bad = true;
+                    }
+                }
+                toff += p.time_stride;
             }
         }
-    }
+    };
+    if (count_dl) walk(std::true_type{});
+    else walk(std::false_type{});
 }
 
 // the shared-memory sink holds one block per SM (the histogram fills the shared memory):
