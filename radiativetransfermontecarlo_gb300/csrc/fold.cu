@@ -268,31 +268,36 @@ __global__ void __launch_bounds__(kTbThreads) rt_fold_tb(const TbParams t)
 #pragma unroll
         for (int r = 0; r < 4; ++r) x[r] = r < nr && q < q1 ? __ldcs(row[r] + q) : make_int4(-1, -1, -1, -1);
     };
-    auto vector = [&](const int4 (&x)[4], int64_t q, bool use_hash, int *nvalid) {
+    // masks are kept as floats (compare-selects and products, no int-to-float conversions);
+    // the mode bit of an entry becomes the second half of the slice: v + (v >> 30) *
+    // (slice_bins - 2^30)
+    const int mode_shift = t.slice_bins - (1 << 30);
+    auto vector = [&](const int4 (&x)[4], int64_t q, bool use_hash, bool count, int *nvalid) {
         int e[4][4]; // [instant][particle]
 #pragma unroll
         for (int r = 0; r < 4; ++r) {
             e[r][0] = x[r].x; e[r][1] = x[r].y; e[r][2] = x[r].z; e[r][3] = x[r].w;
         }
-        auto emit = [&](int v, int m0, int m1, int m2, int m3) {
-            const int key = (v & 0x3fffffff) + ((v >> 30) ? t.slice_bins : 0);
-            ++*nvalid;
-            const int m[4] = {m0, m1, m2, m3};
-            if (use_hash && *((volatile int *)&used) < 3 * kTbSlots / 4 && tb_hash_insert(keys, cnt, &used, key, m))
-                return;
-            red_v4(acc + (size_t)key * 4, (float)m0, (float)m1, (float)m2, (float)m3);
+        auto emit = [&](int v, float f0, float f1, float f2, float f3) {
+            const int key = v + (v >> 30) * mode_shift;
+            if (count) ++*nvalid;
+            if (use_hash && *((volatile int *)&used) < 3 * kTbSlots / 4) {
+                const int m[4] = {f0 != 0.f, f1 != 0.f, f2 != 0.f, f3 != 0.f};
+                if (tb_hash_insert(keys, cnt, &used, key, m)) return;
+            }
+            red_v4(acc + (size_t)key * 4, f0, f1, f2, f3);
         };
 #pragma unroll
         for (int u = 0; u < 4; ++u) {
             if (q * 4 + u >= p1) continue;
             const int a = e[0][u], b = e[1][u], c = e[2][u], d = e[3][u];
-            const int e01 = a == b, e12 = b == c, e23 = c == d;
+            const float f01 = a == b ? 1.f : 0.f, f12 = b == c ? 1.f : 0.f, f23 = c == d ? 1.f : 0.f;
             // a run starts at every instant whose bin differs from the one before; -1
             // (not observed) is never emitted
-            if (a >= 0) emit(a, 1, e01, e01 & e12, e01 & e12 & e23);
-            if (b >= 0 && !e01) emit(b, 0, 1, e12, e12 & e23);
-            if (c >= 0 && !e12) emit(c, 0, 0, 1, e23);
-            if (d >= 0 && !e23) emit(d, 0, 0, 0, 1);
+            if (a >= 0) emit(a, 1.f, f01, f01 * f12, f01 * f12 * f23);
+            if (b >= 0 && a != b) emit(b, 0.f, 1.f, f12, f12 * f23);
+            if (c >= 0 && b != c) emit(c, 0.f, 0.f, 1.f, f23);
+            if (d >= 0 && c != d) emit(d, 0.f, 0.f, 0.f, 1.f);
         }
     };
     // probe window: one vector per thread through the hash
@@ -301,7 +306,7 @@ __global__ void __launch_bounds__(kTbThreads) rt_fold_tb(const TbParams t)
     int4 x[kTbAhead][4];
     if (q < q1) {
         load(q, x[0]);
-        vector(x[0], q, true, &nv);
+        vector(x[0], q, true, true, &nv);
     }
     if (nv) atomicAdd(&valid, nv);
     __syncthreads();
@@ -316,7 +321,7 @@ __global__ void __launch_bounds__(kTbThreads) rt_fold_tb(const TbParams t)
         for (int w = 0; w < kTbAhead; ++w) load(q + w * T, x[w]);
 #pragma unroll
         for (int w = 0; w < kTbAhead; ++w)
-            if (q + w * T < q1) vector(x[w], q + w * T, h, &nv);
+            if (q + w * T < q1) vector(x[w], q + w * T, h, false, &nv);
     }
     __syncthreads();
     for (int k = threadIdx.x; k < kTbSlots; k += blockDim.x) {
