@@ -47,7 +47,6 @@ struct rtmc_context {
     cudaStream_t stream = nullptr;
     cudaEvent_t ev_start = nullptr, ev_k0 = nullptr, ev_k1 = nullptr, ev_k2 = nullptr, ev_end = nullptr, ev_km = nullptr;
     cudaEvent_t ev_kc = nullptr; // before the time-blocked conversion
-    cudaEvent_t ev_clr = nullptr; // the accumulator clear on the second stream is done
     std::string err;
     DevBuf hist, tabs, aux, stats, flush, trace, idx, adj, partial;
     DevBuf narrow; // uint32 copy of the histogram (rtmc_forward_u32)
@@ -694,22 +693,15 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         tpl.slice_bins = (int32_t)P->time_stride;
         tb_grid = (int)std::max<int64_t>(1, std::min<int64_t>((chunk + 8191) / 8192, 2 * ctx->num_sms));
     }
-    // the clear: the FP32 accumulator of a split run is zeroed on the second stream while the
-    // transport runs (the fold waits for it; rt_events is bound by issue, the memset by
-    // DRAM, so they overlap; zeroing it inside rt_events cost 0.28 of its 2.36 ms on the 3D
-    // elastic workload); the histogram of the other sinks in the first rt_events launch;
-    // else one memset ahead of the transport
+    // the clear: fused into the first rt_events launch of a split run (the FP32 accumulator
+    // of the time-blocked fold, else the histogram), else one memset ahead of the transport.
+    // Measured on the 3D elastic workload: the fused clear of the 3.47 GB accumulator costs
+    // rt_events 0.28 of 2.36 ms; a memset on the second stream during the transport cost it
+    // 0.22 ms and the fold 0.4 ms (its blocks take SM slots from both kernels).
     unsigned long long *to_clear = use_tb ? static_cast<unsigned long long *>(ctx->tbacc.p)
                                           : static_cast<unsigned long long *>(ctx->hist.p);
     const int64_t clear_words = use_tb ? (int64_t)(roll ? roll : ntb) * tpl.S * 2 : P->hist_len;
-    bool side_clear = false; // the fold must wait for ev_clr
-    if (split && use_tb && ensure_pipeline(ctx) == 0) {
-        CK(cudaEventRecord(ctx->ev_a0[0], ctx->stream), "event");
-        CK(cudaStreamWaitEvent(ctx->fold_stream, ctx->ev_a0[0], 0), "clear wait");
-        CK(cudaMemsetAsync(to_clear, 0, (size_t)clear_words * 8, ctx->fold_stream), "accumulator clear");
-        CK(cudaEventRecord(ctx->ev_clr, ctx->fold_stream), "event");
-        side_clear = true;
-    } else if (split) {
+    if (split) {
         p.clear = to_clear;
         p.clear_words = clear_words;
     } else {
@@ -822,10 +814,6 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         CK(cudaEventRecord(ctx->ev_k1, ctx->stream), "event");
         const bool last = base + chunk >= P->n_particles;
         if (!le && use_tb) {
-            if (side_clear) {
-                CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_clr, 0), "clear join");
-                side_clear = false;
-            }
             TbParams tp = tpl;
             tp.n = q.n_particles;
             tp.part_per_block = ((tp.n + tb_grid - 1) / tb_grid + 3) / 4 * 4;
@@ -955,9 +943,7 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         }
     }
     if (le) return cuda_fail(ctx, (cudaError_t)le, "transport launch");
-    if (side_clear) CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_clr, 0), "clear join"); // no fold ran
-    if (p.clear || side_clear) // no launch ran
-        CK(cudaMemsetAsync(ctx->hist.p, 0, hist_bytes, ctx->stream), "histogram clear");
+    if (p.clear) CK(cudaMemsetAsync(ctx->hist.p, 0, hist_bytes, ctx->stream), "histogram clear"); // no launch ran
     ctx->hist_may_exceed_int64 = may_exceed_int64(P);
     if (host_out && ctx->hist_may_exceed_int64) {
         le = launch_check_int64(p.hist, P->hist_len, p.status, narrow_grid, ctx->stream);
@@ -1459,7 +1445,6 @@ extern "C" int rtmc_create(int32_t device, rtmc_context **out)
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_end);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_km);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_kc);
-    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_clr, cudaEventDisableTiming);
     if (e != cudaSuccess) {
         rtmc_destroy(ctx);
         return fail(nullptr, RTMC_ERR_CUDA, std::string("rtmc_create: ") + cudaGetErrorString(e));
@@ -1491,7 +1476,6 @@ extern "C" void rtmc_destroy(rtmc_context *ctx)
     if (ctx->ev_k0) cudaEventDestroy(ctx->ev_k0);
     if (ctx->ev_km) cudaEventDestroy(ctx->ev_km);
     if (ctx->ev_kc) cudaEventDestroy(ctx->ev_kc);
-    if (ctx->ev_clr) cudaEventDestroy(ctx->ev_clr);
     if (ctx->ev_k1) cudaEventDestroy(ctx->ev_k1);
     if (ctx->ev_k2) cudaEventDestroy(ctx->ev_k2);
     if (ctx->ev_end) cudaEventDestroy(ctx->ev_end);

@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(kCheckThreads) rt_check_int64(const unsigned l
 // instant; the fold's cost is the L2's reduction rate, so fewer reductions is faster.
 // Counts are exact in FP32 below 2^24 per bin and instant.  Crowded chunks (early
 // instants) aggregate in a shared-memory hash first, as rt_bin_slices does.
-constexpr int kTbThreads = 512;
+constexpr int kTbThreads = 384;
 constexpr int kTbAhead = 1; // index vectors a thread loads before folding them
 constexpr int kTbSlots = 2048;
 
