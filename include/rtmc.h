@@ -386,6 +386,12 @@ int rtmc_set_fold(rtmc_context *ctx, int32_t mode);
  * calls; with 0 every call uploads its tables again (end-to-end timing) */
 int rtmc_set_table_cache(rtmc_context *ctx, int32_t enable);
 
+/* FP64 problems on the radius-only observation path bin each observation through an FP32
+ * estimate with a proven error bound, and in FP64 only when the estimate lies within that
+ * bound of a bin edge: the same bins as the FP64 formula, at FP32 cost.  0 turns the
+ * estimate off (every observation in FP64); 1, the default, turns it on. */
+int rtmc_set_fp64_estimate(rtmc_context *ctx, int32_t enable);
+
 /* writes a device buffer larger than L2 (timing hygiene between measured runs) */
 int rtmc_flush_l2(rtmc_context *ctx);
 

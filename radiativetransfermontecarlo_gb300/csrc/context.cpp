@@ -67,6 +67,7 @@ struct rtmc_context {
     int opt_chunks = 0, opt_k1_bps = 0;
     int opt_event_major = -1; // -1 automatic, 0 two-cursor batches, 1 one particle per thread, 2 split
     int opt_fold = 0;         // 0 automatic, 1 64-bit slice fold, 2 time-blocked FP32 fold, 3 the same, rolling
+    int opt_bin32 = 1;        // FP64 radius-only observations through an exact FP32 estimate
     static constexpr int kPipe = 32;
     cudaStream_t fold_stream = nullptr;
     cudaEvent_t ev_a0[kPipe] = {}, ev_a1[kPipe] = {}, ev_b0[kPipe] = {}, ev_b1[kPipe] = {};
@@ -377,6 +378,8 @@ void fill_params(rtmc_context *ctx, const rtmc_problem *P, const DevTables<R> &t
         }
         std::memcpy(&p->cart_bias, &bias, sizeof(bias));
     }
+    p->r32_iw = (float)p->ax_inv_w[0];
+    p->r32_a0 = 0.f;
     // observation path (see obs_offset in transport.cuh)
     p->obs_kind = 0;
     if (P->frame == RTMC_FRAME_CARTESIAN) {
@@ -389,6 +392,10 @@ void fill_params(rtmc_context *ctx, const rtmc_problem *P, const DevTables<R> &t
         p->radial_3d = (P->frame == RTMC_FRAME_SPHERICAL && P->d == 3) ? 1 : 0;
         p->ax_a0 = (R)(-P->axis_edges[0][0] * (double)(P->axis_nedges[0] - 1) /
                        (P->axis_edges[0][P->axis_nedges[0] - 1] - P->axis_edges[0][0]));
+        p->r32_a0 = (float)p->ax_a0;
+        // FP64: the observation kernel bins through an FP32 estimate (exact, see
+        // obs_offset_radial64) while sub-step offsets stay exact in FP32
+        p->bin32 = sizeof(R) == 8 && p->s_end < (1 << 24) && (!ctx || ctx->opt_bin32) ? 1 : 0;
     }
     p->time_stride = P->time_stride; p->mode_stride = P->mode_stride; p->hist_len = P->hist_len;
     // schedule: events per particle against observations (event-heavy problems run one
@@ -1623,6 +1630,13 @@ extern "C" int rtmc_set_fold(rtmc_context *ctx, int32_t mode)
     if (!ctx) return fail(nullptr, RTMC_ERR_ARG, "rtmc_set_fold: NULL context");
     if (mode < 0 || mode > 3) return fail(&ctx->err, RTMC_ERR_ARG, "fold mode must be 0, 1, 2 or 3");
     ctx->opt_fold = mode;
+    return RTMC_OK;
+}
+
+extern "C" int rtmc_set_fp64_estimate(rtmc_context *ctx, int32_t enable)
+{
+    if (!ctx) return fail(nullptr, RTMC_ERR_ARG, "rtmc_set_fp64_estimate: NULL context");
+    ctx->opt_bin32 = enable ? 1 : 0;
     return RTMC_OK;
 }
 

@@ -75,6 +75,8 @@ template <typename R> struct DevParams {
     int32_t ring_cap;  // trajectory segments per lane in the shared-memory ring
     int32_t event_major; // 1: one particle per thread, events and their observations in turn
     int32_t obs_kind;  // 0 general, 1 cartesian linear, 2 radius only
+    int32_t bin32;     // FP64 radius-only observation kernel: FP32 estimate first, FP64 near an edge
+    float r32_iw, r32_a0; // 1 / width and -lo / width of axis 0 in FP32 (the estimate)
     int32_t radial_3d; // radius-only path: 1 = |x|, 0 = |(x, y)|
     int32_t ax_nbe[4]; // bins of a binned axis, 1 for a range-checked or ignored axis
     R ax_a0;           // -lo / width of axis 0 (radius-only path)

@@ -865,6 +865,49 @@ __device__ __forceinline__ int obs_offset_cart32(const DevParams<float> &p, cons
 }
 __device__ __forceinline__ int obs_offset_cart32(const DevParams<double> &, const Seg<double> &, double, int) { return -1; }
 
+// FP64 radius-only binning through an FP32 estimate.  Per segment: the start position and
+// the step in FP32 (xf, Bf) and the sums of their magnitudes (sx, sb).  The FP32 bin
+// coordinate t' = |xf + Bf dl| / w - lo / w differs from the FP64 one by at most
+//   2^-23 (sb dl + sx) / w        (the positions: two roundings to FP32, one multiply-add)
+// + 2^-21 r' / w                  (|x|^2 in FP32 and x * rsqrt(x) for the root)
+// + 2^-24 (r' / w + |lo / w| + |t'|)   (the rounded 1/w and -lo/w, the final multiply-add)
+// + the FP64 roundings (far below 2^-30 for coordinates below 2^23); M = 2^-19 (...)
+// bounds all of it.  When t' - M and t' + M floor to the same integer, so does the FP64
+// coordinate, and that is the bin; otherwise (an observation within M of a bin edge) the
+// FP64 formula decides.  The bins are those of the FP64 path exactly.
+struct SegF {
+    float xf[3], Bf[3], sx, sb;
+};
+__device__ __forceinline__ void segf_from(const Seg<double> &g, SegF &f)
+{
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { f.xf[a] = (float)g.x[a]; f.Bf[a] = (float)g.B[a]; }
+    f.sx = fabsf(f.xf[0]) + fabsf(f.xf[1]) + fabsf(f.xf[2]);
+    f.sb = fabsf(f.Bf[0]) + fabsf(f.Bf[1]) + fabsf(f.Bf[2]);
+}
+__device__ __forceinline__ void segf_from(const Seg<float> &, SegF &) {}
+
+template <typename R>
+__device__ __forceinline__ int obs_offset_radial64(const DevParams<R> &p, const R *sedges, const Seg<R> &g, const SegF &f,
+                                                   R dl)
+{
+    if (g.doff < 0) return -1;
+    const float d = (float)dl; // exact: the estimate runs only while sub-steps stay below 2^24
+    const float x0 = fmaf(f.Bf[0], d, f.xf[0]), x1 = fmaf(f.Bf[1], d, f.xf[1]);
+    float r2 = fmaf(x1, x1, x0 * x0);
+    if (p.radial_3d) {
+        const float x2 = fmaf(f.Bf[2], d, f.xf[2]);
+        r2 = fmaf(x2, x2, r2);
+    }
+    const float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
+    const float t = fmaf(r, p.r32_iw, p.r32_a0);
+    const float m = 0x1p-19f * (fmaf(fmaf(f.sb, d, f.sx) + r, p.r32_iw, fabsf(p.r32_a0) + fabsf(t)) + 1.f);
+    const int bl = bin_floor(__fsub_rd(t, m)), bh = bin_floor(__fadd_ru(t, m));
+    if (bl != bh) return obs_offset_dl<R, OBS_RADIAL>(p, sedges, g, dl); // near an edge: FP64 decides
+    return (unsigned)bl < (unsigned)p.ax_nbe[0] ? g.doff + bl * p.ax_stride32[0] : -1;
+}
+
+
 // the same at sub-step so
 template <typename R, int OBS>
 __device__ __forceinline__ int obs_offset(const DevParams<R> &p, const R *sedges, const Seg<R> &g, int so)
@@ -1508,7 +1551,9 @@ __device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *se
     // needs no count or limit checks
     const R *rec = static_cast<const R *>(p.segs) + (size_t)(have ? i : 0) * p.seg_cap * kRecWords;
     constexpr bool C32 = sizeof(R) == 4 && OBS == OBS_CART;
+    constexpr bool R64 = sizeof(R) == 8 && OBS == OBS_RADIAL; // FP64 radius-only: FP32 estimate
     Seg<R> cur, nxt;
+    SegF cf; // the segment in force in FP32 (R64)
     int k = 1, next_start = kNeverStart;
     if (have) {
         rec_get<R, OBS>(rec, cur);
@@ -1521,8 +1566,10 @@ __device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *se
     // the offset from the segment start is carried as a float counter while it stays an
     // exact integer (below 2^24), else converted afresh each instant
     const bool count_dl = sizeof(R) == 8 || p.s_end < (1 << 24);
-    auto walk = [&](auto count_tag) {
+    auto walk = [&](auto count_tag, auto est_tag) {
         constexpr bool CDL = decltype(count_tag)::value;
+        constexpr bool EST = R64 && decltype(est_tag)::value;
+        if (EST) segf_from(cur, cf);
         const int s_last = p.n_obs * p.n_sub;
         const R dstep = (R)p.n_sub;
         int so = p.n_sub;
@@ -1540,12 +1587,14 @@ __device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *se
                     rec_get<R, OBS>(rec + (size_t)k * kRecWords, nxt);
                     next_start = nxt.s0;
                 } while (so >= next_start);
+                if (EST) segf_from(cur, cf);
                 dl = (R)(so - cur.s0);
             } else if (!CDL) {
                 dl = (R)(so - cur.s0);
             }
             int v;
             if constexpr (C32) v = obs_offset_cart32(p, cur, dl, cur.doff);
+            else if constexpr (EST) v = obs_offset_radial64(p, sedges, cur, cf, dl);
             else v = obs_offset_dl<R, OBS>(p, sedges, cur, dl);
             if (CDL) dl += dstep;
             if (INDEX) {
@@ -1567,8 +1616,9 @@ __device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *se
             }
         }
     };
-    if (count_dl) walk(std::true_type{});
-    else walk(std::false_type{});
+    if (R64 && p.bin32) walk(std::true_type{}, std::true_type{}); // FP64 counts dl exactly
+    else if (count_dl) walk(std::true_type{}, std::false_type{});
+    else walk(std::false_type{}, std::false_type{});
 }
 
 // the shared-memory sink holds one block per SM (the histogram fills the shared memory):

@@ -704,3 +704,33 @@ def test_time_blocked_fold_equals_slice_fold(index_mb, width):
     assert np.array_equal(h1, h2) and np.array_equal(u1, u2) and np.array_equal(d1, d2) and np.array_equal(h1, d1)
     assert np.array_equal(h1, h3) and np.array_equal(u1, u3) and np.array_equal(d1, d3)
     assert s1["observations"] == s2["observations"] == s3["observations"] == int(h1.sum() >> prob.hist_shift)
+
+
+@pytest.mark.parametrize("frame", ["spherical", "cylindrical2d"])
+def test_fp64_radial_estimate_gives_fp64_bins(frame):
+    """FP64 radius-only observations binned through the FP32 estimate (default) and wholly in
+    FP64 (rtmc_set_fp64_estimate(ctx, 0)) give the same histogram bit for bit: the estimate
+    decides only observations farther than its error bound from a bin edge.  Fine radial
+    bins (0.01 wide) put many observations near edges."""
+    if frame == "spherical":
+        geo, src, mat, obs, opts = W.c1_acoustic3d(n=200_000, precision="fp64")
+        obs = dict(obs, x=colon(0, 0.01, 6))
+    else:
+        geo = {"dimension": 2, "frame": "cylindrical"}
+        mat = MaterialClass(geo, 10, True, 1, [0.05, 0.05], 0, "exp", 0.1)
+        src = {"numberParticles": 200_000, "lambda": 0.05}
+        obs = {"x": colon(0, 0.01, 6), "time": colon(0, 0.02, 5)}
+        opts = {"precision": "fp64", "seed": 3}
+    prob, grid, N = build_problem(geo, src, mat, obs, dict(opts, exact_count=True))
+    assert prob.n_particles == 200_000
+    P, keep = prob.to_ctypes()
+    ctx = get_context(0)
+    try:
+        h1, s1 = ctx.forward(P, prob.tables)
+        ctx.set_fp64_estimate(False)
+        h0, s0 = ctx.forward(P, prob.tables)
+    finally:
+        ctx.set_fp64_estimate(True)
+    assert s1["device_status"] == 0 and s0["device_status"] == 0 and s1["sink"] == s0["sink"]
+    assert s1["observations"] == s0["observations"] > 0
+    assert np.array_equal(h1, h0)
