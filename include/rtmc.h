@@ -392,6 +392,13 @@ int rtmc_set_table_cache(rtmc_context *ctx, int32_t enable);
  * estimate off (every observation in FP64); 1, the default, turns it on. */
 int rtmc_set_fp64_estimate(rtmc_context *ctx, int32_t enable);
 
+/* On the index path of the split schedule, the particles are binned in the order of their
+ * starting directions (a counting sort by direction cell between the event and the
+ * observation kernels), so that the fold's blocks see particles that are close together
+ * while they fly out and aggregate their counts in shared memory.  The histogram does not
+ * depend on it.  0 keeps the particles in id order; 1, the default, sorts them. */
+int rtmc_set_particle_order(rtmc_context *ctx, int32_t enable);
+
 /* writes a device buffer larger than L2 (timing hygiene between measured runs) */
 int rtmc_flush_l2(rtmc_context *ctx);
 

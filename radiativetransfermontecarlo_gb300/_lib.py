@@ -111,6 +111,7 @@ SIGNATURES = {
     "rtmc_flush_l2": (C.c_int, [_P]),
     "rtmc_set_table_cache": (C.c_int, [_P, C.c_int32]),
     "rtmc_set_fp64_estimate": (C.c_int, [_P, C.c_int32]),
+    "rtmc_set_particle_order": (C.c_int, [_P, C.c_int32]),
     "rtmc_set_launch": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32]),
     "rtmc_set_pipeline": (C.c_int, [_P, C.c_int32, C.c_int32]),
     "rtmc_set_schedule": (C.c_int, [_P, C.c_int32]),
@@ -348,6 +349,10 @@ class Context:
 
     def set_table_cache(self, enable: bool):
         check(self.lib.rtmc_set_table_cache(self.handle, 1 if enable else 0), self.handle)
+
+    def set_particle_order(self, enable: bool):
+        """rtmc_set_particle_order: bin the index path's particles in starting-direction order."""
+        check(self.lib.rtmc_set_particle_order(self.handle, 1 if enable else 0), self.handle)
 
     def set_fp64_estimate(self, enable: bool):
         """rtmc_set_fp64_estimate: FP64 radius-only observations through the exact FP32 estimate."""

@@ -51,6 +51,7 @@ struct rtmc_context {
     DevBuf hist, tabs, aux, stats, flush, trace, idx, adj, partial;
     DevBuf narrow; // uint32 copy of the histogram (rtmc_forward_u32)
     DevBuf segs, ovf; // split schedule: trajectory segment records, overflow list
+    DevBuf order;     // the particle order of the index path: keys, perm, iperm, cell cursors
     DevBuf tbacc;               // time-blocked FP32 fold accumulator
     uint64_t tabs_gen = 0;
     int tabs_prec = -1;
@@ -68,6 +69,7 @@ struct rtmc_context {
     int opt_event_major = -1; // -1 automatic, 0 two-cursor batches, 1 one particle per thread, 2 split
     int opt_fold = 0;         // 0 automatic, 1 64-bit slice fold, 2 time-blocked FP32 fold, 3 the same, rolling
     int opt_bin32 = 1;        // FP64 radius-only observations through an exact FP32 estimate
+    int opt_order = 1;        // index path: particles binned in the order of their starting directions
     static constexpr int kPipe = 32;
     cudaStream_t fold_stream = nullptr;
     cudaEvent_t ev_a0[kPipe] = {}, ev_a1[kPipe] = {}, ev_b0[kPipe] = {}, ev_b1[kPipe] = {};
@@ -632,6 +634,17 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         const int64_t rows_max = std::max<int64_t>(chunk, 1);
         if (ctx->segs.grow((size_t)rows_max * K * rec) || ctx->ovf.grow((size_t)rows_max * 4))
             return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for trajectory segments failed");
+        // the index path bins the particles in the order of their starting directions
+        if (sink == kSinkIndex && ctx->opt_order) {
+            if (ctx->order.grow((size_t)rows_max * 3 * sizeof(int32_t) + kOrderCells * sizeof(int32_t)))
+                return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for the particle order failed");
+            int32_t *o = static_cast<int32_t *>(ctx->order.p);
+            p.okey = o;
+            p.perm = o + rows_max;
+            p.iperm = o + 2 * rows_max;
+            sl.order.cursor = o + 3 * rows_max;
+            sl.grid_order = 2 * ctx->num_sms;
+        }
         p.split = 1;
         p.seg_cap = K;
         p.segs = ctx->segs.p;
@@ -1478,6 +1491,7 @@ extern "C" void rtmc_destroy(rtmc_context *ctx)
     ctx->partial.release();
     ctx->segs.release();
     ctx->ovf.release();
+    ctx->order.release();
     ctx->tbacc.release();
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
     if (ctx->ev_k0) cudaEventDestroy(ctx->ev_k0);
@@ -1630,6 +1644,13 @@ extern "C" int rtmc_set_fold(rtmc_context *ctx, int32_t mode)
     if (!ctx) return fail(nullptr, RTMC_ERR_ARG, "rtmc_set_fold: NULL context");
     if (mode < 0 || mode > 3) return fail(&ctx->err, RTMC_ERR_ARG, "fold mode must be 0, 1, 2 or 3");
     ctx->opt_fold = mode;
+    return RTMC_OK;
+}
+
+extern "C" int rtmc_set_particle_order(rtmc_context *ctx, int32_t enable)
+{
+    if (!ctx) return fail(nullptr, RTMC_ERR_ARG, "rtmc_set_particle_order: NULL context");
+    ctx->opt_order = enable ? 1 : 0;
     return RTMC_OK;
 }
 

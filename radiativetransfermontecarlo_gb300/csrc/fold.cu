@@ -367,6 +367,79 @@ __global__ void __launch_bounds__(kConvThreads) rt_tb_convert(const TbParams t, 
 
 } // namespace
 
+namespace {
+// ---------------------------------------------------------------------------------
+// Particle order for the index path: a counting sort of the chunk's particles by the
+// direction cell rt_events recorded (see OrderParams).  Each block takes a contiguous
+// range of particles; block-level counts go to the cell totals with one atomic per
+// (block, cell), the totals become cell offsets, and each block then reserves a column
+// range per cell and places its particles there.
+// ---------------------------------------------------------------------------------
+constexpr int kOrderThreads = 512;
+
+__global__ void __launch_bounds__(kOrderThreads) rt_order_count(const OrderParams o)
+{
+    __shared__ int h[kOrderCells];
+    for (int c = threadIdx.x; c < kOrderCells; c += blockDim.x) h[c] = 0;
+    __syncthreads();
+    const int64_t per = (o.n + gridDim.x - 1) / gridDim.x;
+    const int64_t a = (int64_t)blockIdx.x * per, b = min(o.n, a + per);
+    for (int64_t i = a + threadIdx.x; i < b; i += blockDim.x) atomicAdd(&h[o.key[i]], 1);
+    __syncthreads();
+    for (int c = threadIdx.x; c < kOrderCells; c += blockDim.x)
+        if (h[c]) atomicAdd(&o.cursor[c], h[c]);
+}
+
+// cell totals -> first column of each cell (one block of kOrderCells threads)
+__global__ void __launch_bounds__(kOrderCells) rt_order_scan(const OrderParams o)
+{
+    __shared__ int v[kOrderCells];
+    const int c = threadIdx.x;
+    const int total = o.cursor[c];
+    v[c] = total;
+    __syncthreads();
+    for (int d = 1; d < kOrderCells; d <<= 1) { // inclusive scan
+        const int x = c >= d ? v[c - d] : 0;
+        __syncthreads();
+        v[c] += x;
+        __syncthreads();
+    }
+    o.cursor[c] = v[c] - total;
+}
+
+__global__ void __launch_bounds__(kOrderThreads) rt_order_place(const OrderParams o)
+{
+    __shared__ int h[kOrderCells]; // the block's count per cell, then its next column there
+    for (int c = threadIdx.x; c < kOrderCells; c += blockDim.x) h[c] = 0;
+    __syncthreads();
+    const int64_t per = (o.n + gridDim.x - 1) / gridDim.x;
+    const int64_t a = (int64_t)blockIdx.x * per, b = min(o.n, a + per);
+    for (int64_t i = a + threadIdx.x; i < b; i += blockDim.x) atomicAdd(&h[o.key[i]], 1);
+    __syncthreads();
+    for (int c = threadIdx.x; c < kOrderCells; c += blockDim.x)
+        if (h[c]) h[c] = atomicAdd(&o.cursor[c], h[c]);
+    __syncthreads();
+    for (int64_t i = a + threadIdx.x; i < b; i += blockDim.x) {
+        const int pos = atomicAdd(&h[o.key[i]], 1);
+        o.perm[pos] = (int32_t)i;
+        o.iperm[i] = pos;
+    }
+}
+
+} // namespace
+
+int launch_order(const OrderParams &o, int grid, void *stream)
+{
+    if (o.n <= 0) return 0;
+    cudaError_t e = cudaMemsetAsync(o.cursor, 0, kOrderCells * sizeof(int32_t), (cudaStream_t)stream);
+    if (e != cudaSuccess) return (int)e;
+    const int g = (int)std::max<int64_t>(1, std::min<int64_t>(grid, (o.n + kOrderThreads - 1) / kOrderThreads));
+    rt_order_count<<<g, kOrderThreads, 0, (cudaStream_t)stream>>>(o);
+    rt_order_scan<<<1, kOrderCells, 0, (cudaStream_t)stream>>>(o);
+    rt_order_place<<<g, kOrderThreads, 0, (cudaStream_t)stream>>>(o);
+    return (int)cudaGetLastError();
+}
+
 int launch_fold_tb(const TbParams &t, int grid_x, void *stream)
 {
     if (t.tb_count < 1 || (t.part_per_block & 3)) return (int)cudaErrorInvalidValue;

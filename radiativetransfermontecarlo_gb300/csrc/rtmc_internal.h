@@ -118,6 +118,12 @@ template <typename R> struct DevParams {
     int32_t *status;
     double *trace;  // optional [n_particles][16] final particle states
     int32_t *obs_idx;  // index sink: [n_obs][obs_rows] in-slice bin | mode << 30, or -1
+    // split schedule on the index path: the columns of the index array hold the particles in
+    // the order of their starting directions (okey: a direction cell per particle, written
+    // by rt_events; perm: column -> particle; iperm: particle -> column), so that a fold
+    // block's particles stay close together while they fly out; null: column = particle
+    int32_t *okey;
+    int32_t *perm, *iperm;
     int64_t obs_rows;
     // split schedule (rt_events, then rt_observe): seg_cap records per particle in segs, its
     // trajectory segments followed by end records (a particle with more than seg_cap - 2
@@ -198,10 +204,23 @@ struct AdjointArgs {
 };
 
 // Launch shape of the split schedule (rt_events, rt_observe, rt_transport_list).
+// A counting sort of particles by direction cell (kOrderCells cells), between rt_events
+// and rt_observe: per-block cell counts, the cells' offsets, then each block places its
+// particles.  Order within a cell is not fixed; the folds' integer sums do not depend on it.
+constexpr int kOrderCells = 512;
+struct OrderParams {
+    const int32_t *key; // [n] cells
+    int32_t *perm, *iperm;
+    int32_t *cursor;    // [kOrderCells] cell totals, then the next free column of each cell
+    int64_t n;
+};
+
 struct SplitLaunch {
     int grid_events, grid_observe, block_observe, grid_list;
     size_t smem_events, smem_observe;
     void *mid_event; // optional cudaEvent_t recorded after rt_events
+    OrderParams order; // order.n > 0: sort the chunk's particles before rt_observe
+    int grid_order;
 };
 
 // Launch wrappers (kernels.cu, fold.cu).  Return a cudaError_t value.
@@ -240,6 +259,8 @@ int launch_bin_slices(const BinParams &b, int grid_x, size_t smem, void *stream)
 int launch_narrow_u32(const unsigned long long *src, uint32_t *dst, int64_t n, int shift, int max_grid, void *stream);
 // time-blocked fold of one chunk over t-blocks [tb_first, tb_first + tb_count)
 int launch_fold_tb(const TbParams &t, int grid_x, void *stream);
+// the particle order of OrderParams (three kernels)
+int launch_order(const OrderParams &o, int grid, void *stream);
 // acc t-blocks [tb_first, tb_first + tb_count) -> the int64 histogram (count << shift) and,
 // when u32 is non-null, the uint32 counts; slice 0 (t = 0, never observed) is zeroed with
 // t-block 0

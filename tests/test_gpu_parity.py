@@ -734,3 +734,29 @@ def test_fp64_radial_estimate_gives_fp64_bins(frame):
     assert s1["device_status"] == 0 and s0["device_status"] == 0 and s1["sink"] == s0["sink"]
     assert s1["observations"] == s0["observations"] > 0
     assert np.array_equal(h1, h0)
+
+
+@pytest.mark.parametrize("segs", [0, 2])
+def test_particle_order_leaves_histogram_unchanged(segs):
+    """The index path bins particles in the order of their starting directions; the
+    histogram equals the one in particle-id order bit for bit, also when most particles
+    overflow their segment records (2 per particle) and are rerun into their columns."""
+    geo, src, mat, obs, opts = W.c2_elastic3d(t_end=1.0)
+    prob, grid, N = build_problem(geo, dict(src, numberParticles=30001), mat, obs, dict(opts, exact_count=True))
+    P, keep = prob.to_ctypes()
+    ctx = get_context(0)
+    out = []
+    try:
+        ctx.set_launch(0, segs, 0)
+        for order in (True, False):
+            ctx.set_particle_order(order)
+            h, st = ctx.forward(P, prob.tables)
+            u, _ = ctx.forward_u32(P, prob.tables)
+            out.append((h, u, st))
+    finally:
+        ctx.set_particle_order(True)
+        ctx.set_launch(0, 0, 0)
+    (h1, u1, s1), (h0, u0, s0) = out
+    assert s1["sink"] == 2 and s1["device_status"] == 0 and s0["device_status"] == 0
+    assert s1["observations"] == s0["observations"] > 0
+    assert np.array_equal(h1, h0) and np.array_equal(u1, u0)
