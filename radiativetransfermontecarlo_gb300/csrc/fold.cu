@@ -390,21 +390,29 @@ __global__ void __launch_bounds__(kOrderThreads) rt_order_count(const OrderParam
         if (h[c]) atomicAdd(&o.cursor[c], h[c]);
 }
 
-// cell totals -> first column of each cell (one block of kOrderCells threads)
-__global__ void __launch_bounds__(kOrderCells) rt_order_scan(const OrderParams o)
+// cell totals -> first column of each cell (one block; each thread scans a run of cells)
+constexpr int kScanThreads = 512;
+__global__ void __launch_bounds__(kScanThreads) rt_order_scan(const OrderParams o)
 {
-    __shared__ int v[kOrderCells];
-    const int c = threadIdx.x;
-    const int total = o.cursor[c];
-    v[c] = total;
+    constexpr int per = (kOrderCells + kScanThreads - 1) / kScanThreads;
+    __shared__ int v[kScanThreads];
+    const int t = threadIdx.x, c0 = t * per;
+    int sum = 0;
+    for (int c = c0; c < c0 + per && c < kOrderCells; ++c) sum += o.cursor[c];
+    v[t] = sum;
     __syncthreads();
-    for (int d = 1; d < kOrderCells; d <<= 1) { // inclusive scan
-        const int x = c >= d ? v[c - d] : 0;
+    for (int d = 1; d < kScanThreads; d <<= 1) { // inclusive scan of the runs' sums
+        const int x = t >= d ? v[t - d] : 0;
         __syncthreads();
-        v[c] += x;
+        v[t] += x;
         __syncthreads();
     }
-    o.cursor[c] = v[c] - total;
+    int run = v[t] - sum; // the cells before this thread's run
+    for (int c = c0; c < c0 + per && c < kOrderCells; ++c) {
+        const int total = o.cursor[c];
+        o.cursor[c] = run;
+        run += total;
+    }
 }
 
 __global__ void __launch_bounds__(kOrderThreads) rt_order_place(const OrderParams o)
@@ -435,7 +443,7 @@ int launch_order(const OrderParams &o, int grid, void *stream)
     if (e != cudaSuccess) return (int)e;
     const int g = (int)std::max<int64_t>(1, std::min<int64_t>(grid, (o.n + kOrderThreads - 1) / kOrderThreads));
     rt_order_count<<<g, kOrderThreads, 0, (cudaStream_t)stream>>>(o);
-    rt_order_scan<<<1, kOrderCells, 0, (cudaStream_t)stream>>>(o);
+    rt_order_scan<<<1, kScanThreads, 0, (cudaStream_t)stream>>>(o);
     rt_order_place<<<g, kOrderThreads, 0, (cudaStream_t)stream>>>(o);
     return (int)cudaGetLastError();
 }
