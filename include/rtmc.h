@@ -369,7 +369,9 @@ int rtmc_set_pipeline(rtmc_context *ctx, int32_t chunks, int32_t transport_block
  * per particle follow the expected events, or the ring capacity of rtmc_set_launch when
  * one is set; particles with more are rerun one per thread); -1 = automatic (1 when 8 x
  * expected events per particle >= observation instants and the histogram does not go
- * through the index array, else 2).  All give the same histogram. */
+ * through the index array, else 2).  All give the same histogram.  rtmc_gradient with
+ * up to 4 parameters replays on the split schedule under -1 and 2, and with the lockstep
+ * ring under 0 and 1 (the same sums up to rounding order). */
 int rtmc_set_schedule(rtmc_context *ctx, int32_t event_major);
 
 /* Fold of the index path (large histograms): 1 = each observation one 64-bit reduction

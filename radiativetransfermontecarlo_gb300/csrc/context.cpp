@@ -52,6 +52,7 @@ struct rtmc_context {
     DevBuf narrow; // uint32 copy of the histogram (rtmc_forward_u32)
     DevBuf segs, ovf; // split schedule: trajectory segment records, overflow list
     DevBuf order;     // the particle order of the index path: keys, perm, iperm, cell cursors
+    DevBuf segth;     // split replay of the gradient: the scattering angle of each segment
     DevBuf tbacc;               // time-blocked FP32 fold accumulator
     uint64_t tabs_gen = 0;
     int tabs_prec = -1;
@@ -1056,6 +1057,119 @@ int check_score(rtmc_context *ctx, const rtmc_problem *P, const rtmc_score *sc, 
     return RTMC_OK;
 }
 
+// The split replay of rtmc_gradient: per particle chunk, rt_events writes the segment
+// records and each segment's scattering angle, rt_observe_adj sums the adjoint weights per
+// segment in lockstep, rt_adjoint_list replays the particles that overflowed; block sums
+// are added on the host in a fixed order (chunks, then the observation blocks, then the
+// list blocks), so a call is reproducible.
+template <typename R>
+int gradient_split(rtmc_context *ctx, const rtmc_problem *P, const rtmc_score *sc, DevParams<R> p, AdjointArgs a,
+                   int n_edges, size_t hb, size_t sb, size_t n_aux, double *grad, rtmc_stats *st)
+{
+    const int prec = sizeof(R) == 4 ? RTMC_FP32 : RTMC_FP64;
+    const int nm = P->acoustics ? 1 : 2;
+    double rate = 0;
+    for (int m = 0; m < nm; ++m)
+        if (std::isfinite(P->mft[m])) rate = std::max(rate, 1.0 / P->mft[m]);
+    const double mean = rate * P->h * (double)P->n_sub * (double)P->n_obs;
+    int K = (int)std::ceil(1.0 + mean + 4.0 * std::sqrt(mean) + 4.0);
+    K = std::min(64, std::max(8, (K + 3) / 4 * 4));
+    if (ctx->opt_ring) K = ctx->opt_ring; // an explicit ring capacity sets the segments per particle
+    K = std::max(1, K) + 2;               // and two end records
+    const size_t rec = 8 * sizeof(R);
+    constexpr int64_t kSegBudget = (int64_t)8 << 30;
+    const int64_t chunk = std::min<int64_t>(
+        P->n_particles, std::max<int64_t>(32, kSegBudget / ((int64_t)K * (int64_t)(rec + sizeof(R))) / 32 * 32));
+    if (ctx->segs.grow((size_t)chunk * K * rec) || ctx->segth.grow((size_t)chunk * K * sizeof(R)) ||
+        ctx->ovf.grow((size_t)chunk * 4))
+        return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for trajectory segments failed");
+    p.sink = 3; // no histogram: the records keep the mode apart from the direction offset
+    p.split = 1;
+    p.seg_cap = K;
+    p.segs = ctx->segs.p;
+    p.seg_th = ctx->segth.p;
+    p.ovf_list = static_cast<int32_t *>(ctx->ovf.p);
+    p.ovf_count = reinterpret_cast<uint32_t *>(static_cast<unsigned char *>(ctx->stats.p) + 192);
+    p.clear = nullptr;
+    p.clear_words = 0;
+    const size_t smem = align_up((size_t)n_edges * sizeof(R), 16);
+    int be = 0, bo = 0, bl = 0;
+    void *fe = kernel_of(prec, 5, 0, p.obs_kind);
+    if (kernel_set_smem(prec, 5, 0, p.obs_kind, smem) != 0 ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&be, fe, 256, smem) != cudaSuccess || be < 1 ||
+        adjoint_split_occupancy(prec, 8, p.obs_kind, kAdjointThreads, smem, &bo) != 0 || bo < 1 ||
+        adjoint_split_occupancy(prec, 9, p.obs_kind, kAdjointThreads, smem, &bl) != 0 || bl < 1)
+        return fail(&ctx->err, RTMC_ERR_CUDA, "split adjoint kernels do not fit on the device");
+    const int ge = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)ctx->num_sms * be, (chunk + 255) / 256));
+    const int go = (int)std::max<int64_t>(
+        1, std::min<int64_t>((int64_t)ctx->num_sms * bo, (chunk + kAdjointThreads - 1) / kAdjointThreads));
+    const int gl = ctx->num_sms;
+    const int np = sc->n_params;
+    if (ctx->partial.grow((size_t)(go + gl) * np * sizeof(double)))
+        return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for the gradient failed");
+    a.partial = static_cast<double *>(ctx->partial.p);
+    a.partial_list = a.partial + (size_t)go * np;
+    std::vector<double> part((size_t)(go + gl) * np);
+    std::vector<double> acc(np, 0.0);
+    double kms = 0;
+    int launches = 0;
+    for (int64_t base = 0; base < P->n_particles; base += chunk) {
+        DevParams<R> q = p;
+        q.pid0 = P->pid0 + base;
+        q.n_particles = std::min<int64_t>(chunk, P->n_particles - base);
+        CK(cudaMemsetAsync(q.ovf_count, 0, sizeof(uint32_t), ctx->stream), "overflow count");
+        CK(cudaEventRecord(ctx->ev_k0, ctx->stream), "event");
+        void *ea[] = {(void *)&q};
+        void *oa[] = {(void *)&q, (void *)&a};
+        cudaError_t e = cudaLaunchKernel(fe, dim3(ge), dim3(256), ea, smem, ctx->stream);
+        if (e == cudaSuccess)
+            e = cudaLaunchKernel(kernel_of(prec, 8, 0, p.obs_kind), dim3(go), dim3(kAdjointThreads), oa, smem, ctx->stream);
+        if (e == cudaSuccess)
+            e = cudaLaunchKernel(kernel_of(prec, 9, 0, p.obs_kind), dim3(gl), dim3(kAdjointThreads), oa, smem, ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "split adjoint launch");
+        launches += 3;
+        CK(cudaEventRecord(ctx->ev_k1, ctx->stream), "event");
+        CK(cudaMemcpyAsync(part.data(), a.partial, part.size() * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream),
+           "partial sums");
+        CK(cudaStreamSynchronize(ctx->stream), "adjoint");
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev_k0, ctx->ev_k1);
+        kms += ms;
+        for (int qq = 0; qq < np; ++qq) {
+            double v = 0.0;
+            for (int b = 0; b < go + gl; ++b) v += part[(size_t)b * np + qq];
+            acc[qq] += v;
+        }
+    }
+    int64_t dstats[32];
+    CK(cudaMemcpyAsync(dstats, ctx->stats.p, 256, cudaMemcpyDeviceToHost, ctx->stream), "counters");
+    CK(cudaEventRecord(ctx->ev_end, ctx->stream), "event");
+    CK(cudaStreamSynchronize(ctx->stream), "adjoint");
+    for (int qq = 0; qq < np; ++qq) grad[qq] = acc[qq];
+    float tms = 0;
+    cudaEventElapsedTime(&tms, ctx->ev_start, ctx->ev_end);
+    ctx->last_kernel_ms = kms;
+    ctx->last_launches = launches;
+    const int32_t status = (int32_t)(dstats[16] & 0xffffffff);
+    if (st) {
+        std::memset(st, 0, sizeof *st);
+        st->scatter_events = dstats[0];
+        st->boundary_hits = dstats[1];
+        st->kills = dstats[2];
+        st->absorbed = dstats[3];
+        st->observations = dstats[4];
+        st->conversions = dstats[5];
+        st->device_status = status;
+        st->kernel_ms = kms;
+        st->launches = launches;
+        st->total_ms = tms;
+        st->h2d_bytes = (double)(hb + sb + n_aux * sizeof(R));
+        st->d2h_bytes = (double)(part.size() * sizeof(double) + 256);
+    }
+    if (status) return fail(&ctx->err, RTMC_ERR_DEVICE, "an adjoint guard tripped (event cap or histogram index)");
+    return RTMC_OK;
+}
+
 template <typename R>
 int gradient_run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, const rtmc_score *sc,
                  const double *adjoint, double *grad, rtmc_stats *st)
@@ -1124,9 +1238,13 @@ int gradient_run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t,
         a.b_obs[q] = -sc->dlogSigma[q] * hS * (double)P->n_sub;
     }
     const int block = kAdjointThreads;
-    // up to 4 parameters: the converged two-phase replay with a segment ring; more: one
-    // particle per thread
+    // up to 4 parameters: the split replay (rt_events, then rt_observe_adj and the overflow
+    // reruns), or the converged two-phase replay with a segment ring; more: one particle
+    // per thread
     const bool ring = sc->n_params <= kAdjointRingParams;
+    // (schedules 0 and 1 of rtmc_set_schedule keep the ring replay)
+    if (ring && ctx->opt_event_major != 0 && ctx->opt_event_major != 1 && P->n_particles > 0)
+        return gradient_split<R>(ctx, P, sc, p, a, n_edges, hb, sb, edges.size() + zoe.size(), grad, st);
     // FP32: 4 ring slots let 3 blocks share an SM (C5: 12.5 ms against 14.4 with 8 slots
     // and 2 blocks)
     const int cap = ctx->opt_ring ? ctx->opt_ring : (sizeof(R) == 4 ? 4 : 6);
@@ -1492,6 +1610,7 @@ extern "C" void rtmc_destroy(rtmc_context *ctx)
     ctx->segs.release();
     ctx->ovf.release();
     ctx->order.release();
+    ctx->segth.release();
     ctx->tbacc.release();
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
     if (ctx->ev_k0) cudaEventDestroy(ctx->ev_k0);

@@ -574,6 +574,11 @@ int adjoint_ring_occupancy(int precision, int obs, int block, size_t smem, int *
     return set_and_occupancy(precision, 4, obs, block, smem, blocks_per_sm);
 }
 
+int adjoint_split_occupancy(int precision, int kind, int obs, int block, size_t smem, int *blocks_per_sm)
+{
+    return set_and_occupancy(precision, kind, obs, block, smem, blocks_per_sm);
+}
+
 int kernel_set_smem(int precision, int kind, int sink, int obs, size_t smem)
 {
     return (int)cudaFuncSetAttribute(kernel_of(precision, kind, sink, obs), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -585,7 +590,8 @@ void *kernel_of(int precision, int kind, int sink, int obs)
     switch (kind) {
     case 0: return d ? kernel_of_transport_f64(sink, obs) : kernel_of_transport_f32(sink, obs);
     case 1: case 2: return d ? kernel_of_batch_f64(kind == 2, obs) : kernel_of_batch_f32(kind == 2, obs);
-    case 3: case 4: return d ? kernel_of_adjoint_f64(kind == 4, obs) : kernel_of_adjoint_f32(kind == 4, obs);
+    case 3: case 4: return d ? kernel_of_adjoint_f64(kind - 3, obs) : kernel_of_adjoint_f32(kind - 3, obs);
+    case 8: case 9: return d ? kernel_of_adjoint_f64(kind - 6, obs) : kernel_of_adjoint_f32(kind - 6, obs);
     default: return d ? kernel_of_split_f64(kind, sink, obs) : kernel_of_split_f32(kind, sink, obs);
     }
 }

@@ -57,9 +57,14 @@ int RTMC_NAME(launch_adjoint_ring)(const DevParams<RTMC_REAL> &p, const AdjointA
     return launch_adjoint_t<RTMC_REAL>(p, a, grid, block, smem, stream, true);
 }
 
-void *RTMC_NAME(kernel_of_adjoint)(int ring, int obs)
+void *RTMC_NAME(kernel_of_adjoint)(int which, int obs)
 {
-    return ring ? pick_adjoint_ring<RTMC_REAL>(obs) : pick_adjoint<RTMC_REAL>(obs);
+    switch (which) {
+    case 0: return pick_adjoint<RTMC_REAL>(obs);
+    case 1: return pick_adjoint_ring<RTMC_REAL>(obs);
+    case 2: return pick_observe_adj<RTMC_REAL>(obs);
+    default: return pick_adjoint_list<RTMC_REAL>(obs);
+    }
 }
 #endif
 

@@ -129,6 +129,7 @@ template <typename R> struct DevParams {
     // trajectory segments followed by end records (a particle with more than seg_cap - 2
     // segments gets end records only, is listed in ovf_list and rerun by rt_transport_list)
     void *segs;
+    void *seg_th;  // split adjoint: [n][seg_cap] theta / pi of the scattering that starts each segment, or -1
     int32_t *ovf_list;
     uint32_t *ovf_count;
     int32_t seg_cap, split;
@@ -201,6 +202,7 @@ struct AdjointArgs {
     double b_obs[RTMC_MAX_PARAMS];
     float a_inc_f[RTMC_MAX_PARAMS];
     double *partial;          // [gridDim.x][n_params] block sums
+    double *partial_list;     // split replay: block sums of the overflow reruns (rt_adjoint_list)
 };
 
 // Launch shape of the split schedule (rt_events, rt_observe, rt_transport_list).
@@ -237,8 +239,9 @@ void *kernel_of_transport_f32(int sink, int obs);
 void *kernel_of_transport_f64(int sink, int obs);
 void *kernel_of_batch_f32(int em, int obs);
 void *kernel_of_batch_f64(int em, int obs);
-void *kernel_of_adjoint_f32(int ring, int obs);
-void *kernel_of_adjoint_f64(int ring, int obs);
+// which: 0 rt_adjoint, 1 rt_adjoint_ring, 2 rt_observe_adj, 3 rt_adjoint_list
+void *kernel_of_adjoint_f32(int which, int obs);
+void *kernel_of_adjoint_f64(int which, int obs);
 void *kernel_of(int precision, int kind, int sink, int obs);
 int kernel_set_smem(int precision, int kind, int sink, int obs, size_t smem);
 int launch_transport_f32(const DevParams<float> &p, int grid, int block, size_t smem, void *stream);
@@ -250,6 +253,8 @@ int adjoint_occupancy(int precision, int obs, int block, size_t smem, int *block
 int launch_adjoint_ring_f32(const DevParams<float> &p, const AdjointArgs &a, int grid, int block, size_t smem, void *stream);
 int launch_adjoint_ring_f64(const DevParams<double> &p, const AdjointArgs &a, int grid, int block, size_t smem, void *stream);
 int adjoint_ring_occupancy(int precision, int obs, int block, size_t smem, int *blocks_per_sm);
+// the split replay's kernels: kind 8 rt_observe_adj, 9 rt_adjoint_list (sets the dynamic shared memory)
+int adjoint_split_occupancy(int precision, int kind, int obs, int block, size_t smem, int *blocks_per_sm);
 constexpr int kAdjointRingParams = 4; // parameters the ring-based adjoint carries
 constexpr int kAdjointThreads = 256;
 int transport_set_smem(int precision, int sink, int obs, size_t smem);

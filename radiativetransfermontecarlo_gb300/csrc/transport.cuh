@@ -1488,6 +1488,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) rt_events(const D
             seg_from(s, g);
             seg_prepare<R, OBS>(p, sedges, g);
             rec_put_seg<R, OBS>(p, segs + (size_t)i * K * kRecWords, g);
+            if (p.seg_th) static_cast<R *>(p.seg_th)[(size_t)i * K] = (R)-1;
             nseg = 1;
             have = true;
         }
@@ -1496,7 +1497,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) rt_events(const D
         if (next_event(s) > p.s_end) {
             done = 1;
         } else {
-            process_event(p, (uint64_t)(p.pid0 + i), s, cnt);
+            const int kind = process_event(p, (uint64_t)(p.pid0 + i), s, cnt);
             if ((int)s.k > p.max_events) { s.alive = 0; s.s_death = s.s0; bad = true; }
             if (!s.alive) {
                 done = 1;
@@ -1504,6 +1505,7 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) rt_events(const D
                 seg_from(s, g);
                 seg_prepare<R, OBS>(p, sedges, g);
                 rec_put_seg<R, OBS>(p, segs + ((size_t)i * K + nseg) * kRecWords, g);
+                if (p.seg_th) static_cast<R *>(p.seg_th)[(size_t)i * K + nseg] = kind == 0 ? s.th : (R)-1;
                 ++nseg;
             } else {
                 done = 2;
@@ -1512,7 +1514,10 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) rt_events(const D
         if (done) {
             R *r = segs + (size_t)i * K * kRecWords;
             if (done == 1) {
-                if (!s.alive) rec_put_end(r + (size_t)nseg++ * kRecWords, s.s_death);
+                if (!s.alive) {
+                    if (p.seg_th) static_cast<R *>(p.seg_th)[(size_t)i * K + nseg] = (R)-1;
+                    rec_put_end(r + (size_t)nseg++ * kRecWords, s.s_death);
+                }
                 rec_put_end(r + (size_t)nseg * kRecWords, kNeverStart);
                 if (p.trace) { // final state of the particle, the oracle's layout
                     double *f = p.trace + 16 * i;
@@ -1841,6 +1846,99 @@ template <typename R, int SINK> void *pick_obs(int obs)
 // FP64, adjoint[bin] * score over every observation instant.  Between two events the
 // score is A + b_obs * j, so a segment only sums adjoint[bin] and j * adjoint[bin]; the
 // scattering that ends it adds d log sigma(theta) / dp (table lookup) + a_inc to A.
+template <typename R, int OBS>
+__device__ __forceinline__ void adjoint_particle(const DevParams<R> &p, const AdjointArgs &a, const R *sedges,
+                                                 const R *wts, const R *dls, int64_t i, double (&g)[RTMC_MAX_PARAMS],
+                                                 Counters &cnt, bool &bad)
+{
+    const int np = a.n_params;
+    const R tmax = (R)(a.n_theta - 1);
+    const uint64_t pid = (uint64_t)(p.pid0 + i);
+    Part<R> s;
+    init_particle(p, pid, s);
+    // this particle's score (scattering part) and sum of A * segment weights, in the
+    // transport's precision; FP64 once per particle
+    R A[RTMC_MAX_PARAMS], G[RTMC_MAX_PARAMS];
+#pragma unroll
+    for (int q = 0; q < RTMC_MAX_PARAMS; ++q) { A[q] = (R)0; G[q] = (R)0; }
+    R SAJ = (R)0;
+    int j = 1;
+    for (;;) {
+        const int e = next_event(s);
+        const int lim = e <= p.s_end ? e : p.s_end + 1;
+        Seg<R> sg;
+        seg_from(s, sg);
+        seg_prepare<R, OBS>(p, sedges, sg);
+        R sa = (R)0, saj = (R)0;
+        for (; j <= p.n_obs && j * p.n_sub < lim; ++j) { // observations strictly before the event
+            const int v = obs_offset<R, OBS>(p, sedges, sg, j * p.n_sub);
+            if (v < 0) continue;
+            const int64_t idx = (int64_t)j * p.time_stride + (sg.mode ? p.mode_stride : 0) + v;
+            if (idx >= p.hist_len) { bad = true; continue; }
+            const R w = __ldg(wts + idx);
+            sa += w;
+            saj += w * (R)j;
+            cnt.obs++;
+        }
+#pragma unroll
+        for (int q = 0; q < RTMC_MAX_PARAMS; ++q)
+            if (q < np) G[q] += A[q] * sa;
+        SAJ += saj;
+        if (j > p.n_obs || e > p.s_end) break;
+        const int kind = process_event(p, pid, s, cnt);
+        if ((int)s.k > p.max_events) { bad = true; break; }
+        if (!s.alive) break;
+        if (kind == 0) {
+            R f = s.th < (R)0 ? (R)0 : (s.th > (R)1 ? (R)1 : s.th);
+            f *= tmax;
+            int k = (int)f;
+            k = k > a.n_theta - 2 ? a.n_theta - 2 : k;
+            const R w = f - (R)k;
+#pragma unroll
+            for (int q = 0; q < RTMC_MAX_PARAMS; ++q) {
+                if (q < np) {
+                    const R *t = dls + (size_t)q * a.n_theta + k;
+                    const R t0 = __ldg(t), t1 = __ldg(t + 1);
+                    A[q] += t0 + w * (t1 - t0) + (sizeof(R) == 4 ? (R)a.a_inc_f[q] : (R)a.a_inc[q]);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int q = 0; q < RTMC_MAX_PARAMS; ++q)
+        if (q < np) g[q] += (double)G[q] + a.b_obs[q] * (double)SAJ;
+}
+
+// A block's gradient sums in a fixed order (warp shuffles, then warp 0 over the warps) to
+// out[blockIdx.x][n_params], and its counters and status; red holds a row per warp.
+template <int NP>
+__device__ __forceinline__ void adjoint_block_sums(const unsigned long long *, unsigned long long *stats, int32_t *status,
+                                                   int np, double (&g)[NP], double (*red)[NP], double *out,
+                                                   const Counters &cnt, bool bad)
+{
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NP; ++q) {
+        double v = g[q];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (lane == 0) red[warp][q] = v;
+    }
+    __syncthreads();
+    if (threadIdx.x < NP && threadIdx.x < np) {
+        double v = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w][threadIdx.x];
+        out[(size_t)blockIdx.x * np + threadIdx.x] = v;
+    }
+    const unsigned full = 0xffffffffu;
+    unsigned cv[6] = {cnt.scat, cnt.bnd, cnt.kill, cnt.absorb, cnt.obs, cnt.conv};
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        const unsigned t = __reduce_add_sync(full, cv[c]);
+        if (lane == 0 && t) atomicAdd(stats + c, (unsigned long long)t);
+    }
+    if (bad) atomicExch(status, 1);
+}
+
 // Block sums go to a.partial in a fixed order, so the result is reproducible.
 template <typename R, int OBS>
 __global__ void __launch_bounds__(kAdjointThreads, sizeof(R) == 4 ? 3 : 2) rt_adjoint(const DevParams<R> p, const AdjointArgs a)
@@ -1852,92 +1950,128 @@ __global__ void __launch_bounds__(kAdjointThreads, sizeof(R) == 4 ? 3 : 2) rt_ad
     __syncthreads();
     const R *wts = static_cast<const R *>(a.adjoint);
     const R *dls = sizeof(R) == 4 ? reinterpret_cast<const R *>(a.dlogsigma_f) : reinterpret_cast<const R *>(a.dlogsigma);
-    const int np = a.n_params;
     double g[RTMC_MAX_PARAMS];
 #pragma unroll
     for (int q = 0; q < RTMC_MAX_PARAMS; ++q) g[q] = 0.0;
     Counters cnt = {0u, 0u, 0u, 0u, 0u, 0u};
     bool bad = false;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    const R tmax = (R)(a.n_theta - 1);
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.n_particles; i += stride) {
-        const uint64_t pid = (uint64_t)(p.pid0 + i);
-        Part<R> s;
-        init_particle(p, pid, s);
-        // this particle's score (scattering part) and sum of A * segment weights, in the
-        // transport's precision; FP64 once per particle
-        R A[RTMC_MAX_PARAMS], G[RTMC_MAX_PARAMS];
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < p.n_particles; i += stride)
+        adjoint_particle<R, OBS>(p, a, sedges, wts, dls, i, g, cnt, bad);
+    adjoint_block_sums<RTMC_MAX_PARAMS>(p.stats, p.stats, p.status, a.n_params, g, red, a.partial, cnt, bad);
+}
+
+// The split replay's particles whose segments overflowed, rerun whole one per thread;
+// their block sums go to a.partial_list.  The list length is read on the device.
+template <typename R, int OBS>
+__global__ void __launch_bounds__(kAdjointThreads, sizeof(R) == 4 ? 3 : 2) rt_adjoint_list(const DevParams<R> p, const AdjointArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R *sedges = reinterpret_cast<R *>(smem_raw);
+    __shared__ double red[kAdjointThreads / 32][RTMC_MAX_PARAMS];
+    for (int k = threadIdx.x; k < p.n_edges; k += blockDim.x) sedges[k] = p.edges[k];
+    __syncthreads();
+    const R *wts = static_cast<const R *>(a.adjoint);
+    const R *dls = sizeof(R) == 4 ? reinterpret_cast<const R *>(a.dlogsigma_f) : reinterpret_cast<const R *>(a.dlogsigma);
+    double g[RTMC_MAX_PARAMS];
 #pragma unroll
-        for (int q = 0; q < RTMC_MAX_PARAMS; ++q) { A[q] = (R)0; G[q] = (R)0; }
-        R SAJ = (R)0;
-        int j = 1;
-        for (;;) {
-            const int e = next_event(s);
-            const int lim = e <= p.s_end ? e : p.s_end + 1;
-            Seg<R> sg;
-            seg_from(s, sg);
-            seg_prepare<R, OBS>(p, sedges, sg);
-            R sa = (R)0, saj = (R)0;
-            for (; j <= p.n_obs && j * p.n_sub < lim; ++j) { // observations strictly before the event
-                const int v = obs_offset<R, OBS>(p, sedges, sg, j * p.n_sub);
-                if (v < 0) continue;
-                const int64_t idx = (int64_t)j * p.time_stride + (sg.mode ? p.mode_stride : 0) + v;
-                if (idx >= p.hist_len) { bad = true; continue; }
-                const R w = __ldg(wts + idx);
-                sa += w;
-                saj += w * (R)j;
-                cnt.obs++;
+    for (int q = 0; q < RTMC_MAX_PARAMS; ++q) g[q] = 0.0;
+    Counters cnt = {0u, 0u, 0u, 0u, 0u, 0u};
+    bool bad = false;
+    const unsigned n = *reinterpret_cast<volatile const uint32_t *>(p.ovf_count);
+    for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
+        adjoint_particle<R, OBS>(p, a, sedges, wts, dls, p.ovf_list[t], g, cnt, bad);
+    adjoint_block_sums<RTMC_MAX_PARAMS>(p.stats, p.stats, p.status, a.n_params, g, red, a.partial_list, cnt, bad);
+}
+
+// Split replay, observation side: rt_events has written every particle's segment records
+// and the scattering angle that starts each segment (seg_th); like rt_observe, a warp walks
+// the observation instants of 32 particles in lockstep, and instead of binning each lane
+// sums the adjoint weights of its bins (AdjLane: the score of the segment in force is
+// A + b_obs j, and a segment that a scattering starts adds d log sigma(theta) + a_inc to
+// A).  Overflowing particles contribute nothing here (their lists hold only end records)
+// and are replayed by rt_adjoint_list.
+template <typename R, int OBS>
+__global__ void __launch_bounds__(kAdjointThreads, sizeof(R) == 4 ? 4 : 2) rt_observe_adj(const DevParams<R> p, const AdjointArgs a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    R *sedges = reinterpret_cast<R *>(smem_raw);
+    __shared__ double red[kAdjointThreads / 32][kAdjRingParams];
+    for (int k = threadIdx.x; k < p.n_edges; k += blockDim.x) sedges[k] = p.edges[k];
+    __syncthreads();
+    constexpr bool C32 = sizeof(R) == 4 && OBS == OBS_CART;
+    AdjLane<R> adj;
+    adj.a = &a;
+    adj.wts = static_cast<const R *>(a.adjoint);
+    adj.dls = sizeof(R) == 4 ? reinterpret_cast<const R *>(a.dlogsigma_f) : reinterpret_cast<const R *>(a.dlogsigma);
+#pragma unroll
+    for (int q = 0; q < kAdjRingParams; ++q) adj.g[q] = 0.0;
+    Counters cnt = {0u, 0u, 0u, 0u, 0u, 0u};
+    bool bad = false;
+    const int lane = threadIdx.x & 31;
+    const int K = p.seg_cap;
+    const bool count_dl = sizeof(R) == 8 || p.s_end < (1 << 24);
+    const R dstep = (R)p.n_sub;
+    const int64_t warps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t base = (((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5) << 5; base < p.n_particles;
+         base += warps * 32) {
+        const int64_t i = base + lane;
+        const bool have = i < p.n_particles;
+        const R *rec = static_cast<const R *>(p.segs) + (size_t)(have ? i : 0) * K * kRecWords;
+        const R *th = static_cast<const R *>(p.seg_th) + (size_t)(have ? i : 0) * K;
+        Seg<R> cur, nxt;
+        R nth = (R)-1;
+        int k = 1, next_start = kNeverStart;
+        adj.start();
+        if (have) {
+            rec_get<R, OBS>(rec, cur);
+            rec_get<R, OBS>(rec + kRecWords, nxt);
+            next_start = nxt.s0;
+            nth = __ldg(th + 1);
+            adj.enter(__ldg(th));
+        } else {
+            cur.s0 = 0; cur.mode = 0; cur.doff = -1;
+            cur.A[0] = (R)INFINITY; cur.A[1] = cur.A[2] = cur.B[0] = cur.B[1] = cur.B[2] = (R)0;
+            cur.x[0] = (R)INFINITY; cur.x[1] = cur.x[2] = (R)0;
+        }
+        int so = p.n_sub;
+        R dl = (R)(so - cur.s0);
+        int64_t toff = p.time_stride;
+#pragma unroll 1
+        for (int j = 1; j <= p.n_obs; ++j, so += p.n_sub, toff += p.time_stride) {
+            if (so >= next_start) { // the next segment comes into force; load the one after it
+                do {
+                    cur = nxt;
+                    adj.enter(nth);
+                    ++k;
+                    rec_get<R, OBS>(rec + (size_t)k * kRecWords, nxt);
+                    nth = __ldg(th + k);
+                    next_start = nxt.s0;
+                } while (so >= next_start);
+                dl = (R)(so - cur.s0);
+            } else if (!count_dl) {
+                dl = (R)(so - cur.s0);
             }
-#pragma unroll
-            for (int q = 0; q < RTMC_MAX_PARAMS; ++q)
-                if (q < np) G[q] += A[q] * sa;
-            SAJ += saj;
-            if (j > p.n_obs || e > p.s_end) break;
-            const int kind = process_event(p, pid, s, cnt);
-            if ((int)s.k > p.max_events) { bad = true; break; }
-            if (!s.alive) break;
-            if (kind == 0) {
-                R f = s.th < (R)0 ? (R)0 : (s.th > (R)1 ? (R)1 : s.th);
-                f *= tmax;
-                int k = (int)f;
-                k = k > a.n_theta - 2 ? a.n_theta - 2 : k;
-                const R w = f - (R)k;
-#pragma unroll
-                for (int q = 0; q < RTMC_MAX_PARAMS; ++q) {
-                    if (q < np) {
-                        const R *t = dls + (size_t)q * a.n_theta + k;
-                        const R t0 = __ldg(t), t1 = __ldg(t + 1);
-                        A[q] += t0 + w * (t1 - t0) + (sizeof(R) == 4 ? (R)a.a_inc_f[q] : (R)a.a_inc[q]);
-                    }
+            int v;
+            if constexpr (C32) v = obs_offset_cart32(p, cur, dl, cur.doff);
+            else v = obs_offset_dl<R, OBS>(p, sedges, cur, dl);
+            dl += dstep;
+            if (v >= 0) {
+                const int64_t idx = toff + (cur.mode ? p.mode_stride : 0) + v;
+                if (idx < p.hist_len) {
+                    adj.observe(idx, j);
+                    cnt.obs++;
+                } else {
+                    bad = true;
                 }
             }
         }
+        if (have) adj.finish();
+    }
+    double g[kAdjRingParams];
 #pragma unroll
-        for (int q = 0; q < RTMC_MAX_PARAMS; ++q)
-            if (q < np) g[q] += (double)G[q] + a.b_obs[q] * (double)SAJ;
-    }
-    // block reduction in a fixed order: warp shuffles, then warp 0 over the warps
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int q = 0; q < RTMC_MAX_PARAMS; ++q) {
-        double v = g[q];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-        if (lane == 0) red[warp][q] = v;
-    }
-    __syncthreads();
-    if (threadIdx.x < RTMC_MAX_PARAMS && threadIdx.x < np) {
-        double v = 0.0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w][threadIdx.x];
-        a.partial[(size_t)blockIdx.x * np + threadIdx.x] = v;
-    }
-    const unsigned full = 0xffffffffu;
-    unsigned cv[6] = {cnt.scat, cnt.bnd, cnt.kill, cnt.absorb, cnt.obs, cnt.conv};
-#pragma unroll
-    for (int c = 0; c < 6; ++c) {
-        const unsigned t = __reduce_add_sync(full, cv[c]);
-        if (lane == 0 && t) atomicAdd(p.stats + c, (unsigned long long)t);
-    }
-    if (bad) atomicExch(p.status, 1);
+    for (int q = 0; q < kAdjRingParams; ++q) g[q] = adj.g[q];
+    adjoint_block_sums<kAdjRingParams>(p.stats, p.stats, p.status, a.n_params, g, red, a.partial, cnt, bad);
 }
 
 // Adjoint replay on the converged two-phase transport (at most kAdjRingParams
@@ -2003,6 +2137,18 @@ template <typename R> void *pick_adjoint_ring(int obs)
 {
     return obs == OBS_CART ? (void *)rt_adjoint_ring<R, OBS_CART>
                            : (obs == OBS_RADIAL ? (void *)rt_adjoint_ring<R, OBS_RADIAL> : (void *)rt_adjoint_ring<R, OBS_GENERAL>);
+}
+
+template <typename R> void *pick_observe_adj(int obs)
+{
+    return obs == OBS_CART ? (void *)rt_observe_adj<R, OBS_CART>
+                           : (obs == OBS_RADIAL ? (void *)rt_observe_adj<R, OBS_RADIAL> : (void *)rt_observe_adj<R, OBS_GENERAL>);
+}
+
+template <typename R> void *pick_adjoint_list(int obs)
+{
+    return obs == OBS_CART ? (void *)rt_adjoint_list<R, OBS_CART>
+                           : (obs == OBS_RADIAL ? (void *)rt_adjoint_list<R, OBS_RADIAL> : (void *)rt_adjoint_list<R, OBS_GENERAL>);
 }
 
 template <typename R> void *pick_adjoint(int obs)

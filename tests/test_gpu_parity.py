@@ -326,6 +326,23 @@ def test_gradient_replay_matches_oracle(precision):
         assert np.all(np.abs(g - go) <= 0.05 * scale), (g, go)
     g2, _ = get_context(0).gradient(P, prob.tables, dls, dlS, adj)
     assert np.array_equal(g, g2)  # fixed launch shape: reproducible bits
+    # the lockstep ring replay (schedule 0), and the split replay with 2 segments per
+    # particle (nearly every particle overflows and is replayed whole): the same sums
+    ctx = get_context(0)
+    tol = 1e-8 if precision == "fp64" else 1e-4
+    try:
+        ctx.set_schedule(0)
+        gr, str_ = ctx.gradient(P, prob.tables, dls, dlS, adj)
+        ctx.set_schedule(-1)
+        ctx.set_launch(0, 2, 0)
+        gs, sts = ctx.gradient(P, prob.tables, dls, dlS, adj)
+    finally:
+        ctx.set_schedule(-1)
+        ctx.set_launch(0, 0, 0)
+    for other, so in ((gr, str_), (gs, sts)):
+        assert so["device_status"] == 0
+        assert so["scatter_events"] == st["scatter_events"] and so["observations"] == st["observations"]
+        assert np.all(np.abs(other - g) <= tol * scale), (other, g)
     # five parameters take the one-particle-per-thread replay: the same numbers
     g5, _ = get_context(0).gradient(P, prob.tables, np.vstack([dls, dls[:1]]), np.append(dlS, dlS[0]), adj)
     tol = 1e-8 if precision == "fp64" else 1e-3
