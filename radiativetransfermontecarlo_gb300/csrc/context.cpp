@@ -388,7 +388,10 @@ void fill_params(rtmc_context *ctx, const rtmc_problem *P, const DevTables<R> &t
     if (P->frame == RTMC_FRAME_CARTESIAN) {
         bool ok = true;
         for (int a = 0; a < 3; ++a) ok = ok && (am[a] == RTMC_AXIS_IGNORED || finite_uniform[a]);
-        if (ok) p->obs_kind = 1;
+        if (ok) {
+            p->obs_kind = 1;
+            p->bin32 = sizeof(R) == 8 && p->s_end < (1 << 24) && (!ctx || ctx->opt_bin32) ? 1 : 0; // FP32 estimates
+        }
     } else if (am[1] == RTMC_AXIS_IGNORED && am[2] == RTMC_AXIS_IGNORED && am[0] != RTMC_AXIS_IGNORED &&
                finite_uniform[0]) {
         p->obs_kind = 2;
@@ -397,7 +400,7 @@ void fill_params(rtmc_context *ctx, const rtmc_problem *P, const DevTables<R> &t
                        (P->axis_edges[0][P->axis_nedges[0] - 1] - P->axis_edges[0][0]));
         p->r32_a0 = (float)p->ax_a0;
         // FP64: the observation kernel bins through an FP32 estimate (exact, see
-        // obs_offset_radial64) while sub-step offsets stay exact in FP32
+        // obs_offset_radial64 and obs_offset_cart64) while sub-step offsets stay exact in FP32
         p->bin32 = sizeof(R) == 8 && p->s_end < (1 << 24) && (!ctx || ctx->opt_bin32) ? 1 : 0;
     }
     p->time_stride = P->time_stride; p->mode_stride = P->mode_stride; p->hist_len = P->hist_len;
@@ -1243,7 +1246,8 @@ int gradient_run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t,
     // per thread
     const bool ring = sc->n_params <= kAdjointRingParams;
     // (schedules 0 and 1 of rtmc_set_schedule keep the ring replay)
-    if (ring && ctx->opt_event_major != 0 && ctx->opt_event_major != 1 && P->n_particles > 0)
+    if (ring && ctx->opt_event_major != 0 && ctx->opt_event_major != 1 && P->n_particles > 0 &&
+        P->hist_len < ((int64_t)1 << 31) && P->n_obs < (1 << 24))
         return gradient_split<R>(ctx, P, sc, p, a, n_edges, hb, sb, edges.size() + zoe.size(), grad, st);
     // FP32: 4 ring slots let 3 blocks share an SM (C5: 12.5 ms against 14.4 with 8 slots
     // and 2 blocks)

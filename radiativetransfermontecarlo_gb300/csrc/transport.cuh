@@ -878,14 +878,44 @@ __device__ __forceinline__ int obs_offset_cart32(const DevParams<double> &, cons
 struct SegF {
     float xf[3], Bf[3], sx, sb;
 };
-__device__ __forceinline__ void segf_from(const Seg<double> &g, SegF &f)
+// the segment in FP32: start position (radius-only) or start coordinates A (cartesian),
+// and the step
+template <int OBS> __device__ __forceinline__ void segf_from(const Seg<double> &g, SegF &f)
 {
+    const double *u = OBS == OBS_CART ? g.A : g.x;
 #pragma unroll
-    for (int a = 0; a < 3; ++a) { f.xf[a] = (float)g.x[a]; f.Bf[a] = (float)g.B[a]; }
+    for (int a = 0; a < 3; ++a) { f.xf[a] = (float)u[a]; f.Bf[a] = (float)g.B[a]; }
     f.sx = fabsf(f.xf[0]) + fabsf(f.xf[1]) + fabsf(f.xf[2]);
     f.sb = fabsf(f.Bf[0]) + fabsf(f.Bf[1]) + fabsf(f.Bf[2]);
 }
-__device__ __forceinline__ void segf_from(const Seg<float> &, SegF &) {}
+template <int OBS> __device__ __forceinline__ void segf_from(const Seg<float> &, SegF &) {}
+
+// FP64 cartesian binning through FP32 estimates, axis by axis: t' = A' + B' dl from the
+// segment's coordinates rounded to FP32 differs from the FP64 coordinate by at most
+// 2^-23 (|B| dl + |A| + |t'|) (two roundings to FP32, one multiply-add; the FP64 roundings
+// are far smaller), so M = 2^-21 (|B'| dl + |A'| + |t'|) bounds it.  An axis whose
+// interval t' -/+ M floors to one integer has that bin; if any axis is within M of an edge
+// the FP64 formula decides for the observation.  Axes a problem ignores have A = B = 0
+// and so M = 0.
+template <typename R>
+__device__ __forceinline__ int obs_offset_cart64(const DevParams<R> &p, const R *sedges, const Seg<R> &g, const SegF &f,
+                                                 R dl)
+{
+    if (g.doff < 0) return -1;
+    const float d = (float)dl; // exact: the estimate runs only while sub-steps stay below 2^24
+    int idx = g.doff;
+    bool ok = true;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        const float t = fmaf(f.Bf[a], d, f.xf[a]);
+        const float m = 0x1p-21f * (fmaf(fabsf(f.Bf[a]), d, fabsf(f.xf[a])) + fabsf(t));
+        const int bl = bin_floor(__fsub_rd(t, m)), bh = bin_floor(__fadd_ru(t, m));
+        if (bl != bh) return obs_offset_dl<R, OBS_CART>(p, sedges, g, dl); // near an edge: FP64 decides
+        ok = ok && (unsigned)bl < (unsigned)p.ax_nbe[a];
+        idx += bl * p.ax_stride32[a];
+    }
+    return ok ? idx : -1;
+}
 
 template <typename R>
 __device__ __forceinline__ int obs_offset_radial64(const DevParams<R> &p, const R *sedges, const Seg<R> &g, const SegF &f,
@@ -1026,6 +1056,13 @@ template <typename R> struct AdjLane {
         const R w = __ldg(wts + idx);
         sa += w;
         saj += w * (R)j;
+    }
+    // the same with a 32-bit index and the instant as a float
+    __device__ __forceinline__ void observe_f(int idx, R fj)
+    {
+        const R w = __ldg(wts + idx);
+        sa += w;
+        saj = m_fma(w, fj, saj);
     }
     // the particle's end
     __device__ __forceinline__ void finish()
@@ -1570,7 +1607,7 @@ __device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *se
     // needs no count or limit checks
     const R *rec = static_cast<const R *>(p.segs) + (size_t)(have ? i : 0) * p.seg_cap * kRecWords;
     constexpr bool C32 = sizeof(R) == 4 && OBS == OBS_CART;
-    constexpr bool R64 = sizeof(R) == 8 && OBS == OBS_RADIAL; // FP64 radius-only: FP32 estimate
+    constexpr bool R64 = sizeof(R) == 8 && (OBS == OBS_RADIAL || OBS == OBS_CART); // FP64: FP32 estimates
     Seg<R> cur, nxt;
     SegF cf; // the segment in force in FP32 (R64)
     int k = 1, next_start = kNeverStart;
@@ -1588,7 +1625,7 @@ __device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *se
     auto walk = [&](auto count_tag, auto est_tag) {
         constexpr bool CDL = decltype(count_tag)::value;
         constexpr bool EST = R64 && decltype(est_tag)::value;
-        if (EST) segf_from(cur, cf);
+        if (EST) segf_from<OBS>(cur, cf);
         const int s_last = p.n_obs * p.n_sub;
         const R dstep = (R)p.n_sub;
         int so = p.n_sub;
@@ -1606,14 +1643,15 @@ __device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *se
                     rec_get<R, OBS>(rec + (size_t)k * kRecWords, nxt);
                     next_start = nxt.s0;
                 } while (so >= next_start);
-                if (EST) segf_from(cur, cf);
+                if (EST) segf_from<OBS>(cur, cf);
                 dl = (R)(so - cur.s0);
             } else if (!CDL) {
                 dl = (R)(so - cur.s0);
             }
             int v;
             if constexpr (C32) v = obs_offset_cart32(p, cur, dl, cur.doff);
-            else if constexpr (EST) v = obs_offset_radial64(p, sedges, cur, cf, dl);
+            else if constexpr (EST && OBS == OBS_RADIAL) v = obs_offset_radial64(p, sedges, cur, cf, dl);
+            else if constexpr (EST) v = obs_offset_cart64(p, sedges, cur, cf, dl);
             else v = obs_offset_dl<R, OBS>(p, sedges, cur, dl);
             if (CDL) dl += dstep;
             if (INDEX) {
@@ -2036,9 +2074,13 @@ __global__ void __launch_bounds__(kAdjointThreads, sizeof(R) == 4 ? 4 : 2) rt_ob
         }
         int so = p.n_sub;
         R dl = (R)(so - cur.s0);
-        int64_t toff = p.time_stride;
+        // the weights' index fits 32 bits (the host takes this replay only then); j is also
+        // carried as a float, exact below 2^24
+        int toff = (int)p.time_stride;
+        const int tstep = (int)p.time_stride, mstep = (int)p.mode_stride, hlen = (int)p.hist_len;
+        R fj = (R)1;
 #pragma unroll 1
-        for (int j = 1; j <= p.n_obs; ++j, so += p.n_sub, toff += p.time_stride) {
+        for (int j = 1; j <= p.n_obs; ++j, so += p.n_sub, toff += tstep, fj += (R)1) {
             if (so >= next_start) { // the next segment comes into force; load the one after it
                 do {
                     cur = nxt;
@@ -2057,9 +2099,9 @@ __global__ void __launch_bounds__(kAdjointThreads, sizeof(R) == 4 ? 4 : 2) rt_ob
             else v = obs_offset_dl<R, OBS>(p, sedges, cur, dl);
             dl += dstep;
             if (v >= 0) {
-                const int64_t idx = toff + (cur.mode ? p.mode_stride : 0) + v;
-                if (idx < p.hist_len) {
-                    adj.observe(idx, j);
+                const int idx = toff + (cur.mode ? mstep : 0) + v;
+                if (idx < hlen) {
+                    adj.observe_f(idx, fj);
                     cnt.obs++;
                 } else {
                     bad = true;

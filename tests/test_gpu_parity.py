@@ -723,13 +723,18 @@ def test_time_blocked_fold_equals_slice_fold(index_mb, width):
     assert s1["observations"] == s2["observations"] == s3["observations"] == int(h1.sum() >> prob.hist_shift)
 
 
-@pytest.mark.parametrize("frame", ["spherical", "cylindrical2d"])
+@pytest.mark.parametrize("frame", ["spherical", "cylindrical2d", "cartesian"])
 def test_fp64_radial_estimate_gives_fp64_bins(frame):
-    """FP64 radius-only observations binned through the FP32 estimate (default) and wholly in
-    FP64 (rtmc_set_fp64_estimate(ctx, 0)) give the same histogram bit for bit: the estimate
-    decides only observations farther than its error bound from a bin edge.  Fine radial
-    bins (0.01 wide) put many observations near edges."""
-    if frame == "spherical":
+    """FP64 radius-only and cartesian observations binned through FP32 estimates (default)
+    and wholly in FP64 (rtmc_set_fp64_estimate(ctx, 0)) give the same histogram bit for
+    bit: an estimate decides only observations farther than its error bound from a bin
+    edge.  Fine radial bins (0.01 wide) put many observations near edges; the cartesian
+    case is the 3D elastic grid (4 axes, index path)."""
+    if frame == "cartesian":
+        geo, src, mat, obs, opts = W.c2_elastic3d(t_end=1.0)
+        src = dict(src, numberParticles=200_000)
+        opts = dict(opts, precision="fp64")
+    elif frame == "spherical":
         geo, src, mat, obs, opts = W.c1_acoustic3d(n=200_000, precision="fp64")
         obs = dict(obs, x=colon(0, 0.01, 6))
     else:
