@@ -641,9 +641,11 @@ def run_c5(args):
     mat.Q = 400
     params = ("lc", "cv_kappa", "cv_rho", "Q", "mfp")
     o = dict(o, seed=5)
-    if args.block or args.ring or args.index_mb:
+    if args.block or args.ring or args.index_mb or args.schedule >= 0:
         from radiativetransfermontecarlo_gb300 import get_context
         get_context(0).set_launch(args.block, args.ring, args.index_mb)
+        if args.schedule >= 0:  # 0 or 1: the lockstep ring replay; 2: the split replay
+            get_context(0).set_schedule(args.schedule)
     for _ in range(args.warmup):
         A.radiativeTransferGradient(geo, src, mat, obs, Et, params, o)
     fwd, adj, wall, ev = [], [], [], 0
