@@ -453,14 +453,24 @@ inline int64_t index_row_stride(int64_t particles) { return (particles + 31) / 3
 // First slice (1-based) of copy group g in [0, kCopyGroups]; g = kCopyGroups gives n_obs + 1.
 // The first group is small (1/25 of the slices), so the first copy starts soon after the
 // transport; the fold outruns the host link, so later copies follow back to back.
-// First t-block of copy group g of the time-blocked fold (g = kCopyGroups gives ntb), with
-// the same proportions as copy_group_start.
-int tb_group_start(int ntb, int g)
+// Copy groups of the time-blocked fold: t-blocks [b[g], b[g + 1]), growing 1, 2, 3, ... up
+// to max(9, ntb / 16) t-blocks (at most 23 groups).  The early t-blocks fold slowest (most particles are in
+// the grid) and the host link is the bottleneck from the second group on, so small first
+// groups start the copies early and keep the link busy: modelled on the 3D elastic
+// workload's measured per-t-block fold times, 19.0 ms from the end of the transport to the
+// last copy, against 21.1 with 5 groups of which the first held 1/25 of the slices.
+int tb_groups(int ntb, int *b)
 {
-    if (g <= 0) return 0;
-    if (g >= kCopyGroups) return ntb;
-    const int first = std::max(1, ntb / 25);
-    return first + (int)((int64_t)(ntb - first) * (g - 1) / (kCopyGroups - 1));
+    const int cap = std::max(9, (ntb + 15) / 16);
+    int n = 0, t = 0, size = 1;
+    b[0] = 0;
+    while (t < ntb && n < 23) {
+        t = std::min(ntb, t + size);
+        b[++n] = t;
+        size = std::min(size + 1, cap);
+    }
+    if (t < ntb) b[n] = ntb; // the last group takes the rest
+    return n;
 }
 
 int copy_group_start(int n_obs, int g)
@@ -846,12 +856,13 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
             // group's slices are final, so their copy runs on the second stream while the
             // next group folds
             const bool groups = last && (host_out || host_u32) && ntb >= 2 * kCopyGroups && ensure_pipeline(ctx) == 0;
-            const int ng = groups ? kCopyGroups : 1;
+            int gb_[25];
+            const int ng = groups ? tb_groups(ntb, gb_) : 1;
             const int64_t ts = P->time_stride;
             // one fold launch and one conversion: the conversion is timed apart
             timed_convert = last && !groups && !roll && ntb <= 65535;
             for (int g = 0; g < ng && !le; ++g) {
-                const int ga = groups ? tb_group_start(ntb, g) : 0, gb = groups ? tb_group_start(ntb, g + 1) : ntb;
+                const int ga = groups ? gb_[g] : 0, gb = groups ? gb_[g + 1] : ntb;
                 if (gb <= ga) continue;
                 // a rolling accumulator takes `roll` t-blocks at a time and is zeroed again by
                 // their conversion; the full one takes the group at once
