@@ -550,9 +550,10 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
     }
 
     // Sink: the whole histogram in shared memory when it fits beside a segment ring of at
-    // least 2 slots per lane at 512 threads; otherwise a dense index array folded slice
-    // by slice (rt_bin_slices), or plain global 64-bit atomics when the index array is
-    // switched off or does not fit.
+    // least 2 slots per lane at 512 threads; otherwise, for histograms larger than the L2,
+    // a dense index array folded afterwards (time-blocked FP32, or slice by slice with
+    // rt_bin_slices), or plain global 64-bit atomics when the histogram stays in the L2 or
+    // the index array is switched off or does not fit.
     const size_t edge_smem = align_up((size_t)n_edges * sizeof(R), 16);
     const size_t hist_smem = align_up((size_t)P->hist_len * sizeof(uint32_t), 16);
     const size_t seg_bytes = 6 * sizeof(R) + 2 * sizeof(int32_t);
