@@ -354,7 +354,9 @@ __global__ void __launch_bounds__(kConvThreads) rt_tb_convert(const TbParams t, 
         for (int r = 0; r < 4; ++r) {
             const int j = 4 * tb + r + 1;
             if (j > t.n_obs) break;
-            const unsigned long long v = (unsigned long long)cv[r];
+            // counts are exact integers below 2^24: a 32-bit conversion (the 64-bit one runs
+            // on the FP64 pipe, which then bounds the kernel next to DRAM)
+            const unsigned long long v = (unsigned long long)__float2uint_rz(cv[r]);
             __stcs(hist + (int64_t)j * time_stride + off, v << shift);
             if (u32) __stcs(u32 + (int64_t)j * time_stride + off, (uint32_t)v);
         }

@@ -899,10 +899,10 @@ template <int OBS> __device__ __forceinline__ void segf_from(const Seg<float> &,
 // and so M = 0.
 template <typename R>
 __device__ __forceinline__ int obs_offset_cart64(const DevParams<R> &p, const R *sedges, const Seg<R> &g, const SegF &f,
-                                                 R dl)
+                                                 float d)
 {
+    // d, the sub-steps since the segment start, is an exact integer (below 2^24 here)
     if (g.doff < 0) return -1;
-    const float d = (float)dl; // exact: the estimate runs only while sub-steps stay below 2^24
     int idx = g.doff;
     bool ok = true;
 #pragma unroll
@@ -910,7 +910,7 @@ __device__ __forceinline__ int obs_offset_cart64(const DevParams<R> &p, const R 
         const float t = fmaf(f.Bf[a], d, f.xf[a]);
         const float m = 0x1p-21f * (fmaf(fabsf(f.Bf[a]), d, fabsf(f.xf[a])) + fabsf(t));
         const int bl = bin_floor(__fsub_rd(t, m)), bh = bin_floor(__fadd_ru(t, m));
-        if (bl != bh) return obs_offset_dl<R, OBS_CART>(p, sedges, g, dl); // near an edge: FP64 decides
+        if (bl != bh) return obs_offset_dl<R, OBS_CART>(p, sedges, g, (R)d); // near an edge: FP64 decides
         ok = ok && (unsigned)bl < (unsigned)p.ax_nbe[a];
         idx += bl * p.ax_stride32[a];
     }
@@ -919,10 +919,10 @@ __device__ __forceinline__ int obs_offset_cart64(const DevParams<R> &p, const R 
 
 template <typename R>
 __device__ __forceinline__ int obs_offset_radial64(const DevParams<R> &p, const R *sedges, const Seg<R> &g, const SegF &f,
-                                                   R dl)
+                                                   float d)
 {
+    // d, the sub-steps since the segment start, is an exact integer (below 2^24 here)
     if (g.doff < 0) return -1;
-    const float d = (float)dl; // exact: the estimate runs only while sub-steps stay below 2^24
     const float x0 = fmaf(f.Bf[0], d, f.xf[0]), x1 = fmaf(f.Bf[1], d, f.xf[1]);
     float r2 = fmaf(x1, x1, x0 * x0);
     if (p.radial_3d) {
@@ -933,7 +933,7 @@ __device__ __forceinline__ int obs_offset_radial64(const DevParams<R> &p, const 
     const float t = fmaf(r, p.r32_iw, p.r32_a0);
     const float m = 0x1p-19f * (fmaf(fmaf(f.sb, d, f.sx) + r, p.r32_iw, fabsf(p.r32_a0) + fabsf(t)) + 1.f);
     const int bl = bin_floor(__fsub_rd(t, m)), bh = bin_floor(__fadd_ru(t, m));
-    if (bl != bh) return obs_offset_dl<R, OBS_RADIAL>(p, sedges, g, dl); // near an edge: FP64 decides
+    if (bl != bh) return obs_offset_dl<R, OBS_RADIAL>(p, sedges, g, (R)d); // near an edge: FP64 decides
     return (unsigned)bl < (unsigned)p.ax_nbe[0] ? g.doff + bl * p.ax_stride32[0] : -1;
 }
 
@@ -1627,9 +1627,12 @@ __device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *se
         constexpr bool EST = R64 && decltype(est_tag)::value;
         if (EST) segf_from<OBS>(cur, cf);
         const int s_last = p.n_obs * p.n_sub;
-        const R dstep = (R)p.n_sub;
+        // FP64 with the FP32 estimates carries the offset as a float (an exact integer:
+        // sub-steps stay below 2^24 there), so no FP64 instruction runs per instant
+        using D = typename std::conditional<EST, float, R>::type;
+        const D dstep = (D)p.n_sub;
         int so = p.n_sub;
-        R dl = (R)(so - cur.s0);
+        D dl = (D)(so - cur.s0);
         // every lane of a warp owns a column of the index array (rows are padded to 32
         // particles), so lanes past the last particle store their -1 there unconditionally
         int32_t *optr = INDEX ? p.obs_idx + col : nullptr;
@@ -1644,9 +1647,9 @@ __device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *se
                     next_start = nxt.s0;
                 } while (so >= next_start);
                 if (EST) segf_from<OBS>(cur, cf);
-                dl = (R)(so - cur.s0);
+                dl = (D)(so - cur.s0);
             } else if (!CDL) {
-                dl = (R)(so - cur.s0);
+                dl = (D)(so - cur.s0);
             }
             int v;
             if constexpr (C32) v = obs_offset_cart32(p, cur, dl, cur.doff);
