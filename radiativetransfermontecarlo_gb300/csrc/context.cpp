@@ -730,11 +730,11 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
     }
     // the clear: fused into the first rt_events launch of a split run (the FP32 accumulator
     // of the time-blocked fold, else the histogram), else one memset ahead of the transport.
-    // Measured on the 3D elastic workload: the fused clear of the 3.47 GB accumulator costs
-    // rt_events 0.28 of 2.36 ms; a memset on the second stream during the transport cost it
-    // 0.22 ms and the fold 0.4 ms (its blocks take SM slots from both kernels), and
-    // device-to-device copies from a zero buffer on the copy engines slowed rt_observe by
-    // 0.15 ms.
+    // Measured on the 3D elastic workload (rt_events 2.37 ms with the fused clear of the
+    // 3.47 GB accumulator): a memset on the second stream during the transport cost
+    // rt_events 0.22 ms and the fold 0.4 ms (its blocks take SM slots from both kernels);
+    // device-to-device copies from a zero buffer on the copy engines saved rt_events 0.02 ms
+    // and cost rt_observe 0.15 ms.
     unsigned long long *to_clear = use_tb ? static_cast<unsigned long long *>(ctx->tbacc.p)
                                           : static_cast<unsigned long long *>(ctx->hist.p);
     const int64_t clear_words = use_tb ? (int64_t)(roll ? roll : ntb) * tpl.S * 2 : P->hist_len;
