@@ -291,8 +291,15 @@ typedef struct rtmc_batch rtmc_batch;
 int rtmc_batch_create(rtmc_context *ctx, int32_t n, const rtmc_problem *problems, const rtmc_tables *const *tables,
                       rtmc_batch **out);
 
-/* Launch shape (0 = automatic): threads per block, ring capacity, particles per work
- * item.  Rebuilds the work list and the graph, keeps the staged tables. */
+/* Launch shape of the lockstep instances: threads per block (0: 512), ring capacity
+ * (0: 8) and particles per work item (0: automatic) of the ring kernel
+ * (rt_transport_batch).  block = 0 with ring_cap = -1 selects the split kernel instead
+ * (rt_transport_batch_split): per work item, the events of its particles into
+ * device-memory segment records, then the observations of 32 particles per warp in
+ * lockstep.  Its segment records per particle follow the instance's expected events, or
+ * the context's ring capacity (rtmc_set_launch) when one was set at rtmc_batch_create;
+ * particles with more are run whole at once.  Rebuilds the work list and the graph,
+ * keeps the staged tables. */
 int rtmc_batch_set_launch(rtmc_batch *batch, int32_t block, int32_t ring_cap, int64_t chunk);
 
 /* One replay of the graph; histograms stay on the device.  stats sums all instances. */

@@ -93,20 +93,20 @@ class Batch:
             pass
 
 
-def autotune(batch: Batch, blocks=(256, 512), rings=(4, 8), chunks=(4096, 16384, 65536), repeats: int = 2):
+def autotune(batch: Batch, blocks=(256, 512), rings=(4, 8), chunks=(4096, 16384, 65536),
+             split_chunks=(2048, 4096, 8192), repeats: int = 2):
     """Time every launch shape of the grid on the batch itself and keep the fastest
-    (block, ring capacity, particles per work item).  Returns (best shape, {shape: ms})."""
+    (block, ring capacity, particles per work item); (0, -1, chunk) is the split kernel.
+    Returns (best shape, {shape: ms})."""
+    shapes = [(0, -1, c) for c in split_chunks] + [(b, r, c) for b in blocks for r in rings for c in chunks]
     times = {}
-    for b in blocks:
-        for r in rings:
-            for c in chunks:
-                try:
-                    batch.set_launch(b, r, c)
-                except _lib.RtmcError:
-                    continue
-                batch.run()  # warm-up
-                best = min(batch.run()["kernel_ms"] for _ in range(repeats))
-                times[(b, r, c)] = best
+    for shape in shapes:
+        try:
+            batch.set_launch(*shape)
+        except _lib.RtmcError:
+            continue
+        batch.run()  # warm-up
+        times[shape] = min(batch.run()["kernel_ms"] for _ in range(repeats))
     shape = min(times, key=times.get)
     batch.set_launch(*shape)
     return shape, times

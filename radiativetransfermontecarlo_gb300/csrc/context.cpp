@@ -1831,6 +1831,9 @@ struct rtmc_batch {
     int n = 0, prec = RTMC_FP32, obs_kind = 0, n_obs = 0;
     int block = 0, ring = 0, grid = 0, n_items = 0;
     int grid_em = 0, n_items_em = 0; // event-heavy instances, one particle per thread
+    int split = 0;                   // lockstep instances on the split kernel (0: the ring kernel)
+    int kmax = 0;                    // the largest seg_cap of the lockstep instances
+    DevBuf scratch;                  // the split kernel's per-block segment records
     int64_t chunk = 0, hist_len = 0;
     size_t smem = 0, smem_em = 0;
     DevBuf params, items, items_em, tabs, edges, hists, ctl;
@@ -1871,20 +1874,37 @@ template <typename R> int batch_build_graph(rtmc_batch *b)
     const size_t seg_bytes = 6 * sizeof(R) + 2 * sizeof(int32_t);
     const size_t fixed = align_up((size_t)b->n_edges * sizeof(R), 16) + align_up((size_t)b->hist_len * 4, 16);
     const size_t budget = (size_t)ctx->max_smem_optin - 1024 - sizeof(DevParams<R>) - 64;
-    int block = b->block ? b->block : 512;
-    if (block > 512) block = 512;
-    if (fixed + (size_t)block * 2 * seg_bytes > budget) block = 256;
-    if (fixed + (size_t)block * 2 * seg_bytes > budget)
-        return fail(&ctx->err, RTMC_ERR_ARG, "batched runs need a histogram that fits in shared memory");
-    int ring = b->ring ? b->ring : 8;
-    ring = std::min<int>(ring, (int)((budget - fixed) / ((size_t)block * seg_bytes)));
-    b->smem = fixed + (size_t)block * ring * seg_bytes;
+    int block, ring = 0;
+    int64_t chunk;
     int bps = 0;
-    if (transport_batch_setup(b->prec, b->obs_kind, block, b->smem, &bps) != 0 || bps < 1)
-        return fail(&ctx->err, RTMC_ERR_CUDA, "batched transport kernel does not fit on the device");
-    b->grid = ctx->num_sms * bps;
+    if (b->split) {
+        // the split kernel: 1024 threads, the histogram alone in shared memory, segment
+        // records of one work item per block in device memory
+        block = kBatchSplitThreads;
+        if (fixed > budget) return fail(&ctx->err, RTMC_ERR_ARG, "batched runs need a histogram that fits in shared memory");
+        b->smem = fixed;
+        chunk = b->chunk ? b->chunk : 4096;
+        if (transport_batch_setup(b->prec, b->obs_kind, block, b->smem, &bps, 1) != 0 || bps < 1)
+            return fail(&ctx->err, RTMC_ERR_CUDA, "batched transport kernel does not fit on the device");
+        b->grid = ctx->num_sms * bps;
+        const int64_t stride = chunk * std::max(1, b->kmax) * 8;
+        if (b->scratch.grow((size_t)b->grid * stride * sizeof(R)))
+            return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for batched segment records failed");
+    } else {
+        block = b->block ? b->block : 512;
+        if (block > 512) block = 512;
+        if (fixed + (size_t)block * 2 * seg_bytes > budget) block = 256;
+        if (fixed + (size_t)block * 2 * seg_bytes > budget)
+            return fail(&ctx->err, RTMC_ERR_ARG, "batched runs need a histogram that fits in shared memory");
+        ring = b->ring > 0 ? b->ring : 8;
+        ring = std::min<int>(ring, (int)((budget - fixed) / ((size_t)block * seg_bytes)));
+        b->smem = fixed + (size_t)block * ring * seg_bytes;
+        if (transport_batch_setup(b->prec, b->obs_kind, block, b->smem, &bps, 0) != 0 || bps < 1)
+            return fail(&ctx->err, RTMC_ERR_CUDA, "batched transport kernel does not fit on the device");
+        b->grid = ctx->num_sms * bps;
+        chunk = b->chunk ? b->chunk : 8192;
+    }
     // work items: chunks of each instance, largest expected cost first
-    const int64_t chunk = b->chunk ? b->chunk : 8192;
     // two work lists: lockstep-batch instances (shared-memory histogram kernel) and
     // event-heavy instances (event-major kernel), each sorted by expected cost
     std::vector<BatchItem> sorted, sorted_em;
@@ -1938,6 +1958,8 @@ template <typename R> int batch_build_graph(rtmc_batch *b)
     a->edges = static_cast<const R *>(b->edges.p);
     a->n_edges = b->n_edges;
     a->obs_kind = b->obs_kind;
+    a->scratch = b->split ? b->scratch.p : nullptr;
+    a->scratch_stride = b->split ? chunk * std::max(1, b->kmax) * 8 : 0;
     auto *ae = static_cast<BatchArgs<R> *>(b->args_em_host);
     *ae = *a;
     ae->items = static_cast<const BatchItem *>(b->items_em.p);
@@ -1948,8 +1970,8 @@ template <typename R> int batch_build_graph(rtmc_batch *b)
     cudaMemsetAsync(b->ctl.p, 0, 256, ctx->stream);
     int le = 0;
     if (b->n_items) {
-        if constexpr (sizeof(R) == 4) le = launch_transport_batch_f32(*a, b->grid, block, b->smem, ctx->stream);
-        else le = launch_transport_batch_f64(*a, b->grid, block, b->smem, ctx->stream);
+        if constexpr (sizeof(R) == 4) le = launch_transport_batch_f32(*a, b->grid, block, b->smem, ctx->stream, b->split);
+        else le = launch_transport_batch_f64(*a, b->grid, block, b->smem, ctx->stream, b->split);
     }
     if (!le && b->n_items_em) {
         if constexpr (sizeof(R) == 4) le = launch_transport_batch_em_f32(*ae, b->grid_em, 256, b->smem_em, ctx->stream);
@@ -1959,7 +1981,7 @@ template <typename R> int batch_build_graph(rtmc_batch *b)
     if (le) return cuda_fail(ctx, (cudaError_t)le, "batched launch capture");
     if (e != cudaSuccess) return cuda_fail(ctx, e, "graph capture");
     CK(cudaGraphInstantiate(&b->exec, b->graph, 0), "graph instantiate");
-    b->block = block;
+    b->block = b->split ? 0 : block;
     b->ring = ring;
     b->chunk = chunk;
     return RTMC_OK;
@@ -2009,6 +2031,15 @@ int batch_create(rtmc_context *ctx, int n, const rtmc_problem *P, const rtmc_tab
         b->cost_per_particle[i] = P[i].n_obs + 4.0 * rate * P[i].h * P[i].n_sub * P[i].n_obs;
         if (i == 0) b->obs_kind = params[0].obs_kind;
         b->event_major[i] = params[i].event_major;
+        // the split kernel's segment records per particle: as for rtmc_forward's split schedule
+        const double mean = rate * P[i].h * (double)P[i].n_sub * (double)P[i].n_obs;
+        int K = (int)std::ceil(1.0 + mean + 4.0 * std::sqrt(mean) + 4.0);
+        K = std::min(64, std::max(8, (K + 3) / 4 * 4));
+        if (ctx->opt_ring) K = ctx->opt_ring; // the context's ring capacity, when one is set
+        K = std::max(1, K) + 2;
+        params[i].seg_cap = K;
+        params[i].split = 1;
+        if (!params[i].event_major) b->kmax = std::max(b->kmax, K);
     }
     CK(cudaMemcpy(b->tabs.p, host.data(), total, cudaMemcpyHostToDevice), "batched tables");
     if (b->edges.grow(std::max<size_t>(1, edges.size()) * sizeof(R)) || b->params.grow((size_t)n * sizeof(DevParams<R>)) ||
@@ -2055,10 +2086,14 @@ extern "C" int rtmc_batch_create(rtmc_context *ctx, int32_t n, const rtmc_proble
 extern "C" int rtmc_batch_set_launch(rtmc_batch *b, int32_t block, int32_t ring_cap, int64_t chunk)
 {
     if (!b) return fail(nullptr, RTMC_ERR_ARG, "rtmc_batch_set_launch: NULL batch");
-    if (block < 0 || block > 512 || block % 32 || ring_cap < 0 || ring_cap == 1 || ring_cap > 64 || chunk < 0)
-        return fail(&b->ctx->err, RTMC_ERR_ARG, "rtmc_batch_set_launch: block <= 512 (multiple of 32), ring 0 or 2..64, chunk >= 0");
+    const bool split = ring_cap == -1;
+    if (block < 0 || block > 512 || block % 32 || ring_cap < -1 || ring_cap == 1 || ring_cap > 64 || chunk < 0 ||
+        (split && block != 0))
+        return fail(&b->ctx->err, RTMC_ERR_ARG,
+                    "rtmc_batch_set_launch: block <= 512 (multiple of 32) with ring 0 or 2..64, or block 0 with ring -1; chunk >= 0");
     rtmc_context *ctx = b->ctx;
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    b->split = split ? 1 : 0;
     b->block = block;
     b->ring = ring_cap;
     b->chunk = chunk;
@@ -2132,6 +2167,7 @@ extern "C" void rtmc_batch_destroy(rtmc_batch *b)
     b->edges.release();
     b->hists.release();
     b->ctl.release();
+    b->scratch.release();
     for (void *h : {b->args_host, b->args_em_host}) {
         if (!h) continue;
         if (b->prec == RTMC_FP64) delete static_cast<BatchArgs<double> *>(h);

@@ -33,17 +33,18 @@ void *RTMC_NAME(kernel_of_split)(int kind, int sink, int obs)
     return kind == 5 ? pick_events<RTMC_REAL>(obs) : (kind == 6 ? pick_observe<RTMC_REAL>(sink, obs) : pick_list<RTMC_REAL>(sink, obs));
 }
 #elif RTMC_PART == 2
-int RTMC_NAME(launch_transport_batch)(const BatchArgs<RTMC_REAL> &a, int grid, int block, size_t smem, void *stream)
+int RTMC_NAME(launch_transport_batch)(const BatchArgs<RTMC_REAL> &a, int grid, int block, size_t smem, void *stream,
+                                      int split)
 {
-    return launch_batch_t<RTMC_REAL>(a, grid, block, smem, stream, false);
+    return launch_batch_t<RTMC_REAL>(a, grid, block, smem, stream, split ? 2 : 0);
 }
 
 int RTMC_NAME(launch_transport_batch_em)(const BatchArgs<RTMC_REAL> &a, int grid, int block, size_t smem, void *stream)
 {
-    return launch_batch_t<RTMC_REAL>(a, grid, block, smem, stream, true);
+    return launch_batch_t<RTMC_REAL>(a, grid, block, smem, stream, 1);
 }
 
-void *RTMC_NAME(kernel_of_batch)(int em, int obs) { return em ? pick_batch_em<RTMC_REAL>(obs) : pick_batch<RTMC_REAL>(obs); }
+void *RTMC_NAME(kernel_of_batch)(int which, int obs) { return pick_batch_kind<RTMC_REAL>(which, obs); }
 #elif RTMC_PART == 3
 int RTMC_NAME(launch_adjoint)(const DevParams<RTMC_REAL> &p, const AdjointArgs &a, int grid, int block, size_t smem,
                               void *stream)

@@ -175,6 +175,12 @@ struct BatchItem {
     int64_t first, count;
 };
 
+// Threads per block of rt_transport_batch_split (one block per SM).
+#ifndef RTMC_BATCH_SPLIT_THREADS
+#define RTMC_BATCH_SPLIT_THREADS 512
+#endif
+constexpr int kBatchSplitThreads = RTMC_BATCH_SPLIT_THREADS;
+
 template <typename R> struct BatchArgs {
     const DevParams<R> *params; // per instance (device)
     const BatchItem *items;     // sorted by expected cost, largest first
@@ -186,6 +192,9 @@ template <typename R> struct BatchArgs {
     int32_t n_edges, obs_kind;
     unsigned long long *stats;  // [8]
     int32_t *status;
+    // rt_transport_batch_split: each block's segment records for one work item
+    void *scratch;              // [gridDim.x][scratch_stride] in R
+    int64_t scratch_stride;     // R values per block: work-item size x the largest seg_cap x 8
 };
 
 // Score-function adjoint replay (rt_adjoint): the per-particle score of parameter q up to
@@ -237,8 +246,9 @@ void *kernel_of_split_f64(int kind, int sink, int obs);
 // rerun (7) variant; kernel_set_smem sets its dynamic shared-memory limit.
 void *kernel_of_transport_f32(int sink, int obs);
 void *kernel_of_transport_f64(int sink, int obs);
-void *kernel_of_batch_f32(int em, int obs);
-void *kernel_of_batch_f64(int em, int obs);
+// which: 0 rt_transport_batch, 1 rt_transport_batch_em, 2 rt_transport_batch_split
+void *kernel_of_batch_f32(int which, int obs);
+void *kernel_of_batch_f64(int which, int obs);
 // which: 0 rt_adjoint, 1 rt_adjoint_ring, 2 rt_observe_adj, 3 rt_adjoint_list
 void *kernel_of_adjoint_f32(int which, int obs);
 void *kernel_of_adjoint_f64(int which, int obs);
@@ -278,9 +288,10 @@ inline bool may_exceed_int64(const rtmc_problem *P)
 {
     return P->hist_shift >= 1 && P->n_particles >= ((int64_t)1 << (63 - P->hist_shift));
 }
-int launch_transport_batch_f32(const BatchArgs<float> &a, int grid, int block, size_t smem, void *stream);
-int launch_transport_batch_f64(const BatchArgs<double> &a, int grid, int block, size_t smem, void *stream);
-int transport_batch_setup(int precision, int obs, int block, size_t smem, int *blocks_per_sm);
+// split: the split kernel (rt_transport_batch_split) instead of the lockstep ring kernel
+int launch_transport_batch_f32(const BatchArgs<float> &a, int grid, int block, size_t smem, void *stream, int split);
+int launch_transport_batch_f64(const BatchArgs<double> &a, int grid, int block, size_t smem, void *stream, int split);
+int transport_batch_setup(int precision, int obs, int block, size_t smem, int *blocks_per_sm, int split);
 int launch_transport_batch_em_f32(const BatchArgs<float> &a, int grid, int block, size_t smem, void *stream);
 int launch_transport_batch_em_f64(const BatchArgs<double> &a, int grid, int block, size_t smem, void *stream);
 int transport_batch_em_setup(int precision, int obs, int block, size_t smem, int *blocks_per_sm);

@@ -1593,19 +1593,20 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 4 : 2) rt_events(const D
 // offset is carried as a float counter while it stays an exact integer (below 2^24).
 template <typename R, int SINK, int OBS>
 __device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *sedges, unsigned *shist, int64_t base,
-                                              Counters &cnt, bool &bad)
+                                              Counters &cnt, bool &bad, const R *segs_in = nullptr, int64_t n_in = -1)
 {
+    // segs_in / n_in: another record array and particle count (a batch block's work item)
     constexpr bool SMEM = SINK == SINK_SMEM;
     constexpr bool INDEX = SINK == SINK_INDEX;
     const int lane = threadIdx.x & 31;
     const unsigned long long inc = 1ull << p.hist_shift;
     const int64_t col = base + lane; // the lane's column of the index array
-    const bool have = col < p.n_particles;
+    const bool have = col < (n_in >= 0 ? n_in : p.n_particles);
     const int64_t i = have && p.perm ? (int64_t)__ldg(p.perm + col) : col; // its particle
     // record k (in cur) is in force and record k + 1 waits in nxt; every particle's list
     // ends in records that bin nothing and never end (rec_put_end), so a change of segment
     // needs no count or limit checks
-    const R *rec = static_cast<const R *>(p.segs) + (size_t)(have ? i : 0) * p.seg_cap * kRecWords;
+    const R *rec = (segs_in ? segs_in : static_cast<const R *>(p.segs)) + (size_t)(have ? i : 0) * p.seg_cap * kRecWords;
     constexpr bool C32 = sizeof(R) == 4 && OBS == OBS_CART;
     constexpr bool R64 = sizeof(R) == 8 && (OBS == OBS_RADIAL || OBS == OBS_CART); // FP64: FP32 estimates
     Seg<R> cur, nxt;
@@ -1865,6 +1866,131 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2) rt_transport_batc
             run_particle<R, SINK_GLOBAL, OBS>(sp, sedges, nullptr, i, cnt, bad);
     }
     const unsigned full = 0xffffffffu;
+    unsigned v[6] = {cnt.scat, cnt.bnd, cnt.kill, cnt.absorb, cnt.obs, cnt.conv};
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+        const unsigned t = __reduce_add_sync(full, v[c]);
+        if (lane == 0 && t) atomicAdd(a.stats + c, (unsigned long long)t);
+    }
+    if (bad) atomicExch(a.status, 1);
+}
+
+// Batched transport of the lockstep instances on the split schedule, inside one persistent
+// launch: for each work item a block first runs its particles' events (a thread a particle
+// at a time, new particles started by 16 lanes together as in rt_events), writing the
+// prepared segment records to the block's scratch; after a barrier its warps walk the
+// observation instants of 32 particles each in lockstep (observe_batch) into the
+// instance's shared-memory histogram.  A particle with more segments than the instance's
+// seg_cap - 2 gets end records and is run whole at once (run_particle).
+template <typename R, int OBS>
+__global__ void __launch_bounds__(kBatchSplitThreads, 1) rt_transport_batch_split(const BatchArgs<R> a)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ DevParams<R> sp;
+    __shared__ int s_item;
+    R *sedges = reinterpret_cast<R *>(smem_raw);
+    const size_t off = (((size_t)a.n_edges * sizeof(R) + 15) / 16) * 16;
+    unsigned *shist = reinterpret_cast<unsigned *>(smem_raw + off);
+    R *scratch = static_cast<R *>(a.scratch) + (size_t)blockIdx.x * a.scratch_stride;
+    const int T = blockDim.x;
+    for (int k = threadIdx.x; k < a.n_edges; k += T) sedges[k] = a.edges[k];
+    for (int64_t k = threadIdx.x; k < a.hist_len; k += T) shist[k] = 0u;
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = T >> 5;
+    Counters cnt = {0u, 0u, 0u, 0u, 0u, 0u};
+    bool bad = false;
+    int cur = -1; // instance held in shared memory
+    auto flush = [&](int inst) {
+        unsigned long long *h = a.hists + (int64_t)inst * a.hist_len;
+        const int sh = sp.hist_shift;
+        for (int64_t k = threadIdx.x; k < a.hist_len; k += T) {
+            const unsigned c = shist[k];
+            if (c) {
+                atomicAdd(h + k, (unsigned long long)c << sh);
+                shist[k] = 0u;
+            }
+        }
+    };
+    for (;;) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_item = atomicAdd(a.counter, 1);
+        __syncthreads();
+        const int it = s_item;
+        if (it >= a.n_items) break;
+        const BatchItem bi = a.items[it];
+        if (bi.inst != cur) {
+            if (cur >= 0) flush(cur);
+            __syncthreads();
+            const uint32_t *src = reinterpret_cast<const uint32_t *>(a.params + bi.inst);
+            uint32_t *dst = reinterpret_cast<uint32_t *>(&sp);
+            for (int k = threadIdx.x; k < (int)(sizeof(DevParams<R>) / 4); k += T) dst[k] = src[k];
+            cur = bi.inst;
+            __syncthreads();
+        }
+        const int K = sp.seg_cap;
+        const int64_t n = bi.count;
+        // ---- events: local particle li (global bi.first + li) into scratch[li][K][8]
+        {
+            int64_t li = threadIdx.x;
+            bool have = false;
+            int nseg = 0;
+            Part<R> s;
+            Seg<R> g;
+            Counters c0 = cnt;
+            for (;;) {
+                const bool idle = !have && li < n;
+                const unsigned idle_mask = __ballot_sync(full, idle), busy_mask = __ballot_sync(full, have);
+                if (!(idle_mask | busy_mask)) break;
+                const uint64_t pid = (uint64_t)(sp.pid0 + bi.first + li);
+                if (idle && (__popc(idle_mask) >= kEventStartLanes || !busy_mask)) {
+                    init_particle(sp, pid, s);
+                    c0 = cnt;
+                    seg_from(s, g);
+                    seg_prepare<R, OBS>(sp, sedges, g);
+                    rec_put_seg<R, OBS>(sp, scratch + (size_t)li * K * kRecWords, g);
+                    nseg = 1;
+                    have = true;
+                }
+                if (!have) continue;
+                int done = 0; // 1: the particle's run is over, 2: its segments overflow
+                if (next_event(s) > sp.s_end) {
+                    done = 1;
+                } else {
+                    process_event(sp, pid, s, cnt);
+                    if ((int)s.k > sp.max_events) { s.alive = 0; s.s_death = s.s0; bad = true; }
+                    if (!s.alive) {
+                        done = 1;
+                    } else if (nseg < K - 2) {
+                        seg_from(s, g);
+                        seg_prepare<R, OBS>(sp, sedges, g);
+                        rec_put_seg<R, OBS>(sp, scratch + ((size_t)li * K + nseg) * kRecWords, g);
+                        ++nseg;
+                    } else {
+                        done = 2;
+                    }
+                }
+                if (done) {
+                    R *r = scratch + (size_t)li * K * kRecWords;
+                    if (done == 1) {
+                        if (!s.alive) rec_put_end(r + (size_t)nseg++ * kRecWords, s.s_death);
+                        rec_put_end(r + (size_t)nseg * kRecWords, kNeverStart);
+                    } else { // run whole now; its list bins nothing
+                        rec_put_end(r, 0);
+                        rec_put_end(r + kRecWords, kNeverStart);
+                        cnt = c0;
+                        run_particle<R, SINK_SMEM, OBS>(sp, sedges, shist, bi.first + li, cnt, bad);
+                    }
+                    have = false;
+                    li += T;
+                }
+            }
+        }
+        __syncthreads();
+        // ---- observations: 32 particles per warp in lockstep
+        for (int64_t base = 32 * warp; base < n; base += 32 * nwarps)
+            observe_batch<R, SINK_SMEM, OBS>(sp, sedges, shist, base, cnt, bad, scratch, n);
+    }
+    if (cur >= 0) flush(cur);
     unsigned v[6] = {cnt.scat, cnt.bnd, cnt.kill, cnt.absorb, cnt.obs, cnt.conv};
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
@@ -2230,11 +2356,24 @@ template <typename R> void *pick_batch(int obs)
                            : (obs == OBS_RADIAL ? (void *)rt_transport_batch<R, OBS_RADIAL> : (void *)rt_transport_batch<R, OBS_GENERAL>);
 }
 
-template <typename R> int launch_batch_t(const BatchArgs<R> &a, int grid, int block, size_t smem, void *stream, bool em)
+template <typename R> void *pick_batch_split(int obs)
+{
+    return obs == OBS_CART ? (void *)rt_transport_batch_split<R, OBS_CART>
+                           : (obs == OBS_RADIAL ? (void *)rt_transport_batch_split<R, OBS_RADIAL>
+                                                : (void *)rt_transport_batch_split<R, OBS_GENERAL>);
+}
+
+// which: 0 the lockstep ring kernel, 1 the event-major kernel, 2 the split kernel
+template <typename R> void *pick_batch_kind(int which, int obs)
+{
+    return which == 1 ? pick_batch_em<R>(obs) : (which == 2 ? pick_batch_split<R>(obs) : pick_batch<R>(obs));
+}
+
+template <typename R> int launch_batch_t(const BatchArgs<R> &a, int grid, int block, size_t smem, void *stream, int which)
 {
     void *args[] = {(void *)&a};
-    void *fn = em ? pick_batch_em<R>(a.obs_kind) : pick_batch<R>(a.obs_kind);
-    return (int)cudaLaunchKernel(fn, dim3(grid), dim3(block), args, smem, (cudaStream_t)stream);
+    return (int)cudaLaunchKernel(pick_batch_kind<R>(which, a.obs_kind), dim3(grid), dim3(block), args, smem,
+                                 (cudaStream_t)stream);
 }
 
 template <typename R> void *pick_events(int obs)

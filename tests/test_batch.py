@@ -98,3 +98,31 @@ def test_batch_instances_match_oracle_fp64():
             tot[key] += rs[key]
     assert st["scatter_events"] == tot["scatter_events"] and st["kills"] == tot["kills"]
     b.close()
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_batch_split_kernel_equals_ring_kernel(precision):
+    """The lockstep instances on the split kernel (rt_transport_batch_split) and on the ring
+    kernel (rt_transport_batch) give the same histograms, with segment lists long enough
+    and with two segments per particle (most particles then run whole in the events
+    phase), for several work-item sizes."""
+    inst = [(g, s, m, o, dict(op, precision=precision)) for g, s, m, o, op in _instances(8, 5000)]
+    ctx = get_context(0)
+    out = []
+    try:
+        for segs in (0, 2):
+            ctx.set_launch(0, segs, 0)
+            b = Batch(inst)
+            for shape in ((512, 8, 0), (0, -1, 0), (0, -1, 1000), (256, 4, 3000)):
+                b.set_launch(*shape)
+                st = b.run()
+                assert st["device_status"] == 0
+                out.append((segs, shape, b.histograms(), st["scatter_events"], st["observations"]))
+            b.close()
+    finally:
+        ctx.set_launch(0, 0, 0)
+    h0, ev0, ob0 = out[0][2:]
+    assert h0.any()
+    for segs, shape, h, ev, ob in out[1:]:
+        assert np.array_equal(h, h0), (segs, shape)
+        assert ev == ev0 and ob == ob0, (segs, shape)
