@@ -302,6 +302,13 @@ int rtmc_batch_create(rtmc_context *ctx, int32_t n, const rtmc_problem *problems
  * keeps the staged tables. */
 int rtmc_batch_set_launch(rtmc_batch *batch, int32_t block, int32_t ring_cap, int64_t chunk);
 
+/* Where the event-major instances (rt_transport_batch_em) bin: 1 = the block's
+ * shared-memory copy of the instance's histogram (512 threads, one block per SM, flushed
+ * with 64-bit atomics when the block moves to another instance), 0 = 64-bit atomics into
+ * the instance's histogram in device memory (256 threads, three blocks per SM; the
+ * default, and -1), which hides more latency.  Rebuilds the graph. */
+int rtmc_batch_set_em_histogram(rtmc_batch *batch, int32_t shared);
+
 /* One replay of the graph; histograms stay on the device.  stats sums all instances. */
 int rtmc_batch_run(rtmc_batch *batch, rtmc_stats *stats);
 

@@ -52,6 +52,11 @@ class Batch:
     def set_launch(self, block: int = 0, ring_cap: int = 0, chunk: int = 0):
         _lib.check(self.ctx.lib.rtmc_batch_set_launch(self.handle, block, ring_cap, chunk), self.ctx.handle)
 
+    def set_em_histogram(self, shared: int = -1):
+        """rtmc_batch_set_em_histogram: 1 shared-memory, 0 (default) or -1 device-memory
+        histogram for the event-major instances."""
+        _lib.check(self.ctx.lib.rtmc_batch_set_em_histogram(self.handle, shared), self.ctx.handle)
+
     def run(self) -> dict:
         st = _lib.RtmcStats()
         _lib.check(self.ctx.lib.rtmc_batch_run(self.handle, C.byref(st)), self.ctx.handle)

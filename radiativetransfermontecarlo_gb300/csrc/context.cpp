@@ -1832,6 +1832,8 @@ struct rtmc_batch {
     int block = 0, ring = 0, grid = 0, n_items = 0;
     int grid_em = 0, n_items_em = 0; // event-heavy instances, one particle per thread
     int split = 0;                   // lockstep instances on the split kernel (0: the ring kernel)
+    int em_shist = 0;                // event-major instances bin into shared memory (0: device memory)
+    int em_block = 256;
     int kmax = 0;                    // the largest seg_cap of the lockstep instances
     DevBuf scratch;                  // the split kernel's per-block segment records
     int64_t chunk = 0, hist_len = 0;
@@ -1939,9 +1941,16 @@ template <typename R> int batch_build_graph(rtmc_batch *b)
     if (!sorted_em.empty())
         CK(cudaMemcpy(b->items_em.p, sorted_em.data(), sorted_em.size() * sizeof(BatchItem), cudaMemcpyHostToDevice),
            "work list");
-    b->smem_em = align_up((size_t)b->n_edges * sizeof(R), 16);
+    // the event-major kernel bins into device memory unless the shared-memory histogram is
+    // asked for (on the 256-instance sweep: 646 ms per launch against 591, as one 512-thread
+    // block per SM hides less latency than three of 256)
+    const int em_shist = b->em_shist < 0 ? 0 : b->em_shist;
+    if (em_shist && fixed > budget)
+        return fail(&ctx->err, RTMC_ERR_ARG, "the histogram does not fit in shared memory");
+    b->smem_em = em_shist ? fixed : align_up((size_t)b->n_edges * sizeof(R), 16);
+    b->em_block = em_shist ? 512 : 256;
     int bps_em = 0;
-    if (transport_batch_em_setup(b->prec, b->obs_kind, 256, b->smem_em, &bps_em) != 0 || bps_em < 1)
+    if (transport_batch_em_setup(b->prec, b->obs_kind, b->em_block, b->smem_em, &bps_em, em_shist) != 0 || bps_em < 1)
         return fail(&ctx->err, RTMC_ERR_CUDA, "batched event-major kernel does not fit on the device");
     b->grid_em = ctx->num_sms * bps_em;
     // capture: clear histograms and counters, persistent launch
@@ -1974,8 +1983,9 @@ template <typename R> int batch_build_graph(rtmc_batch *b)
         else le = launch_transport_batch_f64(*a, b->grid, block, b->smem, ctx->stream, b->split);
     }
     if (!le && b->n_items_em) {
-        if constexpr (sizeof(R) == 4) le = launch_transport_batch_em_f32(*ae, b->grid_em, 256, b->smem_em, ctx->stream);
-        else le = launch_transport_batch_em_f64(*ae, b->grid_em, 256, b->smem_em, ctx->stream);
+        const int sh = b->em_block == 512 ? 1 : 0;
+        if constexpr (sizeof(R) == 4) le = launch_transport_batch_em_f32(*ae, b->grid_em, b->em_block, b->smem_em, ctx->stream, sh);
+        else le = launch_transport_batch_em_f64(*ae, b->grid_em, b->em_block, b->smem_em, ctx->stream, sh);
     }
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &b->graph);
     if (le) return cuda_fail(ctx, (cudaError_t)le, "batched launch capture");
@@ -2097,6 +2107,16 @@ extern "C" int rtmc_batch_set_launch(rtmc_batch *b, int32_t block, int32_t ring_
     b->block = block;
     b->ring = ring_cap;
     b->chunk = chunk;
+    return b->prec == RTMC_FP64 ? batch_build_graph<double>(b) : batch_build_graph<float>(b);
+}
+
+extern "C" int rtmc_batch_set_em_histogram(rtmc_batch *b, int32_t shared)
+{
+    if (!b) return fail(nullptr, RTMC_ERR_ARG, "rtmc_batch_set_em_histogram: NULL batch");
+    if (shared < -1 || shared > 1) return fail(&b->ctx->err, RTMC_ERR_ARG, "rtmc_batch_set_em_histogram: -1, 0 or 1");
+    rtmc_context *ctx = b->ctx;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    b->em_shist = shared;
     return b->prec == RTMC_FP64 ? batch_build_graph<double>(b) : batch_build_graph<float>(b);
 }
 

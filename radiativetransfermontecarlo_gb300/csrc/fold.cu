@@ -561,9 +561,9 @@ int transport_batch_setup(int precision, int obs, int block, size_t smem, int *b
     return set_and_occupancy(precision, split ? 10 : 1, obs, block, smem, blocks_per_sm);
 }
 
-int transport_batch_em_setup(int precision, int obs, int block, size_t smem, int *blocks_per_sm)
+int transport_batch_em_setup(int precision, int obs, int block, size_t smem, int *blocks_per_sm, int shist)
 {
-    return set_and_occupancy(precision, 2, obs, block, smem, blocks_per_sm);
+    return set_and_occupancy(precision, shist ? 11 : 2, obs, block, smem, blocks_per_sm);
 }
 
 int adjoint_occupancy(int precision, int obs, int block, size_t smem, int *blocks_per_sm)
@@ -593,6 +593,7 @@ void *kernel_of(int precision, int kind, int sink, int obs)
     case 0: return d ? kernel_of_transport_f64(sink, obs) : kernel_of_transport_f32(sink, obs);
     case 1: case 2: return d ? kernel_of_batch_f64(kind == 2, obs) : kernel_of_batch_f32(kind == 2, obs);
     case 10: return d ? kernel_of_batch_f64(2, obs) : kernel_of_batch_f32(2, obs);
+    case 11: return d ? kernel_of_batch_f64(3, obs) : kernel_of_batch_f32(3, obs);
     case 3: case 4: return d ? kernel_of_adjoint_f64(kind - 3, obs) : kernel_of_adjoint_f32(kind - 3, obs);
     case 8: case 9: return d ? kernel_of_adjoint_f64(kind - 6, obs) : kernel_of_adjoint_f32(kind - 6, obs);
     default: return d ? kernel_of_split_f64(kind, sink, obs) : kernel_of_split_f32(kind, sink, obs);

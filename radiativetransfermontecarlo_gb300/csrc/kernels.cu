@@ -39,9 +39,10 @@ int RTMC_NAME(launch_transport_batch)(const BatchArgs<RTMC_REAL> &a, int grid, i
     return launch_batch_t<RTMC_REAL>(a, grid, block, smem, stream, split ? 2 : 0);
 }
 
-int RTMC_NAME(launch_transport_batch_em)(const BatchArgs<RTMC_REAL> &a, int grid, int block, size_t smem, void *stream)
+int RTMC_NAME(launch_transport_batch_em)(const BatchArgs<RTMC_REAL> &a, int grid, int block, size_t smem, void *stream,
+                                         int shist)
 {
-    return launch_batch_t<RTMC_REAL>(a, grid, block, smem, stream, 1);
+    return launch_batch_t<RTMC_REAL>(a, grid, block, smem, stream, shist ? 3 : 1);
 }
 
 void *RTMC_NAME(kernel_of_batch)(int which, int obs) { return pick_batch_kind<RTMC_REAL>(which, obs); }

@@ -242,11 +242,13 @@ void *kernel_of_split_f32(int kind, int sink, int obs);
 void *kernel_of_split_f64(int kind, int sink, int obs);
 // kernel_of(precision, kind, sink, obs): the kernel function of a transport (kind 0, with
 // its sink and observation path), batch (1), event-major batch (2), adjoint (3), ring
-// adjoint (4), split-schedule events (5), observations (6, with its sink) or overflow
-// rerun (7) variant; kernel_set_smem sets its dynamic shared-memory limit.
+// adjoint (4), split-schedule events (5), observations (6, with its sink), overflow
+// rerun (7), split replay (8, 9), split batch (10) or shared-histogram event-major batch
+// (11) variant; kernel_set_smem sets its dynamic shared-memory limit.
 void *kernel_of_transport_f32(int sink, int obs);
 void *kernel_of_transport_f64(int sink, int obs);
-// which: 0 rt_transport_batch, 1 rt_transport_batch_em, 2 rt_transport_batch_split
+// which: 0 rt_transport_batch, 1 rt_transport_batch_em (device histogram),
+// 2 rt_transport_batch_split, 3 rt_transport_batch_em (shared-memory histogram)
 void *kernel_of_batch_f32(int which, int obs);
 void *kernel_of_batch_f64(int which, int obs);
 // which: 0 rt_adjoint, 1 rt_adjoint_ring, 2 rt_observe_adj, 3 rt_adjoint_list
@@ -292,9 +294,10 @@ inline bool may_exceed_int64(const rtmc_problem *P)
 int launch_transport_batch_f32(const BatchArgs<float> &a, int grid, int block, size_t smem, void *stream, int split);
 int launch_transport_batch_f64(const BatchArgs<double> &a, int grid, int block, size_t smem, void *stream, int split);
 int transport_batch_setup(int precision, int obs, int block, size_t smem, int *blocks_per_sm, int split);
-int launch_transport_batch_em_f32(const BatchArgs<float> &a, int grid, int block, size_t smem, void *stream);
-int launch_transport_batch_em_f64(const BatchArgs<double> &a, int grid, int block, size_t smem, void *stream);
-int transport_batch_em_setup(int precision, int obs, int block, size_t smem, int *blocks_per_sm);
+// shist: the event-major kernel with the shared-memory histogram (else 64-bit device atomics)
+int launch_transport_batch_em_f32(const BatchArgs<float> &a, int grid, int block, size_t smem, void *stream, int shist);
+int launch_transport_batch_em_f64(const BatchArgs<double> &a, int grid, int block, size_t smem, void *stream, int shist);
+int transport_batch_em_setup(int precision, int obs, int block, size_t smem, int *blocks_per_sm, int shist);
 int bin_slices_set_smem(size_t smem);
 // device address of the static scratch of rtmc_forward_noalloc (noalloc.cu); device current
 int static_scratch(int device, unsigned char **ptr, size_t *bytes);

@@ -1830,21 +1830,44 @@ __global__ void __launch_bounds__(512, 1) rt_transport_batch(const BatchArgs<R> 
 }
 
 // Batched transport of the event-heavy instances: the same work-item loop, one particle
-// per thread (event-major), observations as 64-bit atomics into the instance's histogram
-// (no shared-memory copy, so three blocks fit on an SM instead of one).
-template <typename R, int OBS>
-__global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2) rt_transport_batch_em(const BatchArgs<R> a)
+// per thread (event-major).  SHIST: observations go to the block's shared-memory copy of
+// the instance's histogram, flushed when the block moves to another instance (512 threads,
+// one block per SM); else 64-bit atomics into the instance's histogram in device memory
+// (no shared-memory copy, so three blocks fit on an SM).
+template <typename R, bool SHIST> struct BatchEmBounds {
+    static constexpr int threads = SHIST ? 512 : 256;
+    static constexpr int min_blocks = SHIST ? 1 : (sizeof(R) == 4 ? 3 : 2);
+};
+
+template <typename R, int OBS, bool SHIST>
+__global__ void __launch_bounds__(BatchEmBounds<R, SHIST>::threads, BatchEmBounds<R, SHIST>::min_blocks)
+    rt_transport_batch_em(const BatchArgs<R> a)
 {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ DevParams<R> sp;
     __shared__ int s_item;
     R *sedges = reinterpret_cast<R *>(smem_raw);
+    unsigned *shist = SHIST ? reinterpret_cast<unsigned *>(smem_raw + (((size_t)a.n_edges * sizeof(R) + 15) / 16) * 16)
+                            : nullptr;
     const int T = blockDim.x;
     for (int k = threadIdx.x; k < a.n_edges; k += T) sedges[k] = a.edges[k];
+    if (SHIST)
+        for (int64_t k = threadIdx.x; k < a.hist_len; k += T) shist[k] = 0u;
     const int lane = threadIdx.x & 31;
     Counters cnt = {0u, 0u, 0u, 0u, 0u, 0u};
     bool bad = false;
     int cur = -1;
+    auto flush = [&](int inst) {
+        unsigned long long *h = a.hists + (int64_t)inst * a.hist_len;
+        const int sh = sp.hist_shift;
+        for (int64_t k = threadIdx.x; k < a.hist_len; k += T) {
+            const unsigned c = shist[k];
+            if (c) {
+                atomicAdd(h + k, (unsigned long long)c << sh);
+                shist[k] = 0u;
+            }
+        }
+    };
     for (;;) {
         __syncthreads();
         if (threadIdx.x == 0) s_item = atomicAdd(a.counter, 1);
@@ -1853,6 +1876,8 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2) rt_transport_batc
         if (it >= a.n_items) break;
         const BatchItem bi = a.items[it];
         if (bi.inst != cur) {
+            if (SHIST && cur >= 0) flush(cur);
+            __syncthreads();
             const uint32_t *src = reinterpret_cast<const uint32_t *>(a.params + bi.inst);
             uint32_t *dst = reinterpret_cast<uint32_t *>(&sp);
             for (int k = threadIdx.x; k < (int)(sizeof(DevParams<R>) / 4); k += T) dst[k] = src[k];
@@ -1863,8 +1888,9 @@ __global__ void __launch_bounds__(256, sizeof(R) == 4 ? 3 : 2) rt_transport_batc
         }
         const int64_t end = bi.first + bi.count;
         for (int64_t i = bi.first + threadIdx.x; i < end; i += T)
-            run_particle<R, SINK_GLOBAL, OBS>(sp, sedges, nullptr, i, cnt, bad);
+            run_particle<R, SHIST ? SINK_SMEM : SINK_GLOBAL, OBS>(sp, sedges, shist, i, cnt, bad);
     }
+    if (SHIST && cur >= 0) flush(cur);
     const unsigned full = 0xffffffffu;
     unsigned v[6] = {cnt.scat, cnt.bnd, cnt.kill, cnt.absorb, cnt.obs, cnt.conv};
 #pragma unroll
@@ -2343,11 +2369,11 @@ template <typename R> int launch_transport_t(const DevParams<R> &p, int grid, in
     return (int)cudaLaunchKernel(pick_t<R>(p.sink, p.obs_kind), dim3(grid), dim3(block), args, smem, (cudaStream_t)stream);
 }
 
-template <typename R> void *pick_batch_em(int obs)
+template <typename R, bool SHIST> void *pick_batch_em(int obs)
 {
-    return obs == OBS_CART ? (void *)rt_transport_batch_em<R, OBS_CART>
-                           : (obs == OBS_RADIAL ? (void *)rt_transport_batch_em<R, OBS_RADIAL>
-                                                : (void *)rt_transport_batch_em<R, OBS_GENERAL>);
+    return obs == OBS_CART ? (void *)rt_transport_batch_em<R, OBS_CART, SHIST>
+                           : (obs == OBS_RADIAL ? (void *)rt_transport_batch_em<R, OBS_RADIAL, SHIST>
+                                                : (void *)rt_transport_batch_em<R, OBS_GENERAL, SHIST>);
 }
 
 template <typename R> void *pick_batch(int obs)
@@ -2363,10 +2389,16 @@ template <typename R> void *pick_batch_split(int obs)
                                                 : (void *)rt_transport_batch_split<R, OBS_GENERAL>);
 }
 
-// which: 0 the lockstep ring kernel, 1 the event-major kernel, 2 the split kernel
+// which: 0 the lockstep ring kernel, 1 the event-major kernel (device-memory histogram),
+// 2 the split kernel, 3 the event-major kernel with the shared-memory histogram
 template <typename R> void *pick_batch_kind(int which, int obs)
 {
-    return which == 1 ? pick_batch_em<R>(obs) : (which == 2 ? pick_batch_split<R>(obs) : pick_batch<R>(obs));
+    switch (which) {
+    case 1: return pick_batch_em<R, false>(obs);
+    case 2: return pick_batch_split<R>(obs);
+    case 3: return pick_batch_em<R, true>(obs);
+    default: return pick_batch<R>(obs);
+    }
 }
 
 template <typename R> int launch_batch_t(const BatchArgs<R> &a, int grid, int block, size_t smem, void *stream, int which)

@@ -126,3 +126,29 @@ def test_batch_split_kernel_equals_ring_kernel(precision):
     for segs, shape, h, ev, ob in out[1:]:
         assert np.array_equal(h, h0), (segs, shape)
         assert ev == ev0 and ob == ob0, (segs, shape)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_batch_em_shared_histogram_equals_device_histogram(precision):
+    """The event-major instances binned in the block's shared-memory histogram and with
+    64-bit atomics into device memory give the same histograms (instances 0, 13 and 36 are
+    event-heavy; 1 and 8 run on the lockstep kernel beside them)."""
+    picks = [0, 1, 8, 13, 36]
+    inst = []
+    for i in picks:
+        geo, src, mat, obs, opts = W.c4_instance(i)
+        inst.append((geo, dict(src, numberParticles=3000), mat, obs,
+                     dict(opts, exact_count=True, seed=300 + i, precision=precision)))
+    b = Batch(inst)
+    assert list(b.schedule()) == [1, 0, 0, 1, 1]
+    out = []
+    for shared in (0, 1, -1):
+        b.set_em_histogram(shared)
+        st = b.run()
+        assert st["device_status"] == 0 and st["launches"] == 2
+        out.append((b.histograms(), st["scatter_events"], st["observations"]))
+    b.close()
+    h0, ev0, ob0 = out[0]
+    assert h0[[0, 3, 4]].any()
+    for h, ev, ob in out[1:]:
+        assert np.array_equal(h, h0) and ev == ev0 and ob == ob0
