@@ -463,14 +463,16 @@ def run_c4(args):
     spherical 120 x 251 grid, one persistent CUDA-graph launch per step."""
     from oracle import oracle as O
     from radiativetransfermontecarlo_gb300 import workloads as W
-    from radiativetransfermontecarlo_gb300.batch import Batch, autotune
+    from radiativetransfermontecarlo_gb300.batch import Batch, autotune, tune_schedule
     t0 = time.perf_counter()
     batch = Batch([W.c4_instance(i) for i in range(args.instances)])
     setup_s = time.perf_counter() - t0
     if args.no_tune:
-        shape, tune = (0, 0, 0), {}
+        shape, tune, factor, tune_f = (0, 0, 0), {}, 8, {}
     else:
         shape, tune = autotune(batch, repeats=1)
+        factor, tune_f = tune_schedule(batch, repeats=1)
+    n_em = int(batch.schedule().sum())
     for _ in range(args.warmup):
         batch.run()
     ms, ev = [], 0
@@ -496,12 +498,14 @@ def run_c4(args):
             "config": {"workload": f"{args.instances}-instance 3D acoustic sweep: lc log-U[0.02,1], cv U[0.01,0.2], "
                                    "f log-U[1,20], Q in {Inf,100,500}, N log-U[1e4,1e7]; spherical 120 x 251 grid",
                        "particles_total": n_total, "launch_shape": list(shape), "table_setup_s": setup_s,
+                       "event_major_factor": factor, "event_major_instances": n_em,
                        "l2": "512 MB device write between steps"},
             "gpu_launches": args.steps, "clocks": clk.summary(),
             "events_per_step": ev / args.steps,
             "e2e": {"value": ev2 / sum(times), "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": int(H.nbytes), "ms_per_step": 1000 * float(np.mean(times))},
-            "autotune_ms": {f"{b}x{r}x{c}": t for (b, r, c), t in tune.items()}}
+            "autotune_ms": {f"{b}x{r}x{c}": t for (b, r, c), t in tune.items()},
+            "schedule_tune_ms": {str(f): t for f, t in tune_f.items()}}
     if not args.no_cpu:
         prob = batch.problems[int(np.argmax(batch.N))]
         line["cpu_baseline"] = baseline_fields(cpu_sample(prob, O.table_knots(prob.tables), target_s=args.cpu_seconds))

@@ -319,6 +319,12 @@ int rtmc_batch_run(rtmc_batch *batch, rtmc_stats *stats);
  * the batch runs one kernel per non-empty group (rtmc_stats.launches). */
 int rtmc_batch_schedule(const rtmc_batch *batch, int32_t *event_major);
 
+/* Sets which kernel runs each instance (event_major[i] = 1: rt_transport_batch_em, 0: the
+ * lockstep kernel; both give the instance's histogram), or restores the automatic choice
+ * (event_major = NULL: 1 when 8 x expected events per particle >= observation instants).
+ * Rebuilds the work lists and the graph. */
+int rtmc_batch_set_schedule(rtmc_batch *batch, const int32_t *event_major);
+
 /* Copies the int64 histograms of instances [first, first + count) into out (host),
  * instance-major, hist_len each. */
 int rtmc_batch_histograms(rtmc_batch *batch, int32_t first, int32_t count, int64_t *out);

@@ -119,6 +119,7 @@ SIGNATURES = {
     "rtmc_batch_create": (C.c_int, [_P, C.c_int32, C.POINTER(RtmcProblem), C.POINTER(_P), C.POINTER(_P)]),
     "rtmc_batch_set_launch": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int64]),
     "rtmc_batch_set_em_histogram": (C.c_int, [_P, C.c_int32]),
+    "rtmc_batch_set_schedule": (C.c_int, [_P, C.POINTER(C.c_int32)]),
     "rtmc_batch_run": (C.c_int, [_P, C.POINTER(RtmcStats)]),
     "rtmc_batch_histograms": (C.c_int, [_P, C.c_int32, C.c_int32, C.POINTER(C.c_int64)]),
     "rtmc_batch_schedule": (C.c_int, [_P, C.POINTER(C.c_int32)]),

@@ -69,6 +69,28 @@ class Batch:
                    self.ctx.handle)
         return out
 
+    def set_schedule(self, event_major=None):
+        """rtmc_batch_set_schedule: event_major[i] = 1 runs instance i on the event-major
+        kernel, 0 on the lockstep kernel; None restores the automatic choice."""
+        if event_major is None:
+            ptr = None
+        else:
+            em = np.ascontiguousarray(event_major, dtype=np.int32)
+            if em.shape != (len(self.problems),):
+                raise ValueError("event_major needs one entry per instance")
+            ptr = em.ctypes.data_as(C.POINTER(C.c_int32))
+        _lib.check(self.ctx.lib.rtmc_batch_set_schedule(self.handle, ptr), self.ctx.handle)
+
+    def expected_events(self) -> np.ndarray:
+        """Expected scatterings per particle of each instance over the observed time (the
+        quantity the automatic kernel choice compares with the observation instants)."""
+        out = np.zeros(len(self.problems))
+        for i in range(len(self.problems)):
+            P = self._arr[i]
+            rates = [1.0 / P.mft[m] for m in range(1 if P.acoustics else 2) if np.isfinite(P.mft[m]) and P.mft[m] > 0]
+            out[i] = (max(rates) if rates else 0.0) * P.h * P.n_sub * P.n_obs
+        return out
+
     def histograms(self, first: int = 0, count: int | None = None) -> np.ndarray:
         count = len(self.problems) - first if count is None else count
         out = np.empty((count, self.hist_len), dtype=np.int64)
@@ -99,7 +121,7 @@ class Batch:
 
 
 def autotune(batch: Batch, blocks=(256, 512), rings=(4, 8), chunks=(4096, 16384, 65536),
-             split_chunks=(2048, 4096, 8192), repeats: int = 2):
+             split_chunks=(4096,), repeats: int = 2):
     """Time every launch shape of the grid on the batch itself and keep the fastest
     (block, ring capacity, particles per work item); (0, -1, chunk) is the split kernel.
     Returns (best shape, {shape: ms})."""
@@ -117,11 +139,35 @@ def autotune(batch: Batch, blocks=(256, 512), rings=(4, 8), chunks=(4096, 16384,
     return shape, times
 
 
+def tune_schedule(batch: Batch, factors=(2, 4, 8, 16, 32), repeats: int = 2):
+    """Time the split of the instances between the two kernels on the batch itself: an
+    instance runs event-major when factor x its expected events per particle >= its
+    observation instants (8 is the automatic choice).  Keeps the fastest and returns
+    (best factor, {factor: ms})."""
+    ev = batch.expected_events()
+    n_obs = np.array([batch._arr[i].n_obs for i in range(len(batch.problems))], dtype=np.float64)
+    times, seen = {}, {}
+    for f in factors:
+        em = (f * ev >= n_obs).astype(np.int32)
+        key = em.tobytes()
+        if key in seen:  # the same split as an earlier factor
+            times[f] = times[seen[key]]
+            continue
+        seen[key] = f
+        batch.set_schedule(em)
+        batch.run()  # warm-up
+        times[f] = min(batch.run()["kernel_ms"] for _ in range(repeats))
+    best = min(times, key=times.get)
+    batch.set_schedule((best * ev >= n_obs).astype(np.int32))
+    return best, times
+
+
 def radiative_transfer_batch(instances, device: int = 0, tune: bool = False) -> list[dict]:
     """radiativeTransfer for every instance in one batched launch."""
     b = Batch(instances, device)
     if tune:
         autotune(b)
+        tune_schedule(b)
     b.run()
     res = b.results()
     b.close()

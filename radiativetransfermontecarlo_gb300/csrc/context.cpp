@@ -1841,7 +1841,9 @@ struct rtmc_batch {
     DevBuf params, items, items_em, tabs, edges, hists, ctl;
     std::vector<int64_t> n_part;
     std::vector<double> cost_per_particle;
-    std::vector<int> event_major;
+    std::vector<int> event_major;    // the kernel of each instance (1: event-major)
+    std::vector<int> event_major_auto; // the automatic choice
+    std::vector<int> seg_cap;        // the split kernel's segment records per particle
     int n_edges = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -1879,6 +1881,9 @@ template <typename R> int batch_build_graph(rtmc_batch *b)
     int block, ring = 0;
     int64_t chunk;
     int bps = 0;
+    b->kmax = 0;
+    for (int i = 0; i < b->n; ++i)
+        if (!b->event_major[i]) b->kmax = std::max(b->kmax, b->seg_cap[i]);
     if (b->split) {
         // the split kernel: 1024 threads, the histogram alone in shared memory, segment
         // records of one work item per block in device memory
@@ -2020,6 +2025,8 @@ int batch_create(rtmc_context *ctx, int n, const rtmc_problem *P, const rtmc_tab
     b->n_part.resize(n);
     b->cost_per_particle.resize(n);
     b->event_major.assign(n, 0);
+    b->event_major_auto.assign(n, 0);
+    b->seg_cap.assign(n, 0);
     for (int i = 0; i < n; ++i) {
         DevTables<R> dt{};
         size_t o = toff[i];
@@ -2040,16 +2047,15 @@ int batch_create(rtmc_context *ctx, int n, const rtmc_problem *P, const rtmc_tab
             if (std::isfinite(P[i].mft[m])) rate = std::max(rate, 1.0 / P[i].mft[m]);
         b->cost_per_particle[i] = P[i].n_obs + 4.0 * rate * P[i].h * P[i].n_sub * P[i].n_obs;
         if (i == 0) b->obs_kind = params[0].obs_kind;
-        b->event_major[i] = params[i].event_major;
+        b->event_major[i] = b->event_major_auto[i] = params[i].event_major;
         // the split kernel's segment records per particle: as for rtmc_forward's split schedule
         const double mean = rate * P[i].h * (double)P[i].n_sub * (double)P[i].n_obs;
         int K = (int)std::ceil(1.0 + mean + 4.0 * std::sqrt(mean) + 4.0);
         K = std::min(64, std::max(8, (K + 3) / 4 * 4));
         if (ctx->opt_ring) K = ctx->opt_ring; // the context's ring capacity, when one is set
         K = std::max(1, K) + 2;
-        params[i].seg_cap = K;
+        params[i].seg_cap = b->seg_cap[i] = K;
         params[i].split = 1;
-        if (!params[i].event_major) b->kmax = std::max(b->kmax, K);
     }
     CK(cudaMemcpy(b->tabs.p, host.data(), total, cudaMemcpyHostToDevice), "batched tables");
     if (b->edges.grow(std::max<size_t>(1, edges.size()) * sizeof(R)) || b->params.grow((size_t)n * sizeof(DevParams<R>)) ||
@@ -2154,6 +2160,19 @@ extern "C" int rtmc_batch_run(rtmc_batch *b, rtmc_stats *st)
     }
     if (status) return fail(&ctx->err, RTMC_ERR_DEVICE, "a transport guard tripped in a batched run");
     return RTMC_OK;
+}
+
+extern "C" int rtmc_batch_set_schedule(rtmc_batch *b, const int32_t *event_major)
+{
+    if (!b) return fail(nullptr, RTMC_ERR_ARG, "rtmc_batch_set_schedule: NULL batch");
+    if (event_major)
+        for (int i = 0; i < b->n; ++i)
+            if (event_major[i] != 0 && event_major[i] != 1)
+                return fail(&b->ctx->err, RTMC_ERR_ARG, "rtmc_batch_set_schedule: event_major[i] must be 0 or 1");
+    rtmc_context *ctx = b->ctx;
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    for (int i = 0; i < b->n; ++i) b->event_major[i] = event_major ? event_major[i] : b->event_major_auto[i];
+    return b->prec == RTMC_FP64 ? batch_build_graph<double>(b) : batch_build_graph<float>(b);
 }
 
 extern "C" int rtmc_batch_schedule(const rtmc_batch *b, int32_t *event_major)

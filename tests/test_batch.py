@@ -152,3 +152,33 @@ def test_batch_em_shared_histogram_equals_device_histogram(precision):
     assert h0[[0, 3, 4]].any()
     for h, ev, ob in out[1:]:
         assert np.array_equal(h, h0) and ev == ev0 and ob == ob0
+
+
+def test_batch_set_schedule_moves_instances_between_kernels():
+    """Every instance gives the same histogram on either kernel: all lockstep, all
+    event-major, and the automatic split restored; tune_schedule keeps the results."""
+    from radiativetransfermontecarlo_gb300.batch import tune_schedule
+    picks = [0, 1, 8, 13, 36]
+    inst = []
+    for i in picks:
+        geo, src, mat, obs, opts = W.c4_instance(i)
+        inst.append((geo, dict(src, numberParticles=2500), mat, obs, dict(opts, exact_count=True, seed=400 + i)))
+    b = Batch(inst)
+    auto = b.schedule()
+    assert list(auto) == [1, 0, 0, 1, 1]
+    b.run()
+    H = b.histograms()
+    for em in ([0] * 5, [1] * 5, None):
+        b.set_schedule(em)
+        assert list(b.schedule()) == (list(auto) if em is None else em)
+        st = b.run()
+        assert st["device_status"] == 0
+        assert np.array_equal(b.histograms(), H), em
+    ev = b.expected_events()
+    n_obs = np.array([b._arr[i].n_obs for i in range(len(picks))])
+    assert list((8 * ev >= n_obs).astype(int)) == list(auto)
+    best, times = tune_schedule(b, factors=(1, 8, 1000), repeats=1)
+    assert best in times and len(times) == 3
+    b.run()
+    assert np.array_equal(b.histograms(), H)
+    b.close()
