@@ -408,6 +408,15 @@ int rtmc_set_fold(rtmc_context *ctx, int32_t mode);
  * calls; with 0 every call uploads its tables again (end-to-end timing) */
 int rtmc_set_table_cache(rtmc_context *ctx, int32_t enable);
 
+/* Calls that return the histogram to the host, on the split schedule with the time-blocked
+ * fold and one particle chunk: rt_observe first bins the instants of the first copy groups
+ * (at least first_percent of the instants), those groups are folded and their copies to
+ * the host start, and then rt_observe bins the remaining instants, so that the host link
+ * starts after a fraction of the observation pass.  0: one observation pass, then the
+ * groups; -1: the default (40).  The histogram is the same; rtmc_stats.kernel_ms then
+ * covers the events and the first instants, fold_ms the rest. */
+int rtmc_set_early_copy(rtmc_context *ctx, int32_t first_percent);
+
 /* FP64 problems on the radius-only observation path bin each observation through an FP32
  * estimate with a proven error bound, and in FP64 only when the estimate lies within that
  * bound of a bin edge: the same bins as the FP64 formula, at FP32 cost.  0 turns the

@@ -111,6 +111,7 @@ SIGNATURES = {
     "rtmc_flush_l2": (C.c_int, [_P]),
     "rtmc_set_table_cache": (C.c_int, [_P, C.c_int32]),
     "rtmc_set_fp64_estimate": (C.c_int, [_P, C.c_int32]),
+    "rtmc_set_early_copy": (C.c_int, [_P, C.c_int32]),
     "rtmc_set_particle_order": (C.c_int, [_P, C.c_int32]),
     "rtmc_set_launch": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_int32]),
     "rtmc_set_pipeline": (C.c_int, [_P, C.c_int32, C.c_int32]),
@@ -359,6 +360,11 @@ class Context:
     def set_fp64_estimate(self, enable: bool):
         """rtmc_set_fp64_estimate: FP64 radius-only observations through the exact FP32 estimate."""
         check(self.lib.rtmc_set_fp64_estimate(self.handle, 1 if enable else 0), self.handle)
+
+    def set_early_copy(self, first_percent: int = -1):
+        """rtmc_set_early_copy: host-output calls bin the first first_percent of the instants,
+        fold them and start their copies before binning the rest (0: off, -1: default)."""
+        check(self.lib.rtmc_set_early_copy(self.handle, int(first_percent)), self.handle)
 
     def flush_l2(self):
         check(self.lib.rtmc_flush_l2(self.handle), self.handle)

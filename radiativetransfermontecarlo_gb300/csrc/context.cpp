@@ -70,6 +70,7 @@ struct rtmc_context {
     int opt_event_major = -1; // -1 automatic, 0 two-cursor batches, 1 one particle per thread, 2 split
     int opt_fold = 0;         // 0 automatic, 1 64-bit slice fold, 2 time-blocked FP32 fold, 3 the same, rolling
     int opt_bin32 = 1;        // FP64 radius-only observations through an exact FP32 estimate
+    int opt_early_copy = kEarlyCopyPercent; // host-output calls: copies start after the first instants (percent)
     int opt_order = 1;        // index path: particles binned in the order of their starting directions
     static constexpr int kPipe = 32;
     cudaStream_t fold_stream = nullptr;
@@ -250,8 +251,9 @@ int check_problem(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t
     }
     if (!(P->h > 0) || !std::isfinite(P->h)) return fail(e, RTMC_ERR_ARG, "sub-step h must be positive");
     if (!std::isfinite(P->src_lambda) || P->src_lambda < 0) return fail(e, RTMC_ERR_ARG, "source lambda must be >= 0");
-    int st = validate_tables(t, e);
-    if (st) return st;
+    // the knots were validated when the handle was made (rtmc_tables_build and
+    // rtmc_tables_from_knots; a handle never changes): no per-call scan of the ~40 MB
+    if (!t) return fail(e, RTMC_ERR_NOTABLES, "tables handle is NULL");
     if (t->n_tables != (P->acoustics ? 1 : 4))
         return fail(e, RTMC_ERR_NOTABLES, "acoustic problems need 1 table, elastic problems 4");
     if (P->hist_len <= 0) return fail(e, RTMC_ERR_ARG, "hist_len must be positive");
@@ -846,26 +848,51 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
         q.pid0 = P->pid0 + base;
         q.n_particles = std::min<int64_t>(chunk, P->n_particles - base);
         if (p.trace) q.trace = p.trace + 16 * base;
+        const bool last = base + chunk >= P->n_particles;
+        // the last fold in groups of t-blocks when the histogram goes to the host: each
+        // group's slices are final, so their copy runs on the second stream while the next
+        // group folds
+        const bool groups =
+            use_tb && last && (host_out || host_u32) && ntb >= 2 * kCopyGroups && ensure_pipeline(ctx) == 0;
+        int gb_[25];
+        const int ng = groups ? tb_groups(ntb, gb_) : 1;
+        // early copy (split schedule, one chunk): rt_observe bins the instants of the first
+        // groups (at least a fifth of them), those groups fold and start their copies, and
+        // only then does rt_observe bin the rest, so the host link starts working after a
+        // fraction of the observation pass instead of all of it
+        int g_split = 0;
+        if (groups && split && !roll && base == 0 && last && ctx->opt_early_copy > 0) {
+            for (int g = 1; g < ng; ++g)
+                if (100 * 4 * (int64_t)gb_[g] >= (int64_t)ctx->opt_early_copy * P->n_obs) { g_split = g; break; }
+        }
         CK(cudaEventRecord(ctx->ev_k0, ctx->stream), "event");
+        if (g_split) {
+            q.obs_j0 = 1;
+            q.obs_j1 = 4 * gb_[g_split];
+        }
         le = launch_one(q);
         CK(cudaEventRecord(ctx->ev_k1, ctx->stream), "event");
-        const bool last = base + chunk >= P->n_particles;
         if (!le && use_tb) {
             TbParams tp = tpl;
             tp.n = q.n_particles;
             tp.part_per_block = ((tp.n + tb_grid - 1) / tb_grid + 3) / 4 * 4;
             unsigned long long *hist = p.hist;
-            // the last fold in groups of t-blocks when the histogram goes to the host: each
-            // group's slices are final, so their copy runs on the second stream while the
-            // next group folds
-            const bool groups = last && (host_out || host_u32) && ntb >= 2 * kCopyGroups && ensure_pipeline(ctx) == 0;
-            int gb_[25];
-            const int ng = groups ? tb_groups(ntb, gb_) : 1;
             const int64_t ts = P->time_stride;
             // one fold launch and one conversion: the conversion is timed apart
             timed_convert = last && !groups && !roll && ntb <= 65535;
             for (int g = 0; g < ng && !le; ++g) {
                 const int ga = groups ? gb_[g] : 0, gb = groups ? gb_[g + 1] : ntb;
+                if (g_split && g == g_split) { // the remaining instants, then their groups
+                    DevParams<R> qb = q;
+                    qb.obs_j0 = q.obs_j1 + 1;
+                    qb.obs_j1 = P->n_obs;
+                    SplitLaunch s2 = sl;
+                    s2.part = 2;
+                    if constexpr (sizeof(R) == 4) le = launch_split_f32(qb, s2, ctx->stream);
+                    else le = launch_split_f64(qb, s2, ctx->stream);
+                    launches += 2;
+                    if (le) break;
+                }
                 if (gb <= ga) continue;
                 // a rolling accumulator takes `roll` t-blocks at a time and is zeroed again by
                 // their conversion; the full one takes the group at once
@@ -1795,6 +1822,15 @@ extern "C" int rtmc_set_fp64_estimate(rtmc_context *ctx, int32_t enable)
 {
     if (!ctx) return fail(nullptr, RTMC_ERR_ARG, "rtmc_set_fp64_estimate: NULL context");
     ctx->opt_bin32 = enable ? 1 : 0;
+    return RTMC_OK;
+}
+
+extern "C" int rtmc_set_early_copy(rtmc_context *ctx, int32_t first_percent)
+{
+    if (!ctx) return fail(nullptr, RTMC_ERR_ARG, "rtmc_set_early_copy: NULL context");
+    if (first_percent < -1 || first_percent > 99)
+        return fail(&ctx->err, RTMC_ERR_ARG, "rtmc_set_early_copy: first_percent in [0, 99], or -1 for the default");
+    ctx->opt_early_copy = first_percent < 0 ? kEarlyCopyPercent : first_percent;
     return RTMC_OK;
 }
 

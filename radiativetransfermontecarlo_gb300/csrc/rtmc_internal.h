@@ -133,6 +133,9 @@ template <typename R> struct DevParams {
     int32_t *ovf_list;
     uint32_t *ovf_count;
     int32_t seg_cap, split;
+    // instants obs_j0..obs_j1 (inclusive) that rt_observe and rt_transport_list bin into
+    // the index array (0, 0: all); the rerun counts its events only in the range from 1
+    int32_t obs_j0, obs_j1;
     // rt_events zeroes clear_words 64-bit words at `clear` as it goes (the histogram, on
     // the first chunk of a split run), so no separate memset pass precedes the transport
     unsigned long long *clear;
@@ -174,6 +177,14 @@ struct BatchItem {
     int32_t inst, pad;
     int64_t first, count;
 };
+
+// Early copy of host-output calls: the first observation pass covers the instants of the
+// copy groups that hold at least this percent of them (rtmc_set_early_copy).  On the 3D
+// elastic workload's uint32 output (1e7 particles, 250 instants, 3.47 GB to the host), the
+// median call took 26.7 ms with one observation pass and 26.9 / 26.5 / 26.1 / 25.0 / 25.0 /
+// 25.5 ms with 5 / 10 / 20 / 35 / 50 / 70 %: the copies slow down while the fold runs
+// (its L2 reductions), so they gain most when they overlap the second observation pass.
+constexpr int kEarlyCopyPercent = 40;
 
 // Threads per block of rt_transport_batch_split (one block per SM).
 #ifndef RTMC_BATCH_SPLIT_THREADS
@@ -227,6 +238,7 @@ struct OrderParams {
 };
 
 struct SplitLaunch {
+    int part; // 0: all kernels; 1: rt_events and the order sort; 2: rt_observe and rt_transport_list
     int grid_events, grid_observe, block_observe, grid_list;
     size_t smem_events, smem_observe;
     void *mid_event; // optional cudaEvent_t recorded after rt_events

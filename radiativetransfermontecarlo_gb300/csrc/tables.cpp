@@ -424,6 +424,13 @@ extern "C" int rtmc_tables_build(const rtmc_material *m, rtmc_tables **out)
         I.p2p = S[0] / (S[0] + S[1]);
         I.s2s = S[3] / (S[2] + S[3]);
     }
+    // the knots are checked once here; the handle is immutable afterwards
+    std::string err;
+    const int st = validate_tables(t, &err);
+    if (st) {
+        delete t;
+        return fail(nullptr, st, err);
+    }
     t->gen = next_generation();
     *out = t;
     return RTMC_OK;
@@ -449,7 +456,7 @@ extern "C" int rtmc_tables_from_knots(int32_t n_tables, const int64_t *n_knots, 
         t->info.n_knots[i] = n_knots[i];
     }
     std::string err;
-    int st = validate_tables(t, &err);
+    int st = validate_tables(t, &err); // once: the handle is immutable afterwards
     if (st) {
         delete t;
         return fail(nullptr, st, err);

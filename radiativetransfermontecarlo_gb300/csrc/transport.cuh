@@ -1277,6 +1277,8 @@ __device__ __forceinline__ void run_particle(const DevParams<R> &p, const R *sed
     init_particle(p, pid, s);
     // row j - 1 holds instant j; the particle's column (its place in the particle order)
     int32_t *optr = SINK == SINK_INDEX ? p.obs_idx + (p.iperm ? p.iperm[i] : i) : nullptr;
+    // the index sink writes the rows of instants jr0..jr1 only (all by default)
+    const int jr0 = p.obs_j0 > 1 ? p.obs_j0 : 1, jr1 = p.obs_j1 > 0 ? p.obs_j1 : p.n_obs;
     const unsigned scat0 = cnt.scat, bnd0 = cnt.bnd;
     int j = 1;
     for (;;) {
@@ -1288,9 +1290,11 @@ __device__ __forceinline__ void run_particle(const DevParams<R> &p, const R *sed
         for (; j <= p.n_obs && j * p.n_sub < lim; ++j) { // observations strictly before the event
             const int v = obs_offset<R, OBS>(p, sedges, g, j * p.n_sub);
             if (SINK == SINK_INDEX) {
-                *optr = v < 0 ? -1 : (v | (g.mode << 30));
+                if (j >= jr0 && j <= jr1) {
+                    *optr = v < 0 ? -1 : (v | (g.mode << 30));
+                    if (v >= 0) cnt.obs++;
+                }
                 optr += p.obs_rows;
-                if (v >= 0) cnt.obs++;
             } else if (v >= 0) {
                 const int64_t idx = (int64_t)j * p.time_stride + (g.mode ? p.mode_stride : 0) + v;
                 if (idx < p.hist_len) {
@@ -1307,7 +1311,8 @@ __device__ __forceinline__ void run_particle(const DevParams<R> &p, const R *sed
         if ((int)s.k > p.max_events) { s.alive = 0; s.s_death = s.s0; bad = true; }
     }
     if (SINK == SINK_INDEX)
-        for (; j <= p.n_obs; ++j, optr += p.obs_rows) *optr = -1; // after death
+        for (; j <= p.n_obs; ++j, optr += p.obs_rows)
+            if (j >= jr0 && j <= jr1) *optr = -1; // after death
     if (p.trace) { // final state of the particle, the oracle's layout
         double *f = p.trace + 16 * i;
 #pragma unroll
@@ -1627,17 +1632,20 @@ __device__ __forceinline__ void observe_batch(const DevParams<R> &p, const R *se
         constexpr bool CDL = decltype(count_tag)::value;
         constexpr bool EST = R64 && decltype(est_tag)::value;
         if (EST) segf_from<OBS>(cur, cf);
-        const int s_last = p.n_obs * p.n_sub;
+        // instants j0..j1 (all by default); the first pass of the loop moves the cursor to
+        // the segment in force at j0
+        const int j0 = p.obs_j0 > 1 ? p.obs_j0 : 1;
+        const int s_last = (p.obs_j1 > 0 ? p.obs_j1 : p.n_obs) * p.n_sub;
         // FP64 with the FP32 estimates carries the offset as a float (an exact integer:
         // sub-steps stay below 2^24 there), so no FP64 instruction runs per instant
         using D = typename std::conditional<EST, float, R>::type;
         const D dstep = (D)p.n_sub;
-        int so = p.n_sub;
+        int so = j0 * p.n_sub;
         D dl = (D)(so - cur.s0);
         // every lane of a warp owns a column of the index array (rows are padded to 32
         // particles), so lanes past the last particle store their -1 there unconditionally
-        int32_t *optr = INDEX ? p.obs_idx + col : nullptr;
-        int64_t toff = p.time_stride; // slice offset of instant j (shared and global sinks)
+        int32_t *optr = INDEX ? p.obs_idx + (int64_t)(j0 - 1) * p.obs_rows + col : nullptr;
+        int64_t toff = (int64_t)j0 * p.time_stride; // slice offset of instant j (shared and global sinks)
 #pragma unroll 1
         for (; so <= s_last; so += p.n_sub) {
             if (so >= next_start) { // the next segment comes into force; load the one after it
@@ -1741,6 +1749,7 @@ __global__ void __launch_bounds__(256) rt_transport_list(const DevParams<R> p)
     for (unsigned t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += gridDim.x * blockDim.x)
         run_particle<R, SINK, OBS>(p, sedges, nullptr, p.ovf_list[t], cnt, bad);
     const unsigned full = 0xffffffffu;
+    if (p.obs_j0 > 1) cnt.scat = cnt.bnd = cnt.kill = cnt.absorb = cnt.conv = 0u; // counted with the first range
     unsigned v[6] = {cnt.scat, cnt.bnd, cnt.kill, cnt.absorb, cnt.obs, cnt.conv};
 #pragma unroll
     for (int c = 0; c < 6; ++c) {
@@ -2439,15 +2448,21 @@ template <typename R> void *pick_list(int sink, int obs)
     return sink == SINK_INDEX ? pick_list_obs<R, SINK_INDEX>(obs) : pick_list_obs<R, SINK_GLOBAL>(obs);
 }
 
-// the split schedule: rt_events, rt_observe, rt_transport_list, in stream order
+// the split schedule: rt_events, rt_observe, rt_transport_list, in stream order (l.part
+// 1: the events and the order sort only; 2: the observations and the reruns only)
 template <typename R>
 int launch_split_t(const DevParams<R> &p, const SplitLaunch &l, void *stream)
 {
     void *args[] = {(void *)&p};
-    cudaError_t e = cudaLaunchKernel(pick_events<R>(p.obs_kind), dim3(l.grid_events), dim3(256), args, l.smem_events,
-                                     (cudaStream_t)stream);
-    if (e == cudaSuccess && l.mid_event) e = cudaEventRecord((cudaEvent_t)l.mid_event, (cudaStream_t)stream);
-    if (e == cudaSuccess && p.okey) {
+    cudaError_t e = cudaSuccess;
+    if (l.part != 2) {
+        e = cudaLaunchKernel(pick_events<R>(p.obs_kind), dim3(l.grid_events), dim3(256), args, l.smem_events,
+                             (cudaStream_t)stream);
+        if (e == cudaSuccess && l.mid_event) e = cudaEventRecord((cudaEvent_t)l.mid_event, (cudaStream_t)stream);
+    }
+    if (l.part == 2) {
+        // the particle order is in place already
+    } else if (e == cudaSuccess && p.okey) {
         OrderParams o = l.order;
         o.key = p.okey;
         o.perm = p.perm;
@@ -2455,6 +2470,7 @@ int launch_split_t(const DevParams<R> &p, const SplitLaunch &l, void *stream)
         o.n = p.n_particles;
         e = (cudaError_t)launch_order(o, l.grid_order, stream);
     }
+    if (l.part == 1) return (int)e;
     if (e == cudaSuccess)
         e = cudaLaunchKernel(pick_observe<R>(p.sink, p.obs_kind), dim3(l.grid_observe), dim3(l.block_observe), args,
                              l.smem_observe, (cudaStream_t)stream);

@@ -723,6 +723,37 @@ def test_time_blocked_fold_equals_slice_fold(index_mb, width):
     assert s1["observations"] == s2["observations"] == s3["observations"] == int(h1.sum() >> prob.hist_shift)
 
 
+@pytest.mark.parametrize("segs", [0, 2])
+def test_early_copy_equals_one_observation_pass(segs):
+    """Host-output calls with the early copy (rt_observe over the first copy groups'
+    instants, their fold and copies, then rt_observe over the rest) give the histogram and
+    the counters of one observation pass, with segment lists long enough (segs 0) and with
+    two segments per particle, where most particles are rerun by rt_transport_list once per
+    instant range (segs 2)."""
+    geo, src, mat, obs, opts = W.c2_elastic3d(t_end=1.0)
+    prob, grid, N = build_problem(geo, dict(src, numberParticles=20000), mat, obs, dict(opts, exact_count=True))
+    P, keep = prob.to_ctypes()
+    ctx = get_context(0)
+    out = {}
+    try:
+        ctx.set_launch(0, segs, 0)
+        for early in (0, 40):
+            ctx.set_early_copy(early)
+            h, st = ctx.forward(P, prob.tables)
+            u, su = ctx.forward_u32(P, prob.tables)
+            out[early] = (h, u, st, su)
+    finally:
+        ctx.set_early_copy(-1)
+        ctx.set_launch(0, 0, 0)
+    (h0, u0, s0, su0), (h1, u1, s1, su1) = out[0], out[40]
+    assert s0["sink"] == 2 and s0["device_status"] == 0 and s1["device_status"] == 0
+    assert s1["launches"] == s0["launches"] + 2 and su1["launches"] == su0["launches"] + 2
+    assert np.array_equal(h0, h1) and np.array_equal(u0, u1)
+    for key in ("scatter_events", "boundary_hits", "kills", "observations", "conversions"):
+        assert s0[key] == s1[key] == su0[key] == su1[key], key
+    assert s0["observations"] == int(h0.sum() >> prob.hist_shift)
+
+
 @pytest.mark.parametrize("frame", ["spherical", "cylindrical2d", "cartesian"])
 def test_fp64_radial_estimate_gives_fp64_bins(frame):
     """FP64 radius-only and cartesian observations binned through FP32 estimates (default)
