@@ -482,6 +482,17 @@ int copy_group_start(int n_obs, int g)
     return 1 + first + (int)((int64_t)(n_obs - first) * (g - 1) / (kCopyGroups - 1));
 }
 
+// True for host memory that the CUDA runtime has not page-locked or registered
+bool host_is_pageable(const void *ptr)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return true;
+    }
+    return a.type == cudaMemoryTypeUnregistered;
+}
+
 int ensure_pipeline(rtmc_context *ctx)
 {
     cudaError_t e = cudaSuccess;
@@ -880,6 +891,29 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
             const int64_t ts = P->time_stride;
             // one fold launch and one conversion: the conversion is timed apart
             timed_convert = last && !groups && !roll && ntb <= 65535;
+            // a pageable destination (a MEX array, a NumPy array) makes each copy call block
+            // the host until it is done: those copies are issued after every launch is queued
+            const bool deferred = groups && host_is_pageable(host_u32 ? (const void *)host_u32 : (const void *)host_out);
+            int deferred_g[25], n_deferred = 0;
+            auto issue_copies = [&](int g) -> int {
+                const int ga = gb_[g], gb = gb_[g + 1];
+                const int64_t ja = g == 0 ? 0 : 4 * (int64_t)ga + 1; // slice 0 with the first group
+                const int64_t jb = std::min<int64_t>(4 * (int64_t)gb, P->n_obs) + 1;
+                CK(cudaStreamWaitEvent(ctx->fold_stream, ctx->ev_a1[g], 0), "copy wait");
+                for (int m = 0; m < nm; ++m) {
+                    const int64_t o = m * P->mode_stride + ja * ts;
+                    const size_t cnt = (size_t)((jb - ja) * ts);
+                    if (host_u32)
+                        CK(cudaMemcpyAsync(host_u32 + o, narrow + o, cnt * sizeof(uint32_t), cudaMemcpyDeviceToHost,
+                                           ctx->fold_stream),
+                           "histogram copy");
+                    else
+                        CK(cudaMemcpyAsync(host_out + o, static_cast<int64_t *>(ctx->hist.p) + o, cnt * sizeof(int64_t),
+                                           cudaMemcpyDeviceToHost, ctx->fold_stream),
+                           "histogram copy");
+                }
+                return RTMC_OK;
+            };
             for (int g = 0; g < ng && !le; ++g) {
                 const int ga = groups ? gb_[g] : 0, gb = groups ? gb_[g + 1] : ntb;
                 if (g_split && g == g_split) { // the remaining instants, then their groups
@@ -913,26 +947,21 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
                     }
                 }
                 if (le || !groups) break;
-                const int64_t ja = g == 0 ? 0 : 4 * (int64_t)ga + 1; // slice 0 with the first group
-                const int64_t jb = std::min<int64_t>(4 * (int64_t)gb, P->n_obs) + 1;
                 CK(cudaEventRecord(ctx->ev_a1[g], ctx->stream), "event");
-                CK(cudaStreamWaitEvent(ctx->fold_stream, ctx->ev_a1[g], 0), "copy wait");
-                for (int m = 0; m < nm; ++m) {
-                    const int64_t o = m * P->mode_stride + ja * ts;
-                    const size_t cnt = (size_t)((jb - ja) * ts);
-                    if (host_u32)
-                        CK(cudaMemcpyAsync(host_u32 + o, narrow + o, cnt * sizeof(uint32_t), cudaMemcpyDeviceToHost,
-                                           ctx->fold_stream),
-                           "histogram copy");
-                    else
-                        CK(cudaMemcpyAsync(host_out + o, static_cast<int64_t *>(ctx->hist.p) + o, cnt * sizeof(int64_t),
-                                           cudaMemcpyDeviceToHost, ctx->fold_stream),
-                           "histogram copy");
+                if (deferred) {
+                    deferred_g[n_deferred++] = g;
+                } else {
+                    const int c = issue_copies(g);
+                    if (c) return c;
                 }
             }
             if (groups && !le) {
-                CK(cudaEventRecord(ctx->ev_b1[0], ctx->fold_stream), "event");
                 CK(cudaEventRecord(ctx->ev_k2, ctx->stream), "event");
+                for (int k = 0; k < n_deferred; ++k) {
+                    const int c = issue_copies(deferred_g[k]);
+                    if (c) return c;
+                }
+                CK(cudaEventRecord(ctx->ev_b1[0], ctx->fold_stream), "event");
                 CK(cudaStreamWaitEvent(ctx->stream, ctx->ev_b1[0], 0), "copy join");
                 copied = true;
             } else {

@@ -16,6 +16,7 @@ import pytest
 
 from oracle import oracle as O
 from radiativetransfermontecarlo_gb300 import MaterialClass, build_problem, colon, get_context, normalise, radiativeTransfer
+from radiativetransfermontecarlo_gb300 import _lib
 from radiativetransfermontecarlo_gb300 import workloads as W
 
 pytestmark = pytest.mark.gpu
@@ -737,11 +738,17 @@ def test_early_copy_equals_one_observation_pass(segs):
     out = {}
     try:
         ctx.set_launch(0, segs, 0)
+        pinned = _lib.PinnedBuffer(prob.hist_len * 8)
         for early in (0, 40):
             ctx.set_early_copy(early)
-            h, st = ctx.forward(P, prob.tables)
+            h, st = ctx.forward(P, prob.tables)  # pageable destinations: copies issued after the launches
             u, su = ctx.forward_u32(P, prob.tables)
             out[early] = (h, u, st, su)
+            # page-locked destinations: copies queued on the second stream as groups complete
+            hp, _ = ctx.forward(P, prob.tables, pinned.array(np.int64, prob.hist_len))
+            assert np.array_equal(hp, h)
+            up, _ = ctx.forward_u32(P, prob.tables, pinned.array(np.uint32, prob.hist_len))
+            assert np.array_equal(up, u)
     finally:
         ctx.set_early_copy(-1)
         ctx.set_launch(0, 0, 0)
