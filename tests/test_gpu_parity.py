@@ -724,15 +724,16 @@ def test_time_blocked_fold_equals_slice_fold(index_mb, width):
     assert s1["observations"] == s2["observations"] == s3["observations"] == int(h1.sum() >> prob.hist_shift)
 
 
-@pytest.mark.parametrize("segs", [0, 2])
-def test_early_copy_equals_one_observation_pass(segs):
+@pytest.mark.parametrize("segs,precision", [(0, "fp32"), (2, "fp32"), (0, "fp64")])
+def test_early_copy_equals_one_observation_pass(segs, precision):
     """Host-output calls with the early copy (rt_observe over the first copy groups'
     instants, their fold and copies, then rt_observe over the rest) give the histogram and
     the counters of one observation pass, with segment lists long enough (segs 0) and with
     two segments per particle, where most particles are rerun by rt_transport_list once per
     instant range (segs 2)."""
     geo, src, mat, obs, opts = W.c2_elastic3d(t_end=1.0)
-    prob, grid, N = build_problem(geo, dict(src, numberParticles=20000), mat, obs, dict(opts, exact_count=True))
+    prob, grid, N = build_problem(geo, dict(src, numberParticles=20000), mat, obs,
+                                  dict(opts, exact_count=True, precision=precision))
     P, keep = prob.to_ctypes()
     ctx = get_context(0)
     out = {}
