@@ -1057,10 +1057,10 @@ template <typename R> struct AdjLane {
         sa += w;
         saj += w * (R)j;
     }
-    // the same with a 32-bit index and the instant as a float
-    __device__ __forceinline__ void observe_f(int idx, R fj)
+    // an observation of weight w at instant fj, carried as a float (w = 0: none; adding
+    // zeros leaves both sums bit for bit as they were)
+    __device__ __forceinline__ void observe_w(R w, R fj)
     {
-        const R w = __ldg(wts + idx);
         sa += w;
         saj = m_fma(w, fj, saj);
     }
@@ -2262,15 +2262,12 @@ __global__ void __launch_bounds__(kAdjointThreads, sizeof(R) == 4 ? 4 : 2) rt_ob
             if constexpr (C32) v = obs_offset_cart32(p, cur, dl, cur.doff);
             else v = obs_offset_dl<R, OBS>(p, sedges, cur, dl);
             dl += dstep;
-            if (v >= 0) {
-                const int idx = toff + (cur.mode ? mstep : 0) + v;
-                if (idx < hlen) {
-                    adj.observe_f(idx, fj);
-                    cnt.obs++;
-                } else {
-                    bad = true;
-                }
-            }
+            // branch-free: a lane without an observation adds a zero weight
+            const int idx = toff + (cur.mode ? mstep : 0) + v;
+            const bool take = v >= 0 && idx < hlen;
+            bad |= v >= 0 && idx >= hlen;
+            adj.observe_w(take ? __ldg(adj.wts + idx) : (R)0, fj);
+            cnt.obs += take ? 1u : 0u;
         }
         if (have) adj.finish();
     }
