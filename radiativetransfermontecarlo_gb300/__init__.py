@@ -10,6 +10,7 @@ from .material import MaterialClass
 from .observation import colon, initialize_observation
 from .radiative_transfer import (TransportProblem, build_problem, get_context, normalise, radiativeTransfer,
                                  run_transport)
+from .resumable import radiative_transfer_resumable
 
 __all__ = ["MaterialClass", "radiativeTransfer", "radiativeTransferGradient", "build_problem", "run_transport", "normalise",
-           "initialize_observation", "colon", "TransportProblem", "get_context"]
+           "initialize_observation", "colon", "TransportProblem", "get_context", "radiative_transfer_resumable"]
