@@ -7,6 +7,7 @@
 #include "rtmc_internal.h"
 
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <algorithm>
 #include <numeric>
@@ -17,6 +18,15 @@
 #include <vector>
 
 using namespace rtmc;
+
+// NVTX range over a scope: the phases of a call show by name in a timeline profiler (the
+// header-only NVTX v3 does nothing unless a tool is attached)
+struct Range {
+    explicit Range(const char *name) { nvtxRangePushA(name); }
+    ~Range() { nvtxRangePop(); }
+    Range(const Range &) = delete;
+    Range &operator=(const Range &) = delete;
+};
 
 struct DevBuf {
     void *p = nullptr;
@@ -518,6 +528,7 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
     if constexpr (sizeof(R) == 4) dt = &ctx->tf; else dt = &ctx->td;
     const int prec = sizeof(R) == 4 ? RTMC_FP32 : RTMC_FP64;
     if (!ctx->cache_tables || ctx->tabs_gen != t->gen || ctx->tabs_prec != prec) {
+        Range r("tables upload");
         int s = upload_tables<R>(ctx, t, dt);
         if (s) { ctx->tabs_gen = 0; return s; }
         ctx->tabs_gen = t->gen;
@@ -881,7 +892,10 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
             q.obs_j0 = 1;
             q.obs_j1 = 4 * gb_[g_split];
         }
-        le = launch_one(q);
+        {
+            Range r("transport launches");
+            le = launch_one(q);
+        }
         CK(cudaEventRecord(ctx->ev_k1, ctx->stream), "event");
         if (!le && use_tb) {
             TbParams tp = tpl;
@@ -957,6 +971,7 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
             }
             if (groups && !le) {
                 CK(cudaEventRecord(ctx->ev_k2, ctx->stream), "event");
+                Range r("deferred histogram copies"); // pageable destinations (empty otherwise)
                 for (int k = 0; k < n_deferred; ++k) {
                     const int c = issue_copies(deferred_g[k]);
                     if (c) return c;
@@ -1016,7 +1031,10 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
                 ++launches;
             }
         }
-        CK(cudaEventSynchronize(sink == kSinkIndex ? ctx->ev_k2 : ctx->ev_k1), "transport");
+        {
+            Range r("wait for the transport");
+            CK(cudaEventSynchronize(sink == kSinkIndex ? ctx->ev_k2 : ctx->ev_k1), "transport");
+        }
         float a = 0, b = 0;
         cudaEventElapsedTime(&a, ctx->ev_k0, ctx->ev_k1);
         kms += a;
@@ -1103,6 +1121,7 @@ int run(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t 
 int forward(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, int64_t *host_out, rtmc_stats *st,
             double *trace_out = nullptr, uint32_t *host_u32 = nullptr)
 {
+    Range range(host_u32 ? "rtmc_forward_u32" : (host_out ? "rtmc_forward" : "rtmc_forward_device"));
     if (!ctx || !P) return fail(ctx ? &ctx->err : nullptr, RTMC_ERR_ARG, "rtmc_forward: NULL argument");
     int s = check_problem(ctx, P, t);
     if (s) return s;
@@ -1740,6 +1759,7 @@ extern "C" int rtmc_forward_trace(rtmc_context *ctx, const rtmc_problem *P, cons
 extern "C" int rtmc_gradient(rtmc_context *ctx, const rtmc_problem *P, const rtmc_tables *t, const rtmc_score *score,
                              const double *adjoint, double *grad, rtmc_stats *st)
 {
+    Range range("rtmc_gradient");
     if (!ctx || !P) return fail(ctx ? &ctx->err : nullptr, RTMC_ERR_ARG, "rtmc_gradient: NULL argument");
     int s = check_problem(ctx, P, t);
     if (s) return s;
@@ -2193,6 +2213,7 @@ extern "C" int rtmc_batch_set_em_histogram(rtmc_batch *b, int32_t shared)
 
 extern "C" int rtmc_batch_run(rtmc_batch *b, rtmc_stats *st)
 {
+    Range range("rtmc_batch_run");
     if (!b) return fail(nullptr, RTMC_ERR_ARG, "rtmc_batch_run: NULL batch");
     rtmc_context *ctx = b->ctx;
     CK(cudaSetDevice(ctx->device), "cudaSetDevice");
