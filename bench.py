@@ -473,7 +473,7 @@ def run_c4(args):
     batch = Batch([W.c4_instance(i) for i in range(args.instances)])
     setup_s = time.perf_counter() - t0
     if args.no_tune:
-        shape, tune, factor, tune_f = (0, 0, 0), {}, 8, {}
+        shape, tune, factor, tune_f = (0, 0, 0), {}, 4, {}
     else:
         shape, tune = autotune(batch, repeats=1)
         factor, tune_f = tune_schedule(batch, repeats=1)

@@ -321,7 +321,8 @@ int rtmc_batch_schedule(const rtmc_batch *batch, int32_t *event_major);
 
 /* Sets which kernel runs each instance (event_major[i] = 1: rt_transport_batch_em, 0: the
  * lockstep kernel; both give the instance's histogram), or restores the automatic choice
- * (event_major = NULL: 1 when 8 x expected events per particle >= observation instants).
+ * (event_major = NULL: 1 when 4 x expected events per particle >= observation instants,
+ * unless rtmc_set_schedule fixed the schedule when the batch was made).
  * Rebuilds the work lists and the graph. */
 int rtmc_batch_set_schedule(rtmc_batch *batch, const int32_t *event_major);
 

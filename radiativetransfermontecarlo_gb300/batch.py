@@ -142,7 +142,7 @@ def autotune(batch: Batch, blocks=(256, 512), rings=(4, 8), chunks=(4096, 16384,
 def tune_schedule(batch: Batch, factors=(2, 4, 8, 16, 32), repeats: int = 2):
     """Time the split of the instances between the two kernels on the batch itself: an
     instance runs event-major when factor x its expected events per particle >= its
-    observation instants (8 is the automatic choice).  Keeps the fastest and returns
+    observation instants (4 is the automatic choice).  Keeps the fastest and returns
     (best factor, {factor: ms})."""
     ev = batch.expected_events()
     n_obs = np.array([batch._arr[i].n_obs for i in range(len(batch.problems))], dtype=np.float64)

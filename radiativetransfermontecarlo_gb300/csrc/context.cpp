@@ -1929,6 +1929,7 @@ struct rtmc_batch {
     std::vector<int> event_major;    // the kernel of each instance (1: event-major)
     std::vector<int> event_major_auto; // the automatic choice
     std::vector<int> seg_cap;        // the split kernel's segment records per particle
+    std::vector<unsigned char> params_host; // the instances' DevParams as uploaded
     int n_edges = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -1966,6 +1967,15 @@ template <typename R> int batch_build_graph(rtmc_batch *b)
     int block, ring = 0;
     int64_t chunk;
     int bps = 0;
+    {
+        // each instance's event_major flag follows the kernel that runs it
+        auto *hp = reinterpret_cast<DevParams<R> *>(b->params_host.data());
+        bool changed = false;
+        for (int i = 0; i < b->n; ++i)
+            if (hp[i].event_major != b->event_major[i]) { hp[i].event_major = b->event_major[i]; changed = true; }
+        if (changed)
+            CK(cudaMemcpy(b->params.p, hp, (size_t)b->n * sizeof(DevParams<R>), cudaMemcpyHostToDevice), "params");
+    }
     b->kmax = 0;
     for (int i = 0; i < b->n; ++i)
         if (!b->event_major[i]) b->kmax = std::max(b->kmax, b->seg_cap[i]);
@@ -2132,9 +2142,15 @@ int batch_create(rtmc_context *ctx, int n, const rtmc_problem *P, const rtmc_tab
             if (std::isfinite(P[i].mft[m])) rate = std::max(rate, 1.0 / P[i].mft[m]);
         b->cost_per_particle[i] = P[i].n_obs + 4.0 * rate * P[i].h * P[i].n_sub * P[i].n_obs;
         if (i == 0) b->obs_kind = params[0].obs_kind;
+        // the kernel of an instance: event-major when 4 x its expected events per particle
+        // reach its observation instants (on the 256-instance sweep: 578 ms per launch,
+        // against 589 / 592 / 628 / 691 ms with 2 / 8 / 16 / 32; tune_schedule times it on a
+        // batch), unless the context's schedule fixes it
+        const double mean = rate * P[i].h * (double)P[i].n_sub * (double)P[i].n_obs;
+        const int o = ctx->opt_event_major;
+        params[i].event_major = o == 1 ? 1 : ((o == 0 || o == 2) ? 0 : (4.0 * mean >= (double)P[i].n_obs ? 1 : 0));
         b->event_major[i] = b->event_major_auto[i] = params[i].event_major;
         // the split kernel's segment records per particle: as for rtmc_forward's split schedule
-        const double mean = rate * P[i].h * (double)P[i].n_sub * (double)P[i].n_obs;
         int K = (int)std::ceil(1.0 + mean + 4.0 * std::sqrt(mean) + 4.0);
         K = std::min(64, std::max(8, (K + 3) / 4 * 4));
         if (ctx->opt_ring) K = ctx->opt_ring; // the context's ring capacity, when one is set
@@ -2149,6 +2165,8 @@ int batch_create(rtmc_context *ctx, int n, const rtmc_problem *P, const rtmc_tab
     for (int i = 0; i < n; ++i) params[i].edges = static_cast<const R *>(b->edges.p);
     if (!edges.empty())
         CK(cudaMemcpy(b->edges.p, edges.data(), edges.size() * sizeof(R), cudaMemcpyHostToDevice), "edges");
+    b->params_host.assign(reinterpret_cast<const unsigned char *>(params.data()),
+                          reinterpret_cast<const unsigned char *>(params.data() + n));
     CK(cudaMemcpy(b->params.p, params.data(), (size_t)n * sizeof(DevParams<R>), cudaMemcpyHostToDevice), "params");
     b->n_edges = n_edges;
     b->args_host = new BatchArgs<R>();

@@ -176,8 +176,8 @@ def test_batch_set_schedule_moves_instances_between_kernels():
         assert np.array_equal(b.histograms(), H), em
     ev = b.expected_events()
     n_obs = np.array([b._arr[i].n_obs for i in range(len(picks))])
-    assert list((8 * ev >= n_obs).astype(int)) == list(auto)
-    best, times = tune_schedule(b, factors=(1, 8, 1000), repeats=1)
+    assert list((4 * ev >= n_obs).astype(int)) == list(auto)
+    best, times = tune_schedule(b, factors=(1, 4, 1000), repeats=1)
     assert best in times and len(times) == 3
     b.run()
     assert np.array_equal(b.histograms(), H)
