@@ -2147,8 +2147,9 @@ int batch_create(rtmc_context *ctx, int n, const rtmc_problem *P, const rtmc_tab
         // against 589 / 592 / 628 / 691 ms with 2 / 8 / 16 / 32; tune_schedule times it on a
         // batch), unless the context's schedule fixes it
         const double mean = rate * P[i].h * (double)P[i].n_sub * (double)P[i].n_obs;
-        const int o = ctx->opt_event_major;
-        params[i].event_major = o == 1 ? 1 : ((o == 0 || o == 2) ? 0 : (4.0 * mean >= (double)P[i].n_obs ? 1 : 0));
+        const int sched = ctx->opt_event_major;
+        params[i].event_major =
+            sched == 1 ? 1 : ((sched == 0 || sched == 2) ? 0 : (4.0 * mean >= (double)P[i].n_obs ? 1 : 0));
         b->event_major[i] = b->event_major_auto[i] = params[i].event_major;
         // the split kernel's segment records per particle: as for rtmc_forward's split schedule
         int K = (int)std::ceil(1.0 + mean + 4.0 * std::sqrt(mean) + 4.0);
