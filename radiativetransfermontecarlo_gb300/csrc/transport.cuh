@@ -808,6 +808,9 @@ __device__ __forceinline__ void seg_prepare(const DevParams<R> &p, const R *sedg
     } else if (OBS == OBS_RADIAL) {
 #pragma unroll
         for (int a = 0; a < 3; ++a) g.B[a] = m_mul(step, g.d[a]);
+        // |(x, y)| (2D, or the cylindrical frame): the third coordinate of the observation
+        // copy is zero, so every radius is |x| over three coordinates without a branch
+        if (!p.radial_3d) g.x[2] = g.B[2] = (R)0;
     }
 }
 
@@ -828,12 +831,9 @@ __device__ __forceinline__ int obs_offset_dl(const DevParams<R> &p, const R *sed
         }
         return ok ? idx : -1;
     } else if (OBS == OBS_RADIAL) {
-        const R x0 = m_fma(g.B[0], dl, g.x[0]), x1 = m_fma(g.B[1], dl, g.x[1]);
-        R r2 = m_fma(x1, x1, m_mul(x0, x0));
-        if (p.radial_3d) {
-            const R x2 = m_fma(g.B[2], dl, g.x[2]);
-            r2 = m_fma(x2, x2, r2);
-        }
+        // the segment's third coordinate is zero where the radius is |(x, y)| (seg_prepare)
+        const R x0 = m_fma(g.B[0], dl, g.x[0]), x1 = m_fma(g.B[1], dl, g.x[1]), x2 = m_fma(g.B[2], dl, g.x[2]);
+        const R r2 = m_fma(x2, x2, m_fma(x1, x1, m_mul(x0, x0)));
         const int b = bin_floor(m_fma(m_fast_sqrt(r2), p.ax_inv_w[0], p.ax_a0));
         return (g.doff >= 0 && (unsigned)b < (unsigned)p.ax_nbe[0]) ? g.doff + b * p.ax_stride32[0] : -1;
     } else {
@@ -923,12 +923,8 @@ __device__ __forceinline__ int obs_offset_radial64(const DevParams<R> &p, const 
 {
     // d, the sub-steps since the segment start, is an exact integer (below 2^24 here)
     if (g.doff < 0) return -1;
-    const float x0 = fmaf(f.Bf[0], d, f.xf[0]), x1 = fmaf(f.Bf[1], d, f.xf[1]);
-    float r2 = fmaf(x1, x1, x0 * x0);
-    if (p.radial_3d) {
-        const float x2 = fmaf(f.Bf[2], d, f.xf[2]);
-        r2 = fmaf(x2, x2, r2);
-    }
+    const float x0 = fmaf(f.Bf[0], d, f.xf[0]), x1 = fmaf(f.Bf[1], d, f.xf[1]), x2 = fmaf(f.Bf[2], d, f.xf[2]);
+    const float r2 = fmaf(x2, x2, fmaf(x1, x1, x0 * x0)); // x2 = 0 for |(x, y)| (seg_prepare)
     const float r = r2 > 0.f ? r2 * rsqrtf(r2) : 0.f;
     const float t = fmaf(r, p.r32_iw, p.r32_a0);
     const float m = 0x1p-19f * (fmaf(fmaf(f.sb, d, f.sx) + r, p.r32_iw, fabsf(p.r32_a0) + fabsf(t)) + 1.f);
@@ -2247,32 +2243,39 @@ __global__ void __launch_bounds__(kAdjointThreads, sizeof(R) == 4 ? 4 : 2) rt_ob
         int toff = (int)p.time_stride;
         const int tstep = (int)p.time_stride, mstep = (int)p.mode_stride, hlen = (int)p.hist_len;
         R fj = (R)1;
+        // CDL: the offset dl is counted up per instant (an exact integer below 2^24), else
+        // converted afresh; fixed per launch, so the loop has no test for it
+        auto walk = [&](auto count_tag) {
+            constexpr bool CDL = decltype(count_tag)::value;
 #pragma unroll 1
-        for (int j = 1; j <= p.n_obs; ++j, so += p.n_sub, toff += tstep, fj += (R)1) {
-            if (so >= next_start) { // the next segment comes into force; load the one after it
-                do {
-                    cur = nxt;
-                    adj.enter(nth);
-                    ++k;
-                    rec_get<R, OBS>(rec + (size_t)k * kRecWords, nxt);
-                    nth = __ldg(th + k);
-                    next_start = nxt.s0;
-                } while (so >= next_start);
-                dl = (R)(so - cur.s0);
-            } else if (!count_dl) {
-                dl = (R)(so - cur.s0);
+            for (int j = 1; j <= p.n_obs; ++j, so += p.n_sub, toff += tstep, fj += (R)1) {
+                if (so >= next_start) { // the next segment comes into force; load the one after it
+                    do {
+                        cur = nxt;
+                        adj.enter(nth);
+                        ++k;
+                        rec_get<R, OBS>(rec + (size_t)k * kRecWords, nxt);
+                        nth = __ldg(th + k);
+                        next_start = nxt.s0;
+                    } while (so >= next_start);
+                    dl = (R)(so - cur.s0);
+                } else if (!CDL) {
+                    dl = (R)(so - cur.s0);
+                }
+                int v;
+                if constexpr (C32) v = obs_offset_cart32(p, cur, dl, cur.doff);
+                else v = obs_offset_dl<R, OBS>(p, sedges, cur, dl);
+                dl += dstep;
+                // branch-free: a lane without an observation adds a zero weight
+                const int idx = toff + (cur.mode ? mstep : 0) + v;
+                const bool take = v >= 0 && idx < hlen;
+                bad |= v >= 0 && idx >= hlen;
+                adj.observe_w(take ? __ldg(adj.wts + idx) : (R)0, fj);
+                cnt.obs += take ? 1u : 0u;
             }
-            int v;
-            if constexpr (C32) v = obs_offset_cart32(p, cur, dl, cur.doff);
-            else v = obs_offset_dl<R, OBS>(p, sedges, cur, dl);
-            dl += dstep;
-            // branch-free: a lane without an observation adds a zero weight
-            const int idx = toff + (cur.mode ? mstep : 0) + v;
-            const bool take = v >= 0 && idx < hlen;
-            bad |= v >= 0 && idx >= hlen;
-            adj.observe_w(take ? __ldg(adj.wts + idx) : (R)0, fj);
-            cnt.obs += take ? 1u : 0u;
-        }
+        };
+        if (count_dl) walk(std::true_type{});
+        else walk(std::false_type{});
         if (have) adj.finish();
     }
     double g[kAdjRingParams];
