@@ -111,14 +111,15 @@ def measured_peak_hbm():
         return 6800.0, "fallback"
 
 
-def load_traffic():
-    """DRAM bytes (read + write) of each kernel in one full-size launch of this workload, from
-    a one-pass ncu capture (dram__bytes_read.sum, dram__bytes_write.sum), summarised in
-    profiles/c2_traffic.json; {} when absent."""
+def load_traffic(field: str = "dram_bytes_full_launch"):
+    """Per kernel, a figure of one full-size launch of this workload from one-pass ncu
+    captures summarised in profiles/c2_traffic.json: DRAM bytes read + written (default),
+    or the L2 reduction requests of the fold ("l2_reduction_requests",
+    lts__t_requests_srcunit_tex_op_red.sum); {} when absent."""
     p = ROOT / "profiles" / "c2_traffic.json"
     try:
         d = json.loads(p.read_text())
-        return {k: v["dram_bytes_full_launch"] for k, v in d["kernels"].items()}
+        return {k: v[field] for k, v in d["kernels"].items() if field in v}
     except Exception:
         return {}
 
@@ -349,6 +350,14 @@ def run_our_arm(args, rank, world, dist):
                                      "frac": fb / tmean / 1e6 / peak,
                                      "observations_per_s": obs_per_step / tmean * 1e3,
                                      "traffic": traffic.get("rt_fold_tb")}
+            # its actual bound: the L2's rate of 16-byte vector reductions, measured here by
+            # rtmc_probe_l2_reductions; the requests per launch come from a one-pass capture
+            reds = load_traffic("l2_reduction_requests").get("rt_fold_tb")
+            red_peak = ctx.probe_l2_reductions()
+            kernels["rt_fold_tb"]["l2_reductions"] = {
+                "per_launch": reds, "peak_per_s": red_peak, "unit": "red.global.add.v4.f32 per second",
+                "achieved_per_s": reds / tmean * 1e3 if reds else None,
+                "frac": reds / tmean * 1e3 / red_peak if reds and red_peak else None}
             kernels["rt_tb_convert"] = {"ms": cmean, "bound": "hbm", "algorithmic_bytes": cb,
                                         "achieved": cb / cmean / 1e6, "peak": peak, "unit": "GB/s",
                                         "frac": cb / cmean / 1e6 / peak, "traffic": traffic.get("rt_tb_convert")}

@@ -434,6 +434,11 @@ int rtmc_set_particle_order(rtmc_context *ctx, int32_t enable);
 /* writes a device buffer larger than L2 (timing hygiene between measured runs) */
 int rtmc_flush_l2(rtmc_context *ctx);
 
+/* The L2's rate of 16-byte vector reductions (red.global.add.v4.f32, none awaited) into an
+ * L2-resident 64 MB buffer at random slots, the bound of the time-blocked fold: the best of
+ * three timed launches, in reductions per second (a measurement for the roofline) */
+int rtmc_probe_l2_reductions(rtmc_context *ctx, double *reductions_per_s);
+
 /* kernel time of the last forward call in ms (CUDA events) and its launch count */
 int rtmc_last_timing(const rtmc_context *ctx, double *kernel_ms, int32_t *launches);
 

@@ -126,6 +126,7 @@ SIGNATURES = {
     "rtmc_batch_schedule": (C.c_int, [_P, C.POINTER(C.c_int32)]),
     "rtmc_batch_destroy": (None, [_P]),
     "rtmc_last_timing": (C.c_int, [_P, C.POINTER(C.c_double), C.POINTER(C.c_int32)]),
+    "rtmc_probe_l2_reductions": (C.c_int, [_P, C.POINTER(C.c_double)]),
 }
 
 _lock = threading.Lock()
@@ -368,6 +369,12 @@ class Context:
 
     def flush_l2(self):
         check(self.lib.rtmc_flush_l2(self.handle), self.handle)
+
+    def probe_l2_reductions(self) -> float:
+        """rtmc_probe_l2_reductions: the L2's 16-byte vector-reduction rate (per second)."""
+        r = C.c_double()
+        check(self.lib.rtmc_probe_l2_reductions(self.handle, C.byref(r)), self.handle)
+        return r.value
 
 
 class PinnedBuffer:

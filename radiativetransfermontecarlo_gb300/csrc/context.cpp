@@ -1901,6 +1901,33 @@ extern "C" int rtmc_flush_l2(rtmc_context *ctx)
     return RTMC_OK;
 }
 
+extern "C" int rtmc_probe_l2_reductions(rtmc_context *ctx, double *reductions_per_s)
+{
+    if (!ctx || !reductions_per_s) return fail(ctx ? &ctx->err : nullptr, RTMC_ERR_ARG, "rtmc_probe_l2_reductions: NULL argument");
+    CK(cudaSetDevice(ctx->device), "cudaSetDevice");
+    // 4M slots of 16 bytes (64 MB, L2-resident, the size of one t-block of the fold's
+    // accumulator on the 3D elastic workload) in the flush buffer; 8 blocks of 256 per SM
+    constexpr uint32_t kSlots = 1u << 22;
+    constexpr int kIters = 512;
+    if (ctx->flush.grow((size_t)512 << 20)) return fail(&ctx->err, RTMC_ERR_ALLOC, "device allocation for the probe failed");
+    float *buf = static_cast<float *>(ctx->flush.p);
+    const int grid = ctx->num_sms * 8;
+    double best = 0;
+    for (int rep = 0; rep < 4; ++rep) { // the first is a warm-up
+        CK(cudaEventRecord(ctx->ev_k0, ctx->stream), "event");
+        const int le = launch_probe_red(buf, kSlots, grid, kIters, ctx->stream);
+        if (le) return cuda_fail(ctx, (cudaError_t)le, "probe launch");
+        CK(cudaEventRecord(ctx->ev_k1, ctx->stream), "event");
+        CK(cudaEventSynchronize(ctx->ev_k1), "probe");
+        float ms = 0;
+        cudaEventElapsedTime(&ms, ctx->ev_k0, ctx->ev_k1);
+        const double rate = (double)grid * 256.0 * kIters / (ms * 1e-3);
+        if (rep > 0 && rate > best) best = rate;
+    }
+    *reductions_per_s = best;
+    return RTMC_OK;
+}
+
 extern "C" int rtmc_last_timing(const rtmc_context *ctx, double *kernel_ms, int32_t *launches)
 {
     if (!ctx) return fail(nullptr, RTMC_ERR_ARG, "rtmc_last_timing: NULL context");

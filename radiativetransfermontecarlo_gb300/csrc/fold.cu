@@ -219,6 +219,20 @@ __device__ __forceinline__ void red_v4(float *a, float x, float y, float z, floa
     asm volatile("red.global.add.v4.f32 [%0], {%1, %2, %3, %4};" ::"l"(a), "f"(x), "f"(y), "f"(z), "f"(w) : "memory");
 }
 
+// The L2's vector-reduction rate, the bound of rt_fold_tb: every thread issues `iters`
+// reductions of 16 bytes (none awaited, as the fold issues them) to slots spread over an
+// L2-resident buffer of n_vec 16-byte slots by a linear congruential sequence.
+__global__ void __launch_bounds__(256) rt_probe_red_v4(float *buf, uint32_t n_vec, int iters)
+{
+    uint32_t h = (blockIdx.x * 256u + threadIdx.x) * 2654435761u + 12345u;
+#pragma unroll 4
+    for (int k = 0; k < iters; ++k) {
+        h = h * 1664525u + 1013904223u;
+        const uint32_t slot = (uint32_t)(((uint64_t)h * n_vec) >> 32); // below n_vec
+        red_v4(buf + (size_t)slot * 4, 1.f, 1.f, 1.f, 1.f);
+    }
+}
+
 __device__ __forceinline__ bool tb_hash_insert(int *keys, unsigned (*cnt)[4], int *used, int key, const int m[4])
 {
     unsigned h = ((unsigned)key * 2654435761u) >> (32 - 11); // 11 = log2(kTbSlots)
@@ -447,6 +461,13 @@ int launch_order(const OrderParams &o, int grid, void *stream)
     rt_order_count<<<g, kOrderThreads, 0, (cudaStream_t)stream>>>(o);
     rt_order_scan<<<1, kScanThreads, 0, (cudaStream_t)stream>>>(o);
     rt_order_place<<<g, kOrderThreads, 0, (cudaStream_t)stream>>>(o);
+    return (int)cudaGetLastError();
+}
+
+int launch_probe_red(float *buf, uint32_t n_vec, int grid, int iters, void *stream)
+{
+    if (!buf || n_vec == 0 || grid < 1 || iters < 1) return (int)cudaErrorInvalidValue;
+    rt_probe_red_v4<<<grid, 256, 0, (cudaStream_t)stream>>>(buf, n_vec, iters);
     return (int)cudaGetLastError();
 }
 

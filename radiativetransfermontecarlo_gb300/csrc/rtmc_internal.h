@@ -287,6 +287,8 @@ int launch_bin_slices(const BinParams &b, int grid_x, size_t smem, void *stream)
 // n histogram bins as uint32 counts (value >> shift, saturating), at most max_grid blocks
 int launch_narrow_u32(const unsigned long long *src, uint32_t *dst, int64_t n, int shift, int max_grid, void *stream);
 // time-blocked fold of one chunk over t-blocks [tb_first, tb_first + tb_count)
+// the L2 vector-reduction probe (rt_probe_red_v4): grid blocks of 256 threads, iters each
+int launch_probe_red(float *buf, uint32_t n_vec, int grid, int iters, void *stream);
 int launch_fold_tb(const TbParams &t, int grid_x, void *stream);
 // the particle order of OrderParams (three kernels)
 int launch_order(const OrderParams &o, int grid, void *stream);
