@@ -114,3 +114,18 @@ def test_int64_range_reported_and_u32_exact():
     prob.n_particles = 4  # 4 * 2^62 = 2^64 would wrap: refused on the host
     rc, st, msg = _raw_forward(get_context(0).lib.rtmc_forward_u32, prob, np.zeros(prob.hist_len, dtype=np.uint32))
     assert rc == RTMC_ERR_ARG
+
+
+@pytest.mark.gpu
+def test_l2_reduction_probe_reports_a_rate():
+    """rtmc_probe_l2_reductions times its vector reductions and leaves the context usable:
+    a plausible rate (between 1e9 and 1e13 per second), and a forward call afterwards."""
+    from radiativetransfermontecarlo_gb300 import get_context
+    ctx = get_context(0)
+    r = ctx.probe_l2_reductions()
+    assert 1e9 < r < 1e13
+    geo, src, mat, obs, opts = W.c1_acoustic3d(n=2000, precision="fp32")
+    prob, grid, N = build_problem(geo, src, mat, obs, dict(opts, exact_count=True))
+    P, keep = prob.to_ctypes()
+    h, st = ctx.forward(P, prob.tables)
+    assert st["device_status"] == 0 and int(h.sum() >> prob.hist_shift) == st["observations"]
