@@ -402,15 +402,17 @@ def run_our_arm(args, rank, world, dist):
         def e2e_leg(call, out):
             ctx.set_table_cache(False)
             call(P32, prob.tables, out)
-            times, dev, ev, h2d, d2h = [], [], 0, 0.0, 0.0
-            for _ in range(max(3, args.steps // 2)):
-                ctx.flush_l2()
-                t0 = time.perf_counter()
-                _, st = call(P32, prob.tables, out)
-                times.append(time.perf_counter() - t0)
-                dev.append(st["total_ms"])
-                ev += st["scatter_events"]
-                h2d, d2h = st["h2d_bytes"], st["d2h_bytes"]
+            times, dev, kern, ev, h2d, d2h = [], [], [], 0, 0.0, 0.0
+            with ClockSampler(device) as clk:
+                for _ in range(max(3, args.steps // 2)):
+                    ctx.flush_l2()
+                    t0 = time.perf_counter()
+                    _, st = call(P32, prob.tables, out)
+                    times.append(time.perf_counter() - t0)
+                    dev.append(st["total_ms"])
+                    kern.append(st["kernel_ms"] + st["fold_ms"])
+                    ev += st["scatter_events"]
+                    h2d, d2h = st["h2d_bytes"], st["d2h_bytes"]
             ctx.set_table_cache(True)
             return {"value": ev / sum(times), "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "ms_per_step": 1000 * float(np.mean(times)),
@@ -418,8 +420,10 @@ def run_our_arm(args, rank, world, dist):
                     "ms_steps": [round(1000 * t, 2) for t in times],
                     # the same calls' CUDA-event time from their first to their last queued
                     # operation (copies included): a step slow here too was slow on the device
-                    # or the host link, not in host code
-                    "device_ms_steps": [round(t, 2) for t in dev]}
+                    # or the host link, not in host code; and the transport + fold share of it
+                    # (the copies overlap the folds): a step slow there was slow in the kernels
+                    "device_ms_steps": [round(t, 2) for t in dev],
+                    "kernel_ms_steps": [round(t, 2) for t in kern], "clocks": clk.summary()}
         result["e2e"] = dict(e2e_leg(ctx.forward_u32, buf.array(np.uint32, prob.hist_len)),
                              api="rtmc_forward_u32 (uint32 counts, the reference's E type)")
         # the same call into pageable host memory, which is what a MEX gateway receives from
