@@ -941,6 +941,18 @@ __device__ __forceinline__ int obs_offset(const DevParams<R> &p, const R *sedges
     return obs_offset_dl<R, OBS>(p, sedges, g, (R)(so - g.s0));
 }
 
+// The radius-only path for a radius |(x, y)| (2D, the cylindrical frame): the bin of
+// obs_offset_dl<R, OBS_RADIAL> without its third coordinate, which seg_prepare zeroed there
+// (the same operations and value: the skipped multiply-add adds 0 * 0)
+template <typename R>
+__device__ __forceinline__ int obs_offset_radius2(const DevParams<R> &p, const Seg<R> &g, R dl)
+{
+    const R x0 = m_fma(g.B[0], dl, g.x[0]), x1 = m_fma(g.B[1], dl, g.x[1]);
+    const R r2 = m_fma(x1, x1, m_mul(x0, x0));
+    const int b = bin_floor(m_fma(m_fast_sqrt(r2), p.ax_inv_w[0], p.ax_a0));
+    return (g.doff >= 0 && (unsigned)b < (unsigned)p.ax_nbe[0]) ? g.doff + b * p.ax_stride32[0] : -1;
+}
+
 // Per-lane ring of segments in shared memory, field-major so that lane t of every
 // slot sits in bank t % 32.
 template <typename R> struct Ring {
@@ -1283,25 +1295,33 @@ __device__ __forceinline__ void run_particle(const DevParams<R> &p, const R *sed
         Seg<R> g;
         seg_from(s, g);
         seg_prepare<R, OBS>(p, sedges, g);
-        for (; j <= p.n_obs && j * p.n_sub < lim; ++j) { // observations strictly before the event
-            const int v = obs_offset<R, OBS>(p, sedges, g, j * p.n_sub);
-            if (SINK == SINK_INDEX) {
-                if (j >= jr0 && j <= jr1) {
-                    *optr = v < 0 ? -1 : (v | (g.mode << 30));
-                    if (v >= 0) cnt.obs++;
-                }
-                optr += p.obs_rows;
-            } else if (v >= 0) {
-                const int64_t idx = (int64_t)j * p.time_stride + (g.mode ? p.mode_stride : 0) + v;
-                if (idx < p.hist_len) {
-                    cnt.obs++;
-                    if (SINK == SINK_SMEM) atomicAdd(shist + idx, 1u);
-                    else atomicAdd(p.hist + idx, inc);
-                } else {
-                    bad = true;
+        // observations strictly before the event; R2D: a radius |(x, y)| (2D, cylindrical),
+        // whose zero third coordinate is left out (the same value: x2 = 0 adds nothing)
+        auto observe = [&](auto r2d_tag) {
+            constexpr bool R2D = decltype(r2d_tag)::value;
+            for (; j <= p.n_obs && j * p.n_sub < lim; ++j) {
+                const int v = R2D ? obs_offset_radius2(p, g, (R)(j * p.n_sub - g.s0))
+                                  : obs_offset<R, OBS>(p, sedges, g, j * p.n_sub);
+                if (SINK == SINK_INDEX) {
+                    if (j >= jr0 && j <= jr1) {
+                        *optr = v < 0 ? -1 : (v | (g.mode << 30));
+                        if (v >= 0) cnt.obs++;
+                    }
+                    optr += p.obs_rows;
+                } else if (v >= 0) {
+                    const int64_t idx = (int64_t)j * p.time_stride + (g.mode ? p.mode_stride : 0) + v;
+                    if (idx < p.hist_len) {
+                        cnt.obs++;
+                        if (SINK == SINK_SMEM) atomicAdd(shist + idx, 1u);
+                        else atomicAdd(p.hist + idx, inc);
+                    } else {
+                        bad = true;
+                    }
                 }
             }
-        }
+        };
+        if (OBS == OBS_RADIAL && !p.radial_3d) observe(std::true_type{});
+        else observe(std::false_type{});
         if (j > p.n_obs || !s.alive || e > p.s_end) break;
         process_event(p, pid, s, cnt);
         if ((int)s.k > p.max_events) { s.alive = 0; s.s_death = s.s0; bad = true; }
