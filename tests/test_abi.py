@@ -117,3 +117,23 @@ def test_problem_validation_needs_no_gpu():
     refused(lambda P: setattr(P, "n_sub", 1 << 23), "2^30")
     refused(lambda P: setattr(P, "h", -1.0), "sub-step h")
     refused(lambda P: setattr(P, "mft", (C.c_double * 2)(-1.0, -1.0)), "mean free times")
+
+
+def test_null_handles_are_argument_errors():
+    """Every entry point that takes a context or a batch refuses a NULL handle with
+    RTMC_ERR_ARG and a message (no CUDA call, no crash)."""
+    lib = _lib.load()
+    r = C.c_double()
+    em = (C.c_int32 * 4)()
+    calls = {
+        "rtmc_set_early_copy": (None, 40), "rtmc_set_fp64_estimate": (None, 1), "rtmc_set_particle_order": (None, 1),
+        "rtmc_set_fold": (None, 0), "rtmc_set_schedule": (None, -1), "rtmc_set_launch": (None, 0, 0, 0),
+        "rtmc_set_pipeline": (None, 0, 0), "rtmc_set_table_cache": (None, 1),
+        "rtmc_probe_l2_reductions": (None, C.byref(r)), "rtmc_batch_set_launch": (None, 0, 0, 0),
+        "rtmc_batch_set_em_histogram": (None, 1), "rtmc_batch_set_schedule": (None, None),
+        "rtmc_batch_schedule": (None, em), "rtmc_batch_run": (None, None), "rtmc_forward_device": (None, None, None, None),
+        "rtmc_gradient": (None, None, None, None, None, None, None),
+    }
+    for name, args in calls.items():
+        assert getattr(lib, name)(*args) == 1, name
+        assert lib.rtmc_last_error(None), name
