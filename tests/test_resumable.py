@@ -74,6 +74,8 @@ def test_snapshot_of_another_problem_or_damaged_is_refused(tmp_path, monkeypatch
         R.radiative_transfer_resumable(geo, src, mat, obs, dict(opts, seed=1), checkpoint=ck, chunk=5_000)
     with pytest.raises(ValueError, match="another problem"):
         R.radiative_transfer_resumable(geo, dict(src, numberParticles=30_000), mat, obs, opts, checkpoint=ck)
+    with pytest.raises(ValueError, match="another problem"):  # another observation grid (its edges)
+        R.radiative_transfer_resumable(geo, src, mat, dict(obs, x=obs["x"] * 1.5), opts, checkpoint=ck)
     h = np.fromfile(ck + ".hist", dtype=np.uint64)
     h[7] += np.uint64(1)
     h.tofile(ck + ".hist")
